@@ -1,0 +1,248 @@
+/*
+ * plt_gb300.h -- C ABI of the GB300-native PLT (physical light transport) hot path.
+ *
+ * One shared library (libplt_gb300.so) exports every function declared here.  The ABI uses
+ * plain C types only: caller-owned pointers, sizes and status codes.  No exception crosses it.
+ *
+ * Conventions
+ *  - Unless a comment says "host", every buffer pointer is a CUDA device pointer owned by the
+ *    caller, 16-byte aligned, laid out as structure-of-arrays "planes": a field with C
+ *    components over n queries is C consecutive planes of n values (component c of query i
+ *    lives at [c*n + i]).
+ *  - Every call returns a plt_status.  PLT_CUDA_ERROR carries the last cudaError_t, readable
+ *    with plt_last_cuda_error().
+ *  - Launches are asynchronous on the caller's stream (a cudaStream_t passed as void*;
+ *    NULL = legacy default stream).  One context per host thread; distinct contexts are
+ *    independent.
+ *
+ * Reference interfaces this ABI replaces (paths inside ssteinberg/PLTFalcor):
+ *  - Material plugin: IMaterialInstance eval / sample / pdf / lambdaPdf
+ *      Source/Falcor/Rendering/Materials/IMaterialInstance.slang:122-184, implemented per
+ *      material in Source/Falcor/Rendering/Materials/PLT/PLT*BSDF.slang; material parameters
+ *      packed by the PLT*Material.cpp host classes into BasicMaterialData
+ *      (Source/Falcor/Scene/Material/BasicMaterialData.slang:63-85).
+ *  - Spectral tables: SpectralProfile (BasicMaterialData.slang:43-54) built by
+ *      SceneBuilder genSpectralProfile (Source/Falcor/Scene/SceneBuilder.cpp:911-960).
+ *  - Render pass: PLTPT plugin create/execute (Source/RenderPasses/PLTPT/PLTPT.cpp:43-46,
+ *      147-204, 357-499).
+ */
+#ifndef PLT_GB300_H
+#define PLT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLT_ABI_VERSION 1u
+#define PLT_MAX_HWSS 8u                 /* hero wavelengths per beam (reference: <= 4, Utils/HWSS.slang:4-9) */
+#define PLT_SPECTRAL_MAX_BINS 128u      /* SpectralProfile::kMaxBins */
+#define PLT_NO_SPECTRAL_PROFILE 0xFFFFFFFFu
+
+typedef enum plt_status {
+    PLT_OK = 0,
+    PLT_INVALID_ARG = 1,
+    PLT_OOM = 2,
+    PLT_QUEUE_TIMEOUT = 3,
+    PLT_NAN_INPUT = 4,
+    PLT_CUDA_ERROR = 5,
+    PLT_NOT_SUPPORTED = 6,
+    PLT_BAD_MATERIAL = 7
+} plt_status;
+
+/* MaterialType ids, Source/Falcor/Scene/Material/MaterialTypes.slang:36-53 */
+typedef enum plt_material_type {
+    PLT_MATERIAL_UNKNOWN = 0,
+    PLT_MATERIAL_STANDARD = 1,
+    PLT_MATERIAL_DIFFUSE = 2,
+    PLT_MATERIAL_CONDUCTOR = 3,
+    PLT_MATERIAL_DIELECTRIC = 4,
+    PLT_MATERIAL_OPAQUE_DIELECTRIC = 5,
+    PLT_MATERIAL_THIN_DIELECTRIC = 6,
+    PLT_MATERIAL_COATED_CONDUCTOR = 7,
+    PLT_MATERIAL_COATED_OPAQUE_DIELECTRIC = 8,
+    PLT_MATERIAL_GRATED_CONDUCTOR = 9,
+    PLT_MATERIAL_GRATED_OPAQUE_DIELECTRIC = 10,
+    PLT_MATERIAL_MULTILAYERED_STACK = 11,
+    PLT_MATERIAL_TYPE_COUNT = 12
+} plt_material_type;
+
+/* LobeType flags, Source/Falcor/Rendering/Materials/LobeType.slang:36-69 */
+typedef enum plt_lobe_type {
+    PLT_LOBE_NONE = 0x00,
+    PLT_LOBE_DIFFUSE_REFLECTION = 0x01,
+    PLT_LOBE_SCATTER_REFLECTION = 0x02,
+    PLT_LOBE_DELTA_REFLECTION = 0x04,
+    PLT_LOBE_DISPERSIVE_DELTA_REFLECTION = 0x08,
+    PLT_LOBE_DIFFUSE_TRANSMISSION = 0x10,
+    PLT_LOBE_SCATTER_TRANSMISSION = 0x20,
+    PLT_LOBE_DELTA_TRANSMISSION = 0x40,
+    PLT_LOBE_DISPERSIVE_DELTA_TRANSMISSION = 0x80,
+    PLT_LOBE_DELTA = 0xCC,
+    PLT_LOBE_NON_DELTA = 0x33,
+    PLT_LOBE_REFLECTION = 0x0F,
+    PLT_LOBE_TRANSMISSION = 0xF0,
+    PLT_LOBE_ALL = 0xFFFF,
+    PLT_LOBE_MATERIAL_SPECIFIC = 0xFF00
+} plt_lobe_type;
+
+/* SpectralProfile, BasicMaterialData.slang:43-54 (host C++ layout, 1052 bytes). */
+typedef struct plt_spectral_profile {
+    float rgb[3];
+    float intensity;
+    uint32_t bins;
+    float min_wavelength;
+    float max_wavelength;
+    float pdf[PLT_SPECTRAL_MAX_BINS];
+    float icdf[PLT_SPECTRAL_MAX_BINS];
+} plt_spectral_profile;
+
+/* One material: the MaterialHeader type id plus the BasicMaterialData constant fields in their
+ * reference order (BasicMaterialData.slang:63-85).  binary16 fields are raw half bits; integer
+ * fields the reference bit-casts through asuint16 (grating type/lobes, layer count in data1[3])
+ * are stored as those 16 bits.  Texture handles are not part of the record: textures are
+ * unsupported, the constants are used. 80 bytes. */
+typedef struct plt_material_record {
+    uint32_t type;                      /* plt_material_type */
+    uint32_t flags;                     /* BasicMaterialData.flags (unused by the PLT path) */
+    uint16_t base_color[4];
+    uint16_t specular[4];
+    uint16_t data1[4];
+    uint16_t data2[4];
+    uint16_t specular_transmission;
+    uint16_t transmission[3];
+    uint16_t diffuse_transmission;
+    uint16_t volume_scattering[3];
+    uint16_t ior;
+    uint16_t volume_absorption[3];
+    uint16_t volume_anisotropy;
+    uint16_t pad0;
+    uint32_t emission_spectral_id;
+    uint32_t ior_n_spectral_id;
+    uint32_t ior_k_spectral_id;
+} plt_material_record;
+
+/* A batch of BSDF queries in the local shading frame (N = +z, T = +x, B = +y).
+ * Each query mirrors one IMaterialInstance call with ShadingData.V = v:
+ *   eval(sd, toEye = w, lobe, beam)       pdf(sd, toLight = w, lambda_hero)
+ *   sample(sd, sg, lambda_hero)           lambdaPdf(sd, wo = w, lobe, beam, beam.wavelengths)
+ * The incoming beam travels along r = -v (PLTPT forwardUnwindStep: sd.V = -beam.r).  Its
+ * tangent t is beam_t, or, when beam_t is NULL, the canonical frame of r used by
+ * PLTBeam.constructLocalFrame (PLT.slang:218-223). */
+typedef struct plt_bsdf_queries {
+    uint32_t n;                         /* number of queries */
+    uint32_t hwss;                      /* wavelengths per beam, 1..PLT_MAX_HWSS */
+    uint32_t rng_offset;                /* sample(): query i uses UniformSampleGenerator(pixel (j & 0xffff, j >> 16), frame), j = i + rng_offset */
+    uint32_t frame;                     /* sample(): sample number of the generator */
+    const uint32_t* material;           /* [n] index into the context's material table */
+    const float* v;                     /* [3][n] sd.V, unit */
+    const float* w;                     /* [3][n] toEye (eval, lambdaPdf) / toLight (pdf), unit */
+    const uint32_t* lobe;               /* [n] lobe mask for eval / lambdaPdf; NULL = PLT_LOBE_ALL */
+    const float* wavelengths;           /* [hwss][n] nm; plane 0 is the hero wavelength */
+    const float* stokes;                /* [4*hwss][n] plane (c*hwss + j) = Stokes component c of wavelength j */
+    const float* coherence;             /* [4][n] diffusivity D.x, D.y, D.z and distance r_m (m) */
+    const float* beam_t;                /* [3][n] beam tangent, or NULL */
+} plt_bsdf_queries;
+
+/* Outputs; each pointer may be NULL, and only the requested outputs are written. */
+typedef struct plt_bsdf_results {
+    float* stokes;                      /* [4*hwss][n] beam Stokes after eval */
+    float* coherence;                   /* [4][n] beam coherence after eval (D, r_m) */
+    float* beam_t;                      /* [3][n] beam tangent after eval (beam r after eval = w) */
+    float* pdf;                         /* [n] pdf(sd, toLight = w, hero wavelength) */
+    float* lambda_pdf;                  /* [hwss][n] lambdaPdf(sd, w, lobe, beam, wavelengths) */
+    float* sample_wo;                   /* [3][n] sampled direction */
+    float* sample_pdf;                  /* [n] */
+    float* sample_weight;               /* [n] */
+    uint32_t* sample_lobe;              /* [n] sampled LobeType (grating lobe code in bits 8-15) */
+    uint32_t* sample_valid;             /* [n] 1 if sample() returned true */
+} plt_bsdf_results;
+
+/* Operations of plt_bsdf_batch; OR them together.  Outputs of an unrequested op are untouched. */
+#define PLT_OP_EVAL 0x1u
+#define PLT_OP_PDF 0x2u
+#define PLT_OP_SAMPLE 0x4u
+#define PLT_OP_LAMBDA_PDF 0x8u
+
+/* PLTPT pass options (RenderPasses/PLTPT/PLTPT.h:74-108, parsed at PLTPT.cpp:147-175). */
+typedef struct plt_options {
+    uint32_t max_bounces;               /* maxBounces, default 32 */
+    uint32_t tile_size;                 /* tileSize, default 512 */
+    uint32_t hwss;                      /* HWSS, default 4 */
+    uint32_t hwss_do_mis;               /* HWSSDoMIS, default 1 */
+    float sourcing_area_from_emissive_geometry; /* mm^2, default 1 */
+    float sourcing_max_beam_omega;      /* default 0.025 */
+    uint32_t use_direct_light;          /* default 1 */
+    uint32_t use_env_light;             /* default 1 */
+    uint32_t use_emissive_lights;       /* default 1 */
+    uint32_t use_analytic_lights;       /* default 1 */
+    uint32_t do_nee;                    /* default 1 */
+    uint32_t do_mis;                    /* default 1 */
+    uint32_t do_russian_roulette;       /* default 1 */
+    uint32_t nee_use_per_tile_sg;       /* default 0 */
+    uint32_t do_importance_sample_emitters; /* default 1 */
+    uint32_t do_mnee;                   /* default 1 */
+    uint32_t mnee_max_occluders;        /* default 2 */
+    uint32_t mnee_max_iterations;       /* default 60 */
+    float mnee_solver_threshold;        /* default 5e-5 */
+    uint32_t flags;                     /* PLT_OPTION_* */
+} plt_options;
+
+#define PLT_OPTION_FP64_MULTILAYER 0x1u /* multilayer recursion in FP64 instead of the reference FP32 */
+
+typedef struct plt_context plt_context;
+
+/* Library identity. */
+uint32_t plt_abi_version(void);
+const char* plt_status_string(plt_status status);
+
+/* Fills the PLTPT defaults (PLTPT.h:74-108). Host pointer. */
+plt_status plt_options_default(plt_options* out);
+
+/* Replaces PLTPT::create(device, Dictionary) (PLTPT.cpp:147-204): a context on the current
+ * CUDA device.  options may be NULL (defaults).  Host pointers. */
+plt_status plt_create(const plt_options* options, plt_context** out);
+plt_status plt_destroy(plt_context* ctx);
+int plt_last_cuda_error(const plt_context* ctx);
+
+/* Replaces the scene's spectral-profile buffer upload (Scene.cpp:765-792): host array. */
+plt_status plt_set_spectral_profiles(plt_context* ctx, const plt_spectral_profile* profiles, uint32_t count);
+
+/* Replaces MaterialSystem upload of BasicMaterialData + setupMaterialInstance decoding
+ * (MaterialFactory.slang:79-130, PLT*Material.slang): host array.  Records are validated
+ * (type id, spectral ids in range) and decoded once into the device material table. */
+plt_status plt_set_materials(plt_context* ctx, const plt_material_record* materials, uint32_t count);
+
+/* Builds a SpectralProfile from piecewise-linear samples (.spd data), restating
+ * PiecewiseLinearSpectrum::eval (Utils/Color/Spectrum.h:88-107), SampledSpectrum
+ * (Utils/Color/SampledSpectrum.h:64-73,308-317) and genSpectralProfile
+ * (SceneBuilder.cpp:911-960).  Host pointers. */
+plt_status plt_spectral_profile_from_samples(const float* wavelengths_nm, const float* values,
+                                             uint32_t count, float scale, int compute_icdf,
+                                             plt_spectral_profile* out);
+
+/* Batched IMaterialInstance calls (see plt_bsdf_queries).  ops = PLT_OP_* mask.  One fused
+ * launch serves every requested op; queries may mix materials in any order. */
+plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* queries,
+                          const plt_bsdf_results* results, uint32_t ops, void* stream);
+
+/* Synchronises `stream`, then reports and clears the context's device status word, which every
+ * launch since the previous check ORs into: PLT_BAD_MATERIAL (a material index out of range or of
+ * an unknown type; those queries return zeros), PLT_NAN_INPUT (a non-finite direction or
+ * wavelength), PLT_QUEUE_TIMEOUT (a bounded device wait gave up).  Mirrors the reference's
+ * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
+plt_status plt_check_status(plt_context* ctx, void* stream);
+
+/* Single-op conveniences over plt_bsdf_batch. */
+plt_status plt_bsdf_eval(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* stream);
+plt_status plt_bsdf_pdf(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* stream);
+plt_status plt_bsdf_sample(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* stream);
+plt_status plt_bsdf_lambda_pdf(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLT_GB300_H */

@@ -1,0 +1,135 @@
+"""ORACLE -- test infrastructure only.  ctypes wrapper of the CPU oracle (oracle/_build/liboracle_plt.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, and only as
+the checker; the product library never loads it.
+
+Parity status: unpinned by reference tests.  The reference path is Slang shader code that cannot be
+compiled here (no slangc, no graphics stack) and the reference ships no PLT tests or golden
+vectors; the oracle is a line-by-line C++ restatement of the Slang modules, pinned by physics
+known-answer tests (tests/test_oracle_kat.py) and by committed fixtures of its own outputs
+(tests/golden/) against regressions.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle_plt.so")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = C.CDLL(LIB)
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        lib.plto_bsdf_batch.restype = i32
+        lib.plto_bsdf_batch.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32]
+        lib.plto_bsdf_batch_range.restype = i32
+        lib.plto_bsdf_batch_range.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32, C.c_uint64, C.c_uint64]
+        lib.plto_count_ops.restype = i32
+        lib.plto_count_ops.argtypes = [vp, u32, vp, u32, vp, u32, C.POINTER(C.c_double)]
+        lib.plto_rng_stream.restype = None
+        lib.plto_rng_stream.argtypes = [u32, u32, u32, u32, C.POINTER(C.c_uint32)]
+        lib.plto_half_to_float.restype = C.c_float
+        lib.plto_half_to_float.argtypes = [C.c_uint16]
+        lib.plto_rgb_to_spectrum.restype = C.c_float
+        lib.plto_rgb_to_spectrum.argtypes = [C.c_float] * 4
+        lib.plto_fresnel_dielectric.restype = None
+        lib.plto_fresnel_dielectric.argtypes = [C.c_float, C.c_float, C.POINTER(C.c_float)]
+        lib.plto_fresnel_conductor.restype = None
+        lib.plto_fresnel_conductor.argtypes = [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]
+        lib.plto_besselj.restype = C.c_double
+        lib.plto_besselj.argtypes = [i32, C.c_double]
+        lib.plto_diffract.restype = None
+        lib.plto_diffract.argtypes = [C.c_float, C.c_float, C.c_float, i32, i32, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]
+        lib.plto_spectral_profile_from_samples.restype = i32
+        lib.plto_spectral_profile_from_samples.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), u32, C.c_float, i32, vp]
+        _lib = lib
+    return _lib
+
+
+class _Q(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("hwss", C.c_uint32), ("rng_offset", C.c_uint32), ("frame", C.c_uint32),
+                ("material", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p), ("lobe", C.c_void_p),
+                ("wavelengths", C.c_void_p), ("stokes", C.c_void_p), ("coherence", C.c_void_p), ("beam_t", C.c_void_p)]
+
+
+class _R(C.Structure):
+    _fields_ = [("stokes", C.c_void_p), ("coherence", C.c_void_p), ("beam_t", C.c_void_p), ("pdf", C.c_void_p),
+                ("lambda_pdf", C.c_void_p), ("sample_wo", C.c_void_p), ("sample_pdf", C.c_void_p),
+                ("sample_weight", C.c_void_p), ("sample_lobe", C.c_void_p), ("sample_valid", C.c_void_p)]
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def make_queries(wl, rng_offset=0):
+    q = _Q()
+    q.n, q.hwss, q.rng_offset, q.frame = wl.n, wl.hwss, rng_offset, wl.frame
+    q.material, q.v, q.w, q.lobe = _p(wl.material), _p(wl.v), _p(wl.w), _p(wl.lobe)
+    q.wavelengths, q.stokes, q.coherence, q.beam_t = _p(wl.wavelengths), _p(wl.stokes), _p(wl.coherence), None
+    return q
+
+
+def alloc_results(n, hwss):
+    z = lambda k, dt=np.float32: np.zeros(k * n, dt)
+    return {"stokes": z(4 * hwss), "coherence": z(4), "pdf": z(1), "lambda_pdf": z(hwss), "sample_wo": z(3),
+            "sample_pdf": z(1), "sample_weight": z(1), "sample_lobe": z(1, np.uint32), "sample_valid": z(1, np.uint32)}
+
+
+def results_struct(res):
+    r = _R()
+    for k in res:
+        setattr(r, k, _p(res[k]))
+    return r
+
+
+def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, end=None, res=None):
+    """Runs the oracle over queries [begin, end) of workload `wl`; returns the results dict."""
+    lib = load()
+    ops = wl.ops if ops is None else ops
+    end = wl.n if end is None else end
+    q = make_queries(wl)
+    res = alloc_results(wl.n, wl.hwss) if res is None else res
+    r = results_struct(res)
+    recs = np.ascontiguousarray(wl.records)
+    prof = wl.profiles
+    st = lib.plto_bsdf_batch_range(precision, int(fp64_multilayer), C.c_void_p(recs.ctypes.data), len(recs),
+                                   C.cast(prof, C.c_void_p) if prof is not None else None, len(prof) if prof is not None else 0,
+                                   C.byref(q), C.byref(r), ops, threads, begin, end)
+    if st != 0:
+        raise RuntimeError("oracle batch failed with status %d" % st)
+    return res
+
+
+def count_ops(wl, ops=None):
+    """Mean (fp, sfu, div, count) per material type of the op-counting build."""
+    lib = load()
+    ops = wl.ops if ops is None else ops
+    q = make_queries(wl)
+    out = (C.c_double * (12 * 4))()
+    recs = np.ascontiguousarray(wl.records)
+    prof = wl.profiles
+    st = lib.plto_count_ops(C.c_void_p(recs.ctypes.data), len(recs), C.cast(prof, C.c_void_p) if prof is not None else None,
+                            len(prof) if prof is not None else 0, C.byref(q), ops, out)
+    if st != 0:
+        raise RuntimeError("oracle count failed with status %d" % st)
+    a = np.frombuffer(out, dtype=np.float64).reshape(12, 4)
+    return {t: {"fp": a[t, 0], "sfu": a[t, 1], "div": a[t, 2], "count": int(a[t, 3])} for t in range(12) if a[t, 3] > 0}
+
+
+def rng_stream(px, py, frame, count):
+    out = (C.c_uint32 * count)()
+    load().plto_rng_stream(px, py, frame, count, out)
+    return np.frombuffer(out, dtype=np.uint32).copy()

@@ -1,0 +1,152 @@
+"""Python mirror of the batched IMaterialInstance interface over libplt_gb300.so.
+
+`PLTContext` owns one C-ABI context (plt_create / plt_destroy).  Queries and results are CUDA
+tensors (torch is only the device-memory and stream plumbing); every call goes through the C ABI
+and raises PLTError on a non-OK status.  Method names follow the reference interface:
+eval / sample / pdf / lambdaPdf (Source/Falcor/Rendering/Materials/IMaterialInstance.slang:122-184
+in ssteinberg/PLTFalcor).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class DeviceBatch:
+    """A query batch resident on the GPU, with result buffers for the requested ops."""
+
+    def __init__(self, workload, device="cuda", pin=False, results=True):
+        import torch
+        self.workload = workload
+        self.n, self.hwss = workload.n, workload.hwss
+        d = torch.device(device)
+
+        def up(a, dt):
+            if a is None:
+                return None
+            t = torch.from_numpy(a)
+            if dt is not None:
+                t = t.view(dt)
+            return t.to(d, non_blocking=pin)
+        self.material = up(workload.material.view(np.int32), None)
+        self.v = up(workload.v, None)
+        self.w = up(workload.w, None)
+        self.lobe = up(None if workload.lobe is None else workload.lobe.view(np.int32), None)
+        self.wavelengths = up(workload.wavelengths, None)
+        self.stokes = up(workload.stokes, None)
+        self.coherence = up(workload.coherence, None)
+        self.beam_t = None
+        if results:
+            self.alloc_results(d)
+
+    def alloc_results(self, d):
+        import torch
+        n, h = self.n, self.hwss
+        f = lambda k: torch.zeros(k * n, dtype=torch.float32, device=d)
+        self.out_stokes = f(4 * h)
+        self.out_coherence = f(4)
+        self.out_beam_t = None
+        self.out_pdf = f(1)
+        self.out_lambda_pdf = f(h)
+        self.out_sample_wo = f(3)
+        self.out_sample_pdf = f(1)
+        self.out_sample_weight = f(1)
+        self.out_sample_lobe = torch.zeros(n, dtype=torch.int32, device=d)
+        self.out_sample_valid = torch.zeros(n, dtype=torch.int32, device=d)
+
+    def queries(self, rng_offset=0, frame=None, n=None, offset=0):
+        """C struct for queries [offset, offset+n) -- a view into the resident planes is not
+        possible for SoA planes, so sub-ranges are only supported at offset 0 via n."""
+        q = capi.BsdfQueries()
+        q.n = self.n if n is None else n
+        q.hwss = self.hwss
+        q.rng_offset = rng_offset
+        q.frame = self.workload.frame if frame is None else frame
+        q.material, q.v, q.w = _ptr(self.material), _ptr(self.v), _ptr(self.w)
+        q.lobe = _ptr(self.lobe)
+        q.wavelengths, q.stokes, q.coherence = _ptr(self.wavelengths), _ptr(self.stokes), _ptr(self.coherence)
+        q.beam_t = _ptr(self.beam_t)
+        return q
+
+    def results(self, ops):
+        r = capi.BsdfResults()
+        if ops & capi.OP_EVAL:
+            r.stokes, r.coherence, r.beam_t = _ptr(self.out_stokes), _ptr(self.out_coherence), _ptr(self.out_beam_t)
+        if ops & capi.OP_PDF:
+            r.pdf = _ptr(self.out_pdf)
+        if ops & capi.OP_LAMBDA_PDF:
+            r.lambda_pdf = _ptr(self.out_lambda_pdf)
+        if ops & capi.OP_SAMPLE:
+            r.sample_wo, r.sample_pdf = _ptr(self.out_sample_wo), _ptr(self.out_sample_pdf)
+            r.sample_weight, r.sample_lobe = _ptr(self.out_sample_weight), _ptr(self.out_sample_lobe)
+            r.sample_valid = _ptr(self.out_sample_valid)
+        return r
+
+    def fetch(self):
+        """Results as host numpy arrays (same keys as the oracle's results)."""
+        g = lambda t: t.cpu().numpy()
+        return {"stokes": g(self.out_stokes), "coherence": g(self.out_coherence), "pdf": g(self.out_pdf),
+                "lambda_pdf": g(self.out_lambda_pdf), "sample_wo": g(self.out_sample_wo),
+                "sample_pdf": g(self.out_sample_pdf), "sample_weight": g(self.out_sample_weight),
+                "sample_lobe": g(self.out_sample_lobe).view(np.uint32), "sample_valid": g(self.out_sample_valid).view(np.uint32)}
+
+
+class PLTContext:
+    """One context on the current CUDA device: material table, spectral tables, batched BSDF ops."""
+
+    def __init__(self, options=None, fp64_multilayer=False):
+        self.lib = capi.load_library()
+        opts = capi.Options()
+        self.lib.plt_options_default(C.byref(opts))
+        if options:
+            for k, val in options.items():
+                setattr(opts, k, val)
+        if fp64_multilayer:
+            opts.flags |= capi.OPTION_FP64_MULTILAYER
+        h = C.c_void_p()
+        capi.check(self.lib.plt_create(C.byref(opts), C.byref(h)), "plt_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.plt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_spectral_profiles(self, profiles):
+        capi.check(self.lib.plt_set_spectral_profiles(self.handle, profiles, len(profiles)), "plt_set_spectral_profiles")
+
+    def set_materials(self, records):
+        recs = np.ascontiguousarray(records)
+        capi.check(self.lib.plt_set_materials(self.handle, recs.ctypes.data_as(C.POINTER(capi.MaterialRecord)), len(recs)),
+                   "plt_set_materials")
+
+    def batch(self, queries, results, ops, stream=None):
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_bsdf_batch(self.handle, C.byref(queries), C.byref(results), ops, s), "plt_bsdf_batch")
+
+    def eval(self, q, r, stream=None):
+        self.batch(q, r, capi.OP_EVAL, stream)
+
+    def pdf(self, q, r, stream=None):
+        self.batch(q, r, capi.OP_PDF, stream)
+
+    def sample(self, q, r, stream=None):
+        self.batch(q, r, capi.OP_SAMPLE, stream)
+
+    def lambdaPdf(self, q, r, stream=None):
+        self.batch(q, r, capi.OP_LAMBDA_PDF, stream)
+
+    def check_status(self, stream=None):
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        return self.lib.plt_check_status(self.handle, s)

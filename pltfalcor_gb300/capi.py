@@ -1,0 +1,120 @@
+"""ctypes mirror of include/plt_gb300.h and the loader of libplt_gb300.so.
+
+The library is built in-tree (pltfalcor_gb300/_build/libplt_gb300.so) by pltfalcor_gb300.build;
+loading fails loudly when it is missing: there is no CPU fallback for the GPU path.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libplt_gb300.so")
+
+PLT_OK, PLT_INVALID_ARG, PLT_OOM, PLT_QUEUE_TIMEOUT, PLT_NAN_INPUT, PLT_CUDA_ERROR, PLT_NOT_SUPPORTED, PLT_BAD_MATERIAL = range(8)
+STATUS_NAMES = {0: "PLT_OK", 1: "PLT_INVALID_ARG", 2: "PLT_OOM", 3: "PLT_QUEUE_TIMEOUT", 4: "PLT_NAN_INPUT",
+                5: "PLT_CUDA_ERROR", 6: "PLT_NOT_SUPPORTED", 7: "PLT_BAD_MATERIAL"}
+
+OP_EVAL, OP_PDF, OP_SAMPLE, OP_LAMBDA_PDF = 0x1, 0x2, 0x4, 0x8
+OP_ALL = 0xF
+MAX_HWSS = 8
+NO_SPECTRAL_PROFILE = 0xFFFFFFFF
+OPTION_FP64_MULTILAYER = 0x1
+
+
+class SpectralProfile(C.Structure):
+    _fields_ = [("rgb", C.c_float * 3), ("intensity", C.c_float), ("bins", C.c_uint32),
+                ("min_wavelength", C.c_float), ("max_wavelength", C.c_float),
+                ("pdf", C.c_float * 128), ("icdf", C.c_float * 128)]
+
+
+class MaterialRecord(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("flags", C.c_uint32),
+                ("base_color", C.c_uint16 * 4), ("specular", C.c_uint16 * 4),
+                ("data1", C.c_uint16 * 4), ("data2", C.c_uint16 * 4),
+                ("specular_transmission", C.c_uint16), ("transmission", C.c_uint16 * 3),
+                ("diffuse_transmission", C.c_uint16), ("volume_scattering", C.c_uint16 * 3),
+                ("ior", C.c_uint16), ("volume_absorption", C.c_uint16 * 3), ("volume_anisotropy", C.c_uint16),
+                ("pad0", C.c_uint16), ("emission_spectral_id", C.c_uint32), ("ior_n_spectral_id", C.c_uint32),
+                ("ior_k_spectral_id", C.c_uint32)]
+
+
+class BsdfQueries(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("hwss", C.c_uint32), ("rng_offset", C.c_uint32), ("frame", C.c_uint32),
+                ("material", C.c_void_p), ("v", C.c_void_p), ("w", C.c_void_p), ("lobe", C.c_void_p),
+                ("wavelengths", C.c_void_p), ("stokes", C.c_void_p), ("coherence", C.c_void_p), ("beam_t", C.c_void_p)]
+
+
+class BsdfResults(C.Structure):
+    _fields_ = [("stokes", C.c_void_p), ("coherence", C.c_void_p), ("beam_t", C.c_void_p), ("pdf", C.c_void_p),
+                ("lambda_pdf", C.c_void_p), ("sample_wo", C.c_void_p), ("sample_pdf", C.c_void_p),
+                ("sample_weight", C.c_void_p), ("sample_lobe", C.c_void_p), ("sample_valid", C.c_void_p)]
+
+
+class Options(C.Structure):
+    _fields_ = [("max_bounces", C.c_uint32), ("tile_size", C.c_uint32), ("hwss", C.c_uint32),
+                ("hwss_do_mis", C.c_uint32), ("sourcing_area_from_emissive_geometry", C.c_float),
+                ("sourcing_max_beam_omega", C.c_float), ("use_direct_light", C.c_uint32),
+                ("use_env_light", C.c_uint32), ("use_emissive_lights", C.c_uint32),
+                ("use_analytic_lights", C.c_uint32), ("do_nee", C.c_uint32), ("do_mis", C.c_uint32),
+                ("do_russian_roulette", C.c_uint32), ("nee_use_per_tile_sg", C.c_uint32),
+                ("do_importance_sample_emitters", C.c_uint32), ("do_mnee", C.c_uint32),
+                ("mnee_max_occluders", C.c_uint32), ("mnee_max_iterations", C.c_uint32),
+                ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32)]
+
+
+assert C.sizeof(SpectralProfile) == 1052
+assert C.sizeof(MaterialRecord) == 80
+
+# every symbol include/plt_gb300.h declares
+EXPORTED_SYMBOLS = [
+    "plt_abi_version", "plt_status_string", "plt_options_default", "plt_create", "plt_destroy",
+    "plt_last_cuda_error", "plt_set_spectral_profiles", "plt_set_materials", "plt_spectral_profile_from_samples",
+    "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
+]
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads libplt_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libplt_gb300.so is not built (%s); run __graft_entry__.build()" % path)
+    lib = C.CDLL(path)
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+    sig = {
+        "plt_abi_version": (u32, []),
+        "plt_status_string": (C.c_char_p, [i32]),
+        "plt_options_default": (i32, [C.POINTER(Options)]),
+        "plt_create": (i32, [C.POINTER(Options), C.POINTER(vp)]),
+        "plt_destroy": (i32, [vp]),
+        "plt_last_cuda_error": (i32, [vp]),
+        "plt_set_spectral_profiles": (i32, [vp, C.POINTER(SpectralProfile), u32]),
+        "plt_set_materials": (i32, [vp, C.POINTER(MaterialRecord), u32]),
+        "plt_spectral_profile_from_samples": (i32, [C.POINTER(C.c_float), C.POINTER(C.c_float), u32, C.c_float, i32,
+                                                    C.POINTER(SpectralProfile)]),
+        "plt_bsdf_batch": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
+        "plt_check_status": (i32, [vp, vp]),
+        "plt_bsdf_eval": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
+        "plt_bsdf_pdf": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
+        "plt_bsdf_sample": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
+        "plt_bsdf_lambda_pdf": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PLTError(RuntimeError):
+    def __init__(self, status, where):
+        super().__init__("%s failed: %s" % (where, STATUS_NAMES.get(status, status)))
+        self.status = status
+
+
+def check(status, where):
+    if status != PLT_OK:
+        raise PLTError(status, where)

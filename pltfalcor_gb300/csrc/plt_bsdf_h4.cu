@@ -1,0 +1,6 @@
+// Instantiation of the fused BSDF batch kernel for 4 hero wavelength(s) per beam.
+#include "plt_bsdf_kernel.cuh"
+
+namespace plt {
+template cudaError_t launchBsdfBatchH<4>(const BatchParams&, int, cudaStream_t);
+}  // namespace plt

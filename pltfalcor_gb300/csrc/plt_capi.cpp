@@ -1,0 +1,226 @@
+// C ABI of libplt_gb300.so (declared in include/plt_gb300.h): context, material and spectral
+// tables, batched BSDF launches, status.  No exception crosses the ABI.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "plt_host.h"
+#include "plt_internal.h"
+
+struct plt_context {
+    int device = 0;
+    int numSMs = 0;
+    plt_options opt{};
+    pltdev::DevMaterial* dMats = nullptr;
+    uint8_t* dMatType = nullptr;
+    uint32_t nMats = 0, capMats = 0;
+    pltdev::DevProfile* dProfiles = nullptr;
+    uint32_t nProfiles = 0, capProfiles = 0;
+    uint32_t* dStatus = nullptr;
+    int lastCudaError = 0;
+};
+
+namespace {
+
+plt_status cudaFail(plt_context* ctx, cudaError_t e) {
+    if (ctx) ctx->lastCudaError = (int)e;
+    return e == cudaErrorMemoryAllocation ? PLT_OOM : PLT_CUDA_ERROR;
+}
+#define PLT_CUDA(ctx, call)                               \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cudaFail(ctx, e_);  \
+    } while (0)
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+uint32_t plt_abi_version(void) { return PLT_ABI_VERSION; }
+
+const char* plt_status_string(plt_status s) {
+    switch (s) {
+    case PLT_OK: return "ok";
+    case PLT_INVALID_ARG: return "invalid argument";
+    case PLT_OOM: return "out of device memory";
+    case PLT_QUEUE_TIMEOUT: return "queue wait timed out";
+    case PLT_NAN_INPUT: return "non-finite input";
+    case PLT_CUDA_ERROR: return "CUDA error";
+    case PLT_NOT_SUPPORTED: return "not supported";
+    case PLT_BAD_MATERIAL: return "bad material";
+    }
+    return "unknown status";
+}
+
+plt_status plt_options_default(plt_options* o) {
+    if (!o) return PLT_INVALID_ARG;
+    std::memset(o, 0, sizeof(*o));
+    o->max_bounces = 32;
+    o->tile_size = 512;
+    o->hwss = 4;
+    o->hwss_do_mis = 1;
+    o->sourcing_area_from_emissive_geometry = 1.f;
+    o->sourcing_max_beam_omega = .025f;
+    o->use_direct_light = 1;
+    o->use_env_light = 1;
+    o->use_emissive_lights = 1;
+    o->use_analytic_lights = 1;
+    o->do_nee = 1;
+    o->do_mis = 1;
+    o->do_russian_roulette = 1;
+    o->nee_use_per_tile_sg = 0;
+    o->do_importance_sample_emitters = 1;
+    o->do_mnee = 1;
+    o->mnee_max_occluders = 2;
+    o->mnee_max_iterations = 60;
+    o->mnee_solver_threshold = 5e-5f;
+    o->flags = 0;
+    return PLT_OK;
+}
+
+plt_status plt_create(const plt_options* options, plt_context** out) {
+    if (!out) return PLT_INVALID_ARG;
+    *out = nullptr;
+    plt_context* ctx = new (std::nothrow) plt_context();
+    if (!ctx) return PLT_OOM;
+    if (options) ctx->opt = *options;
+    else plt_options_default(&ctx->opt);
+    if (ctx->opt.hwss < 1 || ctx->opt.hwss > PLT_MAX_HWSS) { delete ctx; return PLT_INVALID_ARG; }
+    cudaError_t e = cudaGetDevice(&ctx->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dStatus, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        const plt_status s = e == cudaErrorMemoryAllocation ? PLT_OOM : PLT_CUDA_ERROR;
+        if (ctx->dStatus) cudaFree(ctx->dStatus);
+        delete ctx;
+        return s;
+    }
+    *out = ctx;
+    return PLT_OK;
+}
+
+plt_status plt_destroy(plt_context* ctx) {
+    if (!ctx) return PLT_INVALID_ARG;
+    cudaFree(ctx->dMats);
+    cudaFree(ctx->dMatType);
+    cudaFree(ctx->dProfiles);
+    cudaFree(ctx->dStatus);
+    delete ctx;
+    return PLT_OK;
+}
+
+int plt_last_cuda_error(const plt_context* ctx) { return ctx ? ctx->lastCudaError : 0; }
+
+plt_status plt_set_spectral_profiles(plt_context* ctx, const plt_spectral_profile* profiles, uint32_t count) {
+    if (!ctx || (count > 0 && !profiles)) return PLT_INVALID_ARG;
+    if (count > 64) return PLT_NOT_SUPPORTED;  // staged whole into shared memory by each CTA
+    std::vector<pltdev::DevProfile> h(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const plt_spectral_profile& s = profiles[i];
+        if (s.bins > PLT_SPECTRAL_MAX_BINS) return PLT_INVALID_ARG;
+        std::memset(&h[i], 0, sizeof(h[i]));
+        h[i].intensity = s.intensity;
+        h[i].minl = s.min_wavelength;
+        h[i].maxl = s.max_wavelength;
+        h[i].bins = s.bins;
+        std::memcpy(h[i].pdf, s.pdf, sizeof(h[i].pdf));
+    }
+    if (count > ctx->capProfiles) {
+        cudaFree(ctx->dProfiles);
+        ctx->dProfiles = nullptr;
+        ctx->capProfiles = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dProfiles, sizeof(pltdev::DevProfile) * count));
+        ctx->capProfiles = count;
+    }
+    if (count) PLT_CUDA(ctx, cudaMemcpy(ctx->dProfiles, h.data(), sizeof(pltdev::DevProfile) * count, cudaMemcpyHostToDevice));
+    ctx->nProfiles = count;
+    return PLT_OK;
+}
+
+plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, uint32_t count) {
+    if (!ctx || (count > 0 && !mats)) return PLT_INVALID_ARG;
+    std::vector<pltdev::DevMaterial> h(count);
+    std::vector<uint8_t> types(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const plt_status s = plt::decodeMaterial(mats[i], ctx->nProfiles, h[i]);
+        if (s != PLT_OK) return s;
+        types[i] = (uint8_t)mats[i].type;
+    }
+    if (count > ctx->capMats) {
+        cudaFree(ctx->dMats);
+        cudaFree(ctx->dMatType);
+        ctx->dMats = nullptr;
+        ctx->dMatType = nullptr;
+        ctx->capMats = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dMats, sizeof(pltdev::DevMaterial) * count));
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dMatType, count));
+        ctx->capMats = count;
+    }
+    if (count) {
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dMats, h.data(), sizeof(pltdev::DevMaterial) * count, cudaMemcpyHostToDevice));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dMatType, types.data(), count, cudaMemcpyHostToDevice));
+    }
+    ctx->nMats = count;
+    return PLT_OK;
+}
+
+plt_status plt_spectral_profile_from_samples(const float* wl, const float* values, uint32_t count, float scale, int compute_icdf,
+                                             plt_spectral_profile* out) {
+    return plt::spectralProfileFromSamples(wl, values, count, scale, compute_icdf, out);
+}
+
+plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops, void* stream) {
+    if (!ctx || !q || !r) return PLT_INVALID_ARG;
+    if (q->hwss < 1 || q->hwss > PLT_MAX_HWSS || (q->hwss > 4 && q->hwss != 8)) return q->hwss >= 1 && q->hwss <= PLT_MAX_HWSS ? PLT_NOT_SUPPORTED : PLT_INVALID_ARG;
+    if (ops == 0 || (ops & ~0xFu)) return PLT_INVALID_ARG;
+    if (q->n == 0) return PLT_OK;
+    if (!q->material || !q->v || !q->w || !q->wavelengths || !q->stokes || !q->coherence) return PLT_INVALID_ARG;
+    if (ctx->nMats == 0) return PLT_INVALID_ARG;
+    const void* ins[] = {q->material, q->v, q->w, q->lobe, q->wavelengths, q->stokes, q->coherence, q->beam_t};
+    for (const void* p : ins)
+        if (p && !aligned16(p)) return PLT_INVALID_ARG;
+    const void* outs[] = {r->stokes, r->coherence, r->beam_t, r->pdf, r->lambda_pdf, r->sample_wo, r->sample_pdf, r->sample_weight, r->sample_lobe, r->sample_valid};
+    for (const void* p : outs)
+        if (p && !aligned16(p)) return PLT_INVALID_ARG;
+    plt::BatchParams p{};
+    p.q = *q;
+    p.r = *r;
+    p.ops = ops;
+    p.mats = ctx->dMats;
+    p.matType = ctx->dMatType;
+    p.nMats = ctx->nMats;
+    p.profiles = ctx->dProfiles;
+    p.nProfiles = ctx->nProfiles;
+    p.flags = ctx->opt.flags;
+    p.status = ctx->dStatus;
+    const cudaError_t e = plt::launchBsdfBatch(p, (int)q->hwss, ctx->numSMs, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cudaFail(ctx, e);
+    return PLT_OK;
+}
+
+plt_status plt_bsdf_eval(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_EVAL, s); }
+plt_status plt_bsdf_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_PDF, s); }
+plt_status plt_bsdf_sample(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_SAMPLE, s); }
+plt_status plt_bsdf_lambda_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_LAMBDA_PDF, s); }
+
+// Synchronises the stream and converts the device status word of the context (accumulated by
+// every launch since the last check) into a status, then clears it.
+plt_status plt_check_status(plt_context* ctx, void* stream) {
+    if (!ctx) return PLT_INVALID_ARG;
+    uint32_t st = 0;
+    PLT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    PLT_CUDA(ctx, cudaMemcpy(&st, ctx->dStatus, sizeof(st), cudaMemcpyDeviceToHost));
+    PLT_CUDA(ctx, cudaMemset(ctx->dStatus, 0, sizeof(st)));
+    if (st & plt::kStatusCopyTimeout) return PLT_QUEUE_TIMEOUT;
+    if (st & (plt::kStatusBadMaterialId | plt::kStatusUnknownType)) return PLT_BAD_MATERIAL;
+    if (st & plt::kStatusNanInput) return PLT_NAN_INPUT;
+    return PLT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Internal interface between the C-ABI host code and the CUDA kernels of libplt_gb300.so.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/plt_gb300.h"
+
+namespace pltdev {
+struct DevMaterial;
+struct DevProfile;
+}  // namespace pltdev
+
+namespace plt {
+
+// device status word bits (read back by plt_check_status)
+constexpr uint32_t kStatusBadMaterialId = 0x1u;
+constexpr uint32_t kStatusNanInput = 0x2u;
+constexpr uint32_t kStatusUnknownType = 0x4u;
+constexpr uint32_t kStatusCopyTimeout = 0x8u;
+
+struct BatchParams {
+    plt_bsdf_queries q;
+    plt_bsdf_results r;
+    uint32_t ops;
+    const pltdev::DevMaterial* mats;
+    const uint8_t* matType;
+    uint32_t nMats;
+    const pltdev::DevProfile* profiles;
+    uint32_t nProfiles;
+    uint32_t flags;
+    uint32_t* status;
+};
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchItems = 8;
+constexpr int kBatchTile = kBatchThreads * kBatchItems;
+
+// Launches the fused BSDF batch kernel (templated on the hero-wavelength count).
+cudaError_t launchBsdfBatch(const BatchParams& p, int hwss, int numSMs, cudaStream_t stream);
+
+}  // namespace plt

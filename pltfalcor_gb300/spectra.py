@@ -1,0 +1,50 @@
+"""Spectral tables: the conductor IORs (Au, Ag, Cu, Al) and the D65 emitter of the workloads.
+
+The raw piecewise-linear samples live in data/spectral_tables.json (extracted from the reference's
+Source/Tables by data/make_spectral_tables.py).  Profiles are built by the library's
+plt_spectral_profile_from_samples, the restatement of SceneBuilder::addSpectralProfileFromMaterial
+(IOR tables, no inverse CDF) and addSpectralProfileForEmitterType (emitters, with inverse CDF),
+Source/Falcor/Scene/SceneBuilder.cpp:962-999.
+"""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+from . import capi
+
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "spectral_tables.json")
+METALS = ["Au", "Ag", "Cu", "Al"]
+
+
+def load_tables():
+    with open(DATA) as f:
+        return json.load(f)
+
+
+def profile_from_samples(wavelengths, values, scale=1.0, compute_icdf=False, lib=None):
+    lib = lib or capi.load_library()
+    wl = np.ascontiguousarray(wavelengths, dtype=np.float32)
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    out = capi.SpectralProfile()
+    st = lib.plt_spectral_profile_from_samples(wl.ctypes.data_as(C.POINTER(C.c_float)), v.ctypes.data_as(C.POINTER(C.c_float)),
+                                               len(wl), float(scale), int(compute_icdf), C.byref(out))
+    capi.check(st, "plt_spectral_profile_from_samples")
+    return out
+
+
+def standard_profiles(lib=None):
+    """Profiles in a fixed order: Au.eta, Au.k, Ag.eta, Ag.k, Cu.eta, Cu.k, Al.eta, Al.k, D65.
+    Returns (ctypes array of SpectralProfile, {name: index})."""
+    t = load_tables()
+    names = [m + s for m in METALS for s in (".eta", ".k")] + ["D65"]
+    arr = (capi.SpectralProfile * len(names))()
+    for i, nm in enumerate(names):
+        arr[i] = profile_from_samples(t[nm]["wavelength_nm"], t[nm]["value"], 1.0, nm == "D65", lib)
+    return arr, {nm: i for i, nm in enumerate(names)}
+
+
+def metal_ids(metal_index):
+    """(n, k) profile ids of METALS[metal_index] in standard_profiles()."""
+    return 2 * metal_index, 2 * metal_index + 1
