@@ -1,0 +1,298 @@
+"""Benchmark of the PLT BSDF hot path on GB300.
+
+Workload: the mixed-material batch -- 2^22 eval + sample + pdf queries split equally over the eight
+PLT material types (dielectric, conductor, coated opaque dielectric, coated conductor, grated
+opaque dielectric, grated conductor, birefringent thin dielectric, multilayer stack) in shuffled
+order, HWSS 1, seed 1 (pltfalcor_gb300/workloads.py).  A step is one fused plt_bsdf_batch launch
+over the whole batch.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: queries/s with inputs resident in HBM (CUDA events on the launching stream; inputs and
+outputs together exceed L2, so no flush is needed).  e2e: the same metric through the C ABI with
+host (pinned) buffers -- every step copies the inputs host->device and all outputs device->host.
+The reference arm (--impl reference) times the CPU restatement of the reference's BSDF code (the
+reference's own path is Slang shader code with no CPU build) on all host threads.
+Under torchrun each rank processes its own batch (weak scaling); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 1 << 22
+METRIC = "PLT BSDF queries/s (eval+sample+pdf, 8 PLT materials)"
+WORKLOAD = ("mixed_material_batch: 2^22 eval+sample+pdf queries over 8 PLT material types (2^19 each, shuffled), "
+            "HWSS 1, 32768 random materials, seed 1")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for nm, v in zip(names, r[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(n_sample=1 << 18, seconds=10.0, threads=None):
+    """The oracle (CPU restatement of the reference BSDF code, FP32, OpenMP) on a bounded sample of
+    the same workload: repeated 2^18-query slices until `seconds` have elapsed."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pltfalcor_gb300 import spectra
+    from pltfalcor_gb300 import workloads as W
+    threads = threads or os.cpu_count()
+    prof, _ = spectra.standard_profiles()
+    wl = W.mixed_material_batch(n=n_sample, profiles=prof)
+    oracle.run(wl, threads=threads)  # warm-up
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        oracle.run(wl, threads=threads)
+        done += wl.n
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": "%d queries (%d-query slices of the mixed-material batch, seed 1) in %.1f s, FP32 oracle, OpenMP" % (done, n_sample, dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from pltfalcor_gb300 import spectra
+    from pltfalcor_gb300 import workloads as W
+    threads = os.cpu_count()
+    prof, _ = spectra.standard_profiles()
+    n_step = 1 << 16
+    wl = W.mixed_material_batch(n=n_step, profiles=prof)
+    for _ in range(args.warmup):
+        oracle.run(wl, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.run(wl, threads=threads)
+    dt = time.perf_counter() - t0
+    v = n_step * args.steps / dt
+    line = {"metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": "%d-query slice per step (bounded CPU sample)" % n_step},
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": "%d x %d queries of the mixed-material batch, FP32 oracle restating the reference Slang BSDFs "
+                                       "(the reference path is shader code with no CPU build)" % (args.steps, n_step)},
+            "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from pltfalcor_gb300 import capi, spectra
+    from pltfalcor_gb300 import workloads as W
+    from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext, _ptr
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+
+    prof, _ = spectra.standard_profiles()
+    wl = W.mixed_material_batch(n=args.n, seed=1 + rank, profiles=prof)
+    ctx = PLTContext()
+    ctx.set_spectral_profiles(prof)
+    ctx.set_materials(wl.records)
+    b = DeviceBatch(wl, device=dev)
+    ops = capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF
+    q, r = b.queries(), b.results(ops)
+
+    sampler = ClockSampler(local if "CUDA_VISIBLE_DEVICES" not in os.environ else 0)
+    sampler.start()
+    for _ in range(args.warmup):
+        ctx.batch(q, r, ops, stream)
+    st = ctx.check_status(stream)
+    if st != capi.PLT_OK:
+        raise RuntimeError("device status %s" % capi.STATUS_NAMES[st])
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.batch(q, r, ops, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = args.n * world * args.steps / (ms_max * 1e-3)
+
+    # end to end through the C ABI with host buffers: H2D inputs, launch, D2H outputs per step
+    pin = lambda a: torch.from_numpy(a).pin_memory()
+    h_in = [pin(wl.material.view("int32")), pin(wl.v), pin(wl.w), pin(wl.lobe.view("int32")), pin(wl.wavelengths),
+            pin(wl.stokes), pin(wl.coherence)]
+    d_in = [b.material, b.v, b.w, b.lobe, b.wavelengths, b.stokes, b.coherence]
+    d_out = [b.out_stokes, b.out_coherence, b.out_pdf, b.out_sample_wo, b.out_sample_pdf, b.out_sample_weight,
+             b.out_sample_lobe, b.out_sample_valid]
+    h_out = [torch.empty(t_.shape, dtype=t_.dtype).pin_memory() for t_ in d_out]
+    h2d = sum(x.numel() * x.element_size() for x in h_in)
+    d2h = sum(x.numel() * x.element_size() for x in d_out)
+
+    def e2e_step():
+        for h, d in zip(h_in, d_in):
+            d.copy_(h, non_blocking=True)
+        ctx.batch(q, r, ops, stream)
+        for h, d in zip(h_out, d_out):
+            h.copy_(d, non_blocking=True)
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = f0.elapsed_time(f1)
+    t = torch.tensor([ms_e2e], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = args.n * world * args.steps / (float(t.item()) * 1e-3)
+    clocks = sampler.stop()
+    st = ctx.check_status(stream)
+    if st != capi.PLT_OK:
+        raise RuntimeError("device status %s" % capi.STATUS_NAMES[st])
+
+    if rank == 0:
+        pk, pk_kind = peaks()
+        launch_s = ms_max * 1e-3 / args.steps
+        bytes_per_launch = h2d + d2h
+        achieved = bytes_per_launch / launch_s / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                "kernel": "pltdev::bsdfBatchKernel<1>", "algorithmic_bytes_per_launch": bytes_per_launch,
+                "algorithmic_bytes_per_query": bytes_per_launch / args.n}
+        prof_path = os.path.join(ROOT, "profiles", "bsdf_batch_mixed_material_4M.json")
+        if os.path.exists(prof_path):
+            with open(prof_path) as f:
+                pj = json.load(f)
+            if pj.get("dram_bytes_per_launch"):
+                roof["traffic"] = pj["dram_bytes_per_launch"] * args.n / pj.get("queries_per_launch", args.n)
+        ops_path = os.path.join(ROOT, "profiles", "op_counts_mixed_material.json")
+        if os.path.exists(ops_path):
+            with open(ops_path) as f:
+                oc = json.load(f)
+            mhz = (clocks or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12          # FMA lanes x 2 flops, nominal at the sampled clock
+            sfu_peak = sms * 16 * mhz * 1e6 / 1e12                 # MUFU ops per clock per SM
+            fp_q, sfu_q = oc["mean_fp_per_query"], oc["mean_sfu_per_query"]
+            qps = args.n / launch_s
+            roof["compute"] = {"fp32_tflops": fp_q * qps / 1e12, "fp32_peak_tflops_nominal": fp32_peak,
+                               "fp32_frac": fp_q * qps / 1e12 / fp32_peak, "sfu_tops": sfu_q * qps / 1e12,
+                               "sfu_peak_tops_nominal": sfu_peak, "sfu_frac": sfu_q * qps / 1e12 / sfu_peak,
+                               "fp_ops_per_query": fp_q, "sfu_ops_per_query": sfu_q, "div_per_query": oc.get("mean_div_per_query")}
+        line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "queries_per_gpu": args.n, "hwss": 1, "materials": int(len(wl.records)),
+                           "l2": "inputs %d MB + outputs %d MB per step exceed the 126 MB L2; no flush" % (h2d >> 20, d2h >> 20),
+                           "parallelism": "independent shards per GPU" if world > 1 else "1 GPU"},
+                "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": args.steps, "roofline": roof, "clocks": clocks}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,11 +59,10 @@ class DeviceBatch:
         self.out_sample_lobe = torch.zeros(n, dtype=torch.int32, device=d)
         self.out_sample_valid = torch.zeros(n, dtype=torch.int32, device=d)
 
-    def queries(self, rng_offset=0, frame=None, n=None, offset=0):
-        """C struct for queries [offset, offset+n) -- a view into the resident planes is not
-        possible for SoA planes, so sub-ranges are only supported at offset 0 via n."""
+    def queries(self, rng_offset=0, frame=None):
+        """plt_bsdf_queries over the resident planes (plane stride = n)."""
         q = capi.BsdfQueries()
-        q.n = self.n if n is None else n
+        q.n = self.n
         q.hwss = self.hwss
         q.rng_offset = rng_offset
         q.frame = self.workload.frame if frame is None else frame
