@@ -36,6 +36,8 @@ def load():
         lib.plto_bsdf_batch.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32]
         lib.plto_bsdf_batch_range.restype = i32
         lib.plto_bsdf_batch_range.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32, C.c_uint64, C.c_uint64]
+        lib.plto_set_sr_seed.restype = None
+        lib.plto_set_sr_seed.argtypes = [C.c_uint64]
         lib.plto_count_ops.restype = i32
         lib.plto_count_ops.argtypes = [vp, u32, vp, u32, vp, u32, C.POINTER(C.c_double)]
         lib.plto_rng_stream.restype = None
@@ -95,9 +97,12 @@ def results_struct(res):
     return r
 
 
-def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, end=None, res=None):
-    """Runs the oracle over queries [begin, end) of workload `wl`; returns the results dict."""
+def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, end=None, res=None, sr_seed=None):
+    """Runs the oracle over queries [begin, end) of workload `wl`; returns the results dict.
+    precision: 32 (FP32), 64 (FP64) or 16 (FP32 with random rounding, seed `sr_seed`)."""
     lib = load()
+    if precision == 16:
+        lib.plto_set_sr_seed(1 if sr_seed is None else sr_seed)
     ops = wl.ops if ops is None else ops
     end = wl.n if end is None else end
     q = make_queries(wl)

@@ -49,12 +49,57 @@ inline bool operator>=(CF a, CF b) { op_counts().cmp++; return a.v >= b.v; }
 inline bool operator==(CF a, CF b) { op_counts().cmp++; return a.v == b.v; }
 inline bool operator!=(CF a, CF b) { op_counts().cmp++; return a.v != b.v; }
 
+// ---------------------------------------------------------------------------------------------
+// Monte Carlo arithmetic (random rounding): a binary32 type whose every operation computes the
+// result in double and rounds it to one of the two neighbouring floats at random.  The spread of
+// results between runs with different seeds measures how sensitive a query is to FP32 rounding,
+// which bounds how closely two FP32 implementations can agree (tests use it as the conditioning
+// allowance).
+// ---------------------------------------------------------------------------------------------
+inline uint64_t& sr_state() { static thread_local uint64_t s = 0x9E3779B97F4A7C15ull; return s; }
+inline void sr_seed(uint64_t seed, uint64_t index) { sr_state() = (seed * 0x9E3779B97F4A7C15ull) ^ (index * 0xBF58476D1CE4E5B9ull) ^ 0x94D049BB133111EBull; }
+inline float sr_round(double x) {
+    const float f = (float)x;
+    if (!std::isfinite(x) || (double)f == x) return f;
+    uint64_t& s = sr_state();
+    s ^= s << 13; s ^= s >> 7; s ^= s << 17;
+    const float up = (double)f > x ? f : std::nextafter(f, INFINITY);
+    const float down = (double)f < x ? f : std::nextafter(f, -INFINITY);
+    return (s >> 32) & 1u ? up : down;
+}
+struct SR {
+    float v;
+    SR() : v(0) {}
+    SR(double x) : v((float)x) {}
+    explicit operator double() const { return v; }
+    explicit operator float() const { return v; }
+    explicit operator int() const { return (int)v; }
+    explicit operator unsigned() const { return (unsigned)v; }
+};
+inline SR sr(double x) { SR r; r.v = sr_round(x); return r; }
+inline SR operator+(SR a, SR b) { return sr((double)a.v + (double)b.v); }
+inline SR operator-(SR a, SR b) { return sr((double)a.v - (double)b.v); }
+inline SR operator*(SR a, SR b) { return sr((double)a.v * (double)b.v); }
+inline SR operator/(SR a, SR b) { return sr((double)a.v / (double)b.v); }
+inline SR operator-(SR a) { SR r; r.v = -a.v; return r; }
+inline SR& operator+=(SR& a, SR b) { a = a + b; return a; }
+inline SR& operator-=(SR& a, SR b) { a = a - b; return a; }
+inline SR& operator*=(SR& a, SR b) { a = a * b; return a; }
+inline SR& operator/=(SR& a, SR b) { a = a / b; return a; }
+inline bool operator<(SR a, SR b) { return a.v < b.v; }
+inline bool operator>(SR a, SR b) { return a.v > b.v; }
+inline bool operator<=(SR a, SR b) { return a.v <= b.v; }
+inline bool operator>=(SR a, SR b) { return a.v >= b.v; }
+inline bool operator==(SR a, SR b) { return a.v == b.v; }
+inline bool operator!=(SR a, SR b) { return a.v != b.v; }
+
 // Scalar math shims.  For CF each special function counts as one SFU-class op (sqrt, rsqrt,
 // exp, log, sin, cos, pow = exp+log, atan2/acos = polynomial sequences, counted as 4 FP + 1 SFU).
 #define PLT_ORACLE_UNARY(NAME, STD, SFU, FP)                                                    \
     inline float NAME(float x) { return std::STD(x); }                                          \
     inline double NAME(double x) { return std::STD(x); }                                        \
-    inline CF NAME(CF x) { op_counts().sfu += SFU; op_counts().fp += FP; return CF(std::STD(x.v)); }
+    inline CF NAME(CF x) { op_counts().sfu += SFU; op_counts().fp += FP; return CF(std::STD(x.v)); } \
+    inline SR NAME(SR x) { return sr(std::STD((double)x.v)); }
 PLT_ORACLE_UNARY(o_sqrt, sqrt, 1, 0)
 PLT_ORACLE_UNARY(o_exp, exp, 1, 1)
 PLT_ORACLE_UNARY(o_log, log, 1, 1)
@@ -67,6 +112,11 @@ PLT_ORACLE_UNARY(o_ceil, ceil, 0, 1)
 inline float o_abs(float x) { return std::fabs(x); }
 inline double o_abs(double x) { return std::fabs(x); }
 inline CF o_abs(CF x) { return CF(std::fabs(x.v)); }
+inline SR o_abs(SR x) { SR r; r.v = std::fabs(x.v); return r; }
+inline SR o_pow(SR x, SR y) { return sr(std::pow((double)x.v, (double)y.v)); }
+inline SR o_atan2(SR y, SR x) { return sr(std::atan2((double)y.v, (double)x.v)); }
+inline bool o_isfinite(SR x) { return std::isfinite(x.v); }
+inline float o_fval(SR x) { return x.v; }
 inline float o_pow(float x, float y) { return std::pow(x, y); }
 inline double o_pow(double x, double y) { return std::pow(x, y); }
 inline CF o_pow(CF x, CF y) { op_counts().sfu += 2; op_counts().fp += 2; return CF(std::pow(x.v, y.v)); }

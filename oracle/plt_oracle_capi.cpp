@@ -13,6 +13,10 @@ using namespace plt_oracle;
 
 namespace {
 
+uint64_t g_sr_seed = 1;
+template <class R> inline void seedQuery(uint64_t) {}
+template <> inline void seedQuery<SR>(uint64_t i) { sr_seed(g_sr_seed, i); }
+
 template <class R>
 int runBatch(const plt_material_record* mats, uint32_t nm, const plt_spectral_profile* profs, uint32_t np,
              const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops, int threads, int fp64ml,
@@ -29,6 +33,7 @@ int runBatch(const plt_material_record* mats, uint32_t nm, const plt_spectral_pr
 #endif
     for (long long ii = (long long)q_begin; ii < (long long)q_end; ++ii) {
         const uint32_t i = (uint32_t)ii;
+        seedQuery<R>(i);
         const uint32_t mid = q->material[i];
         if (mid >= nm) { bad |= 1; continue; }
         const Material<R> m = decodeMaterial<R>(mats[mid]);
@@ -82,12 +87,17 @@ int runBatch(const plt_material_record* mats, uint32_t nm, const plt_spectral_pr
 
 extern "C" {
 
-// precision: 32 (FP32 reference), 64 (FP64 reference).  Processes queries [begin, end).
+// Seed of the random-rounding (Monte Carlo arithmetic) build, precision code 16.
+void plto_set_sr_seed(uint64_t seed) { g_sr_seed = seed; }
+
+// precision: 32 (FP32 reference), 64 (FP64 reference), 16 (FP32 with random rounding, seeded by
+// plto_set_sr_seed).  Processes queries [begin, end).
 int plto_bsdf_batch_range(int precision, int fp64_multilayer, const plt_material_record* mats, uint32_t nm,
                           const plt_spectral_profile* profs, uint32_t np, const plt_bsdf_queries* q,
                           const plt_bsdf_results* r, uint32_t ops, int threads, uint64_t begin, uint64_t end) {
     if (!mats || !q || !r || end > q->n || begin > end) return PLT_INVALID_ARG;
     if (precision == 64) return runBatch<double>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
+    if (precision == 16) return runBatch<SR>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
     return runBatch<float>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
 }
 int plto_bsdf_batch(int precision, int fp64_multilayer, const plt_material_record* mats, uint32_t nm,

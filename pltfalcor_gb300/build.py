@@ -45,38 +45,43 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False, ptxas_verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, force=False, ptxas_verbose=False, defines=(), build_dir=None):
+    """Compiles the library.  `defines` (e.g. ["PLT_SHADE_MIN_BLOCKS=6"]) and `build_dir` build a
+    tuning variant elsewhere; the default build is pltfalcor_gb300/_build/libplt_gb300.so."""
+    bdir = build_dir or BUILD
+    lib = os.path.join(bdir, "libplt_gb300.so")
+    os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
+    dflags = ["-D" + d for d in defines]
     inc = os.path.join(_cuda_home(), "include")
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "plt_gb300.h"))
     jobs = []
     objs = []
     for s in CU_SOURCES:
-        src, obj = os.path.join(CSRC, s), os.path.join(BUILD, s + ".o")
+        src, obj = os.path.join(CSRC, s), os.path.join(bdir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                   "--expt-relaxed-constexpr", "-c", src, "-o", obj]
+                   "--expt-relaxed-constexpr", *dflags, "-c", src, "-o", obj]
             if ptxas_verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
     for s in CPP_SOURCES:
-        src, obj = os.path.join(CSRC, s), os.path.join(BUILD, s + ".o")
+        src, obj = os.path.join(CSRC, s), os.path.join(bdir, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I", inc,
-                         "-c", src, "-o", obj])
+                         *dflags, "-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
             if o.strip():
                 print(o)
-    if force or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
-    return LIB
+    if force or _stale(lib, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", lib, *objs, "-lcudart"])
+    return lib
 
 
 if __name__ == "__main__":

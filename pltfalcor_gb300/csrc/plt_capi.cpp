@@ -20,6 +20,8 @@ struct plt_context {
     pltdev::DevProfile* dProfiles = nullptr;
     uint32_t nProfiles = 0, capProfiles = 0;
     uint32_t* dStatus = nullptr;
+    void* dScratch = nullptr;     // batch scratch (sort permutation + work counter), grown on demand
+    size_t scratchCap = 0;
     int lastCudaError = 0;
 };
 
@@ -111,6 +113,7 @@ plt_status plt_destroy(plt_context* ctx) {
     cudaFree(ctx->dMatType);
     cudaFree(ctx->dProfiles);
     cudaFree(ctx->dStatus);
+    cudaFree(ctx->dScratch);
     delete ctx;
     return PLT_OK;
 }
@@ -188,7 +191,18 @@ plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt
     const void* outs[] = {r->stokes, r->coherence, r->beam_t, r->pdf, r->lambda_pdf, r->sample_wo, r->sample_pdf, r->sample_weight, r->sample_lobe, r->sample_valid};
     for (const void* p : outs)
         if (p && !aligned16(p)) return PLT_INVALID_ARG;
+    const size_t need = plt::bsdfScratchBytes(q->n);
+    if (need > ctx->scratchCap) {
+        // grows once to the largest batch seen; the stream is synchronised by cudaFree/cudaMalloc
+        cudaFree(ctx->dScratch);
+        ctx->dScratch = nullptr;
+        ctx->scratchCap = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dScratch, need));
+        ctx->scratchCap = need;
+    }
     plt::BatchParams p{};
+    p.perm = static_cast<uint16_t*>(ctx->dScratch);
+    p.unitCounter = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx->dScratch) + (need - 256));
     p.q = *q;
     p.r = *r;
     p.ops = ops;

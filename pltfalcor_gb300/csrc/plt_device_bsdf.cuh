@@ -101,10 +101,15 @@ PLT_DI float m00Of(const float* __restrict__ tab, float wl) { return __ldg(tab +
 // ------------------------------------------------------------------------------------------
 // Gaussian surface (GaussianSurface.slang:37-110)
 // ------------------------------------------------------------------------------------------
-PLT_DI float gaussAlpha(const float* __restrict__ p, f3 wi, f3 wo, float k) {
+// Specular fraction alpha = exp(-x) together with 1 - alpha.  The shaders form 1 - alpha by
+// subtraction, which loses every digit as alpha -> 1 (smooth surfaces, grazing gratings); here
+// it is -expm1(-x), accurate to an ulp.  Discrete choices (u < alpha) use alpha itself.
+struct Alpha { float a, om; };
+PLT_DI Alpha alphaOf(float x) { return Alpha{expf(-x), -expm1f(-x)}; }
+PLT_DI Alpha gaussAlpha(const float* __restrict__ p, f3 wi, f3 wo, float k) {
     const float q = __ldg(p + PG_Q);
-    const float a = sqr((fabsf(wi.z) + fabsf(wo.z)) * q * k);
-    return q == 0.f ? 1.f : expf(-a);
+    const float x = sqr((fabsf(wi.z) + fabsf(wo.z)) * q * k);
+    return q == 0.f ? Alpha{1.f, 0.f} : alphaOf(x);
 }
 // sample_boxmueller_truncated (MathHelpers.slang:416-434)
 PLT_DI f2 boxMullerTruncated(float u0, float u1, f2 mean, float sigma2, float& pdf) {
@@ -122,7 +127,7 @@ PLT_DI f2 boxMullerTruncated(float u0, float u1, f2 mean, float sigma2, float& p
     pdf = .5f * x / (max_phi * sigma2) * coso;
     return f2{r * cp + mean.x, r * sp + mean.y};
 }
-PLT_DI float boxMullerTruncatedPdf(f2 wo, f2 mean, float sigma2) {
+PLT_NI float boxMullerTruncatedPdf(f2 wo, f2 mean, float sigma2) {
     const float mm = dot(mean, mean);
     const float l = sqrtf(fminf(1.f, mm));
     const float coso = sqrtf(fmaxf(0.f, 1.f - mm));
@@ -133,7 +138,7 @@ PLT_DI float boxMullerTruncatedPdf(f2 wo, f2 mean, float sigma2) {
     const float max_phi = (r < kFltEps || l < kFltEps) ? kPi : acosf(clampf((r * r + l * l - 1.f) / (2.f * r * l), -1.f, 1.f));
     return .5f * x / (max_phi * sigma2) * coso;
 }
-PLT_DI f3 gaussSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
+PLT_NI f3 gaussSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
     const float s2 = __ldg(p + PG_INVSIGMA2) / (k * k);
     const float u0 = sg.next1D(), u1 = sg.next1D();
     const f2 wo = boxMullerTruncated(u0, u1, f2{-wi.x, -wi.y}, s2, pdf);
@@ -169,14 +174,14 @@ PLT_DI float gaussEval(const float* __restrict__ p, const DBeam<H>& b, float k, 
 // ------------------------------------------------------------------------------------------
 // Fractal (K-correlation / ABC) surface (FractalSurface.slang:38-135)
 // ------------------------------------------------------------------------------------------
-PLT_DI float fracAlpha(const float* __restrict__ p, f3 wi, f3 wo, float k) {
-    return expf(-sqr((fabsf(wi.z) + fabsf(wo.z)) * __ldg(p + PF_Q) * k));
+PLT_DI Alpha fracAlpha(const float* __restrict__ p, f3 wi, f3 wo, float k) {
+    return alphaOf(sqr((fabsf(wi.z) + fabsf(wo.z)) * __ldg(p + PF_Q) * k));
 }
-PLT_DI float fracPGF(const float* __restrict__ p, float zx, float zy) {
+PLT_NI float fracPGF(const float* __restrict__ p, float zx, float zy) {
     const float f = 1.f / powf(1.f + __ldg(p + PF_T) * (zx * zx + zy * zy), __ldg(p + PF_EXPO));
     return __ldg(p + PF_C) * f;
 }
-PLT_DI f3 fracSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
+PLT_NI f3 fracSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
     const float s = sqrtf(fmaxf(0.f, 1.f - wi.z * wi.z));
     const float phi_i = s > 0.f ? atan2f(wi.y, wi.x) : 0.f;
     const float T = __ldg(p + PF_T);

@@ -44,19 +44,19 @@ PLT_DI void dielEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
         const float cosM = signf(toLight.z) * LdotH;
 #pragma unroll
         for (int j = 0; j < H; ++j) {
-            const float a = gaussAlpha(p, toLight, toEyeUp, k[j]);
+            const Alpha a = gaussAlpha(p, toLight, toEyeUp, k[j]);
             const float J = isReflection ? 1.f : sqr(toEye.z > 0.f ? eta[j] : 1.f / eta[j]);
             const float D = gaussEval(p, b, k[j], h);
             const FresnelD f = fresnel_dielectric(cosM, eta[j]);
             const MM M1 = isReflection ? muellerFresnelReal(f.rs, f.rp) : muellerFresnelReal(f.ts, f.tp);
-            const float s = m00Of(tab, b.wl[j]) * (1.f - a) * J * fabsf(toLight.z) * D;
+            const float s = m00Of(tab, b.wl[j]) * a.om * J * fabsf(toLight.z) * D;
             b.setSP(j, s * mapply(M1, b.getSP(j)));
         }
     } else {
         const f3 toLightBeam = b.toLocal(toLight);
 #pragma unroll
         for (int j = 0; j < H; ++j) {
-            const float a = gaussAlpha(p, toLight, toEyeUp, k[j]);
+            const float a = gaussAlpha(p, toLight, toEyeUp, k[j]).a;
             const float J = isReflection ? 1.f : sqr(toEye.z > 0.f ? eta[j] : 1.f / eta[j]);
             const FresnelD f = fresnel_dielectric(toLight.z, eta[j]);
             const MM M0 = isReflection ? muellerFresnelReal(f.rs, f.rp) : muellerFresnelReal(f.ts, f.tp);
@@ -75,11 +75,11 @@ PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
                        SampleGen& sg, float wl) {
     const float* p = m->p;
     const float k = kOfWl(wl);
-    const float a = gaussAlpha(p, wi, wi, k);
+    const Alpha a = gaussAlpha(p, wi, wi, k);
     const float eta = dielIor(p, k);
     // lobe mask All: pdfDirect = a
-    const bool isDirect = a == 1.f || sg.next1D() < a;
-    pdf = isDirect ? a : 1.f - a;
+    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
+    pdf = isDirect ? a.a : a.om;
     bool isReflection;
     if (isDirect) {
         const FresnelD f = fresnel_dielectric(wi.z, eta);
@@ -105,14 +105,14 @@ PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
 PLT_DI float dielPdf(const DevMaterial* __restrict__ m, f3 wi, f3 woL, float wl) {
     const float* p = m->p;
     const float k = kOfWl(wl);
-    const float a = gaussAlpha(p, wi, wi, k);
+    const Alpha a = gaussAlpha(p, wi, wi, k);
     const float eta = dielIor(p, k);
     const bool isReflection = wi.z * woL.z > 0.f;
     const f3 wo = isReflection ? woL : dielScatteredWo(woL, eta);
     const f3 mh = normalize(wi + wo);
     const float F = fresnelR(fresnel_dielectric(signf(wi.z) * dot(wi, mh), eta));
     const float pdfF = isReflection ? F : 1.f - F;
-    return (1.f - a) * pdfF * gaussPdf(p, wi, wo, k);
+    return a.om * pdfF * gaussPdf(p, wi, wo, k);
 }
 template <int H>
 PLT_DI void dielLambdaPdf(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, uint32_t lobe, const DBeam<H>& b, float* out) {
@@ -161,17 +161,17 @@ PLT_DI void condEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
 #pragma unroll
     for (int j = 0; j < H; ++j) {
         const float k = kOfWl(b.wl[j]);
-        const float a = fracAlpha(p, toLight, toEye, k);
+        const Alpha a = fracAlpha(p, toLight, toEye, k);
         const f2 ior = conductorIor(m, c, b.wl[j], extEta);
         f2 rs, rp;
         float s;
         MM M;
         if (isScatter) {
             M = muellerRConductor(LdotH, ior, rs, rp);
-            s = (1.f - a) * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y);
+            s = a.om * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y);
         } else {
             M = muellerRConductor(toLight.z, ior, rs, rp);
-            s = a;
+            s = a.a;
         }
         const f4 v = s * mapply(M, b.getSP(j));
         const float m00 = m00Of(m->m00a, b.wl[j]);
@@ -182,9 +182,9 @@ PLT_DI bool condSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
                        SampleGen& sg, float wl) {
     const float* p = m->p;
     const float k = kOfWl(wl);
-    const float a = fracAlpha(p, wi, wi, k);
-    const bool isDirect = a == 1.f || sg.next1D() < a;
-    pdf = isDirect ? a : 1.f - a;
+    const Alpha a = fracAlpha(p, wi, wi, k);
+    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
+    pdf = isDirect ? a.a : a.om;
     weight = m00Of(m->m00a, wl);
     if (isDirect) {
         wo = reflectL(wi);
@@ -199,7 +199,7 @@ PLT_DI bool condSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
 }
 PLT_DI float condPdf(const DevMaterial* __restrict__ m, f3 wi, f3 wo, float wl) {
     const float k = kOfWl(wl);
-    return (1.f - fracAlpha(m->p, wi, wi, k)) * fracPdf(m->p, wi, wo, k);
+    return fracAlpha(m->p, wi, wi, k).om * fracPdf(m->p, wi, wo, k);
 }
 
 // =============================================================================================
@@ -211,11 +211,11 @@ PLT_DI void opaqEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
     const bool isDirect = (lobe & kLobeDelta) != 0, isScatter = (lobe & kLobeNonDelta) != 0;
     if ((!isScatter && !isDirect) || (lobe & kLobeReflection) == 0) { b.setZero(); return; }
     const float mk = meank();
-    const float a = fracAlpha(p, toLight, toEye, mk);
-    float M = a;
+    const Alpha a = fracAlpha(p, toLight, toEye, mk);
+    float M = a.a;
     if (isScatter) {
         const f3 h = toLight + toEye;
-        M = (1.f - a) * fabsf(toLight.z) * fracPGF(p, mk * h.x, mk * h.y);
+        M = a.om * fabsf(toLight.z) * fracPGF(p, mk * h.x, mk * h.y);
     }
 #pragma unroll
     for (int j = 0; j < H; ++j) b.setSP(j, (M * m00Of(m->m00a, b.wl[j])) * b.getSP(j));
@@ -224,9 +224,9 @@ PLT_DI bool opaqSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
                        SampleGen& sg, float wl) {
     const float* p = m->p;
     const float mk = meank();
-    const float a = fracAlpha(p, wi, wi, mk);
-    const bool isDirect = a == 1.f || sg.next1D() < a;
-    pdf = isDirect ? a : 1.f - a;
+    const Alpha a = fracAlpha(p, wi, wi, mk);
+    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
+    pdf = isDirect ? a.a : a.om;
     weight = m00Of(m->m00a, wl);
     if (isDirect) {
         wo = reflectL(wi);
@@ -241,7 +241,7 @@ PLT_DI bool opaqSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
 }
 PLT_DI float opaqPdf(const DevMaterial* __restrict__ m, f3 wi, f3 wo) {
     const float mk = meank();
-    return (1.f - fracAlpha(m->p, wi, wi, mk)) * fracPdf(m->p, wi, wo, mk);
+    return fracAlpha(m->p, wi, wi, mk).om * fracPdf(m->p, wi, wo, mk);
 }
 
 // =============================================================================================
@@ -281,19 +281,19 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
 #pragma unroll
         for (int j = 0; j < H; ++j) {
             const float k = kOfWl(b.wl[j]);
-            const float a = fracAlpha(p, wiIn, woIn, k);
+            const Alpha a = fracAlpha(p, wiIn, woIn, k);
             const float coh = b.mutualCoherenceK(k, quad);
             const float phase = sinf(dist * k * coatior);
             const f4 SP = b.getSP(j);
             f4 newSP = m00Of(m->m00a, b.wl[j]) * mapply(M, SP);
             f4 refl;
             if (isScatter) {
-                const float w = (1.f - a) * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y);
+                const float w = a.om * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y);
                 newSP = w * newSP;
                 refl = w * mapply(MiRs, SP);
             } else {
-                newSP = a * newSP;
-                refl = a * mapply(MiRs, SP);
+                newSP = a.a * newSP;
+                refl = a.a * mapply(MiRs, SP);
             }
             b.setSP(j, interfere(newSP, refl, phase, phase, coh));
         }
@@ -302,7 +302,7 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
 #pragma unroll
         for (int j = 0; j < H; ++j) {
             const float k = kOfWl(b.wl[j]);
-            const float a = fracAlpha(p, wiIn, woIn, k);
+            const Alpha a = fracAlpha(p, wiIn, woIn, k);
             const float coh = b.mutualCoherenceK(k, quad);
             f2 rs, rp;
             const MM M2R = muellerRConductor(LdotH, conductorIor(m, c, b.wl[j], coatior), rs, rp);
@@ -310,11 +310,11 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
             const f4 SP = b.getSP(j);
             f4 newSP = m00Of(m->m00a, b.wl[j]) * mapply(M, SP);
             if (isScatter) {
-                newSP = ((1.f - a) * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y)) * newSP;
+                newSP = (a.om * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y)) * newSP;
             } else {
                 const float pS = sinf(dist * k * coatior + atan2f(rs.y, rs.x));
                 const float pP = sinf(dist * k * coatior + atan2f(rp.y, rp.x));
-                newSP = interfere(a * newSP, mapply(MiR, SP), pS, pP, coh);
+                newSP = interfere(a.a * newSP, mapply(MiR, SP), pS, pP, coh);
             }
             b.setSP(j, newSP);
         }
@@ -340,9 +340,9 @@ PLT_DI bool coatSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
     const f3 wiIn = -coatRefract(wi, eta1, f.cosT);
     if (wiIn.z == 0.f) return false;
     weight = m00Of(m->m00a, wl);
-    const float a = fracAlpha(p, wiIn, wiIn, k);
-    const bool isDirect = a == 1.f || sg.next1D() < a;
-    pdf *= isDirect ? a : 1.f - a;
+    const Alpha a = fracAlpha(p, wiIn, wiIn, k);
+    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
+    pdf *= isDirect ? a.a : a.om;
     if (isDirect) {
         wo = reflectL(wi);
         lobe = kLobeDeltaR;
@@ -366,8 +366,8 @@ PLT_DI float coatPdf(const DevMaterial* __restrict__ m, f3 wi, f3 wo, float wl) 
     const FresnelD f1 = fresnel_dielectric(wo.z, eta1);
     const f3 wiIn = -coatRefract(wi, eta1, f.cosT);
     const f3 woIn = -coatRefract(wo, eta1, f1.cosT);
-    const float a = fracAlpha(p, wiIn, wiIn, k);
-    return wiIn.z * woIn.z == 0.f ? 0.f : (1.f - a) * (1.f - Fd) * fracPdf(p, wiIn, woIn, k);
+    const float om = fracAlpha(p, wiIn, wiIn, k).om;
+    return wiIn.z * woIn.z == 0.f ? 0.f : om * (1.f - Fd) * fracPdf(p, wiIn, woIn, k);
 }
 template <int H>
 PLT_DI void coatLambdaPdf(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, uint32_t lobe, const DBeam<H>& b, float* out) {
@@ -389,8 +389,9 @@ PLT_DI void coatLambdaPdf(const DevMaterial* __restrict__ m, f3 toLight, f3 toEy
 // Diffraction gratings (DiffractionGrating.slang:41-156) and the grated BxDFs
 // (PLTDiffractionGratedOpaqueDielectricBSDF.slang:45-209, PLTDiffractionGratedConductorBSDF.slang:45-213)
 // =============================================================================================
+PLT_DI Alpha gratAlphaFull(const float* __restrict__ p, f3 wi, float k) { return alphaOf(sqr(wi.z * __ldg(p + PD_Q) * k)); }
 PLT_DI float gratAlpha(const float* __restrict__ p, f3 wi, float k) { return expf(-sqr(wi.z * __ldg(p + PD_Q) * k)); }
-PLT_DI float gratLobeIntensity(const DevMaterial* __restrict__ m, int lx, int ly, f3 wi, float lambda) {
+PLT_NI float gratLobeIntensity(const DevMaterial* __restrict__ m, int lx, int ly, f3 wi, float lambda) {
     const float* p = m->p;
     const uint32_t gtype = (m->aux >> 8) & 0xFu;
     const bool is1D = __ldg(p + PD_IPY) == 0.f;
@@ -409,7 +410,7 @@ PLT_DI float gratLobeIntensity(const DevMaterial* __restrict__ m, int lx, int ly
     }
     return __ldg(p + PD_MULT) * ix * iy;
 }
-PLT_DI f3 gratDiffract(const float* __restrict__ p, f3 wi, int lx, int ly, float lambda) {
+PLT_NI f3 gratDiffract(const float* __restrict__ p, f3 wi, int lx, int ly, float lambda) {
     const float px = sqrtf(wi.x * wi.x + wi.z * wi.z), py = sqrtf(wi.y * wi.y + wi.z * wi.z);
     const float sx = px > kFltEps ? wi.x / px : 0.f, sy = py > kFltEps ? wi.y / py : 0.f;
     const float a = lambda * (float)lx * __ldg(p + PD_IPX) - sx;
@@ -433,11 +434,13 @@ template <int H, bool CONDUCTOR>
 PLT_DI void gratEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight, f3 toEye, uint32_t bsdfLobe, DBeam<H>& b) {
     const float* p = m->p;
     const bool isDirect = (bsdfLobe & kLobeDelta) != 0;
-    float a[H];
+    float a[H], om[H];
     bool anyPos = false, anyLt1 = false;
 #pragma unroll
     for (int j = 0; j < H; ++j) {
-        a[j] = gratAlpha(p, toLight, k2Pi / (1e-3f * b.wl[j]));
+        const Alpha al = gratAlphaFull(p, toLight, k2Pi / (1e-3f * b.wl[j]));
+        a[j] = al.a;
+        om[j] = al.om;
         anyPos |= a[j] > 0.f;
         anyLt1 |= a[j] < 1.f;
     }
@@ -456,7 +459,7 @@ PLT_DI void gratEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
             float coh = 1.f;
             if (j > 0) coh = b.mutualCoherenceAngular(b.toLocal(gratDiffract(p, toEye, lx, ly, lambda)), toLightBeam);
             const float inten = gratLobeIntensity(m, lx, ly, toLight, lambda);
-            const float s = m00Of(m->m00a, b.wl[j]) * (1.f - a[j]) * coh * inten;
+            const float s = m00Of(m->m00a, b.wl[j]) * om[j] * coh * inten;
             if (CONDUCTOR) {
                 f2 rs, rp;
                 const MM M0 = muellerRConductor(toLight.z, conductorIor(m, c, b.wl[j], __ldg(p + PF_EXTETA)), rs, rp);
@@ -506,9 +509,9 @@ PLT_DI bool gratSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
                        SampleGen& sg, float wl) {
     const float* p = m->p;
     const float lambda = 1e-3f * wl;
-    const float a = gratAlpha(p, wi, k2Pi / lambda);
-    const bool isDirect = a == 1.f || sg.next1D() < a;
-    pdf = isDirect ? a : 1.f - a;
+    const Alpha a = gratAlphaFull(p, wi, k2Pi / lambda);
+    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
+    pdf = isDirect ? a.a : a.om;
     if (isDirect) {
         float bp = 0.f;
         if (CONDUCTOR) condSample(m, wi, wo, bp, weight, lobe, sg, wl);
@@ -713,17 +716,17 @@ PLT_DI bool thinSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
 // PLTMultiLayeredStack (PLTMultiLayeredStackBSDF.slang:42-139): scalar Airy recursion, FP32 as
 // the reference or FP64 (PLT_OPTION_FP64_MULTILAYER)
 // =============================================================================================
+struct MLLayer { float ct, th, ior, r; };  // one of the two alternating layers
 template <typename RT>
-PLT_DI float mlRecursion(float sqrtm00, uint32_t layers, const float ct[2], const float th[2], const float ior[2], const float rr[2],
-                         float Rout, float k) {
+PLT_NI float mlRecursion(float sqrtm00, uint32_t layers, MLLayer l0, MLLayer l1, float Rout, float k) {
     RT gx = (RT)sqrtm00, gy = (RT)0;
     for (uint32_t l = 0; l < layers; ++l) {
-        const uint32_t idx = l & 1u;
-        const RT d = (RT)2 * (RT)th[idx] / (RT)ct[idx] * (RT)k * (RT)ior[idx];
+        const MLLayer L = (l & 1u) ? l1 : l0;
+        const RT d = (RT)2 * (RT)L.th / (RT)L.ct * (RT)k * (RT)L.ior;
         RT sd, cd;
         if constexpr (sizeof(RT) == 8) sincos(d, &sd, &cd);
         else sincosf(d, &sd, &cd);
-        const RT R = l == layers - 1 ? (RT)Rout : (RT)rr[idx];
+        const RT R = l == layers - 1 ? (RT)Rout : (RT)L.r;
         // G = G * p
         const RT x = gx * cd - gy * sd, y = gx * sd + gy * cd;
         // G = (R + G) / (1 + R G)
@@ -746,17 +749,15 @@ PLT_DI void mlEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight, 
     const FresnelD f1 = fresnel_dielectric(-f0.cosT, eta2);
     const float r0 = sqrtf(fresnelR(f1));
     const float r1 = sqrtf(fresnelR(fresnel_dielectric(f1.cosT, eta2)));
-    const float ct[2] = {fabsf(f0.cosT), fabsf(f1.cosT)};
-    const float th[2] = {__ldg(p + PM_TH1), __ldg(p + PM_TH2)};
-    const float ior[2] = {__ldg(p + PM_IOR1), __ldg(p + PM_IOR2)};
-    const float rr[2] = {r0, r1};
+    const MLLayer l0{fabsf(f0.cosT), __ldg(p + PM_TH1), __ldg(p + PM_IOR1), r0};
+    const MLLayer l1{fabsf(f1.cosT), __ldg(p + PM_TH2), __ldg(p + PM_IOR2), r1};
     const uint32_t layers = m->aux;
 #pragma unroll
     for (int j = 0; j < H; ++j) {
         const float sm = sqrtf(m00Of(m->m00a, b.wl[j]));
         const float k = kOfWl(b.wl[j]);
-        const float g2 = (c.flags & 1u) ? mlRecursion<double>(sm, layers, ct, th, ior, rr, Rout, k)
-                                        : mlRecursion<float>(sm, layers, ct, th, ior, rr, Rout, k);
+        const float g2 = (c.flags & 1u) ? mlRecursion<double>(sm, layers, l0, l1, Rout, k)
+                                        : mlRecursion<float>(sm, layers, l0, l1, Rout, k);
         b.setSP(j, g2 * b.getSP(j));
     }
 }

@@ -16,6 +16,17 @@
 namespace pltdev {
 
 #define PLT_DI __device__ __forceinline__
+// Large helpers with many call sites (Fresnel, pGF, surface sampling, BesselJ, grating lobes,
+// spectra) are emitted once and called, so one material's eval + sample + pdf path stays within
+// the SM instruction cache; PLT_OUTLINE_HELPERS=0 inlines them everywhere.
+#ifndef PLT_OUTLINE_HELPERS
+#define PLT_OUTLINE_HELPERS 1
+#endif
+#if PLT_OUTLINE_HELPERS
+#define PLT_NI static __device__ __noinline__
+#else
+#define PLT_NI __device__ __forceinline__
+#endif
 
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float k2Pi = 6.28318530717958647693f;
@@ -67,7 +78,7 @@ PLT_DI f2 csqrt(f2 z) {
 }
 
 // perp_stark (MathHelpers.slang:609-623)
-PLT_DI f3 perp_stark(f3 u) {
+PLT_NI f3 perp_stark(f3 u) {
     const float ax = fabsf(u.x), ay = fabsf(u.y), az = fabsf(u.z);
     const uint32_t uyx = (ax - ay) < 0.f, uzx = (ax - az) < 0.f, uzy = (ay - az) < 0.f;
     const uint32_t xm = uyx & uzx, ym = (1u ^ xm) & uzy, zm = 1u ^ (xm | ym);
@@ -82,7 +93,7 @@ PLT_DI f3 canonical_tangent(f3 r) {
 
 // ---- Fresnel (Fresnel.slang:30-90) ----
 struct FresnelD { float rs, rp, ts, tp, cosT; };
-PLT_DI FresnelD fresnel_dielectric(float cosI_, float eta) {
+PLT_NI FresnelD fresnel_dielectric(float cosI_, float eta) {
     FresnelD f;
     if (eta == 1.f) {
         f.cosT = -cosI_;
@@ -104,7 +115,7 @@ PLT_DI FresnelD fresnel_dielectric(float cosI_, float eta) {
 }
 PLT_DI float fresnelR(const FresnelD& f) { return 0.5f * (f.rs * f.rs + f.rp * f.rp); }
 
-PLT_DI void fresnel_conductor(float cosI, f2 eta, f2& rs, f2& rp) {
+PLT_NI void fresnel_conductor(float cosI, f2 eta, f2& rs, f2& rp) {
     if ((eta.x == 0.f && eta.y == 0.f) || cosI < 0.f) {
         rs = rp = f2{0.f, 0.f};
         return;
@@ -172,7 +183,7 @@ PLT_DI int spectrumBin(float wl) { return (int)(clampf((wl - 380.0f) / (720.0f -
 #include "plt_layout.h"
 namespace pltdev {
 
-PLT_DI float evalSpectrum(const DevProfile* __restrict__ profiles, uint32_t nprof, uint32_t id, float lambda) {
+PLT_NI float evalSpectrum(const DevProfile* __restrict__ profiles, uint32_t nprof, uint32_t id, float lambda) {
     if (id == kNoProfile || id >= nprof) return 0.f;
     const DevProfile& sp = profiles[id];
     const int bins = (int)sp.bins;
@@ -227,7 +238,7 @@ PLT_DI float factorialf(int n) {
     for (int i = 2; i <= n; ++i) f *= (float)i;
     return f;
 }
-PLT_DI float besselJ(int nu, float x) {
+PLT_NI float besselJ(int nu, float x) {
     const float t = (nu > 0 || ((-nu) % 2) == 0) ? 1.f : -1.f;
     nu = abs(nu);
     const float cutoff = (float)nu + 1.f;

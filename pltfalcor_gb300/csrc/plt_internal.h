@@ -30,11 +30,24 @@ struct BatchParams {
     uint32_t nProfiles;
     uint32_t flags;
     uint32_t* status;
+    uint16_t* perm;            // scratch: per-tile sort permutation, kBatchTile entries per tile
+    uint32_t* unitCounter;     // scratch: shade kernel work counter
 };
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 256;     // classify CTA
 constexpr int kBatchItems = 8;
 constexpr int kBatchTile = kBatchThreads * kBatchItems;
+constexpr int kShadeThreads = 128;     // shade CTA
+#ifndef PLT_SHADE_MIN_BLOCKS
+#define PLT_SHADE_MIN_BLOCKS 4
+#endif
+constexpr int kShadeMinBlocks = PLT_SHADE_MIN_BLOCKS;
+
+// scratch bytes plt_bsdf_batch needs for n queries: the permutation, then the work counter
+inline size_t bsdfScratchBytes(uint32_t n) {
+    const size_t tiles = ((size_t)n + kBatchTile - 1) / kBatchTile;
+    return tiles * kBatchTile * sizeof(uint16_t) + 256;
+}
 
 // Launches the fused BSDF batch kernel (templated on the hero-wavelength count).
 cudaError_t launchBsdfBatch(const BatchParams& p, int hwss, int numSMs, cudaStream_t stream);

@@ -22,10 +22,11 @@ def main():
     prof, _ = spectra.standard_profiles()
     for name, wl in golden_cases.cases(prof).items():
         out = {}
-        for prec in (32, 64):
-            res = oracle.run(wl, ops=0xF, precision=prec)
+        # FP32, FP64 and FP32 with random rounding (seed 1)
+        for tag, prec in (("fp32", 32), ("fp64", 64), ("rr", 16)):
+            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=1)
             for k, v in res.items():
-                out["%s_fp%d" % (k, prec)] = v
+                out["%s_%s" % (k, tag)] = v
         path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")
         np.savez_compressed(path, **out)
         print("wrote", path, wl.n)

@@ -1,7 +1,9 @@
 """GPU parity of the batched BSDF kernels against the CPU oracle, through the C ABI.
 
-Tolerances are stated in tests/parity.py (1e-4 relative vs the FP32 oracle; discrete sample
-outcomes bit-exact up to a 1e-3 fraction of threshold-straddling draws).
+Tolerances are stated in tests/parity.py: 1e-4 relative vs the FP32 oracle, widened per query to
+10x the FP32 oracle's own error against the FP64 oracle where the FP32 arithmetic is
+ill-conditioned; discrete sample outcomes bit-exact up to a 1e-3 fraction of threshold-straddling
+draws.
 """
 import ctypes as C
 import json
@@ -48,8 +50,14 @@ def run_gpu(ctx, wl, ops=None, rng_offset=0):
     return b.fetch()
 
 
+def oracles(wl, ops=0xF, **kw):
+    """FP32 oracle, FP64 oracle and the FP32 oracle with random rounding (conditioning)."""
+    return (oracle.run(wl, ops=ops, precision=32, **kw), oracle.run(wl, ops=ops, precision=64),
+            oracle.run(wl, ops=ops, precision=16, sr_seed=1, **kw))
+
+
 def assert_parity(gpu, ora, wl, ops, label):
-    errs = parity.compare(gpu, ora, wl.n, wl.hwss, ops)
+    errs = parity.compare(gpu, ora[0], wl.n, wl.hwss, ops, ora[1], ora[2])
     types = np.asarray(wl.records["type"])[wl.material]
     fails = []
     for t in np.unique(types):
@@ -62,16 +70,14 @@ def assert_parity(gpu, ora, wl, ops, label):
 def test_rough_dielectric_parity(ctx, profiles):
     wl = W.rough_dielectric_batch(profiles=profiles[0])
     g = run_gpu(ctx, wl, ops=0xF)
-    o = oracle.run(wl, ops=0xF)
-    assert_parity(g, o, wl, 0xF, "rough_dielectric_65536")
+    assert_parity(g, oracles(wl), wl, 0xF, "rough_dielectric_65536")
 
 
 @pytest.mark.parametrize("hwss,n", [(1, 8 * 16384), (4, 8 * 4096), (2, 8 * 1024), (3, 8 * 1024), (8, 8 * 1024)])
 def test_mixed_material_parity(ctx, profiles, hwss, n):
     wl = W.mixed_material_batch(n=n, profiles=profiles[0], hwss=hwss)
     g = run_gpu(ctx, wl, ops=0xF)
-    o = oracle.run(wl, ops=0xF)
-    assert_parity(g, o, wl, 0xF, "mixed_hwss%d" % hwss)
+    assert_parity(g, oracles(wl), wl, 0xF, "mixed_hwss%d" % hwss)
 
 
 def test_transmission_and_grazing_cases(ctx, profiles):
@@ -89,18 +95,19 @@ def test_transmission_and_grazing_cases(ctx, profiles):
     wl.v, wl.w = np.ascontiguousarray(v.reshape(-1)), np.ascontiguousarray(w.reshape(-1))
     wl.lobe = np.where(rng.uniform() < 0.3, np.uint32(0xFFFF), wl.lobe).astype(np.uint32)
     g = run_gpu(ctx, wl, ops=0xF)
-    o = oracle.run(wl, ops=0xF)
-    assert_parity(g, o, wl, 0xF, "transmission_grazing")
+    assert_parity(g, oracles(wl), wl, 0xF, "transmission_grazing")
 
 
 def test_golden_fixtures(ctx, profiles):
     import golden_cases
     for name, wl in golden_cases.cases(profiles[0]).items():
         ref = np.load(os.path.join(GOLDEN, name + ".npz"))
-        ora = {k: ref[k + "_fp32"] for k in ("stokes", "coherence", "pdf", "lambda_pdf", "sample_wo", "sample_pdf",
-                                              "sample_weight", "sample_lobe", "sample_valid")}
+        keys = ("stokes", "coherence", "pdf", "lambda_pdf", "sample_wo", "sample_pdf", "sample_weight", "sample_lobe", "sample_valid")
+        o32 = {k: ref[k + "_fp32"] for k in keys}
+        o64 = {k: ref[k + "_fp64"] for k in keys}
+        orr = {k: ref[k + "_rr"] for k in keys}
         g = run_gpu(ctx, wl, ops=0xF)
-        errs = parity.compare(g, ora, wl.n, wl.hwss, 0xF)
+        errs = parity.compare(g, o32, wl.n, wl.hwss, 0xF, o64, orr)
         fails = parity.check(errs, max_bad_frac=2e-3)
         assert not fails, (name, fails)
 
@@ -113,8 +120,8 @@ def test_fp64_error_report(ctx, profiles, tmp_path):
     o64 = oracle.run(wl, ops=0xF, precision=64)
     types = np.asarray(wl.records["type"])[wl.material]
     report = {}
-    eg = parity.compare(g, o64, wl.n, 1, 0xF)
-    eo = parity.compare(o32, o64, wl.n, 1, 0xF)
+    eg = parity.errors(g, o64, wl.n, 1, 0xF)
+    eo = parity.errors(o32, o64, wl.n, 1, 0xF)
     for t in np.unique(types):
         sel = types == t
         report[M.TYPE_NAMES[int(t)]] = {"gpu_fp32_vs_fp64": parity.summarize(eg, sel=sel),
@@ -136,8 +143,10 @@ def test_fp64_multilayer_option(torch_cuda, product_lib, profiles):
     wl = W.mixed_material_batch(n=8 * 2048, profiles=profiles[0])
     g = run_gpu(c, wl, ops=1)
     o = oracle.run(wl, ops=1, precision=32, fp64_multilayer=True)
+    o64 = oracle.run(wl, ops=1, precision=64)
+    orr = oracle.run(wl, ops=1, precision=16, sr_seed=1, fp64_multilayer=True)
     ml = np.asarray(wl.records["type"])[wl.material] == M.MULTILAYERED_STACK
-    errs = parity.compare(g, o, wl.n, 1, 1)
+    errs = parity.compare(g, o, wl.n, 1, 1, o64, orr)
     assert not parity.check(errs, sel=ml)
     c.close()
 

@@ -170,10 +170,10 @@ def test_oracle_matches_golden_fixture(profiles):
     import golden_cases
     for name, wl in golden_cases.cases(prof).items():
         ref = np.load(os.path.join(GOLDEN, name + ".npz"))
-        for prec in (32, 64):
-            res = oracle.run(wl, ops=0xF, precision=prec)
+        for tag, prec in (("fp32", 32), ("fp64", 64), ("rr", 16)):
+            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=1)
             for k, v in res.items():
-                r = ref["%s_fp%d" % (k, prec)]
+                r = ref["%s_%s" % (k, tag)]
                 if v.dtype == np.uint32:
                     assert (v == r).all(), (name, prec, k)
                 else:
