@@ -166,6 +166,26 @@ typedef struct plt_bsdf_results {
 #define PLT_OP_SAMPLE 0x4u
 #define PLT_OP_LAMBDA_PDF 0x8u
 
+/* A batch of rays (device SoA planes).  Hits are accepted for tmin <= t <= tmax; triangles are
+ * two-sided (the reference traces with RAY_FLAG_NONE / ACCEPT_FIRST_HIT_AND_END_SEARCH, no
+ * culling: RenderPasses/PLTPT/ShadowRays.slangh:65-135, pltpt_sample.rt.slang:168-183). */
+typedef struct plt_rays {
+    uint32_t n;
+    const float* origin;                /* [3][n] */
+    const float* dir;                   /* [3][n], need not be normalised */
+    const float* tmin;                  /* [n], or NULL for 0 */
+    const float* tmax;                  /* [n], or NULL for FLT_MAX */
+    uint64_t* stats;                    /* [2] device counters (+= BVH node visits, triangle tests), or NULL */
+} plt_rays;
+
+/* Closest-hit results: the triangle index (input order of plt_set_scene) with the lowest distance,
+ * ties broken by the lowest index; 0xFFFFFFFF on a miss. */
+typedef struct plt_hits {
+    uint32_t* prim;                     /* [n] */
+    float* t;                           /* [n] distance (-1 on a miss), or NULL */
+    float* bary;                        /* [2][n] barycentrics of vertices 1 and 2, or NULL */
+} plt_hits;
+
 /* PLTPT pass options (RenderPasses/PLTPT/PLTPT.h:74-108, parsed at PLTPT.cpp:147-175). */
 typedef struct plt_options {
     uint32_t max_bounces;               /* maxBounces, default 32 */
@@ -228,10 +248,26 @@ plt_status plt_spectral_profile_from_samples(const float* wavelengths_nm, const 
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* queries,
                           const plt_bsdf_results* results, uint32_t ops, void* stream);
 
+/* Replaces the scene's DXR acceleration-structure build (Scene/Scene.cpp:3092-3764): a binned-SAH
+ * BVH over the triangles is built on the host and uploaded.  Host arrays: vertices [n_vertices][3],
+ * indices [n_triangles][3], material [n_triangles] (material index per triangle, or NULL for 0). */
+plt_status plt_set_scene(plt_context* ctx, const float* vertices, uint32_t n_vertices, const uint32_t* indices,
+                         uint32_t n_triangles, const uint32_t* material);
+
+/* Closest hit per ray (replaces TraceRay with a closest-hit shader), and occlusion per ray
+ * (replaces visibility rays with ACCEPT_FIRST_HIT_AND_END_SEARCH): occluded[i] = 1 if any triangle
+ * is hit with tmin <= t <= tmax.  Device pointers, asynchronous on `stream`. */
+plt_status plt_trace_closest(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, void* stream);
+plt_status plt_trace_any(plt_context* ctx, const plt_rays* rays, uint32_t* occluded, void* stream);
+
+/* BVH statistics of the current scene (host pointer, 4 values: nodes, leaves, max depth, triangles). */
+plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4);
+
 /* Synchronises `stream`, then reports and clears the context's device status word, which every
  * launch since the previous check ORs into: PLT_BAD_MATERIAL (a material index out of range or of
  * an unknown type; those queries return zeros), PLT_NAN_INPUT (a non-finite direction or
- * wavelength), PLT_QUEUE_TIMEOUT (a bounded device wait gave up).  Mirrors the reference's
+ * wavelength), PLT_QUEUE_TIMEOUT (a bounded device wait gave up or a traversal stack overflowed).
+ * Mirrors the reference's
  * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
 plt_status plt_check_status(plt_context* ctx, void* stream);
 

@@ -36,6 +36,8 @@ def load():
         lib.plto_bsdf_batch.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32]
         lib.plto_bsdf_batch_range.restype = i32
         lib.plto_bsdf_batch_range.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32, C.c_uint64, C.c_uint64]
+        lib.plto_trace_brute.restype = None
+        lib.plto_trace_brute.argtypes = [vp, u32, vp, vp, vp, vp, u32, i32, vp, vp, vp, vp, i32]
         lib.plto_set_sr_seed.restype = None
         lib.plto_set_sr_seed.argtypes = [C.c_uint64]
         lib.plto_count_ops.restype = i32
@@ -132,6 +134,30 @@ def count_ops(wl, ops=None):
         raise RuntimeError("oracle count failed with status %d" % st)
     a = np.frombuffer(out, dtype=np.float64).reshape(12, 4)
     return {t: {"fp": a[t, 0], "sfu": a[t, 1], "div": a[t, 2], "count": int(a[t, 3])} for t in range(12) if a[t, 3] > 0}
+
+
+def trace_brute(tri_verts, origin, direction, tmin=None, tmax=None, any_hit=False, threads=0):
+    """Brute-force closest hit (prim, t, bary) or occlusion over all triangles ([n_tri][9] vertices)."""
+    lib = load()
+    tv = np.ascontiguousarray(tri_verts, np.float32)
+    o = np.ascontiguousarray(origin, np.float32)
+    d = np.ascontiguousarray(direction, np.float32)
+    n = len(o) // 3
+    p = lambda a: None if a is None else C.c_void_p(np.ascontiguousarray(a, np.float32).ctypes.data)
+    t0 = None if tmin is None else np.ascontiguousarray(tmin, np.float32)
+    t1 = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+    if any_hit:
+        occ = np.zeros(n, np.uint32)
+        lib.plto_trace_brute(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
+                             n, 1, None, None, None, C.c_void_p(occ.ctypes.data), threads or os.cpu_count())
+        return occ
+    prim = np.zeros(n, np.uint32)
+    t = np.zeros(n, np.float32)
+    bary = np.zeros(2 * n, np.float32)
+    lib.plto_trace_brute(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
+                         n, 0, C.c_void_p(prim.ctypes.data), C.c_void_p(t.ctypes.data), C.c_void_p(bary.ctypes.data), None,
+                         threads or os.cpu_count())
+    return prim, t, bary
 
 
 def rng_stream(px, py, frame, count):

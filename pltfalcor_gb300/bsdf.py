@@ -146,6 +146,37 @@ class PLTContext:
     def lambdaPdf(self, q, r, stream=None):
         self.batch(q, r, capi.OP_LAMBDA_PDF, stream)
 
+    # ---- scene and ray queries (replace the DXR acceleration structure and TraceRay) ----
+    def set_scene(self, vertices, indices, tri_material=None):
+        v = np.ascontiguousarray(vertices, np.float32)
+        f = np.ascontiguousarray(indices, np.uint32)
+        m = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint32)
+        capi.check(self.lib.plt_set_scene(self.handle, C.c_void_p(v.ctypes.data), len(v), C.c_void_p(f.ctypes.data), len(f),
+                                          None if m is None else C.c_void_p(m.ctypes.data)), "plt_set_scene")
+
+    def scene_stats(self):
+        out = (C.c_uint32 * 4)()
+        capi.check(self.lib.plt_scene_stats(self.handle, out), "plt_scene_stats")
+        return {"nodes": out[0], "leaves": out[1], "max_depth": out[2], "triangles": out[3]}
+
+    @staticmethod
+    def rays(origin, direction, tmin=None, tmax=None, stats=None):
+        r = capi.Rays()
+        r.n = origin.numel() // 3
+        r.origin, r.dir = _ptr(origin), _ptr(direction)
+        r.tmin, r.tmax, r.stats = _ptr(tmin), _ptr(tmax), _ptr(stats)
+        return r
+
+    def trace_closest(self, rays, prim, t=None, bary=None, stream=None):
+        h = capi.Hits()
+        h.prim, h.t, h.bary = _ptr(prim), _ptr(t), _ptr(bary)
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_trace_closest(self.handle, C.byref(rays), C.byref(h), s), "plt_trace_closest")
+
+    def trace_any(self, rays, occluded, stream=None):
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_trace_any(self.handle, C.byref(rays), _ptr(occluded), s), "plt_trace_any")
+
     def check_status(self, stream=None):
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
         return self.lib.plt_check_status(self.handle, s)

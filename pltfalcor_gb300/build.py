@@ -15,9 +15,13 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libplt_gb300.so")
 
-CU_SOURCES = ["plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4.cu", "plt_bsdf_h8.cu"]
-CPP_SOURCES = ["plt_capi.cpp", "plt_materials.cpp", "plt_bsdf_dispatch.cpp"]
+CU_SOURCES = ["plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4.cu", "plt_bsdf_h8.cu", "plt_trace.cu"]
+CPP_SOURCES = ["plt_capi.cpp", "plt_materials.cpp", "plt_bsdf_dispatch.cpp", "plt_bvh.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Single-precision division and square root use the SFU approximations (<= 2 ulp, the accuracy
+# class D3D allows the reference shaders); denormals are kept.  The ray/triangle test uses
+# explicitly rounded intrinsics and is unaffected.
+CU_FLAGS = ["-ftz=false", "-prec-div=false", "-prec-sqrt=false"]
 
 
 def _nvcc():
@@ -45,14 +49,16 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False, ptxas_verbose=False, defines=(), build_dir=None):
-    """Compiles the library.  `defines` (e.g. ["PLT_SHADE_MIN_BLOCKS=6"]) and `build_dir` build a
-    tuning variant elsewhere; the default build is pltfalcor_gb300/_build/libplt_gb300.so."""
+def build(verbose=False, force=False, ptxas_verbose=False, defines=(), build_dir=None, nvcc_flags=()):
+    """Compiles the library.  `defines` (e.g. ["PLT_SHADE_MIN_BLOCKS=6"]), `nvcc_flags` and
+    `build_dir` build a tuning variant elsewhere; the default build is
+    pltfalcor_gb300/_build/libplt_gb300.so."""
     bdir = build_dir or BUILD
     lib = os.path.join(bdir, "libplt_gb300.so")
     os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
     dflags = ["-D" + d for d in defines]
+    cuflags = list(CU_FLAGS) + list(nvcc_flags)
     inc = os.path.join(_cuda_home(), "include")
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "plt_gb300.h"))
@@ -63,7 +69,7 @@ def build(verbose=False, force=False, ptxas_verbose=False, defines=(), build_dir
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                   "--expt-relaxed-constexpr", *dflags, "-c", src, "-o", obj]
+                   "--expt-relaxed-constexpr", *cuflags, *dflags, "-c", src, "-o", obj]
             if ptxas_verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

@@ -49,6 +49,15 @@ class BsdfResults(C.Structure):
                 ("sample_weight", C.c_void_p), ("sample_lobe", C.c_void_p), ("sample_valid", C.c_void_p)]
 
 
+class Rays(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("origin", C.c_void_p), ("dir", C.c_void_p), ("tmin", C.c_void_p), ("tmax", C.c_void_p),
+                ("stats", C.c_void_p)]
+
+
+class Hits(C.Structure):
+    _fields_ = [("prim", C.c_void_p), ("t", C.c_void_p), ("bary", C.c_void_p)]
+
+
 class Options(C.Structure):
     _fields_ = [("max_bounces", C.c_uint32), ("tile_size", C.c_uint32), ("hwss", C.c_uint32),
                 ("hwss_do_mis", C.c_uint32), ("sourcing_area_from_emissive_geometry", C.c_float),
@@ -69,6 +78,7 @@ EXPORTED_SYMBOLS = [
     "plt_abi_version", "plt_status_string", "plt_options_default", "plt_create", "plt_destroy",
     "plt_last_cuda_error", "plt_set_spectral_profiles", "plt_set_materials", "plt_spectral_profile_from_samples",
     "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
+    "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats",
 ]
 
 _lib = None
@@ -100,6 +110,10 @@ def load_library(path=LIB_PATH):
         "plt_bsdf_pdf": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
         "plt_bsdf_sample": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
         "plt_bsdf_lambda_pdf": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
+        "plt_set_scene": (i32, [vp, vp, u32, vp, u32, vp]),
+        "plt_trace_closest": (i32, [vp, C.POINTER(Rays), C.POINTER(Hits), vp]),
+        "plt_trace_any": (i32, [vp, C.POINTER(Rays), vp, vp]),
+        "plt_scene_stats": (i32, [vp, C.POINTER(C.c_uint32)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

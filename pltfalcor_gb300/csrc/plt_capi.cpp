@@ -7,6 +7,7 @@
 #include <new>
 #include <vector>
 
+#include "plt_bvh.h"
 #include "plt_host.h"
 #include "plt_internal.h"
 
@@ -22,6 +23,12 @@ struct plt_context {
     uint32_t* dStatus = nullptr;
     void* dScratch = nullptr;     // batch scratch (sort permutation + work counter), grown on demand
     size_t scratchCap = 0;
+    // scene
+    plt::BvhNode* dNodes = nullptr;
+    float4* dTris = nullptr;      // 3 float4 per triangle, leaf order
+    uint32_t* dTriMaterial = nullptr;
+    uint32_t nTris = 0;
+    plt::BvhBuildStats bvhStats{};
     int lastCudaError = 0;
 };
 
@@ -114,6 +121,9 @@ plt_status plt_destroy(plt_context* ctx) {
     cudaFree(ctx->dProfiles);
     cudaFree(ctx->dStatus);
     cudaFree(ctx->dScratch);
+    cudaFree(ctx->dNodes);
+    cudaFree(ctx->dTris);
+    cudaFree(ctx->dTriMaterial);
     delete ctx;
     return PLT_OK;
 }
@@ -223,6 +233,98 @@ plt_status plt_bsdf_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsd
 plt_status plt_bsdf_sample(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_SAMPLE, s); }
 plt_status plt_bsdf_lambda_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_LAMBDA_PDF, s); }
 
+plt_status plt_set_scene(plt_context* ctx, const float* vertices, uint32_t nVerts, const uint32_t* indices, uint32_t nTris,
+                         const uint32_t* material) {
+    if (!ctx || (nTris > 0 && (!vertices || !indices))) return PLT_INVALID_ARG;
+    if (nTris >= (1u << 27)) return PLT_NOT_SUPPORTED;  // leaf encoding holds 27-bit triangle offsets
+    std::vector<float> tv((size_t)nTris * 9);
+    for (uint32_t t = 0; t < nTris; ++t)
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t vi = indices[3 * (size_t)t + k];
+            if (vi >= nVerts) return PLT_INVALID_ARG;
+            for (int a = 0; a < 3; ++a) {
+                const float x = vertices[3 * (size_t)vi + a];
+                if (!std::isfinite(x)) return PLT_NAN_INPUT;
+                tv[9 * (size_t)t + 3 * k + a] = x;
+            }
+        }
+    std::vector<plt::BvhNode> nodes;
+    std::vector<uint32_t> order;
+    plt::BvhBuildStats st;
+    plt::buildBvh(tv.data(), nTris, nodes, order, &st);
+    std::vector<float4> tris((size_t)nTris * 3);
+    for (uint32_t s = 0; s < nTris; ++s) {
+        const uint32_t t = order[s];
+        const float* p = &tv[9 * (size_t)t];
+        float idBits;
+        std::memcpy(&idBits, &t, 4);
+        tris[3 * s] = make_float4(p[0], p[1], p[2], idBits);
+        tris[3 * s + 1] = make_float4(p[3], p[4], p[5], 0.f);
+        tris[3 * s + 2] = make_float4(p[6], p[7], p[8], 0.f);
+    }
+    cudaFree(ctx->dNodes);
+    cudaFree(ctx->dTris);
+    cudaFree(ctx->dTriMaterial);
+    ctx->dNodes = nullptr;
+    ctx->dTris = nullptr;
+    ctx->dTriMaterial = nullptr;
+    ctx->nTris = 0;
+    PLT_CUDA(ctx, cudaMalloc(&ctx->dNodes, sizeof(plt::BvhNode) * nodes.size()));
+    PLT_CUDA(ctx, cudaMemcpy(ctx->dNodes, nodes.data(), sizeof(plt::BvhNode) * nodes.size(), cudaMemcpyHostToDevice));
+    if (nTris) {
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dTris, sizeof(float4) * tris.size()));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dTris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice));
+        std::vector<uint32_t> mat(nTris, 0u);
+        if (material) std::memcpy(mat.data(), material, sizeof(uint32_t) * nTris);
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dTriMaterial, sizeof(uint32_t) * nTris));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dTriMaterial, mat.data(), sizeof(uint32_t) * nTris, cudaMemcpyHostToDevice));
+    }
+    ctx->nTris = nTris;
+    ctx->bvhStats = st;
+    return PLT_OK;
+}
+
+static plt_status traceCommon(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, uint32_t* occluded, bool any, void* stream) {
+    if (!ctx || !rays) return PLT_INVALID_ARG;
+    if (!ctx->dNodes) return PLT_INVALID_ARG;  // no scene
+    if (rays->n == 0) return PLT_OK;
+    if (!rays->origin || !rays->dir) return PLT_INVALID_ARG;
+    if (any ? !occluded : (!hits || !hits->prim)) return PLT_INVALID_ARG;
+    plt::TraceParams p{};
+    p.n = rays->n;
+    p.origin = rays->origin;
+    p.dir = rays->dir;
+    p.tmin = rays->tmin;
+    p.tmax = rays->tmax;
+    p.nodes = ctx->dNodes;
+    p.tris = ctx->dTris;
+    if (!any) {
+        p.prim = hits->prim;
+        p.t = hits->t;
+        p.bary = hits->bary;
+    }
+    p.occluded = occluded;
+    p.stats = reinterpret_cast<unsigned long long*>(rays->stats);
+    p.status = ctx->dStatus;
+    const cudaError_t e = plt::launchTrace(p, any, ctx->numSMs, (cudaStream_t)stream);
+    return e == cudaSuccess ? PLT_OK : cudaFail(ctx, e);
+}
+
+plt_status plt_trace_closest(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, void* stream) {
+    return traceCommon(ctx, rays, hits, nullptr, false, stream);
+}
+plt_status plt_trace_any(plt_context* ctx, const plt_rays* rays, uint32_t* occluded, void* stream) {
+    return traceCommon(ctx, rays, nullptr, occluded, true, stream);
+}
+plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4) {
+    if (!ctx || !out4) return PLT_INVALID_ARG;
+    out4[0] = ctx->bvhStats.nodes;
+    out4[1] = ctx->bvhStats.leaves;
+    out4[2] = ctx->bvhStats.maxDepth;
+    out4[3] = ctx->nTris;
+    return PLT_OK;
+}
+
 // Synchronises the stream and converts the device status word of the context (accumulated by
 // every launch since the last check) into a status, then clears it.
 plt_status plt_check_status(plt_context* ctx, void* stream) {
@@ -231,7 +333,7 @@ plt_status plt_check_status(plt_context* ctx, void* stream) {
     PLT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
     PLT_CUDA(ctx, cudaMemcpy(&st, ctx->dStatus, sizeof(st), cudaMemcpyDeviceToHost));
     PLT_CUDA(ctx, cudaMemset(ctx->dStatus, 0, sizeof(st)));
-    if (st & plt::kStatusCopyTimeout) return PLT_QUEUE_TIMEOUT;
+    if (st & (plt::kStatusCopyTimeout | plt::kStatusStackOverflow)) return PLT_QUEUE_TIMEOUT;
     if (st & (plt::kStatusBadMaterialId | plt::kStatusUnknownType)) return PLT_BAD_MATERIAL;
     if (st & plt::kStatusNanInput) return PLT_NAN_INPUT;
     return PLT_OK;

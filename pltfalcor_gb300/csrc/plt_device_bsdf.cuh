@@ -178,7 +178,7 @@ PLT_DI Alpha fracAlpha(const float* __restrict__ p, f3 wi, f3 wo, float k) {
     return alphaOf(sqr((fabsf(wi.z) + fabsf(wo.z)) * __ldg(p + PF_Q) * k));
 }
 PLT_NI float fracPGF(const float* __restrict__ p, float zx, float zy) {
-    const float f = 1.f / powf(1.f + __ldg(p + PF_T) * (zx * zx + zy * zy), __ldg(p + PF_EXPO));
+    const float f = 1.f / powPos(1.f + __ldg(p + PF_T) * (zx * zx + zy * zy), __ldg(p + PF_EXPO));
     return __ldg(p + PF_C) * f;
 }
 PLT_NI f3 fracSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {

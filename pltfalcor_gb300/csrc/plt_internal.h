@@ -18,6 +18,25 @@ constexpr uint32_t kStatusBadMaterialId = 0x1u;
 constexpr uint32_t kStatusNanInput = 0x2u;
 constexpr uint32_t kStatusUnknownType = 0x4u;
 constexpr uint32_t kStatusCopyTimeout = 0x8u;
+constexpr uint32_t kStatusStackOverflow = 0x10u;
+
+// One batch of ray queries against the context's BVH (device pointers).
+struct TraceParams {
+    uint32_t n;
+    const float* origin;          // [3][n]
+    const float* dir;             // [3][n]
+    const float* tmin;            // [n] or null
+    const float* tmax;            // [n] or null
+    const void* nodes;            // BvhNode[]
+    const float4* tris;           // 3 float4 per triangle in leaf order; v0.w holds the triangle id bits
+    uint32_t* prim;               // closest hit: [n]
+    float* t;                     // closest hit: [n] or null
+    float* bary;                  // closest hit: [2][n] or null
+    uint32_t* occluded;           // any hit: [n]
+    unsigned long long* stats;    // [2] node visits, triangle tests, or null
+    uint32_t* status;
+};
+cudaError_t launchTrace(const TraceParams& p, bool any, int numSMs, cudaStream_t stream);
 
 struct BatchParams {
     plt_bsdf_queries q;

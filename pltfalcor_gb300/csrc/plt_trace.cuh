@@ -1,0 +1,83 @@
+// BVH traversal on sm_103a (GB300 has no RT cores): closest-hit and any-hit queries against the
+// host-built SAH BVH.  Intersection is the reference's watertight ray/triangle test
+// (Source/Falcor/Utils/Geometry/IntersectionHelpers.slang:102-166 in ssteinberg/PLTFalcor), written
+// with explicitly rounded operations (__fmul_rn etc. are never contracted into FMAs) so hits,
+// distances and barycentrics are bit-identical to a CPU evaluation of the same expressions.
+// Ties at equal distance resolve to the lowest primitive index, the brute-force oracle's rule.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "plt_bvh.h"
+
+namespace pltdev {
+
+struct TriHit {
+    float t, b1, b2;   // distance, barycentrics of vertices 1 and 2
+    bool hit;
+};
+
+// intersectRayTriangle with a rounding-exact evaluation; A = v0 - o etc.
+__device__ __forceinline__ TriHit watertight(float ox, float oy, float oz, float dx, float dy, float dz, float4 v0, float4 v1, float4 v2) {
+    TriHit h;
+    h.hit = false;
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    int kz = 0;
+    if (ay > ax && ay > az) kz = 1;
+    if (az > ax && az > ay) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    const float dkz = kz == 0 ? dx : (kz == 1 ? dy : dz);
+    if (dkz < 0.f) { const int s = kx; kx = ky; ky = s; }
+    const float dkx = kx == 0 ? dx : (kx == 1 ? dy : dz);
+    const float dky = ky == 0 ? dx : (ky == 1 ? dy : dz);
+    const float Sx = __fdiv_rn(dkx, dkz);
+    const float Sy = __fdiv_rn(dky, dkz);
+    const float Sz = __fdiv_rn(1.f, dkz);
+    const float A[3] = {__fsub_rn(v0.x, ox), __fsub_rn(v0.y, oy), __fsub_rn(v0.z, oz)};
+    const float B[3] = {__fsub_rn(v1.x, ox), __fsub_rn(v1.y, oy), __fsub_rn(v1.z, oz)};
+    const float C[3] = {__fsub_rn(v2.x, ox), __fsub_rn(v2.y, oy), __fsub_rn(v2.z, oz)};
+    auto pick = [](const float* v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); };
+    const float Akz = pick(A, kz), Bkz = pick(B, kz), Ckz = pick(C, kz);
+    const float Ax = __fsub_rn(pick(A, kx), __fmul_rn(Sx, Akz));
+    const float Ay = __fsub_rn(pick(A, ky), __fmul_rn(Sy, Akz));
+    const float Bx = __fsub_rn(pick(B, kx), __fmul_rn(Sx, Bkz));
+    const float By = __fsub_rn(pick(B, ky), __fmul_rn(Sy, Bkz));
+    const float Cx = __fsub_rn(pick(C, kx), __fmul_rn(Sx, Ckz));
+    const float Cy = __fsub_rn(pick(C, ky), __fmul_rn(Sy, Ckz));
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f) {
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return h;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f) return h;
+    const float Az = __fmul_rn(Sz, Akz), Bz = __fmul_rn(Sz, Bkz), Cz = __fmul_rn(Sz, Ckz);
+    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    const float rcp = __fdiv_rn(1.f, det);
+    h.t = __fmul_rn(T, rcp);
+    h.b1 = __fmul_rn(V, rcp);
+    h.b2 = __fmul_rn(W, rcp);
+    h.hit = true;
+    return h;
+}
+
+// Conservative slab test: entry/exit with the exit widened by 1 + 2^-21 (covers the rounding
+// of the slab products), so a box containing an accepted triangle hit is never culled.
+__device__ __forceinline__ bool slab(const float* mn, const float* mx, float ox, float oy, float oz, float ix, float iy, float iz,
+                                     float tmin, float tmax, float& tenter) {
+    const float tx0 = (mn[0] - ox) * ix, tx1 = (mx[0] - ox) * ix;
+    const float ty0 = (mn[1] - oy) * iy, ty1 = (mx[1] - oy) * iy;
+    const float tz0 = (mn[2] - oz) * iz, tz1 = (mx[2] - oz) * iz;
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax)) * 1.000000477f;
+    tenter = tn;
+    return tn <= tf;
+}
+
+}  // namespace pltdev

@@ -1,0 +1,163 @@
+"""Seeded procedural scenes for the traversal and path-tracing workloads.
+
+`procedural_scene` builds the path-tracing test scene: a closed, subdivided box (the room),
+`n_spheres` subdivided icospheres, `n_quads` randomly placed and oriented quads, one emissive
+quad (PLTDiffuse with a spectral emission profile) under the ceiling and one smooth PLTDielectric
+sphere (roughness 0, so manifold NEE applies) below it.  With the defaults (200 level-4
+icospheres, 500 quads, 32x32 box faces) it holds about 1.04 M triangles.  Every other object gets a
+material drawn uniformly from the eight PLT types with the mixed-material batch's parameter
+ranges.  All randomness comes from the library's counter-based generator (workloads.CounterRNG),
+so the scene is identical on every host.
+"""
+import numpy as np
+
+from . import materials as M
+from .workloads import CounterRNG, mixed_material_records
+
+
+def icosphere(level):
+    """Unit icosphere: 20 * 4^level triangles."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    f = np.array([[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6],
+                  [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11], [6, 2, 10],
+                  [8, 6, 7], [9, 8, 1]], np.int64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    for _ in range(level):
+        edges = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+        uniq, inv = np.unique(edges, axis=0, return_inverse=True)
+        mids = v[uniq[:, 0]] + v[uniq[:, 1]]
+        mids /= np.linalg.norm(mids, axis=1, keepdims=True)
+        m = inv.reshape(3, -1).T + len(v)
+        v = np.concatenate([v, mids])
+        a, b, c = f[:, 0], f[:, 1], f[:, 2]
+        ab, bc, ca = m[:, 0], m[:, 1], m[:, 2]
+        f = np.concatenate([np.stack([a, ab, ca], 1), np.stack([b, bc, ab], 1), np.stack([c, ca, bc], 1), np.stack([ab, bc, ca], 1)])
+    return v, f
+
+
+def grid_quad(corner, e1, e2, n):
+    """n x n subdivided parallelogram corner + s e1 + t e2."""
+    s = np.linspace(0.0, 1.0, n + 1)
+    ss, tt = np.meshgrid(s, s, indexing="ij")
+    v = corner[None, None, :] + ss[..., None] * e1[None, None, :] + tt[..., None] * e2[None, None, :]
+    v = v.reshape(-1, 3)
+    idx = lambda i, j: i * (n + 1) + j
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    f = np.concatenate([np.stack([idx(i, j), idx(i + 1, j), idx(i + 1, j + 1)], 1), np.stack([idx(i, j), idx(i + 1, j + 1), idx(i, j + 1)], 1)])
+    return v, f
+
+
+class Scene:
+    """Triangle soup with per-triangle material indices, material records and light data."""
+
+    def __init__(self, vertices, indices, tri_material, records, emissive_tris, light_material, mnee_material, bounds):
+        self.vertices = np.ascontiguousarray(vertices, np.float32)
+        self.indices = np.ascontiguousarray(indices, np.uint32)
+        self.tri_material = np.ascontiguousarray(tri_material, np.uint32)
+        self.records = records
+        self.emissive_tris = np.asarray(emissive_tris, np.uint32)
+        self.light_material = light_material
+        self.mnee_material = mnee_material
+        self.bounds = bounds
+
+    @property
+    def n_tris(self):
+        return len(self.indices)
+
+    def triangle_vertices(self):
+        """[n_tris][9] vertex coordinates."""
+        return np.ascontiguousarray(self.vertices[self.indices].reshape(-1, 9))
+
+
+def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_subdiv=32, room=10.0, emission_id=8):
+    rng = CounterRNG(seed, max(n_spheres, n_quads, 1) * 16)
+    u = lambda: rng.uniform().astype(np.float64)
+    per_type = 512
+    recs = mixed_material_records(per_type=per_type, seed=seed)
+    # extra materials: the emitter, the smooth dielectric sphere, the room walls
+    light = M.diffuse(1, albedo=(0.8, 0.8, 0.8), emission_id=emission_id)
+    glass = M.dielectric(1, 0.0, ior=1.5, dispersion_b=0.0042)
+    wall = M.opaque_dielectric(1, 0.3, albedo=(0.7, 0.7, 0.7))
+    records = np.concatenate([recs, light, glass, wall])
+    light_mat, glass_mat, wall_mat = len(recs), len(recs) + 1, len(recs) + 2
+    verts, faces, mats = [], [], []
+    nv = 0
+
+    def add(v, f, m):
+        nonlocal nv
+        verts.append(v)
+        faces.append(f + nv)
+        mats.append(np.full(len(f), m, np.uint32))
+        nv += len(v)
+
+    # room: six subdivided faces of [-room, room]^3
+    R = room
+    corners = [(np.array([-R, -R, -R]), np.array([2 * R, 0, 0]), np.array([0, 2 * R, 0])),
+               (np.array([-R, -R, R]), np.array([0, 2 * R, 0]), np.array([2 * R, 0, 0])),
+               (np.array([-R, -R, -R]), np.array([0, 0, 2 * R]), np.array([2 * R, 0, 0])),
+               (np.array([-R, R, -R]), np.array([2 * R, 0, 0]), np.array([0, 0, 2 * R])),
+               (np.array([-R, -R, -R]), np.array([0, 2 * R, 0]), np.array([0, 0, 2 * R])),
+               (np.array([R, -R, -R]), np.array([0, 0, 2 * R]), np.array([0, 2 * R, 0]))]
+    for c, e1, e2 in corners:
+        v, f = grid_quad(c, e1, e2, box_subdiv)
+        add(v, f, wall_mat)
+    # area light under the ceiling (z = +R is the ceiling)
+    v, f = grid_quad(np.array([-1.5, -1.5, R - 0.05]), np.array([3.0, 0, 0]), np.array([0, 3.0, 0]), 1)
+    first_emissive = sum(len(x) for x in faces)
+    add(v, f, light_mat)
+    emissive = np.arange(first_emissive, first_emissive + len(f))
+    # smooth dielectric sphere below the light (manifold NEE occluder)
+    sv, sf = icosphere(min(sphere_level, 4))
+    add(sv * 1.2 + np.array([0.0, 0.0, R - 4.0]), sf, glass_mat)
+    # random icospheres
+    cx, cy, cz, rad, mt, mi = u(), u(), u(), u(), u(), u()
+    for s in range(n_spheres):
+        r = 0.25 + 0.75 * rad[s]
+        c = np.array([(2 * cx[s] - 1) * (R - 1.5), (2 * cy[s] - 1) * (R - 1.5), (2 * cz[s] - 1) * (R - 6.0) - 1.0])
+        t = min(int(mt[s] * 8), 7)
+        add(sv * r + c, sf, t * per_type + min(int(mi[s] * per_type), per_type - 1))
+    # random quads
+    qx, qy, qz, qa, qb, qs, qt, qm = u(), u(), u(), u(), u(), u(), u(), u()
+    for q in range(n_quads):
+        c = np.array([(2 * qx[q] - 1) * (R - 1.0), (2 * qy[q] - 1) * (R - 1.0), (2 * qz[q] - 1) * (R - 5.0) - 1.0])
+        th, ph = np.pi * qa[q], 2 * np.pi * qb[q]
+        nrm = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+        e1 = np.cross(nrm, [0.0, 0.0, 1.0] if abs(nrm[2]) < 0.9 else [1.0, 0.0, 0.0])
+        e1 /= np.linalg.norm(e1)
+        e2 = np.cross(nrm, e1)
+        size = 0.5 + 1.5 * qs[q]
+        v, f = grid_quad(c - 0.5 * size * (e1 + e2), size * e1, size * e2, 1)
+        t = min(int(qt[q] * 8), 7)
+        add(v, f, t * per_type + min(int(qm[q] * per_type), per_type - 1))
+    V = np.concatenate(verts).astype(np.float32)
+    F = np.concatenate(faces).astype(np.uint32)
+    Mt = np.concatenate(mats)
+    return Scene(V, F, Mt, records, emissive, light_mat, glass_mat, (-R, R))
+
+
+def random_rays(n, seed, bounds, scene_tris=None):
+    """n rays from random points inside the bounds in uniformly random directions; a fifth of them
+    aimed exactly at triangle vertices or edge midpoints of `scene_tris` (watertightness)."""
+    rng = CounterRNG(seed, n)
+    lo, hi = bounds
+    o = np.stack([lo + (hi - lo) * rng.uniform().astype(np.float64) for _ in range(3)])
+    z = 2 * rng.uniform().astype(np.float64) - 1
+    ph = 2 * np.pi * rng.uniform().astype(np.float64)
+    s = np.sqrt(np.maximum(0, 1 - z * z))
+    d = np.stack([s * np.cos(ph), s * np.sin(ph), z])
+    if scene_tris is not None:
+        k = rng.uniform().astype(np.float64)
+        sel = k < 0.2
+        pick = (rng.uniform().astype(np.float64) * len(scene_tris)).astype(np.int64) % len(scene_tris)
+        which = (rng.uniform().astype(np.float64) * 6).astype(np.int64)
+        tv = scene_tris[pick].reshape(-1, 3, 3).astype(np.float64)
+        a, b, c = tv[:, 0], tv[:, 1], tv[:, 2]
+        targets = np.select([which[:, None] == 0, which[:, None] == 1, which[:, None] == 2, which[:, None] == 3, which[:, None] == 4],
+                            [a, b, c, 0.5 * (a + b), 0.5 * (b + c)], 0.5 * (c + a))
+        dd = targets.T - o
+        dd /= np.maximum(np.linalg.norm(dd, axis=0, keepdims=True), 1e-12)
+        d = np.where(sel[None, :], dd, d)
+    return np.ascontiguousarray(o.astype(np.float32).reshape(-1)), np.ascontiguousarray(d.astype(np.float32).reshape(-1))
