@@ -117,8 +117,10 @@ PLT_NI FresnelD fresnel_dielectric(float cosI_, float eta) {
     const float cosI = fabsf(cosI_);
     const float cosTSqr = 1.f - (1.f - cosI * cosI) / (eta * eta);
     float cosT = sqrtf(fmaxf(0.f, cosTSqr));
-    f.rs = (cosI - eta * cosT) / (cosI + eta * cosT);
-    f.rp = (eta * cosI - cosT) / (eta * cosI + cosT);
+    // correctly rounded quotients: at total internal reflection (cosT = 0) rs = rp = x / x must be
+    // exactly 1 so that 1 - F vanishes as in the reference
+    f.rs = __fdiv_rn(cosI - eta * cosT, cosI + eta * cosT);
+    f.rp = __fdiv_rn(eta * cosI - cosT, eta * cosI + cosT);
     const float imp = sqrtf(eta * cosT / cosI);
     f.ts = imp * (f.rs + 1.f);
     f.tp = imp * (f.rp + 1.f) / eta;

@@ -83,7 +83,7 @@ __device__ __forceinline__ void traceOne(const TraceParams& P, uint32_t i, uint3
         bool found = false;
         while (sp > 0) {
             const int2 e = stack[--sp];
-            if (__int_as_float(e.y) <= bestT) { node = e.x; found = true; break; }
+            if (__int_as_float(e.y) <= bestT * kTfarScale) { node = e.x; found = true; break; }
         }
         if (!found) break;
     }

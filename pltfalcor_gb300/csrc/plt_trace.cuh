@@ -67,15 +67,20 @@ __device__ __forceinline__ TriHit watertight(float ox, float oy, float oz, float
     return h;
 }
 
-// Conservative slab test: entry/exit with the exit widened by 1 + 2^-21 (covers the rounding
-// of the slab products), so a box containing an accepted triangle hit is never culled.
+// Robust culling margin: computed slab distances carry up to ~2 ulp of relative error (Ize, "Robust
+// BVH Ray Traversal", JCGT 2013: exit * (1 + 2 gamma_3)); a box is culled only when its computed
+// entry exceeds a distance times this factor.  The same factor guards the stack-pop test against
+// the current closest hit, so a box whose face holds the hit point is never dropped.
+constexpr float kTfarScale = 1.000000477f;  // 1 + 2^-21 > 1 + 2 gamma_3 (gamma_3 = 3 u / (1 - 3 u), u = 2^-24)
+
+// Conservative slab test: entry/exit with the exit widened by kTfarScale.
 __device__ __forceinline__ bool slab(const float* mn, const float* mx, float ox, float oy, float oz, float ix, float iy, float iz,
                                      float tmin, float tmax, float& tenter) {
     const float tx0 = (mn[0] - ox) * ix, tx1 = (mx[0] - ox) * ix;
     const float ty0 = (mn[1] - oy) * iy, ty1 = (mx[1] - oy) * iy;
     const float tz0 = (mn[2] - oz) * iz, tz1 = (mx[2] - oz) * iz;
     const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax)) * 1.000000477f;
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax)) * kTfarScale;
     tenter = tn;
     return tn <= tf;
 }
