@@ -113,6 +113,66 @@ def cpu_baseline(n_sample=1 << 18, seconds=10.0, threads=None):
             "sample": "%d queries (%d-query slices of the mixed-material batch, seed 1) in %.1f s, FP32 oracle, OpenMP" % (done, n_sample, dt)}
 
 
+def camera_rays(res, pos, look, up, fov_deg):
+    """Pinhole primary rays through pixel centres (res x res), SoA planes."""
+    import numpy as np
+    w = np.asarray(look, np.float64) - np.asarray(pos, np.float64)
+    w /= np.linalg.norm(w)
+    u = np.cross(w, up)
+    u /= np.linalg.norm(u)
+    v = np.cross(u, w)
+    th = np.tan(np.radians(fov_deg) / 2)
+    px = (np.arange(res) + 0.5) / res * 2 - 1
+    X, Y = np.meshgrid(px, -px)
+    d = w[:, None] + th * (X.ravel()[None, :] * u[:, None] + Y.ravel()[None, :] * v[:, None])
+    d /= np.linalg.norm(d, axis=0, keepdims=True)
+    o = np.repeat(np.asarray(pos, np.float64)[:, None], res * res, axis=1)
+    return np.ascontiguousarray(o.astype(np.float32).reshape(-1)), np.ascontiguousarray(d.astype(np.float32).reshape(-1))
+
+
+def trace_bench(ctx, dev, stream, steps, warmup):
+    """Closest-hit traversal on the 1.04 M-triangle procedural scene: 1024^2 pinhole primary rays
+    and 2^20 rays from random points in random directions.  Algorithmic bytes per ray = BVH node
+    visits x 64 B + triangle tests x 48 B, counted by the kernel in a separate untimed launch."""
+    import torch
+    from pltfalcor_gb300 import scene as S
+    sc = S.procedural_scene()
+    t0 = time.perf_counter()
+    ctx.set_scene(sc.vertices, sc.indices, sc.tri_material)
+    build_s = time.perf_counter() - t0
+    st = ctx.scene_stats()
+    out = {"scene": "procedural room: box + 200 level-4 icospheres + 500 quads + light + glass sphere (seed 2)",
+           "triangles": sc.n_tris, "bvh_nodes": st["nodes"], "bvh_max_depth": st["max_depth"], "bvh_build_s_host": build_s}
+    sets = {"primary_1024x1024": camera_rays(1024, (0.0, -9.5, 0.0), (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 60.0),
+            "random_1M": S.random_rays(1 << 20, 13, sc.bounds)}
+    for name, (o, d) in sets.items():
+        n = len(o) // 3
+        go, gd = torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev)
+        prim = torch.zeros(n, dtype=torch.int32, device=dev)
+        t = torch.zeros(n, dtype=torch.float32, device=dev)
+        bary = torch.zeros(2 * n, dtype=torch.float32, device=dev)
+        stats = torch.zeros(2, dtype=torch.int64, device=dev)
+        ctx.trace_closest(ctx.rays(go, gd, None, None, stats), prim, t, bary, stream)
+        torch.cuda.synchronize()
+        nv, tt = [int(x) for x in stats.cpu()]
+        r = ctx.rays(go, gd)
+        for _ in range(warmup):
+            ctx.trace_closest(r, prim, t, bary, stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.trace_closest(r, prim, t, bary, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        bpr = (nv * 64 + tt * 48) / n + 12 * 2 + 16  # + ray in (24 B) + hit out (prim, t, bary: 16 B)
+        out[name] = {"rays": n, "ms_per_launch": ms, "rays_per_s": n / (ms * 1e-3), "node_visits_per_ray": nv / n,
+                     "tri_tests_per_ray": tt / n, "algorithmic_bytes_per_ray": bpr,
+                     "achieved_gbs": bpr * n / (ms * 1e-3) / 1e9, "miss_frac": float((prim == -1).float().mean().item())}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -270,6 +330,8 @@ def run_ours(args):
                            "parallelism": "independent shards per GPU" if world > 1 else "1 GPU"},
                 "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": args.steps, "roofline": roof, "clocks": clocks}
+        if not args.no_trace:
+            line["trace"] = trace_bench(ctx, dev, stream, max(3, min(args.steps, 50)), max(1, args.warmup))
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         print(json.dumps(line))
@@ -286,6 +348,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-trace", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

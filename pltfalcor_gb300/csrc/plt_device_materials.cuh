@@ -733,8 +733,13 @@ PLT_NI float mlRecursion(float sqrtm00, uint32_t layers, MLLayer l0, MLLayer l1,
         const RT nx = R + x, ny = y;
         const RT dx = (RT)1 + x * R, dy = y * R;
         const RT n = dx * dx + dy * dy;
-        gx = (nx * dx + ny * dy) / n;
-        gy = (ny * dx - nx * dy) / n;
+        if constexpr (sizeof(RT) == 8) {
+            gx = (nx * dx + ny * dy) / n;
+            gy = (ny * dx - nx * dy) / n;
+        } else {  // correctly rounded: the recursion amplifies quotient errors near resonances
+            gx = __fdiv_rn(nx * dx + ny * dy, n);
+            gy = __fdiv_rn(ny * dx - nx * dy, n);
+        }
     }
     return (float)(gx * gx);
 }

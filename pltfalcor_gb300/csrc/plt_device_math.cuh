@@ -77,10 +77,11 @@ PLT_DI f4 operator*(float s, f4 a) { return {s * a.x, s * a.y, s * a.z, s * a.w}
 // complex numbers as f2
 PLT_DI f2 cmul(f2 a, f2 b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 PLT_DI float cnorm2(f2 z) { return z.x * z.x + z.y * z.y; }
+// complex quotients keep correct rounding: they feed the conductor Fresnel and resonant recursions
 PLT_DI f2 cdiv(f2 a, f2 b) {
     const float n = cnorm2(b);
     const f2 c = cmul(a, f2{b.x, -b.y});
-    return {c.x / n, c.y / n};
+    return {__fdiv_rn(c.x, n), __fdiv_rn(c.y, n)};
 }
 PLT_DI f2 csqrt(f2 z) {
     const float r = sqrtf(cnorm2(z));

@@ -22,9 +22,9 @@ def main():
     prof, _ = spectra.standard_profiles()
     for name, wl in golden_cases.cases(prof).items():
         out = {}
-        # FP32, FP64 and FP32 with random rounding (seed 1)
-        for tag, prec in (("fp32", 32), ("fp64", 64), ("rr", 16)):
-            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=1)
+        # FP32, FP64 and FP32 with random rounding (seeds 1 and 2)
+        for tag, prec, seed in (("fp32", 32, 1), ("fp64", 64, 1), ("rr", 16, 1), ("rr2", 16, 2)):
+            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=seed)
             for k, v in res.items():
                 out["%s_%s" % (k, tag)] = v
         path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")

@@ -3,7 +3,7 @@
 Tolerance (FP32 GPU vs the FP32 oracle, the reference arithmetic type), per query:
 
     err(gpu, oracle32) <= max(TOL, K * cond),   TOL = 1e-4, K = 10,
-    cond = max(err(oracle32, oracle64), err(oracle32, oracle32 with random rounding))
+    cond = max(err(oracle32, oracle64), err(oracle32, oracle32 with random rounding, seeds 1 and 2))
 
 where err is the relative error below.  `cond` is the conditioning allowance: where the FP32
 reference arithmetic is itself ill-conditioned (1 - alpha with alpha -> 1 on smooth surfaces,
@@ -69,9 +69,11 @@ def errors(a, ref, n, hwss, ops):
 
 def compare(gpu, ora32, n, hwss, ops, ora64=None, ora32_rr=None):
     """Errors of the GPU against the FP32 oracle, with the per-query allowance derived from the
-    FP32 oracle's own error against the FP64 oracle and its random-rounding spread (when given)."""
+    FP32 oracle's own error against the FP64 oracle and its random-rounding spread (when given;
+    `ora32_rr` may be one run or a list of runs with different seeds)."""
     e = errors(gpu, ora32, n, hwss, ops)
-    refs = [r for r in (ora64, ora32_rr) if r is not None]
+    rr = ora32_rr if isinstance(ora32_rr, (list, tuple)) else [ora32_rr]
+    refs = [r for r in [ora64] + rr if r is not None]
     if refs:
         cs = [errors(ora32, r, n, hwss, ops) for r in refs]
         for k in list(e):

@@ -170,8 +170,8 @@ def test_oracle_matches_golden_fixture(profiles):
     import golden_cases
     for name, wl in golden_cases.cases(prof).items():
         ref = np.load(os.path.join(GOLDEN, name + ".npz"))
-        for tag, prec in (("fp32", 32), ("fp64", 64), ("rr", 16)):
-            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=1)
+        for tag, prec, seed in (("fp32", 32, 1), ("fp64", 64, 1), ("rr", 16, 1), ("rr2", 16, 2)):
+            res = oracle.run(wl, ops=0xF, precision=prec, sr_seed=seed)
             for k, v in res.items():
                 r = ref["%s_%s" % (k, tag)]
                 if v.dtype == np.uint32:
