@@ -49,7 +49,8 @@ typedef enum plt_status {
     PLT_NAN_INPUT = 4,
     PLT_CUDA_ERROR = 5,
     PLT_NOT_SUPPORTED = 6,
-    PLT_BAD_MATERIAL = 7
+    PLT_BAD_MATERIAL = 7,
+    PLT_TOO_LARGE = 8
 } plt_status;
 
 /* MaterialType ids, Source/Falcor/Scene/Material/MaterialTypes.slang:36-53 */
@@ -270,6 +271,23 @@ plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4);
  * Mirrors the reference's
  * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
 plt_status plt_check_status(plt_context* ctx, void* stream);
+
+/* Largest batch plt_bsdf_batch_noalloc accepts. */
+#define PLT_NOALLOC_MAX_QUERIES (1u << 20)
+
+/* plt_bsdf_batch for callers that must not allocate device memory -- for example a renderer's
+ * per-frame loop running under a fixed memory budget, or a host application that owns all device
+ * allocations and forbids libraries to call cudaMalloc (which can synchronise the device and fail
+ * under memory pressure).  It has no counterpart in the reference, whose shaders run inside the
+ * graphics API's own memory management.  Same arguments and results as plt_bsdf_batch; the
+ * batch's sorting scratch lives in a fixed device array of the library (about 2 MB per GPU, held
+ * until exit) instead of context memory, so the call itself allocates nothing.
+ * Limits: queries->n <= PLT_NOALLOC_MAX_QUERIES, else PLT_TOO_LARGE (nothing launched).  The
+ * first call on each device resolves the array's device address (set-up); make that first call
+ * before starting any stream capture.  Calls share the array: calls that overlap on the GPU race,
+ * so serialise them on one stream. */
+plt_status plt_bsdf_batch_noalloc(plt_context* ctx, const plt_bsdf_queries* queries,
+                                  const plt_bsdf_results* results, uint32_t ops, void* stream);
 
 /* Single-op conveniences over plt_bsdf_batch. */
 plt_status plt_bsdf_eval(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* stream);

@@ -78,8 +78,11 @@ EXPORTED_SYMBOLS = [
     "plt_abi_version", "plt_status_string", "plt_options_default", "plt_create", "plt_destroy",
     "plt_last_cuda_error", "plt_set_spectral_profiles", "plt_set_materials", "plt_spectral_profile_from_samples",
     "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
-    "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats",
+    "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats", "plt_bsdf_batch_noalloc",
 ]
+NOALLOC_MAX_QUERIES = 1 << 20
+PLT_TOO_LARGE = 8
+STATUS_NAMES[PLT_TOO_LARGE] = "PLT_TOO_LARGE"
 
 _lib = None
 
@@ -114,6 +117,7 @@ def load_library(path=LIB_PATH):
         "plt_trace_closest": (i32, [vp, C.POINTER(Rays), C.POINTER(Hits), vp]),
         "plt_trace_any": (i32, [vp, C.POINTER(Rays), vp, vp]),
         "plt_scene_stats": (i32, [vp, C.POINTER(C.c_uint32)]),
+        "plt_bsdf_batch_noalloc": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

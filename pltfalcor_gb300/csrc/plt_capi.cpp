@@ -62,6 +62,7 @@ const char* plt_status_string(plt_status s) {
     case PLT_CUDA_ERROR: return "CUDA error";
     case PLT_NOT_SUPPORTED: return "not supported";
     case PLT_BAD_MATERIAL: return "bad material";
+    case PLT_TOO_LARGE: return "batch larger than the allocation-free scratch capacity";
     }
     return "unknown status";
 }
@@ -227,6 +228,43 @@ plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt
     if (e != cudaSuccess) return cudaFail(ctx, e);
     return PLT_OK;
 }
+
+}  // extern "C"
+
+plt_status plt::fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops,
+                                plt::BatchParams* out, int* numSMs) {
+    if (!ctx || !q || !r || !out || !numSMs) return PLT_INVALID_ARG;
+    if (q->hwss < 1 || q->hwss > PLT_MAX_HWSS) return PLT_INVALID_ARG;
+    if (q->hwss > 4 && q->hwss != 8) return PLT_NOT_SUPPORTED;
+    if (ops == 0 || (ops & ~0xFu)) return PLT_INVALID_ARG;
+    if (q->n > 0) {
+        if (!q->material || !q->v || !q->w || !q->wavelengths || !q->stokes || !q->coherence) return PLT_INVALID_ARG;
+        if (ctx->nMats == 0) return PLT_INVALID_ARG;
+        const void* ins[] = {q->material, q->v, q->w, q->lobe, q->wavelengths, q->stokes, q->coherence, q->beam_t};
+        for (const void* ptr : ins)
+            if (ptr && !aligned16(ptr)) return PLT_INVALID_ARG;
+        const void* outs[] = {r->stokes, r->coherence, r->beam_t, r->pdf, r->lambda_pdf, r->sample_wo, r->sample_pdf,
+                              r->sample_weight, r->sample_lobe, r->sample_valid};
+        for (const void* ptr : outs)
+            if (ptr && !aligned16(ptr)) return PLT_INVALID_ARG;
+    }
+    plt::BatchParams p{};
+    p.q = *q;
+    p.r = *r;
+    p.ops = ops;
+    p.mats = ctx->dMats;
+    p.matType = ctx->dMatType;
+    p.nMats = ctx->nMats;
+    p.profiles = ctx->dProfiles;
+    p.nProfiles = ctx->nProfiles;
+    p.flags = ctx->opt.flags;
+    p.status = ctx->dStatus;
+    *out = p;
+    *numSMs = ctx->numSMs;
+    return PLT_OK;
+}
+
+extern "C" {
 
 plt_status plt_bsdf_eval(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_EVAL, s); }
 plt_status plt_bsdf_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_PDF, s); }

@@ -63,10 +63,14 @@ constexpr int kShadeThreads = 128;     // shade CTA
 constexpr int kShadeMinBlocks = PLT_SHADE_MIN_BLOCKS;
 
 // scratch bytes plt_bsdf_batch needs for n queries: the permutation, then the work counter
-inline size_t bsdfScratchBytes(uint32_t n) {
-    const size_t tiles = ((size_t)n + kBatchTile - 1) / kBatchTile;
-    return tiles * kBatchTile * sizeof(uint16_t) + 256;
+constexpr size_t bsdfScratchBytes(uint32_t n) {
+    return (((size_t)n + kBatchTile - 1) / kBatchTile) * kBatchTile * sizeof(uint16_t) + 256;
 }
+
+// Validates a plt_bsdf_batch call and fills every BatchParams field except the scratch pointers
+// (perm, unitCounter); also returns the SM count for the launch.  No allocation.
+plt_status fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops,
+                           BatchParams* out, int* numSMs);
 
 // Launches the fused BSDF batch kernel (templated on the hero-wavelength count).
 cudaError_t launchBsdfBatch(const BatchParams& p, int hwss, int numSMs, cudaStream_t stream);
