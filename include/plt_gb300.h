@@ -272,6 +272,12 @@ plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4);
  * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
 plt_status plt_check_status(plt_context* ctx, void* stream);
 
+/* Per-kernel timing of plt_bsdf_batch (a profiling aid; no counterpart in the reference, whose
+ * shaders are timed only as a whole render pass).  Each later plt_bsdf_batch
+ * on this context records the given cudaEvent_t handles (any may be NULL) on its stream: before the
+ * classify kernel, between classify and shade, and after the shade kernel.  NULLs switch it off. */
+plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* before_shade, void* after_shade);
+
 /* Largest batch plt_bsdf_batch_noalloc accepts. */
 #define PLT_NOALLOC_MAX_QUERIES (1u << 20)
 

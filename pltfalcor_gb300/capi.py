@@ -79,6 +79,7 @@ EXPORTED_SYMBOLS = [
     "plt_last_cuda_error", "plt_set_spectral_profiles", "plt_set_materials", "plt_spectral_profile_from_samples",
     "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
     "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats", "plt_bsdf_batch_noalloc",
+    "plt_set_timing_events",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PLT_TOO_LARGE = 8
@@ -118,6 +119,7 @@ def load_library(path=LIB_PATH):
         "plt_trace_any": (i32, [vp, C.POINTER(Rays), vp, vp]),
         "plt_scene_stats": (i32, [vp, C.POINTER(C.c_uint32)]),
         "plt_bsdf_batch_noalloc": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
+        "plt_set_timing_events": (i32, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -143,8 +143,10 @@ template <int H>
 cudaError_t launchBsdfBatchH(const BatchParams& p, int numSMs, cudaStream_t stream) {
     const uint32_t nTiles = (p.q.n + kBatchTile - 1) / kBatchTile;
     if (nTiles == 0) return cudaSuccess;
+    if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
     pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p.q.material, p.q.lobe, p.matType, p.nMats, p.q.n,
                                                                     p.perm, p.unitCounter);
+    if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
     const size_t smem = (size_t)p.nProfiles * sizeof(pltdev::DevProfile);
     static size_t cachedSmem = (size_t)-1;
     static int blocksPerSM = 1;
@@ -163,6 +165,7 @@ cudaError_t launchBsdfBatchH(const BatchParams& p, int numSMs, cudaStream_t stre
     const uint32_t gridCap = (warpsNeeded + (kShadeThreads / 32) - 1) / (kShadeThreads / 32);
     if (grid > gridCap) grid = gridCap;
     pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
+    if (p.timing[2]) cudaEventRecord((cudaEvent_t)p.timing[2], stream);
     return cudaGetLastError();
 }
 

@@ -30,6 +30,7 @@ struct plt_context {
     uint32_t nTris = 0;
     plt::BvhBuildStats bvhStats{};
     int lastCudaError = 0;
+    void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
 };
 
 namespace {
@@ -224,8 +225,17 @@ plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt
     p.nProfiles = ctx->nProfiles;
     p.flags = ctx->opt.flags;
     p.status = ctx->dStatus;
+    for (int i = 0; i < 3; ++i) p.timing[i] = ctx->timing[i];
     const cudaError_t e = plt::launchBsdfBatch(p, (int)q->hwss, ctx->numSMs, (cudaStream_t)stream);
     if (e != cudaSuccess) return cudaFail(ctx, e);
+    return PLT_OK;
+}
+
+plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* before_shade, void* after_shade) {
+    if (!ctx) return PLT_INVALID_ARG;
+    ctx->timing[0] = before_classify;
+    ctx->timing[1] = before_shade;
+    ctx->timing[2] = after_shade;
     return PLT_OK;
 }
 

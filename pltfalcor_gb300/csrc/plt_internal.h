@@ -51,6 +51,9 @@ struct BatchParams {
     uint32_t* status;
     uint16_t* perm;            // scratch: per-tile sort permutation, kBatchTile entries per tile
     uint32_t* unitCounter;     // scratch: shade kernel work counter
+    // optional cudaEvent_t handles recorded on the launch stream before the classify kernel,
+    // between the two kernels and after the shade kernel (per-kernel timing); null = not recorded
+    void* timing[3];
 };
 
 constexpr int kBatchThreads = 256;     // classify CTA
