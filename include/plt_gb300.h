@@ -107,7 +107,7 @@ typedef struct plt_spectral_profile {
  * unsupported, the constants are used. 80 bytes. */
 typedef struct plt_material_record {
     uint32_t type;                      /* plt_material_type */
-    uint32_t flags;                     /* BasicMaterialData.flags (unused by the PLT path) */
+    uint32_t flags;                     /* PLT_MATERIAL_FLAG_* (MaterialHeader bits the PLT path reads) */
     uint16_t base_color[4];
     uint16_t specular[4];
     uint16_t data1[4];
@@ -263,6 +263,48 @@ plt_status plt_trace_any(plt_context* ctx, const plt_rays* rays, uint32_t* occlu
 
 /* BVH statistics of the current scene (host pointer, 4 values: nodes, leaves, max depth, triangles). */
 plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4);
+
+/* Per-vertex shading attributes of the current scene, StaticVertexData.normal / .tangent
+ * (Scene/SceneTypes.slang) in world space (the scene has identity instance transforms): normals
+ * [n_vertices][3] (required before plt_render), tangents [n_vertices][4] (xyz + handedness sign w;
+ * NULL = no tangent space, the shading frame is then built with perp_stark as in
+ * ShadingUtils.slang:126-153).  Host arrays, copied.  Also builds the emissive-triangle list and
+ * the power sampler's alias table from the materials set with plt_set_materials, so call it after
+ * both plt_set_scene and plt_set_materials (and again when either changes). */
+plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices);
+
+/* Material double-sidedness, MaterialHeader::isDoubleSided (Scene/Material/MaterialData.slang:126-130),
+ * carried in plt_material_record.flags; transmissive records are double-sided regardless
+ * (BasicMaterial::adjustDoubleSidedFlag, BasicMaterial.cpp:719-731). */
+#define PLT_MATERIAL_FLAG_DOUBLE_SIDED 0x1u
+
+/* Pinhole camera: the CameraData fields computeRayPinhole (Scene/Camera/Camera.slang:46-78) and
+ * the solve pass's polarizer (pltpt_solve.rt.slang:110-124) read. */
+typedef struct plt_camera {
+    float pos[3];                       /* posW */
+    float u[3], v[3], w[3];             /* cameraU, cameraV, cameraW as Falcor stores them (unnormalised) */
+    float jitter_x, jitter_y;           /* jitterX, jitterY */
+    float polarizer;                    /* polarizer intensity, 0 = none */
+    float polarizer_theta;              /* polarizer angle (rad) */
+} plt_camera;
+
+/* Renders `frame_count` frames (gFrameCount = frame_begin + f) of the PLTPT pass: per frame a sample
+ * pass (backward path construction into the bounce buffer) and a solve pass (NEE, emissive hits,
+ * forward beam replay, spectral MIS, measurement), as PLTPT::execute (PLTPT.cpp:357-499) does per
+ * tile.  out_rgba [height][width][4] (device) receives the mean of the frames' gOutputColor
+ * (AccumulatePass, scripts/PLTPathTracer.py:19).  Options come from plt_create; hwss 1-4. */
+plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width, uint32_t height, uint32_t frame_begin,
+                      uint32_t frame_count, float* out_rgba, void* stream);
+
+/* Path statistics of the last plt_render frame (host pointer, 4 values: paths, bounces recorded,
+ * shadow rays traced, forward-unwind BSDF evaluations). */
+plt_status plt_render_stats(plt_context* ctx, uint64_t* out4);
+
+/* The bounce buffer of the last plt_render frame (Path.slang BounceData per path and bounce), for
+ * inspection: host arrays [width*height][max_bounces+1] of the hit triangle (0xFFFFFFFF when the
+ * record is absent or a miss), the sampled lobe and the RayFlags word; any may be NULL.
+ * Synchronises the device. */
+plt_status plt_render_bounces(plt_context* ctx, uint32_t* prim, uint32_t* lobe, uint32_t* flags);
 
 /* Synchronises `stream`, then reports and clears the context's device status word, which every
  * launch since the previous check ORs into: PLT_BAD_MATERIAL (a material index out of range or of

@@ -164,3 +164,60 @@ def rng_stream(px, py, frame, count):
     out = (C.c_uint32 * count)()
     load().plto_rng_stream(px, py, frame, count, out)
     return np.frombuffer(out, dtype=np.uint32).copy()
+
+
+class _Scene(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("n_materials", C.c_uint32), ("n_profiles", C.c_uint32),
+                ("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("indices", C.c_void_p),
+                ("tri_material", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p)]
+
+
+def _scene_struct(scene, profiles):
+    keep = [np.ascontiguousarray(scene.vertices, np.float32), np.ascontiguousarray(scene.normals, np.float32),
+            np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
+            np.ascontiguousarray(scene.records)]
+    tan = None if getattr(scene, "tangents", None) is None else np.ascontiguousarray(scene.tangents, np.float32)
+    s = _Scene(len(keep[0]), len(keep[2]), len(keep[4]), len(profiles) if profiles is not None else 0,
+               keep[0].ctypes.data, keep[1].ctypes.data, None if tan is None else tan.ctypes.data, keep[2].ctypes.data,
+               keep[3].ctypes.data, keep[4].ctypes.data, C.cast(profiles, C.c_void_p) if profiles is not None else None)
+    return s, (keep, tan, profiles)
+
+
+def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False):
+    """FP32 oracle render of one frame: rgb [height][width][3]; with records=True also per-path bounce
+    records (prim, lobe, flags) [height*width][max_bounces+1] and stats (paths, shadow rays, evals).
+    `profiles` is a ctypes array of plt_spectral_profile, `camera`/`options` the ctypes structs of
+    include/plt_gb300.h."""
+    lib = load()
+    if not hasattr(lib, "_render_sig"):
+        lib.plto_render.restype = C.c_int
+        lib.plto_render.argtypes = [C.c_void_p] * 3 + [C.c_uint32] * 3 + [C.c_int] + [C.c_void_p] * 5
+        lib.plto_light_table.restype = C.c_uint32
+        lib.plto_light_table.argtypes = [C.c_void_p] * 4
+        lib._render_sig = True
+    s, keep = _scene_struct(scene, profiles)
+    rgb = np.zeros((height, width, 3), np.float32)
+    nb = options.max_bounces + 1
+    recs = [np.zeros((height * width, nb), np.uint32) for _ in range(3)] if records else [None] * 3
+    stats = np.zeros(3, np.uint64)
+    st = lib.plto_render(C.addressof(s), C.addressof(camera), C.addressof(options), width, height, frame,
+                         threads or os.cpu_count(), rgb.ctypes.data, *[None if r is None else r.ctypes.data for r in recs],
+                         stats.ctypes.data)
+    if st != 0:
+        raise RuntimeError("plto_render failed: %d" % st)
+    return (rgb, recs, stats) if records else rgb
+
+
+def light_table(scene, profiles):
+    """(alias [n][2] uint32, light triangles [n], inverse weight sum) as the oracle builds them."""
+    lib = load()
+    if not hasattr(lib, "_render_sig"):
+        lib.plto_light_table.restype = C.c_uint32
+        lib.plto_light_table.argtypes = [C.c_void_p] * 4
+    s, keep = _scene_struct(scene, profiles)
+    n = lib.plto_light_table(C.addressof(s), None, None, None)
+    alias = np.zeros((n, 2), np.uint32)
+    tris = np.zeros(n, np.uint32)
+    inv = C.c_float(0)
+    lib.plto_light_table(C.addressof(s), alias.ctypes.data, tris.ctypes.data, C.byref(inv))
+    return alias, tris, inv.value

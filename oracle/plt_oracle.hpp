@@ -145,6 +145,58 @@ template <class R> inline R evalSpectrum(const SceneTables& sc, uint32_t id, R l
 }
 
 // ---------------------------------------------------------------------------------------------
+// Colour: CIE XYZ multi-lobe fit and the 5-nm D65 table of the shaders (SpectrumUtils.slang:43-82)
+// ---------------------------------------------------------------------------------------------
+inline float gaussLobe(float x, float lambda, float invSigma1, float invSigma2) {
+    const float t = (x - lambda) * (x < lambda ? invSigma1 : invSigma2);
+    return std::exp(-0.5f * t * t);
+}
+inline V3<float> wavelengthToXYZ(float l) {
+    const float x = 0.362f * gaussLobe(l, 442.0f, 0.0624f, 0.0374f) + 1.056f * gaussLobe(l, 599.8f, 0.0264f, 0.0323f) -
+                    0.065f * gaussLobe(l, 501.1f, 0.0490f, 0.0382f);
+    const float y = 0.821f * gaussLobe(l, 568.8f, 0.0213f, 0.0247f) + 0.286f * gaussLobe(l, 530.9f, 0.0613f, 0.0322f);
+    const float z = 1.217f * gaussLobe(l, 437.0f, 0.0845f, 0.0278f) + 0.681f * gaussLobe(l, 459.0f, 0.0385f, 0.0725f);
+    return {x, y, z};
+}
+constexpr float kD65_5nm[69] = {49.9755f, 52.3118f, 54.6482f, 68.7015f, 82.7549f, 87.1204f, 91.486f, 92.4589f, 93.4318f, 90.057f,
+                            86.6823f, 95.7736f, 104.865f, 110.936f, 117.008f, 117.41f, 117.812f, 116.336f, 114.861f, 115.392f,
+                            115.923f, 112.367f, 108.811f, 109.082f, 109.354f, 108.578f, 107.802f, 106.296f, 104.79f, 106.239f,
+                            107.689f, 106.047f, 104.405f, 104.225f, 104.046f, 102.023f, 100.f, 98.1671f, 96.3342f, 96.0611f,
+                            95.788f, 92.2368f, 88.6856f, 89.3459f, 90.0062f, 89.8026f, 89.5991f, 88.6489f, 87.6987f, 85.4936f,
+                            83.2886f, 83.4939f, 83.6992f, 81.863f, 80.0268f, 80.1207f, 80.2146f, 81.2462f, 82.2778f, 80.281f,
+                            78.2842f, 74.0027f, 69.7213f, 70.6652f, 71.6091f, 72.979f, 74.349f, 67.9765f, 61.604f};
+inline float wavelengthToD65(float l) {
+    const float r = (l - SPEC_MIN_WL) * 0.2f;
+    const int t = int(std::ceil(r) + .5f);
+    const int b = int(std::floor(r) + .5f);
+    const float w = r - float(b);
+    return kD65_5nm[t] * w + kD65_5nm[b] * (1.0f - w);
+}
+
+// Profile colour for genSpectralProfile's sp.rgb = SpectrumUtils::toRGB_D65 (SceneBuilder.cpp:913,
+// SpectrumUtils.h:78-151): trapezoid sum over the sampled spectrum of s * xyz * D65, XYZ -> Rec.709,
+// / 10567.0762.  The colour-matching functions are the shaders' analytic fit and D65 the shaders'
+// 5-nm table, zero outside 380-720 nm (the host's 1-nm CIE tables are not restated).
+template <class SS> inline void profileRgb(float l0, float l1, size_t ns, SS ssEval, float rgb[3]) {
+    const float delta = ns > 1 ? (l1 - l0) / (float(ns) - 1.0f) : 0.f;
+    float X = 0.f, Y = 0.f, Z = 0.f;
+    for (size_t q = 0; q < ns; ++q) {
+        const float l = std::min(l0 + delta * float(q), l1);
+        const float s = ssEval(l);
+        const float d65 = (l >= SPEC_MIN_WL && l <= SPEC_MAX_WL) ? wavelengthToD65(l) : 0.f;
+        const V3<float> xyz = wavelengthToXYZ(l);
+        const float wq = s * delta * ((q == 0 || q == ns - 1) ? 0.5f : 1.0f);
+        X += xyz.x * d65 * wq;
+        Y += xyz.y * d65 * wq;
+        Z += xyz.z * d65 * wq;
+    }
+    const float k = 1.0f / 10567.0762f;
+    rgb[0] = (3.240969941904522f * X + -1.537383177570094f * Y + -0.4986107602930032f * Z) * k;
+    rgb[1] = (-0.9692436362808803f * X + 1.875967501507721f * Y + 0.04155505740717569f * Z) * k;
+    rgb[2] = (0.05563007969699373f * X + -0.2039769588889765f * Y + 1.056971514242878f * Z) * k;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Beam: PLTCoherence + PLTBeam, Rendering/PLT.slang:41-245
 // ---------------------------------------------------------------------------------------------
 template <class R> struct Beam {

@@ -222,6 +222,7 @@ int plto_spectral_profile_from_samples(const float* wl, const float* val, uint32
         return hlerp(samples[i], samples[i + 1], ww);
     };
     std::memset(sp, 0, sizeof(*sp));
+    profileRgb(l0, l1, ns, ss_eval, sp->rgb);
     sp->intensity = 1.f;
     sp->min_wavelength = std::max(l0, SPEC_MIN_WL);
     sp->max_wavelength = std::min(l1, SPEC_MAX_WL);

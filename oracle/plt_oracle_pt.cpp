@@ -1,0 +1,971 @@
+// ORACLE -- test infrastructure only.  CPU restatement of the PLTPT render pass (sample pass,
+// solve pass, light sampling, forward beam replay, measurement) of ssteinberg/PLTFalcor, used to
+// check plt_render.  FP32, brute-force ray casting with the reference's watertight test, one path
+// per pixel per frame.  Citations are to Source/RenderPasses/PLTPT/* and Source/Falcor/* in the
+// reference; every function follows the cited lines.  The scene has identity instance transforms
+// and no textures (materials read their constants), no environment map and no analytic lights, so
+// the light-type selection always picks emissive geometry (LightSampling.slangh:40-90).
+#include "plt_oracle.hpp"
+#include "plt_oracle_bsdf.hpp"
+#include "plt_oracle_geom.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <random>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace plt_oracle;
+
+namespace {
+
+using F3 = V3<float>;
+inline F3 f3(const float* p) { return {p[0], p[1], p[2]}; }
+inline void put(F3 v, float* p) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint32_t FLAG_LAST_DELTA = 0x1u, FLAG_DISPERSIVE = 0x2u, FLAG_ONLY_DELTA = 0x4u, FLAG_MISS = 0x10u,
+                   FLAG_TERMINATED = 0x20u;
+constexpr float kQcutoffForMS = .15f;               // IMaterialInstance.slang:44
+constexpr uint32_t PROP_EMISSIVE = 0x1u, PROP_TRANSMISSIVE = 0x2u, PROP_MW_REFLECTIVE = 0x4u, PROP_MW_TRANSMISSIVE = 0x8u;
+
+// Bounce record (Path.slang:113-142): the hit, the oct-encoded incident direction, sampled lobe,
+// flags, path contribution and last non-delta pdf.
+struct Bounce {
+    uint32_t prim = kNone;
+    float b1 = 0.f, b2 = 0.f;
+    float ewi[2] = {0.f, 0.f};
+    uint32_t lobe = 0, flags = 0;
+    float pathContribution = 0.f, lastNonDeltaPdf = 0.f;
+    F3 wi() const { float n[3]; geom::octToNdirEqualArea(ewi, n); return f3(n); }
+};
+
+struct Scene {
+    uint32_t nv = 0, nt = 0;
+    const float* pos = nullptr;
+    const float* nrm = nullptr;
+    const float* tan = nullptr;
+    const uint32_t* idx = nullptr;
+    const uint32_t* triMat = nullptr;
+    std::vector<Material<float>> mats;
+    std::vector<uint32_t> matFlags;
+    SceneTables tables;
+    std::vector<float> triVerts;       // [nt][9]
+    // light collection (LightCollection.cpp, EmissivePowerSampler.cpp)
+    std::vector<uint32_t> lightTri;    // light triangle -> primitive
+    std::vector<uint32_t> primToLight; // primitive -> light triangle or kNone
+    std::vector<float> lightPos;       // [nl][9]
+    std::vector<float> lightNormal;    // [nl][3] (2x16 snorm round trip)
+    std::vector<float> lightArea, lightFlux;
+    std::vector<uint32_t> alias;       // [nl][2]
+    float invWeightsSum = 0.f;
+};
+
+struct Options {
+    uint32_t maxBounces, tileSize, hwss;
+    bool hwssMis, useDirect, useEmissive, doNee, doMis, doRR, perTileSg, importanceSampleEmitters;
+    float sourcingArea, maxBeamOmega;
+};
+
+// ---------------------------------------------------------------------------------------------
+// Light collection and the power sampler's alias table
+// ---------------------------------------------------------------------------------------------
+// Emissive triangles are those of materials with an emission profile (PLTDiffuse, BasicMaterialData
+// .isEmissive(), BasicMaterialData.slang:138), in primitive order.  Face normal and area as
+// computeFaceNormalAndAreaW (Scene.slang:482-497); flux = luminance(profile rgb) * area * pi
+// (FinalizeIntegration.cs.slang:60-110).
+void buildLights(Scene& s) {
+    s.primToLight.assign(s.nt, kNone);
+    for (uint32_t t = 0; t < s.nt; ++t) {
+        const uint32_t m = s.triMat[t];
+        if (m >= s.mats.size()) continue;
+        if (s.mats[m].type != PLT_MATERIAL_DIFFUSE || s.mats[m].emission == PLT_NO_SPECTRAL_PROFILE) continue;
+        s.primToLight[t] = (uint32_t)s.lightTri.size();
+        s.lightTri.push_back(t);
+    }
+    const uint32_t nl = (uint32_t)s.lightTri.size();
+    s.lightPos.resize(9 * (size_t)nl);
+    s.lightNormal.resize(3 * (size_t)nl);
+    s.lightArea.resize(nl);
+    s.lightFlux.resize(nl);
+    for (uint32_t l = 0; l < nl; ++l) {
+        const uint32_t t = s.lightTri[l];
+        F3 p[3];
+        for (int k = 0; k < 3; ++k) {
+            p[k] = f3(s.pos + 3 * (size_t)s.idx[3 * (size_t)t + k]);
+            put(p[k], &s.lightPos[9 * (size_t)l + 3 * k]);
+        }
+        const F3 N = cross(p[1] - p[0], p[2] - p[0]);
+        const float area = 0.5f * length(N);
+        const F3 n = normalize(N);
+        const float nn[3] = {n.x, n.y, n.z};
+        geom::quantizeNormal2x16(nn, &s.lightNormal[3 * (size_t)l]);
+        s.lightArea[l] = area;
+        const uint32_t em = s.mats[s.triMat[t]].emission;
+        float rgb[3] = {0.f, 0.f, 0.f};
+        if (em < s.tables.count) for (int c = 0; c < 3; ++c) rgb[c] = std::max(0.f, s.tables.profiles[em].rgb[c]);
+        const float lum = rgb[0] * 0.2126f + rgb[1] * 0.7152f + rgb[2] * 0.0722f;
+        s.lightFlux[l] = lum * area * (float)K_PI;
+    }
+    // Alias table, EmissivePowerSampler.cpp:86-175: scaled weights, sorted small to large (stable
+    // sort here: the reference's std::sort leaves the order of equal weights unspecified), paired
+    // head/tail, entries shuffled with a default-seeded mt19937, thresholds stored as binary16.
+    const uint32_t N = nl;
+    s.alias.assign(2 * (size_t)N, 0u);
+    if (N == 0) { s.invWeightsSum = 0.f; return; }
+    std::vector<float> w(s.lightFlux);
+    double sum = 0.0;
+    for (float f : w) sum += f;
+    for (float& f : w) f *= N / float(sum);
+    std::vector<uint32_t> perm(N);
+    for (uint32_t i = 0; i < N; ++i) perm[i] = i;
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return w[a] < w[b]; });
+    std::vector<float> thr(N, 0.f);
+    std::vector<uint32_t> red(N, 0u);
+    uint32_t head = 0, tail = N - 1;
+    while (head != tail) {
+        const uint32_t i = perm[head], j = perm[tail];
+        thr[i] = w[i];
+        red[i] = j;
+        w[j] -= 1.0f - w[i];
+        if (head == tail - 1) {
+            thr[j] = 1.0f;
+            red[j] = j;
+            break;
+        } else if (w[j] < 1.0f) {
+            std::swap(perm[head], perm[tail]);
+            tail--;
+        } else {
+            head++;
+        }
+    }
+    for (uint32_t i = 0; i < N; ++i) perm[i] = i;
+    std::mt19937 rng;
+    for (uint32_t i = 0; i < N; ++i) {
+        const uint32_t dst = i + ((uint32_t)rng() % (N - i));
+        std::swap(thr[i], thr[dst]);
+        std::swap(red[i], red[dst]);
+        std::swap(perm[i], perm[dst]);
+    }
+    for (uint32_t i = 0; i < N; ++i) {
+        const uint32_t prob = (uint32_t)geom::floatToHalfRne(thr[i]) << 16u;
+        const uint32_t lx = red[i] & 0xFFFFFFu, ly = perm[i] & 0xFFFFFFu;
+        s.alias[2 * (size_t)i] = prob | ((lx >> 8u) & 0xFFFFu);
+        s.alias[2 * (size_t)i + 1] = ((lx & 0xFFu) << 24u) | ly;
+    }
+    s.invWeightsSum = 1.0f / float(sum);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Vertex and shading data
+// ---------------------------------------------------------------------------------------------
+struct VertexData {
+    F3 posW, normalW, faceNormalW;
+    float tangentW[4];
+};
+// computeVertexData, Scene.slang:530-567 (identity world matrix, front face CCW)
+VertexData vertexData(const Scene& s, uint32_t prim, float b1, float b2) {
+    const float w[3] = {1.f - b1 - b2, b1, b2};
+    VertexData v;
+    const uint32_t* I = s.idx + 3 * (size_t)prim;
+    F3 p[3];
+    for (int k = 0; k < 3; ++k) p[k] = f3(s.pos + 3 * (size_t)I[k]);
+    v.posW = p[0] * w[0];
+    v.posW = v.posW + p[1] * w[1];
+    v.posW = v.posW + p[2] * w[2];
+    F3 n = f3(s.nrm + 3 * (size_t)I[0]) * w[0];
+    n = n + f3(s.nrm + 3 * (size_t)I[1]) * w[1];
+    n = n + f3(s.nrm + 3 * (size_t)I[2]) * w[2];
+    v.normalW = normalize(n);
+    v.faceNormalW = normalize(cross(p[1] - p[0], p[2] - p[0]));
+    if (s.tan) {
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 4; ++c) t[c] = (k == 0) ? s.tan[4 * (size_t)I[0] + c] * w[0] : t[c] + s.tan[4 * (size_t)I[k] + c] * w[k];
+        const F3 tx = normalize(F3{t[0], t[1], t[2]});
+        v.tangentW[0] = tx.x; v.tangentW[1] = tx.y; v.tangentW[2] = tx.z;
+        v.tangentW[3] = geom::hsign(t[3]);
+    } else {
+        v.tangentW[0] = v.tangentW[1] = v.tangentW[2] = v.tangentW[3] = 0.f;
+    }
+    return v;
+}
+
+struct ShadingData {
+    F3 posW, V, N, T, B, faceN;
+    bool frontFacing = true;
+    uint32_t materialID = 0;
+    float opacity = 1.f;
+    F3 toLocal(F3 v) const { return {dot(v, T), dot(v, B), dot(v, N)}; }
+    F3 fromLocal(F3 v) const { return T * v.x + B * v.y + N * v.z; }
+    // ShadingData.computeNewRayOrigin, ShadingData.slang:77-80
+    F3 newRayOrigin(bool viewside = true) const {
+        const F3 n = (frontFacing == viewside) ? faceN : -faceN;
+        const float p[3] = {posW.x, posW.y, posW.z}, nn[3] = {n.x, n.y, n.z};
+        float o[3];
+        geom::computeRayOrigin(p, nn, o);
+        return f3(o);
+    }
+};
+// computeNewRayOrigin(sd, dir), ShadowRays.slangh:50-52
+F3 newRayOriginToward(const ShadingData& sd, F3 dir) {
+    const F3 n = dot(sd.faceN, dir) >= 0.f ? sd.faceN : -sd.faceN;
+    const float p[3] = {sd.posW.x, sd.posW.y, sd.posW.z}, nn[3] = {n.x, n.y, n.z};
+    float o[3];
+    geom::computeRayOrigin(p, nn, o);
+    return f3(o);
+}
+
+// MaterialHeader double-sided flag, forced on for specular or diffuse transmission > 0
+// (BasicMaterial::adjustDoubleSidedFlag, BasicMaterial.cpp:719-731)
+bool recordDoubleSided(const plt_material_record& r) {
+    return (r.flags & PLT_MATERIAL_FLAG_DOUBLE_SIDED) != 0 || half_to_float(r.specular_transmission) > 0.f ||
+           half_to_float(r.diffuse_transmission) > 0.f;
+}
+bool isDoubleSided(const Scene& s, uint32_t m) { return s.matFlags[m] != 0; }
+
+// prepareShadingData, MaterialFactory.slang:79-128 with computeTangentSpace / orthonormalizeSafe
+// (ShadingUtils.slang:126-153,243-251); opacity = evalOpacity of the PLT materials (.5 * alpha,
+// PLTDiffuse: alpha).  No normal maps.
+ShadingData prepareShadingData(const Scene& s, const VertexData& v, uint32_t materialID, F3 viewDir) {
+    ShadingData sd;
+    sd.posW = v.posW;
+    sd.V = viewDir;
+    sd.N = v.normalW;
+    const F3 t = {v.tangentW[0], v.tangentW[1], v.tangentW[2]};
+    const float NdotT = dot(t, sd.N);
+    const bool nonParallel = std::fabs(NdotT) < 0.9999f;
+    const bool nonZero = dot(t, t) > 0.f;
+    const bool valid = std::fabs(v.tangentW[3]) == 1.0f && nonZero && nonParallel;
+    if (valid) {
+        sd.T = normalize(t - sd.N * NdotT);
+        sd.B = cross(sd.N, sd.T) * v.tangentW[3];
+    } else {
+        sd.T = perp_stark(sd.N);
+        sd.B = cross(sd.N, sd.T);
+    }
+    sd.faceN = v.faceNormalW;
+    sd.frontFacing = dot(sd.V, sd.faceN) >= 0.f;
+    sd.materialID = materialID;
+    const Material<float>& m = s.mats[materialID];
+    sd.opacity = m.type == PLT_MATERIAL_DIFFUSE ? m.base[3] : .5f * m.base[3];
+    if (!sd.frontFacing && isDoubleSided(s, materialID)) sd.N = -sd.N;
+    return sd;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Material instance in world space: the IMaterialInstance wrappers (PLT*BSDF.slang), with the
+// grated materials working in the grating shading frame (DiffractionGrating.slang:83-90).
+// ---------------------------------------------------------------------------------------------
+template <class Fn> void withBx(const Material<float>& m, const SceneTables& tb, Fn&& fn) {
+    const V2<float> none = {1.f, 0.f};
+    switch (m.type) {
+    case PLT_MATERIAL_DIFFUSE: { Diffuse<float> b(m); fn(b, false, none); return; }
+    case PLT_MATERIAL_CONDUCTOR: { Conductor<float> b(m, &tb); fn(b, false, none); return; }
+    case PLT_MATERIAL_DIELECTRIC: { Dielectric<float> b(m); fn(b, false, none); return; }
+    case PLT_MATERIAL_OPAQUE_DIELECTRIC: { OpaqueDielectric<float> b(m); fn(b, false, none); return; }
+    case PLT_MATERIAL_THIN_DIELECTRIC: { ThinDielectric<float> b(m); fn(b, false, none); return; }
+    case PLT_MATERIAL_COATED_CONDUCTOR: { Coated<float, true> b(m, &tb); fn(b, false, none); return; }
+    case PLT_MATERIAL_COATED_OPAQUE_DIELECTRIC: { Coated<float, false> b(m, &tb); fn(b, false, none); return; }
+    case PLT_MATERIAL_GRATED_CONDUCTOR: { Grated<float, true> b(m, &tb); fn(b, true, b.grating.gratingX); return; }
+    case PLT_MATERIAL_GRATED_OPAQUE_DIELECTRIC: { Grated<float, false> b(m, &tb); fn(b, true, b.grating.gratingX); return; }
+    case PLT_MATERIAL_MULTILAYERED_STACK: { MultiLayer<float> b(m); fn(b, false, none); return; }
+    default: return;
+    }
+}
+
+Frame<float> sdFrame(const ShadingData& sd) { return {sd.T, sd.B, sd.N}; }
+// localGratingShadingFrame, DiffractionGrating.slang:83-90
+Frame<float> gratingSdFrame(const ShadingData& sd, V2<float> gx) {
+    Frame<float> f;
+    f.T = sd.fromLocal(F3{gx.x, gx.y, 0.f});
+    f.N = sd.N;
+    f.B = cross(f.N, f.T);
+    return f;
+}
+
+struct BSDFSample {
+    F3 wo = {0.f, 0.f, 0.f};
+    float pdf = 0.f, weight = 0.f;
+    uint32_t lobe = 0;
+};
+
+void bsdfEval(const Scene& s, const ShadingData& sd, F3 toEye, uint32_t lobe, Beam<float>& beam) {
+    withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool grated, V2<float> gx) {
+        const Frame<float> F = grated ? gratingSdFrame(sd, gx) : sdFrame(sd);
+        beam.r = F.toLocal(beam.r);
+        beam.t = F.toLocal(beam.t);
+        const F3 wiL = F.toLocal(sd.V), woL = F.toLocal(toEye);
+        beam.constructLocalFrame(woL);
+        bx.eval(wiL, woL, lobe, beam);
+        beam.transformCoherence(bx.coherenceTransform(wiL, woL, lobe));
+        beam.r = F.fromLocal(beam.r);
+        beam.t = F.fromLocal(beam.t);
+    });
+}
+bool bsdfSample(const Scene& s, const ShadingData& sd, SampleGen& sg, BSDFSample& out, float wavelength) {
+    bool valid = false;
+    withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool grated, V2<float> gx) {
+        const Frame<float> F = grated ? gratingSdFrame(sd, gx) : sdFrame(sd);
+        valid = bx.sample(F.toLocal(sd.V), out.wo, out.pdf, out.weight, out.lobe, sg, wavelength, LOBE_ALL);
+        if (valid || !grated) out.wo = F.fromLocal(out.wo);
+    });
+    return valid;
+}
+float bsdfPdf(const Scene& s, const ShadingData& sd, F3 toLight, float wavelength) {
+    float p = 0.f;
+    withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool grated, V2<float> gx) {
+        const Frame<float> F = grated ? gratingSdFrame(sd, gx) : sdFrame(sd);
+        p = bx.pdf(F.toLocal(toLight), F.toLocal(sd.V), wavelength);
+    });
+    return p;
+}
+void bsdfLambdaPdf(const Scene& s, const ShadingData& sd, F3 wo, uint32_t lobe, const Beam<float>& beamIn, float* out) {
+    withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool, V2<float>) {
+        Beam<float> b = beamIn;
+        b.r = sd.toLocal(b.r);
+        b.t = sd.toLocal(b.t);
+        bx.lambdaPdf(sd.toLocal(sd.V), sd.toLocal(wo), lobe, b, out);
+    });
+}
+
+// getProperties / getLobes of each PLT*BSDF.slang
+struct Props {
+    uint32_t flags = 0;
+    uint32_t emissionId = PLT_NO_SPECTRAL_PROFILE;
+    uint32_t lobes = 0;
+};
+Props bsdfProps(const Scene& s, uint32_t materialID) {
+    const Material<float>& m = s.mats[materialID];
+    Props p;
+    auto rough = [](float q, uint32_t deltaLobes, uint32_t scatterLobes) { return q == 0.f ? deltaLobes : (deltaLobes | scatterLobes); };
+    switch (m.type) {
+    case PLT_MATERIAL_DIFFUSE:
+        p.emissionId = m.emission;
+        p.flags = m.emission != PLT_NO_SPECTRAL_PROFILE ? PROP_EMISSIVE : 0u;
+        p.lobes = LOBE_DIFFUSE_REFLECTION;
+        break;
+    case PLT_MATERIAL_DIELECTRIC: {
+        Dielectric<float> b(m);
+        p.flags = PROP_TRANSMISSIVE | (b.gfs.q < kQcutoffForMS ? PROP_MW_TRANSMISSIVE : 0u);
+        const uint32_t dt = b.isDispersive() ? LOBE_DISPERSIVE_DELTA_TRANSMISSION : LOBE_DELTA_TRANSMISSION;
+        p.lobes = rough(b.gfs.q, LOBE_DELTA_REFLECTION | dt, LOBE_SCATTER_REFLECTION | LOBE_SCATTER_TRANSMISSION);
+        break;
+    }
+    case PLT_MATERIAL_CONDUCTOR: {
+        Conductor<float> b(m, &s.tables);
+        p.flags = b.gfs.q() < kQcutoffForMS ? PROP_MW_REFLECTIVE : 0u;
+        p.lobes = rough(b.gfs.q(), LOBE_DELTA_REFLECTION, LOBE_SCATTER_REFLECTION);
+        break;
+    }
+    case PLT_MATERIAL_OPAQUE_DIELECTRIC: {
+        OpaqueDielectric<float> b(m);
+        p.flags = b.gfs.q() < kQcutoffForMS ? PROP_MW_REFLECTIVE : 0u;
+        p.lobes = rough(b.gfs.q(), LOBE_DELTA_REFLECTION, LOBE_SCATTER_REFLECTION);
+        break;
+    }
+    case PLT_MATERIAL_COATED_CONDUCTOR:
+    case PLT_MATERIAL_COATED_OPAQUE_DIELECTRIC: {
+        Coated<float, true> b(m, &s.tables);
+        p.flags = b.gfs.q() < kQcutoffForMS ? PROP_MW_REFLECTIVE : 0u;
+        p.lobes = rough(b.gfs.q(), LOBE_DELTA_REFLECTION, LOBE_SCATTER_REFLECTION);
+        break;
+    }
+    case PLT_MATERIAL_GRATED_CONDUCTOR: {
+        Grated<float, true> b(m, &s.tables);
+        p.flags = PROP_MW_REFLECTIVE;
+        p.lobes = rough(b.baseC.gfs.q(), LOBE_DELTA_REFLECTION, LOBE_SCATTER_REFLECTION) | LOBE_DISPERSIVE_DELTA_REFLECTION;
+        break;
+    }
+    case PLT_MATERIAL_GRATED_OPAQUE_DIELECTRIC: {
+        Grated<float, false> b(m, &s.tables);
+        p.flags = PROP_MW_REFLECTIVE;
+        p.lobes = rough(b.baseD.gfs.q(), LOBE_DELTA_REFLECTION, LOBE_SCATTER_REFLECTION) | LOBE_DISPERSIVE_DELTA_REFLECTION;
+        break;
+    }
+    case PLT_MATERIAL_THIN_DIELECTRIC:
+        p.flags = PROP_TRANSMISSIVE | PROP_MW_REFLECTIVE | PROP_MW_TRANSMISSIVE;
+        p.lobes = LOBE_DELTA_REFLECTION | LOBE_DELTA_TRANSMISSION;
+        break;
+    case PLT_MATERIAL_MULTILAYERED_STACK:
+        p.flags = PROP_MW_REFLECTIVE;
+        p.lobes = LOBE_DELTA_REFLECTION;
+        break;
+    default: break;
+    }
+    return p;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Spectra: SpectrumSampler (SpectrumSampler.slang:38-54), Scene.sampleSpectrum (Scene.slang:295-330),
+// spectrumToRgb (SpectrumUtils.slang:43-104, ColorHelpers.slang:61-70)
+// ---------------------------------------------------------------------------------------------
+constexpr float kMinWl = 380.0f, kMaxWl = 720.0f;
+float sampleOneWavelength(float u) { return kMinWl + u * (kMaxWl - kMinWl); }
+void hwssWavelengths(float hero, uint32_t H, float* out) {
+    const float span = kMaxWl - kMinWl;
+    for (uint32_t i = 0; i < H; ++i) {
+        float w = hero + float(i) * (span / float(H));
+        w -= w > kMaxWl ? span : 0.f;
+        out[i] = w;
+    }
+}
+// returns Le per hwss sample; sampled wavelengths in wl
+void sampleSpectrum(const Scene& s, uint32_t id, float hero, SampleGen& sg, bool importance, uint32_t H, float* le, float* wl) {
+    for (uint32_t j = 0; j < H; ++j) le[j] = 0.f;
+    if (id == PLT_NO_SPECTRAL_PROFILE || id >= s.tables.count) return;   // sampledWavelengths stays unset in the reference
+    if (importance) {
+        const plt_spectral_profile& sp = s.tables.profiles[id];
+        wl[0] = hero;
+        le[0] = evalSpectrum<float>(s.tables, id, hero);
+        float x[3];
+        for (int c = 0; c < 3; ++c) x[c] = float(sp.bins) * sg.next1D();
+        for (uint32_t j = 1; j < H; ++j) {
+            const uint32_t i = (uint32_t)x[j - 1];
+            const float a = i < sp.bins ? sp.icdf[i] : 1.f;
+            const float b = i + 1 < sp.bins ? sp.icdf[i + 1] : 1.f;
+            const float fr = x[j - 1] - std::floor(x[j - 1]);
+            const float cdf = a + (b - a) * fr;
+            wl[j] = sp.min_wavelength + (sp.max_wavelength - sp.min_wavelength) * cdf;
+            le[j] = sp.intensity / (float)sp.bins;
+        }
+    } else {
+        hwssWavelengths(hero, H, wl);
+        for (uint32_t j = 0; j < H; ++j) le[j] = evalSpectrum<float>(s.tables, id, wl[j]);
+    }
+}
+F3 spectrumToRgb(const float* L, const float* wl, uint32_t samples) {
+    F3 res = {0.f, 0.f, 0.f};
+    for (uint32_t i = 0; i < samples; ++i) {
+        const F3 xyz = wavelengthToXYZ(wl[i]) * wavelengthToD65(wl[i]) * L[i];
+        const F3 rgb = {3.240969941904522f * xyz.x + -1.537383177570094f * xyz.y + -0.4986107602930032f * xyz.z,
+                        -0.9692436362808803f * xyz.x + 1.875967501507721f * xyz.y + 0.04155505740717569f * xyz.z,
+                        0.05563007969699373f * xyz.x + -0.2039769588889765f * xyz.y + 1.056971514242878f * xyz.z};
+        res = res + rgb;
+    }
+    const float Y_D65 = 10.5670762f;
+    return res / Y_D65;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Beams: pltSourceBeamArea (PLT.slang:276-290) and propagate (PLT.slang:224-230)
+// ---------------------------------------------------------------------------------------------
+Beam<float> sourceBeamArea(F3 posW, F3 dir, float A, float dist, const float* Le, const float* wl, uint32_t H, float maxBeamOmega) {
+    const float r2 = sqr(dist * 1e+3f);
+    A = std::min(A, maxBeamOmega * r2);
+    Beam<float> b;
+    b.H = (int)H;
+    for (uint32_t j = 0; j < H; ++j) {
+        b.L[0][j] = Le[j];
+        b.L[1][j] = b.L[2][j] = b.L[3][j] = 0.f;
+        b.wl[j] = wl[j];
+        b.spdf[j] = 1.f;
+    }
+    b.D[0] = A; b.D[1] = 0.f; b.D[2] = A;
+    b.r_m = 0.f;
+    b.posW = posW;
+    b.r = dir;
+    b.t = perp_stark(dir);
+    b.distant = false;
+    return b;
+}
+void propagate(Beam<float>& b, F3 p) {
+    if (!b.distant) b.r_m += length(p - b.posW);
+    b.posW = p;
+}
+void scaleBeam(Beam<float>& b, float s) {
+    for (int c = 0; c < 4; ++c) for (int j = 0; j < b.H; ++j) b.L[c][j] *= s;
+}
+
+float MISWeight(float p0, float p1) {
+    const float q0 = p0, q1 = p1;
+    return q0 / (q0 + q1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// The render pass
+// ---------------------------------------------------------------------------------------------
+struct Renderer {
+    const Scene& s;
+    const plt_camera& cam;
+    Options o;
+    uint32_t width, height, frame;
+
+    uint32_t trace(F3 org, F3 dir, float t0, float t1, float& t, float& b1, float& b2) const {
+        const float O[3] = {org.x, org.y, org.z}, D[3] = {dir.x, dir.y, dir.z};
+        return geom::traceBrute(s.triVerts.data(), s.nt, O, D, t0, t1, false, t, b1, b2);
+    }
+    bool visible(F3 org, F3 dir, float t0, float t1) const {
+        const float O[3] = {org.x, org.y, org.z}, D[3] = {dir.x, dir.y, dir.z};
+        float t, b1, b2;
+        return geom::traceBrute(s.triVerts.data(), s.nt, O, D, t0, t1, true, t, b1, b2) == kNone;
+    }
+
+    // Camera.computeRayPinhole, Camera.slang:46-78
+    F3 cameraDir(uint32_t px, uint32_t py) const {
+        float p0 = (float(px) + 0.5f) / float(width);
+        float p1 = (float(py) + 0.5f) / float(height);
+        p0 += -cam.jitter_x;
+        p1 += cam.jitter_y;
+        const float ndcx = 2.f * p0 + -1.f, ndcy = -2.f * p1 + 1.f;
+        const F3 d = f3(cam.u) * ndcx + f3(cam.v) * ndcy + f3(cam.w);
+        return normalize(d);
+    }
+
+    // ---- sample pass, pltpt_sample.rt.slang:36-185 ----
+    void samplePass(uint32_t px, uint32_t py, Bounce* bounces) const {
+        SampleGen sg(px, py, frame);
+        const float wavelength = sampleOneWavelength(sg.next1D());
+        F3 origin = f3(cam.pos), dir = cameraDir(px, py);
+        float weight = 1.f, pdf = 1.f, thp = 1.f, lastNonDeltaPdf = 0.f;
+        uint32_t flags = FLAG_ONLY_DELTA;
+        const uint32_t maxB = o.maxBounces;
+        auto append = [&](uint32_t length, uint32_t prim, float b1, float b2, F3 wi, uint32_t lobe) {
+            Bounce& b = bounces[length];
+            b.flags = flags;
+            b.prim = prim;
+            b.b1 = b1;
+            b.b2 = b2;
+            const float n[3] = {wi.x, wi.y, wi.z};
+            geom::ndirToOctEqualArea(n, b.ewi);
+            b.lobe = lobe;
+            b.lastNonDeltaPdf = lastNonDeltaPdf;
+            b.pathContribution = 1.f / (pdf * thp);
+        };
+        for (uint32_t length = 0; length < maxB + 1 && (flags & (FLAG_MISS | FLAG_TERMINATED)) == 0;) {
+            float t, b1, b2;
+            const uint32_t prim = trace(origin, dir, 0.f, FLT_MAX, t, b1, b2);
+            const F3 wi = -dir;
+            if (prim == kNone) {       // scatterMiss
+                flags |= FLAG_MISS;
+                append(length, kNone, 0.f, 0.f, wi, 0);
+                continue;
+            }
+            // scatterTriangleMeshClosestHit
+            const VertexData v = vertexData(s, prim, b1, b2);
+            const uint32_t mid = s.triMat[prim];
+            const ShadingData sd = prepareShadingData(s, v, mid, wi);
+            const Props props = bsdfProps(s, mid);
+            if (sd.opacity == 0.f) {   // alpha mask
+                origin = sd.newRayOrigin(false);
+                continue;
+            }
+            // shouldTerminatePath: RR(1 - weight, 2, u), pltpt.slangh:170-176; pow follows the
+            // shader semantics (NaN for a negative base)
+            float rcp_thp = 1.f;
+            if (o.doRR) {
+                const float rrVal = 1.f - weight;
+                const float p = rrVal < 0.f ? NAN : std::pow(rrVal, 2.f);
+                const float u = sg.next1D();
+                rcp_thp = u < p ? 0.f : 1.f - p;
+            }
+            bool shouldEnd = length == maxB || (rcp_thp == 0.f && length > 0);
+            BSDFSample bs;
+            if (!shouldEnd) {
+                const bool ok = bsdfSample(s, sd, sg, bs, wavelength);
+                shouldEnd = !ok || bs.pdf == 0.f;
+                const float nc = pdf * bs.pdf * thp * rcp_thp;
+                shouldEnd = shouldEnd || nc < 1e-6f;
+            }
+            const bool isDelta = (bs.lobe & LOBE_DELTA) != 0;
+            const bool isDisp = (bs.lobe & (LOBE_DISPERSIVE_DELTA_REFLECTION | LOBE_DISPERSIVE_DELTA_TRANSMISSION)) != 0;
+            const bool isRefl = (bs.lobe & LOBE_REFLECTION) != 0;
+            const bool isMS = (isRefl && (props.flags & PROP_MW_REFLECTIVE)) || (!isRefl && (props.flags & PROP_MW_TRANSMISSIVE));
+            if (shouldEnd) {
+                flags |= FLAG_TERMINATED;
+                append(length, prim, b1, b2, wi, 0);
+                continue;
+            }
+            weight *= bs.weight;
+            thp *= rcp_thp;
+            pdf *= bs.pdf;
+            if (isDisp) flags |= FLAG_DISPERSIVE;
+            append(length, prim, b1, b2, wi, bs.lobe);
+            ++length;
+            lastNonDeltaPdf = !isDelta ? bs.pdf : lastNonDeltaPdf;
+            const uint32_t msc = isMS ? (flags >> 16) + 1u : 0u;
+            flags = (flags & 0xFFFFu) | (msc << 16);
+            flags = isDelta ? (flags | FLAG_LAST_DELTA) : (flags & ~FLAG_LAST_DELTA);
+            if (!isDelta) flags &= ~FLAG_ONLY_DELTA;
+            origin = sd.newRayOrigin(isRefl);
+            dir = bs.wo;
+        }
+    }
+
+    // ---- solve pass, pltpt_solve.rt.slang ----
+    struct Solve {
+        SampleGen sg, tilesg;
+        F3 Lrgb = {0.f, 0.f, 0.f};
+        F3 pathOrigin, pathNormal;
+        float wavelength = 0.f;
+        uint64_t shadowRays = 0, unwindEvals = 0;
+    };
+
+    bool wasNEEAvailable(int p, uint32_t flags) const {
+        return o.doNee && p > 0 && (flags & FLAG_LAST_DELTA) == 0;   // MNEE off
+    }
+
+    void forwardUnwindStep(uint32_t prim, const VertexData& v, F3 wo, uint32_t lobe, Beam<float>& beam, Solve& sv) const {
+        const uint32_t mid = s.triMat[prim];
+        const ShadingData sd = prepareShadingData(s, v, mid, -beam.r);
+        propagate(beam, sd.posW);
+        bsdfEval(s, sd, wo, lobe, beam);
+        ++sv.unwindEvals;
+        if (o.hwssMis) {
+            float pdfs[MAXH];
+            for (int j = 0; j < MAXH; ++j) pdfs[j] = 1.f;
+            bsdfLambdaPdf(s, sd, wo, lobe, beam, pdfs);
+            for (uint32_t j = 0; j < o.hwss; ++j) beam.spdf[j] *= pdfs[j];
+        }
+    }
+    void forwardUnwind(int bounceIdx, const Bounce* bounces, Beam<float>& beam, Solve& sv) const {
+        for (int p = bounceIdx - 1; p >= 0; --p) {
+            const Bounce& b = bounces[p];
+            const VertexData v = vertexData(s, b.prim, b.b1, b.b2);
+            forwardUnwindStep(b.prim, v, b.wi(), b.lobe, beam, sv);
+        }
+    }
+
+    // measure, pltpt_solve.rt.slang:96-147
+    void measure(Solve& sv, int bounceIdx, float pathContribution, Beam<float>& beam) const {
+        if (!o.useDirect && bounceIdx <= 1) return;
+        propagate(beam, f3(cam.pos));
+        if (cam.polarizer > 0.f) {
+            const F3 W = normalize(f3(cam.w)), U = normalize(f3(cam.u));
+            beam.rotateFrame(U, -W);
+            const float pi = cam.polarizer;
+            const float cth = std::cos(cam.polarizer_theta), sth = std::sin(cam.polarizer_theta);
+            // (1 - p) I + p * MuellerPolarizer(theta), Mueller.slang:60-73
+            const float P[4][4] = {{.5f * 1.f, .5f * cth, .5f * sth, 0.f}, {.5f * cth, .5f * (cth * cth), .5f * (cth * sth), 0.f},
+                                   {.5f * sth, .5f * (cth * sth), .5f * (sth * sth), 0.f}, {0.f, 0.f, 0.f, 0.f}};
+            for (int j = 0; j < beam.H; ++j) {
+                const float in[4] = {beam.L[0][j], beam.L[1][j], beam.L[2][j], beam.L[3][j]};
+                for (int r = 0; r < 4; ++r) {
+                    float acc = 0.f;
+                    for (int c = 0; c < 4; ++c) acc += ((1.f - pi) * (r == c ? 1.f : 0.f) + pi * P[r][c]) * in[c];
+                    beam.L[r][j] = acc;
+                }
+            }
+        }
+        if (o.hwssMis) {
+            float sum = 0.f;
+            for (uint32_t j = 0; j < o.hwss; ++j) sum += beam.spdf[j];
+            pathContribution *= sum > K_FLT_EPSILON ? beam.spdf[0] / sum : 0.f;
+        } else {
+            pathContribution *= 1.f / float(beam.H);
+        }
+        float Li[MAXH];
+        for (int j = 0; j < beam.H; ++j) Li[j] = beam.L[0][j];
+        const F3 rgb = spectrumToRgb(Li, beam.wl, (uint32_t)beam.H) * pathContribution;
+        const F3 L = {std::max(0.f, rgb.x), std::max(0.f, rgb.y), std::max(0.f, rgb.z)};
+        if (std::isfinite(L.x) && std::isfinite(L.y) && std::isfinite(L.z)) sv.Lrgb = sv.Lrgb + L;
+    }
+
+    // evalTrianglePdf (EmissiveLightSamplerHelpers.slang:120-151) x triangle selection pdf
+    // (EmissivePowerSampler.slang:90-122)
+    float emissivePdf(F3 posW, uint32_t light, F3 hitPos, F3 hitNormal) const {
+        if (light == kNone) return 0.f;
+        const float sel = s.lightFlux[light] * s.invWeightsSum;
+        const F3 toLight = hitPos - posW;
+        const float distSqr = dot(toLight, toLight);
+        if (distSqr <= FLT_MIN) return 0.f * sel;
+        const F3 L = toLight / std::sqrt(distSqr);
+        const float cosTheta = dot(hitNormal, -L);
+        if (cosTheta <= 0.f) return 0.f * sel;
+        const float denom = std::max(FLT_MIN, cosTheta * s.lightArea[light]);
+        return sel * (distSqr / denom);
+    }
+
+    struct LightSample {
+        float pdf = 0.f, distance = 0.f;
+        F3 origin = {0.f, 0.f, 0.f}, dir = {0.f, 0.f, 0.f};
+        Beam<float> beam;
+    };
+
+    // generateLightSample with the emissive sampler (LightSampling.slangh:108-206,
+    // EmissivePowerSampler.slang:47-79, EmissiveLightSamplerHelpers.slang:56-118)
+    bool generateLightSample(const ShadingData& sd, bool sampleRefl, bool sampleTrans, Solve& sv, LightSample& ls) const {
+        ls = LightSample();
+        ls.beam.H = (int)o.hwss;
+        for (int c = 0; c < 4; ++c) for (int j = 0; j < MAXH; ++j) ls.beam.L[c][j] = 0.f;
+        for (int j = 0; j < MAXH; ++j) { ls.beam.wl[j] = 0.f; ls.beam.spdf[j] = 1.f; }
+        // selectLightType: probabilities (0, 1, 0) without env map and analytic lights
+        SampleGen& selSg = o.perTileSg ? sv.tilesg : sv.sg;
+        const float uType = selSg.next1D();
+        if (!o.useEmissive || !(uType < 1.f)) return false;
+        const float selectionPdf = 1.f;
+        bool valid = false;
+        const uint32_t nl = (uint32_t)s.lightTri.size();
+        if (nl > 0) {
+            // EmissivePowerSampler.sampleLight
+            const float uLight = sv.sg.next1D();
+            uint32_t ti = std::min((uint32_t)(uLight * nl), nl - 1);
+            const uint32_t px = s.alias[2 * (size_t)ti], py = s.alias[2 * (size_t)ti + 1];
+            const float threshold = half_to_float((uint16_t)(px >> 16));
+            const uint32_t selectAbove = ((px & 0xFFFFu) << 8u) | ((py >> 24u) & 0xFFu);
+            const uint32_t selectBelow = py & 0xFFFFFFu;
+            ti = (sv.sg.next1D() >= threshold) ? selectAbove : selectBelow;
+            const float triSelPdf = s.lightFlux[ti] * s.invWeightsSum;
+            // sampleTriangle
+            const float u0 = sv.sg.next1D(), u1 = sv.sg.next1D();
+            const float su = std::sqrt(u0);
+            const float bx = 1.f - su, by = u1 * su;
+            const float bary[3] = {1.f - bx - by, bx, by};
+            const float* P = &s.lightPos[9 * (size_t)ti];
+            F3 tposW = f3(P) * bary[0];
+            tposW = tposW + f3(P + 3) * bary[1];
+            tposW = tposW + f3(P + 6) * bary[2];
+            const F3 toL = tposW - sd.posW;
+            const float distSqr = std::max(FLT_MIN, dot(toL, toL));
+            const float tdist = std::sqrt(distSqr);
+            const F3 tdir = toL / tdist;
+            const F3 tn = f3(&s.lightNormal[3 * (size_t)ti]);
+            const float cosTheta = dot(tn, -tdir);
+            if (!(cosTheta <= 0.f)) {
+                float Le[MAXH], swl[MAXH];
+                for (int j = 0; j < MAXH; ++j) { Le[j] = 0.f; swl[j] = 0.f; }
+                const Material<float>& lm = s.mats[s.triMat[s.lightTri[ti]]];
+                sampleSpectrum(s, lm.emission, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Le, swl);
+                const float white[3] = {1.f, 1.f, 1.f};
+                for (uint32_t j = 0; j < o.hwss; ++j) Le[j] *= rgbToSpectrum(white, swl[j]);
+                const float denom = std::max(FLT_MIN, cosTheta * s.lightArea[ti]);
+                float tpdf = distSqr / denom;
+                tpdf *= triSelPdf;
+                // generateEmissiveSample
+                float L[MAXH];
+                bool anyPos = false;
+                for (uint32_t j = 0; j < o.hwss; ++j) {
+                    L[j] = tpdf > 0.f ? Le[j] / tpdf : 0.f;
+                    anyPos = anyPos || L[j] > 0.f;
+                }
+                ls.pdf = tpdf;
+                const float tp[3] = {tposW.x, tposW.y, tposW.z}, nn[3] = {tn.x, tn.y, tn.z};
+                float lp[3];
+                geom::computeRayOrigin(tp, nn, lp);
+                const F3 lightPos = f3(lp);
+                ls.origin = newRayOriginToward(sd, lightPos - sd.posW);
+                const F3 toLight = lightPos - ls.origin;
+                ls.distance = length(toLight);
+                ls.dir = normalize(toLight);
+                ls.beam = sourceBeamArea(tposW, -ls.dir, o.sourcingArea, ls.distance, L, swl, o.hwss, o.maxBeamOmega);
+                valid = anyPos;
+            }
+        }
+        ls.pdf *= selectionPdf;
+        scaleBeam(ls.beam, 1.f / selectionPdf);
+        const bool isReflection = dot(sd.faceN, ls.dir) * dot(sd.faceN, sd.V) > 0.f;
+        return valid && ls.pdf > 1e-6f && !(!sampleRefl && isReflection) && !(!sampleTrans && !isReflection);
+    }
+
+    // NEE without manifold walks, pltpt_solve.rt.slang:245-366
+    void NEE(Solve& sv, int p, const Bounce* bounces, const ShadingData& sd, const VertexData& V, uint32_t mid) const {
+        const Props props = bsdfProps(s, mid);
+        const uint32_t lobes = props.lobes;
+        const bool sampleRefl = (lobes & 0x03u) != 0;
+        const bool sampleTrans = (lobes & 0x30u) != 0;
+        if (!sampleRefl && !sampleTrans) return;
+        LightSample ls;
+        if (!generateLightSample(sd, sampleRefl, sampleTrans, sv, ls)) return;
+        bool anyL = false;
+        for (int j = 0; j < ls.beam.H; ++j) anyL = anyL || ls.beam.L[0][j] > 0.f;
+        if (!anyL) return;
+        if (!o.hwssMis && (bounces[p].flags & FLAG_DISPERSIVE)) ls.beam.H = 1;
+        const bool doMis = o.doMis;
+        ++sv.shadowRays;
+        if (!visible(ls.origin, ls.dir, 0.f, ls.distance)) return;
+        if (doMis) {
+            const float bsdfPdfV = bsdfPdf(s, sd, ls.dir, ls.beam.wl[0]);
+            scaleBeam(ls.beam, MISWeight(ls.pdf, bsdfPdfV));
+        }
+        // evalNEE with the current vertex
+        const ShadingData fsd = prepareShadingData(s, V, mid, -ls.beam.r);
+        propagate(ls.beam, fsd.posW);
+        const F3 wi = bounces[p].wi();
+        bsdfEval(s, fsd, wi, LOBE_NON_DELTA, ls.beam);
+        ++sv.unwindEvals;
+        if (o.hwssMis) {
+            float pdfs[MAXH];
+            for (int j = 0; j < MAXH; ++j) pdfs[j] = 1.f;
+            bsdfLambdaPdf(s, fsd, wi, LOBE_NON_DELTA, ls.beam, pdfs);
+            for (uint32_t j = 0; j < o.hwss; ++j) ls.beam.spdf[j] *= pdfs[j];
+        }
+        forwardUnwind(p, bounces, ls.beam, sv);
+        measure(sv, p, bounces[p].pathContribution, ls.beam);
+    }
+
+    // evalEmissive, pltpt_solve.rt.slang:152-200
+    void evalEmissive(Solve& sv, int p, const Bounce* bounces, const ShadingData& sd, uint32_t mid) const {
+        const Bounce& bounce = bounces[p];
+        const Props props = bsdfProps(s, mid);
+        const bool didNEE = wasNEEAvailable(p, bounce.flags);
+        if (!(o.useEmissive && (props.flags & PROP_EMISSIVE) && (o.doMis || !didNEE))) return;
+        const bool needMIS = o.doMis && didNEE;
+        const uint32_t light = s.primToLight[bounce.prim];
+        const F3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
+        const float lightPdf = 1.f * emissivePdf(sv.pathOrigin, light, sd.posW, hn);
+        const float misWeight = needMIS ? MISWeight(bounce.lastNonDeltaPdf, lightPdf) : 1.f;
+        float Le[MAXH], swl[MAXH];
+        for (int j = 0; j < MAXH; ++j) { Le[j] = 0.f; swl[j] = 0.f; }
+        sampleSpectrum(s, props.emissionId, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Le, swl);
+        const float white[3] = {1.f, 1.f, 1.f};
+        bool anyPos = false;
+        for (uint32_t j = 0; j < o.hwss; ++j) {
+            Le[j] *= misWeight * rgbToSpectrum(white, swl[j]);
+            anyPos = anyPos || Le[j] > 0.f;
+        }
+        if (!anyPos) return;
+        const float dist = length(sv.pathOrigin - sd.posW);
+        Beam<float> beam = sourceBeamArea(sd.posW, bounce.wi(), o.sourcingArea, dist, Le, swl, o.hwss, o.maxBeamOmega);
+        if (!o.hwssMis && (bounce.flags & FLAG_DISPERSIVE)) beam.H = 1;
+        forwardUnwind(p, bounces, beam, sv);
+        measure(sv, p, bounce.pathContribution, beam);
+    }
+
+    void solvePass(uint32_t px, uint32_t py, const Bounce* bounces, float* rgb, uint64_t* stats) const {
+        const uint32_t tile = o.tileSize;
+        Solve sv{SampleGen(px, py, frame), SampleGen(px / tile, py / tile, frame << 2)};
+        sv.wavelength = sampleOneWavelength(sv.sg.next1D());
+        sv.pathOrigin = f3(cam.pos);
+        sv.pathNormal = normalize(f3(cam.w));
+        for (int p = 0;; ++p) {
+            const Bounce& b = bounces[p];
+            if (b.flags & FLAG_MISS) break;   // onMiss: no environment light
+            const VertexData v = vertexData(s, b.prim, b.b1, b.b2);
+            const uint32_t mid = s.triMat[b.prim];
+            const ShadingData sd = prepareShadingData(s, v, mid, b.wi());
+            if (o.doNee) NEE(sv, p, bounces, sd, v, mid);
+            evalEmissive(sv, p, bounces, sd, mid);
+            if ((b.flags & FLAG_TERMINATED) || p == (int)o.maxBounces) break;
+            sv.pathOrigin = v.posW;
+            sv.pathNormal = sd.N;
+        }
+        rgb[0] = sv.Lrgb.x;
+        rgb[1] = sv.Lrgb.y;
+        rgb[2] = sv.Lrgb.z;
+        stats[0] += sv.shadowRays;
+        stats[1] += sv.unwindEvals;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+// Scene for the path-tracing oracle (host arrays).
+typedef struct plto_scene {
+    uint32_t n_vertices, n_triangles, n_materials, n_profiles;
+    const float* positions;              // [n_vertices][3]
+    const float* normals;                // [n_vertices][3]
+    const float* tangents;               // [n_vertices][4] or NULL
+    const uint32_t* indices;             // [n_triangles][3]
+    const uint32_t* tri_material;        // [n_triangles]
+    const plt_material_record* materials;
+    const plt_spectral_profile* profiles;
+} plto_scene;
+
+// Renders frame `frame` of a width x height image into rgb [height][width][3].  Optional per-path
+// records [height*width][max_bounces+1] of bounce primitive (0xFFFFFFFF when absent), lobe and flags.
+// stats (optional, 3 values): paths, shadow rays, forward BSDF evaluations.  MNEE is not restated
+// yet: do_mnee must be 0.
+int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* opt, uint32_t width, uint32_t height,
+                uint32_t frame, int threads, float* rgb, uint32_t* rec_prim, uint32_t* rec_lobe, uint32_t* rec_flags,
+                uint64_t* stats) {
+    if (!sc || !cam || !opt || !rgb) return PLT_INVALID_ARG;
+    if (opt->hwss < 1 || opt->hwss > 4 || opt->do_mnee) return PLT_NOT_SUPPORTED;
+    Scene s;
+    s.nv = sc->n_vertices;
+    s.nt = sc->n_triangles;
+    s.pos = sc->positions;
+    s.nrm = sc->normals;
+    s.tan = sc->tangents;
+    s.idx = sc->indices;
+    s.triMat = sc->tri_material;
+    s.tables.profiles = sc->profiles;
+    s.tables.count = sc->n_profiles;
+    s.mats.reserve(sc->n_materials);
+    for (uint32_t i = 0; i < sc->n_materials; ++i) {
+        s.mats.push_back(decodeMaterial<float>(sc->materials[i]));
+        s.matFlags.push_back(recordDoubleSided(sc->materials[i]) ? 1u : 0u);
+    }
+    for (uint32_t t = 0; t < s.nt; ++t)
+        if (s.triMat[t] >= sc->n_materials) return PLT_BAD_MATERIAL;
+    s.triVerts.resize(9 * (size_t)s.nt);
+    for (uint32_t t = 0; t < s.nt; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) s.triVerts[9 * (size_t)t + 3 * k + c] = s.pos[3 * (size_t)s.idx[3 * (size_t)t + k] + c];
+    buildLights(s);
+
+    Options o;
+    o.maxBounces = opt->max_bounces;
+    o.tileSize = opt->tile_size ? opt->tile_size : 512;
+    o.hwss = opt->hwss;
+    o.hwssMis = opt->hwss_do_mis != 0;
+    o.useDirect = opt->use_direct_light != 0;
+    o.useEmissive = opt->use_emissive_lights != 0;
+    o.doNee = opt->do_nee != 0;
+    o.doMis = opt->do_nee != 0 && opt->do_mis != 0;
+    o.doRR = opt->do_russian_roulette != 0;
+    o.perTileSg = opt->do_nee != 0 && opt->nee_use_per_tile_sg != 0;
+    o.importanceSampleEmitters = opt->do_importance_sample_emitters != 0;
+    o.sourcingArea = opt->sourcing_area_from_emissive_geometry;
+    o.maxBeamOmega = opt->sourcing_max_beam_omega;
+
+    Renderer R{s, *cam, o, width, height, frame};
+    const uint32_t nb = o.maxBounces + 1;
+    const int64_t npix = (int64_t)width * height;
+    uint64_t shadow = 0, evals = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(threads > 0 ? threads : 1) if (threads != 1) reduction(+ : shadow, evals)
+#endif
+    {
+        std::vector<Bounce> bounces(nb);
+        uint64_t st[2] = {0, 0};
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+        for (int64_t i = 0; i < npix; ++i) {
+            const uint32_t px = (uint32_t)(i % width), py = (uint32_t)(i / width);
+            for (uint32_t b = 0; b < nb; ++b) bounces[b] = Bounce();
+            R.samplePass(px, py, bounces.data());
+            R.solvePass(px, py, bounces.data(), rgb + 3 * i, st);
+            if (rec_prim || rec_lobe || rec_flags) {
+                for (uint32_t b = 0; b < nb; ++b) {
+                    if (rec_prim) rec_prim[i * nb + b] = bounces[b].prim;
+                    if (rec_lobe) rec_lobe[i * nb + b] = bounces[b].lobe;
+                    if (rec_flags) rec_flags[i * nb + b] = bounces[b].flags;
+                }
+            }
+        }
+        shadow += st[0];
+        evals += st[1];
+    }
+    if (stats) {
+        stats[0] = (uint64_t)npix;
+        stats[1] = shadow;
+        stats[2] = evals;
+    }
+    return PLT_OK;
+}
+
+// The light collection's alias table as the oracle builds it (for the library's table check):
+// returns the light-triangle count; alias [2*count] (may be NULL to query), inv_weight_sum.
+uint32_t plto_light_table(const plto_scene* sc, uint32_t* alias_out, uint32_t* light_tri_out, float* inv_weight_sum) {
+    Scene s;
+    s.nt = sc->n_triangles;
+    s.pos = sc->positions;
+    s.idx = sc->indices;
+    s.triMat = sc->tri_material;
+    s.tables.profiles = sc->profiles;
+    s.tables.count = sc->n_profiles;
+    for (uint32_t i = 0; i < sc->n_materials; ++i) s.mats.push_back(decodeMaterial<float>(sc->materials[i]));
+    buildLights(s);
+    const uint32_t nl = (uint32_t)s.lightTri.size();
+    if (alias_out) std::memcpy(alias_out, s.alias.data(), 8 * (size_t)nl);
+    if (light_tri_out) std::memcpy(light_tri_out, s.lightTri.data(), 4 * (size_t)nl);
+    if (inv_weight_sum) *inv_weight_sum = s.invWeightsSum;
+    return nl;
+}
+
+}  // extern "C"

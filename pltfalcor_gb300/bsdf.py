@@ -180,3 +180,34 @@ class PLTContext:
     def check_status(self, stream=None):
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
         return self.lib.plt_check_status(self.handle, s)
+
+    # ---- PLTPT render pass ----
+    def set_scene_shading(self, normals, tangents=None):
+        n = np.ascontiguousarray(normals, np.float32)
+        t = None if tangents is None else np.ascontiguousarray(tangents, np.float32)
+        capi.check(self.lib.plt_set_scene_shading(self.handle, C.c_void_p(n.ctypes.data), None if t is None else C.c_void_p(t.ctypes.data),
+                                                  len(n)), "plt_set_scene_shading")
+
+    def load_scene(self, scene, profiles):
+        """Spectral profiles, materials, geometry and shading attributes of a scene.Scene."""
+        self.set_spectral_profiles(profiles)
+        self.set_materials(scene.records)
+        self.set_scene(scene.vertices, scene.indices, scene.tri_material)
+        self.set_scene_shading(scene.normals, scene.tangents)
+
+    def render(self, camera, width, height, out_rgba, frame_begin=0, frame_count=1, stream=None):
+        """plt_render into the device tensor out_rgba [height][width][4] (float32)."""
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_render(self.handle, C.byref(camera), width, height, frame_begin, frame_count, _ptr(out_rgba), s),
+                   "plt_render")
+
+    def render_bounces(self, npix, max_bounces):
+        """Bounce records of the last frame: (prim, lobe, flags), each [npix][max_bounces+1] uint32."""
+        out = [np.zeros((npix, max_bounces + 1), np.uint32) for _ in range(3)]
+        capi.check(self.lib.plt_render_bounces(self.handle, *[C.c_void_p(a.ctypes.data) for a in out]), "plt_render_bounces")
+        return out
+
+    def render_stats(self):
+        out = (C.c_uint64 * 4)()
+        capi.check(self.lib.plt_render_stats(self.handle, out), "plt_render_stats")
+        return {"paths": out[0], "bounces": out[1], "shadow_rays": out[2], "bsdf_evals": out[3]}

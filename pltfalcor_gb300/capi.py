@@ -70,6 +70,13 @@ class Options(C.Structure):
                 ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("u", C.c_float * 3), ("v", C.c_float * 3), ("w", C.c_float * 3),
+                ("jitter_x", C.c_float), ("jitter_y", C.c_float), ("polarizer", C.c_float), ("polarizer_theta", C.c_float)]
+
+
+MATERIAL_FLAG_DOUBLE_SIDED = 0x1
+
 assert C.sizeof(SpectralProfile) == 1052
 assert C.sizeof(MaterialRecord) == 80
 
@@ -79,7 +86,7 @@ EXPORTED_SYMBOLS = [
     "plt_last_cuda_error", "plt_set_spectral_profiles", "plt_set_materials", "plt_spectral_profile_from_samples",
     "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
     "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats", "plt_bsdf_batch_noalloc",
-    "plt_set_timing_events",
+    "plt_set_timing_events", "plt_set_scene_shading", "plt_render", "plt_render_stats", "plt_render_bounces",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PLT_TOO_LARGE = 8
@@ -120,6 +127,10 @@ def load_library(path=LIB_PATH):
         "plt_scene_stats": (i32, [vp, C.POINTER(C.c_uint32)]),
         "plt_bsdf_batch_noalloc": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
         "plt_set_timing_events": (i32, [vp, vp, vp, vp]),
+        "plt_set_scene_shading": (i32, [vp, vp, vp, u32]),
+        "plt_render": (i32, [vp, C.POINTER(Camera), u32, u32, u32, u32, vp, vp]),
+        "plt_render_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
+        "plt_render_bounces": (i32, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -11,27 +11,7 @@
 #include "plt_host.h"
 #include "plt_internal.h"
 
-struct plt_context {
-    int device = 0;
-    int numSMs = 0;
-    plt_options opt{};
-    pltdev::DevMaterial* dMats = nullptr;
-    uint8_t* dMatType = nullptr;
-    uint32_t nMats = 0, capMats = 0;
-    pltdev::DevProfile* dProfiles = nullptr;
-    uint32_t nProfiles = 0, capProfiles = 0;
-    uint32_t* dStatus = nullptr;
-    void* dScratch = nullptr;     // batch scratch (sort permutation + work counter), grown on demand
-    size_t scratchCap = 0;
-    // scene
-    plt::BvhNode* dNodes = nullptr;
-    float4* dTris = nullptr;      // 3 float4 per triangle, leaf order
-    uint32_t* dTriMaterial = nullptr;
-    uint32_t nTris = 0;
-    plt::BvhBuildStats bvhStats{};
-    int lastCudaError = 0;
-    void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
-};
+#include "plt_context.h"
 
 namespace {
 
@@ -126,6 +106,7 @@ plt_status plt_destroy(plt_context* ctx) {
     cudaFree(ctx->dNodes);
     cudaFree(ctx->dTris);
     cudaFree(ctx->dTriMaterial);
+    pltReleaseRenderState(ctx);
     delete ctx;
     return PLT_OK;
 }
@@ -154,7 +135,18 @@ plt_status plt_set_spectral_profiles(plt_context* ctx, const plt_spectral_profil
         ctx->capProfiles = count;
     }
     if (count) PLT_CUDA(ctx, cudaMemcpy(ctx->dProfiles, h.data(), sizeof(pltdev::DevProfile) * count, cudaMemcpyHostToDevice));
+    // inverse CDFs for emission importance sampling (Scene.sampleSpectrum)
+    cudaFree(ctx->dProfileIcdf);
+    ctx->dProfileIcdf = nullptr;
+    if (count) {
+        std::vector<float> icdf((size_t)count * PLT_SPECTRAL_MAX_BINS);
+        for (uint32_t i = 0; i < count; ++i) std::memcpy(&icdf[(size_t)i * PLT_SPECTRAL_MAX_BINS], profiles[i].icdf, sizeof(profiles[i].icdf));
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dProfileIcdf, sizeof(float) * icdf.size()));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dProfileIcdf, icdf.data(), sizeof(float) * icdf.size(), cudaMemcpyHostToDevice));
+    }
+    ctx->hProfiles.assign(profiles, profiles + count);
     ctx->nProfiles = count;
+    ctx->shadingReady = false;
     return PLT_OK;
 }
 
@@ -181,7 +173,19 @@ plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, 
         PLT_CUDA(ctx, cudaMemcpy(ctx->dMats, h.data(), sizeof(pltdev::DevMaterial) * count, cudaMemcpyHostToDevice));
         PLT_CUDA(ctx, cudaMemcpy(ctx->dMatType, types.data(), count, cudaMemcpyHostToDevice));
     }
+    // per-material property words of the render pass
+    cudaFree(ctx->dMatProps);
+    ctx->dMatProps = nullptr;
+    if (count) {
+        std::vector<uint2> props(count);
+        for (uint32_t i = 0; i < count; ++i) props[i] = pltMaterialProps(mats[i], h[i]);
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dMatProps, sizeof(uint2) * count));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dMatProps, props.data(), sizeof(uint2) * count, cudaMemcpyHostToDevice));
+    }
+    ctx->hMats.assign(mats, mats + count);
+    ctx->hDevMats = h;
     ctx->nMats = count;
+    ctx->shadingReady = false;
     return PLT_OK;
 }
 
@@ -327,8 +331,29 @@ plt_status plt_set_scene(plt_context* ctx, const float* vertices, uint32_t nVert
         PLT_CUDA(ctx, cudaMalloc(&ctx->dTriMaterial, sizeof(uint32_t) * nTris));
         PLT_CUDA(ctx, cudaMemcpy(ctx->dTriMaterial, mat.data(), sizeof(uint32_t) * nTris, cudaMemcpyHostToDevice));
     }
+    // vertex positions and indices for shading (render pass)
+    cudaFree(ctx->dPos);
+    cudaFree(ctx->dIdx);
+    ctx->dPos = nullptr;
+    ctx->dIdx = nullptr;
+    if (nTris) {
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dPos, sizeof(float) * 3 * (size_t)nVerts));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dPos, vertices, sizeof(float) * 3 * (size_t)nVerts, cudaMemcpyHostToDevice));
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dIdx, sizeof(uint32_t) * 3 * (size_t)nTris));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dIdx, indices, sizeof(uint32_t) * 3 * (size_t)nTris, cudaMemcpyHostToDevice));
+        ctx->hPos.assign(vertices, vertices + 3 * (size_t)nVerts);
+        ctx->hIdx.assign(indices, indices + 3 * (size_t)nTris);
+        ctx->hTriMat.assign(nTris, 0u);
+        if (material) std::memcpy(ctx->hTriMat.data(), material, sizeof(uint32_t) * nTris);
+    } else {
+        ctx->hPos.clear();
+        ctx->hIdx.clear();
+        ctx->hTriMat.clear();
+    }
+    ctx->nVerts = nVerts;
     ctx->nTris = nTris;
     ctx->bvhStats = st;
+    ctx->shadingReady = false;
     return PLT_OK;
 }
 

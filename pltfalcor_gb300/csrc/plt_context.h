@@ -1,0 +1,69 @@
+// The library context (opaque to callers): device tables, scene, render-pass buffers, and the
+// host copies the render pass's light collection is built from.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "plt_bvh.h"
+#include "plt_host.h"
+#include "plt_internal.h"
+
+struct plt_context {
+    int device = 0;
+    int numSMs = 0;
+    plt_options opt{};
+    pltdev::DevMaterial* dMats = nullptr;
+    uint8_t* dMatType = nullptr;
+    uint32_t nMats = 0, capMats = 0;
+    pltdev::DevProfile* dProfiles = nullptr;
+    uint32_t nProfiles = 0, capProfiles = 0;
+    uint32_t* dStatus = nullptr;
+    void* dScratch = nullptr;     // batch scratch (sort permutation + work counter), grown on demand
+    size_t scratchCap = 0;
+    // scene
+    plt::BvhNode* dNodes = nullptr;
+    float4* dTris = nullptr;      // 3 float4 per triangle, leaf order
+    uint32_t* dTriMaterial = nullptr;
+    uint32_t nTris = 0;
+    plt::BvhBuildStats bvhStats{};
+    int lastCudaError = 0;
+    void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
+
+    // host copies for the render pass (light collection, material properties)
+    std::vector<plt_spectral_profile> hProfiles;
+    std::vector<plt_material_record> hMats;
+    std::vector<pltdev::DevMaterial> hDevMats;
+    std::vector<float> hPos;
+    std::vector<uint32_t> hIdx, hTriMat;
+    uint32_t nVerts = 0;
+    float* dProfileIcdf = nullptr;   // [nProfiles][128]
+    uint2* dMatProps = nullptr;      // [nMats]
+    float* dPos = nullptr;           // [nVerts][3]
+    uint32_t* dIdx = nullptr;        // [nTris][3]
+    float* dNrm = nullptr;           // [nVerts][3]
+    float* dTan = nullptr;           // [nVerts][4] or null
+    bool shadingReady = false;
+    // light collection + power sampler
+    float* dLightPos = nullptr;
+    float* dLightNrm = nullptr;
+    float* dLightArea = nullptr;
+    float* dLightFlux = nullptr;
+    uint2* dAlias = nullptr;
+    uint32_t* dPrimToLight = nullptr;
+    uint32_t* dLightEmission = nullptr;
+    uint32_t nLights = 0;
+    float invWeightsSum = 0.f;
+    // render-pass buffers (one allocation, sized for ptNpix paths and ptMaxB bounces)
+    void* dPt = nullptr;
+    size_t ptBytes = 0;
+    uint32_t ptNpix = 0, ptMaxB = 0;
+    plt::PtParams pt{};
+    unsigned long long* dPtStats = nullptr;
+};
+
+// Frees the render-pass state of a context (plt_render.cpp).
+void pltReleaseRenderState(plt_context* ctx);
+// Material property word for the render pass (plt_render.cpp).
+uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& d);

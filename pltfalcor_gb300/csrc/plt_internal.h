@@ -56,6 +56,75 @@ struct BatchParams {
     void* timing[3];
 };
 
+// PLTPT render pass (sample + solve).  Per-material property word (matProps.x):
+// bits 0-3 BSDFProperties flags, 8-15 getLobes() bits, 16 double-sided, 17 alpha == 0;
+// matProps.y = emission profile id.
+constexpr uint32_t kPropEmissive = 0x1u, kPropTransmissive = 0x2u, kPropMwReflective = 0x4u, kPropMwTransmissive = 0x8u;
+constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
+// option bits of PtParams.opt
+constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
+                   kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u;
+
+struct PtParams {
+    // scene
+    const void* nodes;
+    const float4* tris;
+    const float* pos;             // [nv][3]
+    const float* nrm;             // [nv][3]
+    const float* tan;             // [nv][4] or null
+    const uint32_t* idx;          // [nt][3]
+    const uint32_t* triMat;       // [nt]
+    uint32_t nTris;
+    const pltdev::DevMaterial* mats;
+    const uint2* matProps;
+    uint32_t nMats;
+    const pltdev::DevProfile* profiles;
+    const float* profileIcdf;     // [nProfiles][128]
+    uint32_t nProfiles;
+    // light collection
+    const float* lightPos;        // [nl][9]
+    const float* lightNrm;        // [nl][3]
+    const float* lightArea;       // [nl]
+    const float* lightFlux;       // [nl]
+    const uint2* alias;           // [nl]
+    const uint32_t* primToLight;  // [nt]
+    const uint32_t* lightEmission;// [nl] emission profile id
+    uint32_t nLights;
+    float invWeightsSum;
+    // options
+    uint32_t maxBounces, tileSize, hwss, opt, flags;
+    float sourcingArea, maxBeamOmega;
+    plt_camera cam;
+    uint32_t width, height, npix, frame;
+    // path state of the sample pass
+    uint32_t* sg;                 // [4][npix]
+    float* org;                   // [3][npix]
+    float* dir;                   // [3][npix]
+    float* wl;
+    float* weight;
+    float* pdf;
+    float* thp;
+    float* lndp;
+    uint32_t* pflags;
+    uint32_t* plen;
+    uint32_t* queue0;             // [npix]
+    uint32_t* queue1;             // [npix]
+    uint32_t* qcount;             // [maxBounces + 2]
+    // bounce buffer, planes [maxBounces + 1][npix] (two planes per bounce for bary / encoded wi)
+    uint32_t* bPrim;
+    float* bBary;
+    float* bEw;
+    uint32_t* bLobe;
+    uint32_t* bFlags;
+    float* bContrib;
+    float* bLndp;
+    // outputs
+    double* accum;                // [npix][3]
+    unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, paths
+    uint32_t* status;
+};
+cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream);
+
 constexpr int kBatchThreads = 256;     // classify CTA
 constexpr int kBatchItems = 8;
 constexpr int kBatchTile = kBatchThreads * kBatchItems;

@@ -207,6 +207,40 @@ plt_status decodeMaterial(const plt_material_record& r, uint32_t nProfiles, pltd
     }
 }
 
+namespace {
+
+// CIE 1931 XYZ multi-lobe Gaussian fit (Wyman, Sloan, Shirley 2013), as the shaders evaluate it
+// (SpectrumUtils.slang:43-49)
+float cieLobe(float x, float mu, float s1, float s2) {
+    const float t = (x - mu) * (x < mu ? s1 : s2);
+    return std::exp(-0.5f * t * t);
+}
+void cieXyz(float l, float& x, float& y, float& z) {
+    x = 0.362f * cieLobe(l, 442.0f, 0.0624f, 0.0374f) + 1.056f * cieLobe(l, 599.8f, 0.0264f, 0.0323f) -
+        0.065f * cieLobe(l, 501.1f, 0.0490f, 0.0382f);
+    y = 0.821f * cieLobe(l, 568.8f, 0.0213f, 0.0247f) + 0.286f * cieLobe(l, 530.9f, 0.0613f, 0.0322f);
+    z = 1.217f * cieLobe(l, 437.0f, 0.0845f, 0.0278f) + 0.681f * cieLobe(l, 459.0f, 0.0385f, 0.0725f);
+}
+// CIE D65 relative spectral power, 380-720 nm in 5 nm steps (the shaders' table,
+// SpectrumUtils.slang:66-82), linearly interpolated; zero outside the range.
+float d65(float l) {
+    static const float t[69] = {49.9755f, 52.3118f, 54.6482f, 68.7015f, 82.7549f, 87.1204f, 91.486f, 92.4589f, 93.4318f,
+                                90.057f, 86.6823f, 95.7736f, 104.865f, 110.936f, 117.008f, 117.41f, 117.812f, 116.336f,
+                                114.861f, 115.392f, 115.923f, 112.367f, 108.811f, 109.082f, 109.354f, 108.578f, 107.802f,
+                                106.296f, 104.79f, 106.239f, 107.689f, 106.047f, 104.405f, 104.225f, 104.046f, 102.023f,
+                                100.f, 98.1671f, 96.3342f, 96.0611f, 95.788f, 92.2368f, 88.6856f, 89.3459f, 90.0062f,
+                                89.8026f, 89.5991f, 88.6489f, 87.6987f, 85.4936f, 83.2886f, 83.4939f, 83.6992f, 81.863f,
+                                80.0268f, 80.1207f, 80.2146f, 81.2462f, 82.2778f, 80.281f, 78.2842f, 74.0027f, 69.7213f,
+                                70.6652f, 71.6091f, 72.979f, 74.349f, 67.9765f, 61.604f};
+    if (!(l >= 380.0f && l <= 720.0f)) return 0.f;
+    const float r = (l - 380.0f) * 0.2f;
+    const int hi = int(std::ceil(r) + .5f), lo = int(std::floor(r) + .5f);
+    const float w = r - float(lo);
+    return t[hi] * w + t[lo] * (1.0f - w);
+}
+
+}  // namespace
+
 plt_status spectralProfileFromSamples(const float* wl, const float* val, uint32_t count, float scale, int computeIcdf,
                                       plt_spectral_profile* sp) {
     if (!wl || !val || !sp || count == 0) return PLT_INVALID_ARG;
@@ -237,6 +271,27 @@ plt_status spectralProfileFromSamples(const float* wl, const float* val, uint32_
         return hlerp(s[i], s[i + 1], x - (float)i);
     };
     std::memset(sp, 0, sizeof(*sp));
+    {
+        // sp.rgb = toRGB_D65 of the sampled spectrum (SceneBuilder.cpp:913): trapezoid sum of
+        // s * xyz * D65 over the samples, XYZ -> Rec.709 (ColorHelpers.slang:61-70), / 10567.0762.
+        // The analytic CIE fit and the 380-720 nm D65 table stand in for the host's 1-nm tables.
+        const float delta = ns > 1 ? (l1 - l0) / (float(ns) - 1.0f) : 0.f;
+        float X = 0.f, Y = 0.f, Z = 0.f;
+        for (size_t q = 0; q < ns; ++q) {
+            const float l = std::min(l0 + delta * float(q), l1);
+            float x, y, z;
+            cieXyz(l, x, y, z);
+            const float dd = d65(l);
+            const float wq = ss(l) * delta * ((q == 0 || q == ns - 1) ? 0.5f : 1.0f);
+            X += x * dd * wq;
+            Y += y * dd * wq;
+            Z += z * dd * wq;
+        }
+        const float k = 1.0f / 10567.0762f;
+        sp->rgb[0] = (3.240969941904522f * X + -1.537383177570094f * Y + -0.4986107602930032f * Z) * k;
+        sp->rgb[1] = (-0.9692436362808803f * X + 1.875967501507721f * Y + 0.04155505740717569f * Z) * k;
+        sp->rgb[2] = (0.05563007969699373f * X + -0.2039769588889765f * Y + 1.056971514242878f * Z) * k;
+    }
     sp->intensity = 1.f;
     sp->min_wavelength = std::max(l0, 380.0f);
     sp->max_wavelength = std::min(l1, 720.0f);

@@ -1,0 +1,61 @@
+// PLTPT render pass: frame set-up, the per-segment sample wavefront and the launch sequence of one
+// frame (PLTPT::execute, RenderPasses/PLTPT/PLTPT.cpp:357-499 in ssteinberg/PLTFalcor, without the
+// tiling, which only bounds the reference's bounce-buffer memory).
+#include <algorithm>
+
+#define PLT_PT_SAMPLE_PASS
+#include "plt_pt.cuh"
+
+namespace plt {
+
+cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream) {
+    if (p.npix == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 2), stream);
+    if (e != cudaSuccess) return e;
+    static int bpsInit = -1, bpsBounce = -1;
+    if (bpsBounce < 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel, 128, 0);
+        bpsBounce = b > 0 ? b : 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptInitKernel, 128, 0);
+        bpsInit = b > 0 ? b : 1;
+    }
+    const uint32_t need = (p.npix + 127) / 128;
+    pltdev::ptInitKernel<<<std::min<uint32_t>(need, (uint32_t)(numSMs * bpsInit)), 128, 0, stream>>>(p);
+    const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsBounce));
+    for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<<<gridB, 128, 0, stream>>>(p, it);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    switch (p.hwss) {
+    case 1: return pltdev::launchSolveH<1>(p, numSMs, stream);
+    case 2: return pltdev::launchSolveH<2>(p, numSMs, stream);
+    case 3: return pltdev::launchSolveH<3>(p, numSMs, stream);
+    case 4: return pltdev::launchSolveH<4>(p, numSMs, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace plt
+
+namespace pltdev {
+
+__global__ void ptResolveKernel(const double* __restrict__ accum, uint32_t npix, double inv, float* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
+        out[4 * (size_t)i] = (float)(accum[3 * (size_t)i] * inv);
+        out[4 * (size_t)i + 1] = (float)(accum[3 * (size_t)i + 1] * inv);
+        out[4 * (size_t)i + 2] = (float)(accum[3 * (size_t)i + 2] * inv);
+        out[4 * (size_t)i + 3] = 1.f;
+    }
+}
+
+}  // namespace pltdev
+
+namespace plt {
+
+cudaError_t launchResolve(const double* accum, uint32_t npix, uint32_t frames, float* out, int numSMs, cudaStream_t stream) {
+    if (npix == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>((npix + 255) / 256, (uint32_t)numSMs * 8u);
+    pltdev::ptResolveKernel<<<grid, 256, 0, stream>>>(accum, npix, 1.0 / (double)frames, out);
+    return cudaGetLastError();
+}
+
+}  // namespace plt

@@ -1,0 +1,778 @@
+// PLTPT render pass on the GPU: the sample pass (backward path construction,
+// RenderPasses/PLTPT/pltpt_sample.rt.slang) as a wavefront of one kernel per path segment over a
+// compacted queue of live paths, and the solve pass (NEE, emissive hits, forward beam replay,
+// spectral MIS, measurement, pltpt_solve.rt.slang) as one thread per path.  Paths cited are inside
+// ssteinberg/PLTFalcor.  The scene has identity instance transforms and untextured materials; the
+// light types are emissive triangles only (no environment map, no analytic lights), so light-type
+// selection (LightSampling.slangh:40-90) always picks emissive geometry after one draw.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "plt_bsdf_query.cuh"
+#include "plt_trace.cuh"
+
+namespace pltdev {
+
+using plt::PtParams;
+
+constexpr uint32_t kNoHit = 0xFFFFFFFFu;
+// RayFlags, Path.slang:46-106
+constexpr uint32_t kFlagLastDelta = 0x1u, kFlagDispersive = 0x2u, kFlagOnlyDelta = 0x4u, kFlagMiss = 0x10u, kFlagTerminated = 0x20u;
+constexpr float kQcutoffForMS = .15f;
+constexpr float kFltMax = 3.402823466e+38f;
+constexpr float kFltMin = 1.175494351e-38f;
+
+PLT_DI f3 ld3s(const float* p, uint32_t i) { return mk3(__ldg(p + 3 * i), __ldg(p + 3 * i + 1), __ldg(p + 3 * i + 2)); }
+PLT_DI f3 ldPlane3(const float* p, uint32_t i, uint32_t n) { return mk3(p[i], p[n + i], p[2 * n + i]); }
+PLT_DI void stPlane3(float* p, uint32_t i, uint32_t n, f3 v) { p[i] = v.x; p[n + i] = v.y; p[2 * n + i] = v.z; }
+PLT_DI f3 rnormalize(f3 a) { return a / __fsqrt_rn(dot(a, a)); }
+PLT_DI float hsign(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+
+// ---- geometry helpers -----------------------------------------------------------------------
+// computeRayOrigin, Utils/Geometry/GeometryHelpers.slang:47-60
+PLT_DI float rayOriginC(float p, float n) {
+    const float origin = 1.f / 16.f, fScale = 3.f / 65536.f, iScale = 3 * 256.f;
+    const int iOff = (int)(n * iScale);
+    const float iPos = __int_as_float(__float_as_int(p) + (p < 0.f ? -iOff : iOff));
+    const float fOff = n * fScale;
+    return fabsf(p) < origin ? p + fOff : iPos;
+}
+PLT_DI f3 computeRayOrigin(f3 p, f3 n) { return mk3(rayOriginC(p.x, n.x), rayOriginC(p.y, n.y), rayOriginC(p.z, n.z)); }
+
+// ndir_to_oct_equal_area_snorm / oct_to_ndir_equal_area_snorm, Utils/Math/MathHelpers.slang:199-243
+PLT_DI f2 ndirToOctEqualArea(f3 n) {
+    const float r = sqrtf(1.f - fabsf(n.z));
+    const float phi = atan2f(fabsf(n.y), fabsf(n.x));
+    float py = r * phi * 0.636619772367581343076f;
+    float px = r - py;
+    if (n.z < 0.f) {
+        const float tx = 1.f - py, ty = 1.f - px;
+        px = tx;
+        py = ty;
+    }
+    return f2{px * hsign(n.x), py * hsign(n.y)};
+}
+PLT_DI f3 octToNdirEqualArea(f2 p) {
+    const float d = 1.f - (fabsf(p.x) + fabsf(p.y));
+    const float r = 1.f - fabsf(d);
+    const float phi = (r > 0.f) ? ((fabsf(p.y) - fabsf(p.x)) / r + 1.f) * 0.785398163397448309616f : 0.f;
+    const float f = r * sqrtf(2.f - r * r);
+    float s, c;
+    sincosf(phi, &s, &c);
+    return mk3(f * hsign(p.x) * c, f * hsign(p.y) * s, hsign(d) * (1.f - r * r));
+}
+
+// ---- vertex and shading data ----------------------------------------------------------------
+struct VData {
+    f3 posW, normalW, faceN;
+    float tw[4];
+};
+// computeVertexData, Scene/Scene.slang:530-567 (identity world matrix)
+PLT_DI VData vertexData(const PtParams& P, uint32_t prim, float b1, float b2) {
+    const float w0 = 1.f - b1 - b2;
+    const uint32_t i0 = __ldg(P.idx + 3 * prim), i1 = __ldg(P.idx + 3 * prim + 1), i2 = __ldg(P.idx + 3 * prim + 2);
+    const f3 p0 = ld3s(P.pos, i0), p1 = ld3s(P.pos, i1), p2 = ld3s(P.pos, i2);
+    VData v;
+    v.posW = p0 * w0 + p1 * b1 + p2 * b2;
+    v.normalW = rnormalize(ld3s(P.nrm, i0) * w0 + ld3s(P.nrm, i1) * b1 + ld3s(P.nrm, i2) * b2);
+    v.faceN = rnormalize(cross(p1 - p0, p2 - p0));
+    if (P.tan) {
+        float t[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) t[c] = __ldg(P.tan + 4 * i0 + c) * w0 + __ldg(P.tan + 4 * i1 + c) * b1 + __ldg(P.tan + 4 * i2 + c) * b2;
+        const f3 tx = rnormalize(mk3(t[0], t[1], t[2]));
+        v.tw[0] = tx.x; v.tw[1] = tx.y; v.tw[2] = tx.z; v.tw[3] = hsign(t[3]);
+    } else {
+        v.tw[0] = v.tw[1] = v.tw[2] = v.tw[3] = 0.f;
+    }
+    return v;
+}
+
+struct SD {
+    f3 posW, V, N, T, B, faceN;
+    bool frontFacing;
+    PLT_DI f3 toLocal(f3 v) const { return mk3(dot(v, T), dot(v, B), dot(v, N)); }
+    PLT_DI f3 fromLocal(f3 v) const { return T * v.x + B * v.y + N * v.z; }
+    // ShadingData.computeNewRayOrigin, Scene/ShadingData.slang:77-80
+    PLT_DI f3 newRayOrigin(bool viewside) const { return computeRayOrigin(posW, (frontFacing == viewside) ? faceN : -faceN); }
+};
+// computeNewRayOrigin(sd, dir), ShadowRays.slangh:50-52
+PLT_DI f3 newRayOriginToward(const SD& sd, f3 dir) { return computeRayOrigin(sd.posW, dot(sd.faceN, dir) >= 0.f ? sd.faceN : -sd.faceN); }
+
+// prepareShadingData, Scene/Material/MaterialFactory.slang:79-128 with computeTangentSpace
+// (Scene/Material/ShadingUtils.slang:126-153,243-251); double-sided materials flip N on back faces.
+PLT_DI SD prepareSD(const VData& v, uint32_t props, f3 viewDir) {
+    SD sd;
+    sd.posW = v.posW;
+    sd.V = viewDir;
+    sd.N = v.normalW;
+    const f3 t = mk3(v.tw[0], v.tw[1], v.tw[2]);
+    const float NdotT = dot(t, sd.N);
+    const bool valid = fabsf(v.tw[3]) == 1.0f && dot(t, t) > 0.f && fabsf(NdotT) < 0.9999f;
+    if (valid) {
+        sd.T = rnormalize(t - sd.N * NdotT);
+        sd.B = cross(sd.N, sd.T) * v.tw[3];
+    } else {
+        sd.T = perp_stark(sd.N);
+        sd.B = cross(sd.N, sd.T);
+    }
+    sd.faceN = v.faceN;
+    sd.frontFacing = dot(sd.V, sd.faceN) >= 0.f;
+    if (!sd.frontFacing && (props & plt::kPropDoubleSided)) sd.N = -sd.N;
+    return sd;
+}
+
+// ---- material instance in world space (IMaterialInstance wrappers of PLT*BSDF.slang) ----------
+struct WFrame {
+    f3 T, B, N;
+    PLT_DI f3 toLocal(f3 v) const { return mk3(dot(v, T), dot(v, B), dot(v, N)); }
+    PLT_DI f3 fromLocal(f3 v) const { return T * v.x + B * v.y + N * v.z; }
+};
+PLT_DI bool isGrated(uint32_t type) { return type == kMatGratedConductor || type == kMatGratedOpaque; }
+// sd frame, or localGratingShadingFrame (DiffractionGrating.slang:83-90) for the grated materials
+PLT_DI WFrame bsdfFrame(const SD& sd, uint32_t type, const DevMaterial* __restrict__ m) {
+    WFrame f;
+    if (isGrated(type)) {
+        f.T = sd.fromLocal(mk3(__ldg(m->p + PD_GX), __ldg(m->p + PD_GY), 0.f));
+        f.N = sd.N;
+        f.B = cross(f.N, f.T);
+    } else {
+        f.T = sd.T;
+        f.B = sd.B;
+        f.N = sd.N;
+    }
+    return f;
+}
+
+template <int H>
+PLT_DI void ptEval(const DevMaterial* __restrict__ m, uint32_t type, const Ctx& c, const SD& sd, f3 toEye, uint32_t lobe, DBeam<H>& b) {
+    const WFrame F = bsdfFrame(sd, type, m);
+    b.r = F.toLocal(b.r);
+    b.t = F.toLocal(b.t);
+    const f3 wi = F.toLocal(sd.V), wo = F.toLocal(toEye);
+    b.constructLocalFrame(wo);
+    switch (type) {
+    case kMatDielectric: dielEval<H>(m, wi, wo, lobe, b); scatterCoherence(b, wo, (lobe & kLobeDelta) != 0); break;
+    case kMatConductor: condEval<H>(m, c, wi, wo, lobe, b); scatterCoherence(b, wo, (lobe & kLobeDelta) != 0); break;
+    case kMatOpaqueDielectric: opaqEval<H>(m, wi, wo, lobe, b); scatterCoherence(b, wo, (lobe & kLobeDelta) != 0); break;
+    case kMatCoatedConductor: coatEval<H, true>(m, c, wi, wo, lobe, b); scatterCoherence(b, wo, (lobe & kLobeDelta) != 0); break;
+    case kMatCoatedOpaque: coatEval<H, false>(m, c, wi, wo, lobe, b); scatterCoherence(b, wo, (lobe & kLobeDelta) != 0); break;
+    case kMatGratedConductor:
+    case kMatGratedOpaque: {
+        if (type == kMatGratedConductor) gratEval<H, true>(m, c, wi, wo, lobe, b);
+        else gratEval<H, false>(m, c, wi, wo, lobe, b);
+        int lx, ly;
+        decodeGratingLobe(lobe, lx, ly);
+        if (lx == 0 && ly == 0) scatterCoherence(b, wo, (lobe & kLobeDelta) != 0);
+        break;
+    }
+    case kMatThin: thinEval<H>(m, wi, wo, lobe, b); break;
+    case kMatMultilayer: mlEval<H>(m, c, wi, wo, lobe, b); break;
+    case kMatDiffuse: diffEval<H>(m, wi, lobe, b); scatterCoherence(b, wo, false); break;
+    default: b.setZero(); break;
+    }
+    b.r = F.fromLocal(b.r);
+    b.t = F.fromLocal(b.t);
+}
+
+PLT_DI bool ptSample(const DevMaterial* __restrict__ m, uint32_t type, const SD& sd, SampleGen& sg, float wl, f3& wo, float& pdf,
+                     float& weight, uint32_t& lobe) {
+    const WFrame F = bsdfFrame(sd, type, m);
+    const f3 V = F.toLocal(sd.V);
+    bool ok;
+    switch (type) {
+    case kMatDielectric: ok = dielSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatConductor: ok = condSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatOpaqueDielectric: ok = opaqSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatCoatedConductor:
+    case kMatCoatedOpaque: ok = coatSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatGratedConductor: ok = gratSample<true>(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatGratedOpaque: ok = gratSample<false>(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatThin: ok = thinSample(m, V, wo, pdf, weight, lobe, sg); break;
+    case kMatMultilayer:
+        if (V.z <= 0.f) { ok = false; break; }
+        pdf = 1.f;
+        wo = reflectL(V);
+        lobe = kLobeDeltaR;
+        weight = m00Of(m->m00a, wl);
+        ok = V.z * wo.z > 0.f;
+        break;
+    case kMatDiffuse: ok = diffSample(m, wo, pdf, weight, lobe, sg, wl); break;
+    default: ok = false; break;
+    }
+    if (ok || !isGrated(type)) wo = F.fromLocal(wo);
+    return ok;
+}
+
+PLT_DI float ptPdf(const DevMaterial* __restrict__ m, uint32_t type, const SD& sd, f3 toLight, float wl) {
+    const WFrame F = bsdfFrame(sd, type, m);
+    const f3 V = F.toLocal(sd.V), W = F.toLocal(toLight);
+    switch (type) {
+    case kMatDielectric: return dielPdf(m, W, V, wl);
+    case kMatConductor: return condPdf(m, W, V, wl);
+    case kMatOpaqueDielectric: return opaqPdf(m, W, V);
+    case kMatCoatedConductor:
+    case kMatCoatedOpaque: return coatPdf(m, W, V, wl);
+    case kMatGratedConductor: return gratPdf<true>(m, W, V, wl);
+    case kMatGratedOpaque: return gratPdf<false>(m, W, V, wl);
+    case kMatDiffuse: return V.z * k1_Pi;
+    default: return 0.f;
+    }
+}
+
+// lambdaPdf in the sd frame for every material (the grated wrappers too, PLTDiffractionGrated*BSDF)
+template <int H>
+PLT_DI void ptLambdaPdf(const DevMaterial* __restrict__ m, uint32_t type, const SD& sd, f3 wo, uint32_t lobe, const DBeam<H>& bIn, float* out) {
+    DBeam<H> b = bIn;
+    b.r = sd.toLocal(b.r);
+    b.t = sd.toLocal(b.t);
+    lambdaPdfDispatch<H>(type, m, sd.toLocal(sd.V), sd.toLocal(wo), lobe, b, out);
+}
+
+// ---- spectra --------------------------------------------------------------------------------
+// rgbToSpectrum of white (1, 1, 1) = the white basis (SpectrumUtils.slang:106-198)
+PLT_DI float whiteSpectrum(float wl) {
+    const float w[11] = {1.0000f, 1.0000f, 0.9999f, 0.9993f, 0.9992f, 0.9998f, 1.0000f, 1.0000f, 1.0000f, 1.0000f, 0.0f};
+    const int b = spectrumBin(wl);
+    float r = w[0];
+#pragma unroll
+    for (int i = 1; i < 11; ++i) r = b == i ? w[i] : r;
+    return r;
+}
+// SpectrumSampler.hwssWavelengths, Utils/Color/SpectrumSampler.slang:43-54
+template <int H> PLT_DI void hwssWavelengths(float hero, float* wl) {
+    const float span = 720.0f - 380.0f;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+        float w = hero + float(i) * (span / float(H));
+        w -= w > 720.0f ? span : 0.f;
+        wl[i] = w;
+    }
+}
+// Scene.sampleSpectrum, Scene/Scene.slang:295-330 (importance sampling draws three numbers)
+template <int H>
+PLT_DI void sampleSpectrum(const PtParams& P, uint32_t id, float hero, SampleGen& sg, bool importance, float* le, float* wl) {
+#pragma unroll
+    for (int j = 0; j < H; ++j) { le[j] = 0.f; wl[j] = 0.f; }
+    if (id == kNoProfile || id >= P.nProfiles) return;
+    if (importance) {
+        const DevProfile& sp = P.profiles[id];
+        wl[0] = hero;
+        le[0] = evalSpectrum(P.profiles, P.nProfiles, id, hero);
+        float x[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x[c] = float(sp.bins) * sg.next1D();
+        const float* icdf = P.profileIcdf + 128 * id;
+#pragma unroll
+        for (int j = 1; j < H; ++j) {
+            const uint32_t i = (uint32_t)x[j - 1];
+            const float a = i < sp.bins ? __ldg(icdf + i) : 1.f;
+            const float b = i + 1 < sp.bins ? __ldg(icdf + i + 1) : 1.f;
+            const float fr = x[j - 1] - floorf(x[j - 1]);
+            const float cdf = a + (b - a) * fr;
+            wl[j] = sp.minl + (sp.maxl - sp.minl) * cdf;
+            le[j] = sp.intensity / (float)sp.bins;
+        }
+    } else {
+        hwssWavelengths<H>(hero, wl);
+#pragma unroll
+        for (int j = 0; j < H; ++j) le[j] = evalSpectrum(P.profiles, P.nProfiles, id, wl[j]);
+    }
+}
+PLT_DI float cieG(float x, float mu, float s1, float s2) {
+    const float t = (x - mu) * (x < mu ? s1 : s2);
+    return expf(-0.5f * t * t);
+}
+// wavelengthToD65, SpectrumUtils.slang:66-82
+PLT_DI float d65(float l) {
+    constexpr float t[69] = {49.9755f, 52.3118f, 54.6482f, 68.7015f, 82.7549f, 87.1204f, 91.486f, 92.4589f, 93.4318f, 90.057f,
+                             86.6823f, 95.7736f, 104.865f, 110.936f, 117.008f, 117.41f, 117.812f, 116.336f, 114.861f, 115.392f,
+                             115.923f, 112.367f, 108.811f, 109.082f, 109.354f, 108.578f, 107.802f, 106.296f, 104.79f, 106.239f,
+                             107.689f, 106.047f, 104.405f, 104.225f, 104.046f, 102.023f, 100.f, 98.1671f, 96.3342f, 96.0611f,
+                             95.788f, 92.2368f, 88.6856f, 89.3459f, 90.0062f, 89.8026f, 89.5991f, 88.6489f, 87.6987f, 85.4936f,
+                             83.2886f, 83.4939f, 83.6992f, 81.863f, 80.0268f, 80.1207f, 80.2146f, 81.2462f, 82.2778f, 80.281f,
+                             78.2842f, 74.0027f, 69.7213f, 70.6652f, 71.6091f, 72.979f, 74.349f, 67.9765f, 61.604f};
+    const float r = (l - 380.0f) * 0.2f;
+    const int hi = min(68, max(0, int(ceilf(r) + .5f))), lo = min(68, max(0, int(floorf(r) + .5f)));
+    const float w = r - float(lo);
+    return t[hi] * w + t[lo] * (1.0f - w);
+}
+// spectrumToRgb, SpectrumUtils.slang:92-104 (+ XYZtoRGB_Rec709, ColorHelpers.slang:61-70)
+template <int H> PLT_DI f3 spectrumToRgb(const float* L, const float* wl, int samples) {
+    float r = 0.f, g = 0.f, bl = 0.f;
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+        if (i >= samples) break;
+        const float l = wl[i];
+        const float s = d65(l) * L[i];
+        const float X = (0.362f * cieG(l, 442.0f, 0.0624f, 0.0374f) + 1.056f * cieG(l, 599.8f, 0.0264f, 0.0323f) -
+                         0.065f * cieG(l, 501.1f, 0.0490f, 0.0382f)) * s;
+        const float Y = (0.821f * cieG(l, 568.8f, 0.0213f, 0.0247f) + 0.286f * cieG(l, 530.9f, 0.0613f, 0.0322f)) * s;
+        const float Z = (1.217f * cieG(l, 437.0f, 0.0845f, 0.0278f) + 0.681f * cieG(l, 459.0f, 0.0385f, 0.0725f)) * s;
+        r += 3.240969941904522f * X + -1.537383177570094f * Y + -0.4986107602930032f * Z;
+        g += -0.9692436362808803f * X + 1.875967501507721f * Y + 0.04155505740717569f * Z;
+        bl += 0.05563007969699373f * X + -0.2039769588889765f * Y + 1.056971514242878f * Z;
+    }
+    const float inv = 1.f / 10.5670762f;
+    return mk3(r * inv, g * inv, bl * inv);
+}
+
+// ---- beams ----------------------------------------------------------------------------------
+template <int H> struct PBeam {
+    DBeam<H> b;
+    float spdf[H];
+    f3 posW;
+    int comps;
+};
+// pltSourceBeamArea, Rendering/PLT.slang:276-290 (unpolarised, diffusivity A * I, r = 0)
+template <int H>
+PLT_DI void sourceBeamArea(PBeam<H>& pb, f3 posW, f3 dir, float A, float dist, const float* Le, const float* wl, float maxBeamOmega) {
+    const float r2 = sqr(dist * 1e+3f);
+    A = fminf(A, maxBeamOmega * r2);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+        pb.b.L[0][j] = Le[j];
+        pb.b.L[1][j] = pb.b.L[2][j] = pb.b.L[3][j] = 0.f;
+        pb.b.wl[j] = wl[j];
+        pb.spdf[j] = 1.f;
+    }
+    pb.b.D0 = A; pb.b.D1 = 0.f; pb.b.D2 = A;
+    pb.b.r_m = 0.f;
+    pb.b.r = dir;
+    pb.b.t = perp_stark(dir);
+    pb.posW = posW;
+    pb.comps = H;
+}
+template <int H> PLT_DI void propagate(PBeam<H>& pb, f3 p) {
+    pb.b.r_m += sqrtf(dot(p - pb.posW, p - pb.posW));
+    pb.posW = p;
+}
+template <int H> PLT_DI void scaleBeam(PBeam<H>& pb, float s) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int j = 0; j < H; ++j) pb.b.L[c][j] *= s;
+}
+
+PLT_DI float misWeight(float p0, float p1) { return p0 / (p0 + p1); }
+
+// ---- sample pass ----------------------------------------------------------------------------
+// Camera.computeRayPinhole, Scene/Camera/Camera.slang:46-78
+PLT_DI f3 cameraDir(const PtParams& P, uint32_t px, uint32_t py) {
+    float p0 = (float(px) + 0.5f) / float(P.width);
+    float p1 = (float(py) + 0.5f) / float(P.height);
+    p0 += -P.cam.jitter_x;
+    p1 += P.cam.jitter_y;
+    const float ndcx = 2.f * p0 + -1.f, ndcy = -2.f * p1 + 1.f;
+    const f3 U = mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]), V = mk3(P.cam.v[0], P.cam.v[1], P.cam.v[2]);
+    const f3 W = mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]);
+    return rnormalize(U * ndcx + V * ndcy + W);
+}
+
+PLT_DI uint32_t warpAggregatedAdd(uint32_t* counter, bool pred) {
+    const uint32_t mask = __ballot_sync(__activemask(), pred);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = mask ? (uint32_t)(__ffs(mask) - 1) : 0u;
+    uint32_t base = 0;
+    if (mask && lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(__activemask(), base, (int)leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+#ifdef PLT_PT_SAMPLE_PASS   // defined by plt_pt.cu only: one copy of the sample-pass kernels
+__global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npix; i += gridDim.x * blockDim.x) {
+        const uint32_t px = i % P.width, py = i / P.width;
+        SampleGen sg;
+        sg.init(px, py, P.frame);
+        const float wl = 380.0f + sg.next1D() * (720.0f - 380.0f);   // SpectrumSampler.sampleOne
+        const f3 d = cameraDir(P, px, py);
+        const uint32_t n = P.npix;
+        P.sg[i] = sg.s0; P.sg[n + i] = sg.s1; P.sg[2 * n + i] = sg.s2; P.sg[3 * n + i] = sg.s3;
+        stPlane3(P.org, i, n, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
+        stPlane3(P.dir, i, n, d);
+        P.wl[i] = wl;
+        P.weight[i] = 1.f;
+        P.pdf[i] = 1.f;
+        P.thp[i] = 1.f;
+        P.lndp[i] = 0.f;
+        P.pflags[i] = kFlagOnlyDelta;
+        P.plen[i] = 0;
+    }
+}
+
+// One segment of every live path: TraceRay + scatterTriangleMeshClosestHit / scatterMiss
+// (pltpt_sample.rt.slang:56-141), appendBounce (pltpt.slangh:138-154).  Live paths are compacted
+// into the next queue with one atomic per warp.
+__global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t it) {
+    const uint32_t n = P.npix;
+    const uint32_t count = it == 0 ? n : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
+    uint32_t* qout = (it & 1u) ? P.queue1 : P.queue0;
+    const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
+    uint32_t nv = 0, tt = 0, overflow = 0, recorded = 0;
+    const Ctx c{P.profiles, P.nProfiles, P.flags};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (count + stride - 1) / stride;
+    for (uint32_t rr = 0; rr < rounds; ++rr) {
+        const uint32_t slot = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool live = false;
+        uint32_t pid = 0;
+        if (slot < count) {
+            pid = it == 0 ? slot : qin[slot];
+            SampleGen sg;
+            sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
+            f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
+            float weight = P.weight[pid], pdf = P.pdf[pid], thp = P.thp[pid], lndp = P.lndp[pid];
+            uint32_t flags = P.pflags[pid], len = P.plen[pid];
+            const float wavelength = P.wl[pid];
+            auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe) {
+                const size_t o = (size_t)len * n + pid;
+                P.bFlags[o] = flags;
+                P.bPrim[o] = prim;
+                P.bBary[(size_t)len * 2 * n + pid] = b1;
+                P.bBary[(size_t)len * 2 * n + n + pid] = b2;
+                const f2 e = ndirToOctEqualArea(wi);
+                P.bEw[(size_t)len * 2 * n + pid] = e.x;
+                P.bEw[(size_t)len * 2 * n + n + pid] = e.y;
+                P.bLobe[o] = lobe;
+                P.bLndp[o] = lndp;
+                P.bContrib[o] = 1.f / (pdf * thp);
+                ++recorded;
+            };
+            for (int guard = 0; guard < 64; ++guard) {
+                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
+                const f3 wi = -dir;
+                if (h.prim == kNoHit) {
+                    flags |= kFlagMiss;
+                    append(kNoHit, 0.f, 0.f, wi, 0u);
+                    break;
+                }
+                const VData v = vertexData(P, h.prim, h.b1, h.b2);
+                const uint32_t mid = __ldg(P.triMat + h.prim);
+                const uint2 props = __ldg(P.matProps + mid);
+                const SD sd = prepareSD(v, props.x, wi);
+                if (props.x & plt::kPropAlphaZero) {   // alpha mask: continue the same ray
+                    org = sd.newRayOrigin(false);
+                    continue;
+                }
+                // Russian roulette RR(1 - weight, 2, u) (pltpt.slangh:170-176); pow of a negative
+                // base is NaN as in the shader
+                float rcpThp = 1.f;
+                if (P.opt & plt::kPtDoRR) {
+                    const float rrVal = 1.f - weight;
+                    const float p = rrVal < 0.f ? __int_as_float(0x7fffffff) : rrVal * rrVal;
+                    const float u = sg.next1D();
+                    rcpThp = u < p ? 0.f : 1.f - p;
+                }
+                bool shouldEnd = len == P.maxBounces || (rcpThp == 0.f && len > 0);
+                f3 wo = mk3(0.f, 0.f, 0.f);
+                float spdf = 0.f, sweight = 0.f;
+                uint32_t slobe = 0;
+                if (!shouldEnd) {
+                    const DevMaterial* __restrict__ m = P.mats + mid;
+                    const bool ok = ptSample(m, __ldg(&m->type), sd, sg, wavelength, wo, spdf, sweight, slobe);
+                    shouldEnd = !ok || spdf == 0.f;
+                    const float nc = pdf * spdf * thp * rcpThp;
+                    shouldEnd = shouldEnd || nc < 1e-6f;
+                }
+                const bool isDelta = (slobe & kLobeDelta) != 0;
+                const bool isDisp = (slobe & (kLobeDispDeltaR | kLobeDispDeltaT)) != 0;
+                const bool isRefl = (slobe & kLobeReflection) != 0;
+                const bool isMS = (isRefl && (props.x & plt::kPropMwReflective)) || (!isRefl && (props.x & plt::kPropMwTransmissive));
+                if (shouldEnd) {
+                    flags |= kFlagTerminated;
+                    append(h.prim, h.b1, h.b2, wi, 0u);
+                    break;
+                }
+                weight *= sweight;
+                thp *= rcpThp;
+                pdf *= spdf;
+                if (isDisp) flags |= kFlagDispersive;
+                append(h.prim, h.b1, h.b2, wi, slobe);
+                ++len;
+                lndp = !isDelta ? spdf : lndp;
+                const uint32_t msc = isMS ? (flags >> 16) + 1u : 0u;
+                flags = (flags & 0xFFFFu) | (msc << 16);
+                flags = isDelta ? (flags | kFlagLastDelta) : (flags & ~kFlagLastDelta);
+                if (!isDelta) flags &= ~kFlagOnlyDelta;
+                org = sd.newRayOrigin(isRefl);
+                dir = wo;
+                live = len < P.maxBounces + 1;
+                break;
+            }
+            if (!live && (flags & (kFlagMiss | kFlagTerminated)) == 0) {
+                // 64 alpha-masked hits in a row: end the path with an empty terminal record
+                flags |= kFlagTerminated;
+                append(kNoHit, 0.f, 0.f, -dir, 0u);
+            }
+            P.sg[pid] = sg.s0; P.sg[n + pid] = sg.s1; P.sg[2 * n + pid] = sg.s2; P.sg[3 * n + pid] = sg.s3;
+            stPlane3(P.org, pid, n, org);
+            stPlane3(P.dir, pid, n, dir);
+            P.weight[pid] = weight;
+            P.pdf[pid] = pdf;
+            P.thp[pid] = thp;
+            P.lndp[pid] = lndp;
+            P.pflags[pid] = flags;
+            P.plen[pid] = len;
+        }
+        const uint32_t pos = warpAggregatedAdd(P.qcount + it + 1, live);
+        if (live) qout[pos] = pid;
+    }
+    if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    unsigned long long r = recorded;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, o);
+    if ((threadIdx.x & 31u) == 0 && r) atomicAdd(P.stats, r);
+}
+
+#endif  // PLT_PT_SAMPLE_PASS
+
+// ---- solve pass -----------------------------------------------------------------------------
+template <int H> struct Bnc {
+    uint32_t prim, lobe, flags;
+    float b1, b2, contrib, lndp;
+    f3 wi;
+};
+template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p) {
+    const uint32_t n = P.npix;
+    const size_t o = (size_t)p * n + pid;
+    Bnc<H> b;
+    b.prim = P.bPrim[o];
+    b.lobe = P.bLobe[o];
+    b.flags = P.bFlags[o];
+    b.b1 = P.bBary[(size_t)p * 2 * n + pid];
+    b.b2 = P.bBary[(size_t)p * 2 * n + n + pid];
+    b.contrib = P.bContrib[o];
+    b.lndp = P.bLndp[o];
+    b.wi = octToNdirEqualArea(f2{P.bEw[(size_t)p * 2 * n + pid], P.bEw[(size_t)p * 2 * n + n + pid]});
+    return b;
+}
+
+// evalTrianglePdf x triangle-selection pdf (EmissiveLightSamplerHelpers.slang:120-151,
+// EmissivePowerSampler.slang:81-122)
+PLT_DI float emissivePdf(const PtParams& P, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
+    if (light == kNoHit) return 0.f;
+    const float sel = __ldg(P.lightFlux + light) * P.invWeightsSum;
+    const f3 toLight = hitPos - posW;
+    const float distSqr = dot(toLight, toLight);
+    if (distSqr <= kFltMin) return 0.f;
+    const f3 L = toLight / sqrtf(distSqr);
+    const float cosTheta = dot(hitNormal, -L);
+    if (cosTheta <= 0.f) return 0.f;
+    const float denom = fmaxf(kFltMin, cosTheta * __ldg(P.lightArea + light));
+    return sel * (distSqr / denom);
+}
+
+template <int H>
+__global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
+    const uint32_t n = P.npix;
+    const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
+    const Ctx c{P.profiles, P.nProfiles, P.flags};
+    const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
+    const bool doNee = (P.opt & plt::kPtDoNee) != 0, doMis = (P.opt & plt::kPtDoMis) != 0;
+    const bool useEmissive = (P.opt & plt::kPtUseEmissive) != 0;
+    const bool importance = (P.opt & plt::kPtImportanceEmit) != 0;
+    uint32_t nv = 0, tt = 0, overflow = 0, shadowRays = 0, evals = 0;
+    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x) {
+        const uint32_t px = pid % P.width, py = pid / P.width;
+        SampleGen sg, tilesg;
+        sg.init(px, py, P.frame);
+        tilesg.init(px / P.tileSize, py / P.tileSize, P.frame << 2);
+        const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
+        f3 pathOrigin = mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]);
+        float Lr = 0.f, Lg = 0.f, Lb = 0.f;
+        for (int p = 0; p <= (int)P.maxBounces; ++p) {
+            const Bnc<H> bounce = readBounce<H>(P, pid, p);
+            if (bounce.flags & kFlagMiss) break;   // onMiss: no environment light
+            if (bounce.prim >= P.nTris) break;     // empty terminal record
+            const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
+            const uint32_t mid = __ldg(P.triMat + bounce.prim);
+            const uint2 props = __ldg(P.matProps + mid);
+            const SD sd = prepareSD(V, props.x, bounce.wi);
+            const DevMaterial* __restrict__ m = P.mats + mid;
+            const uint32_t type = __ldg(&m->type);
+            const uint32_t lobes = (props.x >> 8) & 0xFFu;
+            const bool didNEE = doNee && p > 0 && (bounce.flags & kFlagLastDelta) == 0;
+            // two beam sources per vertex: NEE (pltpt_solve.rt.slang:245-366) and emission
+            // (evalEmissive, :152-200); each is replayed through vertices p (NEE: non-delta lobes)
+            // and p-1 .. 0 (forwardUnwind, :48-79), then measured (:96-147).
+            for (int src = 0; src < 2; ++src) {
+                PBeam<H> pb;
+                bool evalCurrent = false;
+                if (src == 0) {
+                    if (!doNee) continue;
+                    const bool sampleRefl = (lobes & 0x03u) != 0, sampleTrans = (lobes & 0x30u) != 0;
+                    if (!sampleRefl && !sampleTrans) continue;
+                    // generateLightSample: selectLightType (one draw), emissive power sampler
+                    SampleGen& selSg = (P.opt & plt::kPtPerTileSg) ? tilesg : sg;
+                    const float uType = selSg.next1D();
+                    if (!useEmissive || !(uType < 1.f) || P.nLights == 0) continue;
+                    const float uLight = sg.next1D();
+                    uint32_t ti = min((uint32_t)(uLight * (float)P.nLights), P.nLights - 1);
+                    const uint2 a = __ldg(P.alias + ti);
+                    const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
+                    const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
+                    const uint32_t selectBelow = a.y & 0xFFFFFFu;
+                    ti = (sg.next1D() >= threshold) ? selectAbove : selectBelow;
+                    const float triSelPdf = __ldg(P.lightFlux + ti) * P.invWeightsSum;
+                    const float u0 = sg.next1D(), u1 = sg.next1D();
+                    const float su = sqrtf(u0);
+                    const float bx = 1.f - su, by = u1 * su;
+                    const float* LP = P.lightPos + 9 * ti;
+                    const f3 tposW = ld3s(LP, 0) * (1.f - bx - by) + ld3s(LP, 1) * bx + ld3s(LP, 2) * by;
+                    const f3 toL = tposW - sd.posW;
+                    const float distSqr = fmaxf(kFltMin, dot(toL, toL));
+                    const float tdist = sqrtf(distSqr);
+                    const f3 tdir = toL / tdist;
+                    const f3 tn = ld3s(P.lightNrm, ti);
+                    const float cosTheta = dot(tn, -tdir);
+                    if (cosTheta <= 0.f) continue;
+                    float Le[H], swl[H];
+                    sampleSpectrum<H>(P, __ldg(P.lightEmission + ti), wavelength, sg, importance, Le, swl);
+                    const float tpdf = (distSqr / fmaxf(kFltMin, cosTheta * __ldg(P.lightArea + ti))) * triSelPdf;
+                    bool anyPos = false;
+#pragma unroll
+                    for (int j = 0; j < H; ++j) {
+                        Le[j] *= whiteSpectrum(swl[j]);
+                        Le[j] = tpdf > 0.f ? Le[j] / tpdf : 0.f;
+                        anyPos = anyPos || Le[j] > 0.f;
+                    }
+                    const f3 lightPos = computeRayOrigin(tposW, tn);
+                    const f3 lorg = newRayOriginToward(sd, lightPos - sd.posW);
+                    const f3 toLight = lightPos - lorg;
+                    const float ldist = sqrtf(dot(toLight, toLight));
+                    const f3 ldir = rnormalize(toLight);
+                    sourceBeamArea<H>(pb, tposW, -ldir, P.sourcingArea, ldist, Le, swl, P.maxBeamOmega);
+                    const bool isRefl = dot(sd.faceN, ldir) * dot(sd.faceN, sd.V) > 0.f;
+                    if (!(anyPos && tpdf > 1e-6f && !(!sampleRefl && isRefl) && !(!sampleTrans && !isRefl))) continue;
+                    if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
+                    ++shadowRays;
+                    const TraceResult vis = traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, nv, tt, overflow);
+                    if (vis.prim != kNoHit) continue;
+                    if (doMis) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
+                    evalCurrent = true;
+                } else {
+                    if (!(useEmissive && (props.x & plt::kPropEmissive) && (doMis || !didNEE))) continue;
+                    const bool needMIS = doMis && didNEE;
+                    const uint32_t light = __ldg(P.primToLight + bounce.prim);
+                    const f3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
+                    const float lightPdf = emissivePdf(P, pathOrigin, light, sd.posW, hn);
+                    const float mw = needMIS ? misWeight(bounce.lndp, lightPdf) : 1.f;
+                    float Le[H], swl[H];
+                    sampleSpectrum<H>(P, props.y, wavelength, sg, importance, Le, swl);
+                    bool anyPos = false;
+#pragma unroll
+                    for (int j = 0; j < H; ++j) {
+                        Le[j] *= mw * whiteSpectrum(swl[j]);
+                        anyPos = anyPos || Le[j] > 0.f;
+                    }
+                    if (!anyPos) continue;
+                    const float dist = sqrtf(dot(pathOrigin - sd.posW, pathOrigin - sd.posW));
+                    sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
+                    if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
+                }
+                // forward replay: the current vertex (NEE, non-delta lobes), then p-1 .. 0
+                for (int q = evalCurrent ? p : p - 1; q >= 0; --q) {
+                    uint32_t qprim, qlobe;
+                    float qb1, qb2;
+                    f3 qwo;
+                    if (q == p) {
+                        qprim = bounce.prim; qlobe = kLobeNonDelta; qb1 = bounce.b1; qb2 = bounce.b2; qwo = bounce.wi;
+                    } else {
+                        const Bnc<H> bq = readBounce<H>(P, pid, q);
+                        qprim = bq.prim; qlobe = bq.lobe; qb1 = bq.b1; qb2 = bq.b2; qwo = bq.wi;
+                    }
+                    const VData qv = vertexData(P, qprim, qb1, qb2);
+                    const uint32_t qmid = __ldg(P.triMat + qprim);
+                    const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
+                    propagate(pb, qsd.posW);
+                    const DevMaterial* __restrict__ qm = P.mats + qmid;
+                    const uint32_t qtype = __ldg(&qm->type);
+                    ptEval<H>(qm, qtype, c, qsd, qwo, qlobe, pb.b);
+                    ++evals;
+                    if (hwssMis) {
+                        float lp[H];
+                        ptLambdaPdf<H>(qm, qtype, qsd, qwo, qlobe, pb.b, lp);
+#pragma unroll
+                        for (int j = 0; j < H; ++j) pb.spdf[j] *= lp[j];
+                    }
+                }
+                // measure (no camera polarizer unless set)
+                if (!(P.opt & plt::kPtUseDirect) && p <= 1) continue;
+                propagate(pb, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
+                if (P.cam.polarizer > 0.f) {
+                    const f3 Wc = rnormalize(mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]));
+                    const f3 Uc = rnormalize(mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]));
+                    pb.b.rotateFrame(Uc, -Wc);
+                    const float pi = P.cam.polarizer;
+                    float sth, cth;
+                    sincosf(P.cam.polarizer_theta, &sth, &cth);
+                    const float Pm[4][4] = {{.5f, .5f * cth, .5f * sth, 0.f}, {.5f * cth, .5f * (cth * cth), .5f * (cth * sth), 0.f},
+                                            {.5f * sth, .5f * (cth * sth), .5f * (sth * sth), 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+                    for (int j = 0; j < H; ++j) {
+                        const float in[4] = {pb.b.L[0][j], pb.b.L[1][j], pb.b.L[2][j], pb.b.L[3][j]};
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            float acc = 0.f;
+#pragma unroll
+                            for (int cc = 0; cc < 4; ++cc) acc += ((1.f - pi) * (r == cc ? 1.f : 0.f) + pi * Pm[r][cc]) * in[cc];
+                            pb.b.L[r][j] = acc;
+                        }
+                    }
+                }
+                float contrib = bounce.contrib;
+                if (hwssMis) {
+                    float sum = 0.f;
+#pragma unroll
+                    for (int j = 0; j < H; ++j) sum += pb.spdf[j];
+                    contrib *= sum > kFltEps ? pb.spdf[0] / sum : 0.f;
+                } else {
+                    contrib *= 1.f / float(pb.comps);
+                }
+                float Li[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j) Li[j] = pb.b.L[0][j];
+                const f3 rgb = spectrumToRgb<H>(Li, pb.b.wl, pb.comps);
+                const float r = fmaxf(0.f, rgb.x * contrib), g = fmaxf(0.f, rgb.y * contrib), bb = fmaxf(0.f, rgb.z * contrib);
+                if (isfinite(r) && isfinite(g) && isfinite(bb)) { Lr += r; Lg += g; Lb += bb; }
+            }
+            if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
+            pathOrigin = V.posW;
+        }
+        P.accum[3 * (size_t)pid] += (double)Lr;
+        P.accum[3 * (size_t)pid + 1] += (double)Lg;
+        P.accum[3 * (size_t)pid + 2] += (double)Lb;
+    }
+    if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    unsigned long long s1 = shadowRays, s2 = evals;
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_down_sync(0xFFFFFFFFu, s1, o);
+        s2 += __shfl_down_sync(0xFFFFFFFFu, s2, o);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        if (s1) atomicAdd(P.stats + 1, s1);
+        if (s2) atomicAdd(P.stats + 2, s2);
+    }
+}
+
+template <int H>
+cudaError_t launchSolve(const PtParams& p, int numSMs, cudaStream_t stream) {
+    static int bps = -1;
+    if (bps < 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptSolveKernel<H>, 128, 0);
+        bps = b > 0 ? b : 1;
+    }
+    uint32_t grid = (uint32_t)(numSMs * bps);
+    const uint32_t need = (p.npix + 127) / 128;
+    if (grid > need) grid = need;
+    ptSolveKernel<H><<<grid, 128, 0, stream>>>(p);
+    return cudaGetLastError();
+}
+
+// per-H solve launchers, one translation unit each (plt_pt_h{1,2,3,4}.cu)
+template <int H> cudaError_t launchSolveH(const PtParams& p, int numSMs, cudaStream_t stream);
+
+}  // namespace pltdev

@@ -1,0 +1,6 @@
+// Solve pass instantiated for 3 hero wavelength(s) per path.
+#include "plt_pt.cuh"
+
+namespace pltdev {
+template <> cudaError_t launchSolveH<3>(const PtParams& p, int numSMs, cudaStream_t stream) { return launchSolve<3>(p, numSMs, stream); }
+}  // namespace pltdev

@@ -12,10 +12,6 @@ namespace pltdev {
 using plt::BvhNode;
 using plt::TraceParams;
 
-constexpr int kStackDepth = 64;
-
-__device__ __forceinline__ float safeRcp(float d) { return d != 0.f ? __fdiv_rn(1.f, d) : copysignf(INFINITY, d); }
-
 template <bool ANY>
 __device__ __forceinline__ void traceOne(const TraceParams& P, uint32_t i, uint32_t& nodeVisits, uint32_t& triTests) {
     const uint32_t n = P.n;
@@ -23,77 +19,16 @@ __device__ __forceinline__ void traceOne(const TraceParams& P, uint32_t i, uint3
     const float dx = __ldg(P.dir + i), dy = __ldg(P.dir + n + i), dz = __ldg(P.dir + 2 * n + i);
     const float tmin = P.tmin ? __ldg(P.tmin + i) : 0.f;
     const float tmax = P.tmax ? __ldg(P.tmax + i) : 3.402823466e+38f;
-    const float ix = safeRcp(dx), iy = safeRcp(dy), iz = safeRcp(dz);
-    const float4* __restrict__ nodes = reinterpret_cast<const float4*>(P.nodes);
-    const float4* __restrict__ tris = P.tris;
-
-    float bestT = tmax, bestB1 = 0.f, bestB2 = 0.f;
-    uint32_t bestPrim = 0xFFFFFFFFu;
-    bool done = false;
-    int2 stack[kStackDepth];
-    int sp = 0;
-    int32_t node = 0;
     uint32_t overflow = 0;
-
-    auto leaf = [&](int32_t ref) {
-        const uint32_t v = (uint32_t)~ref;
-        const uint32_t first = v >> 4, count = (v & 15u) + 1u;
-        for (uint32_t k = first; k < first + count; ++k) {
-            const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
-            ++triTests;
-            const TriHit h = watertight(ox, oy, oz, dx, dy, dz, v0, v1, v2);
-            if (!h.hit || !(h.t >= tmin) || !(h.t <= bestT)) continue;
-            const uint32_t prim = __float_as_uint(v0.w);
-            if (ANY) {
-                bestT = h.t;
-                bestPrim = prim;
-                done = true;
-                return;
-            }
-            if (h.t < bestT || prim < bestPrim) {
-                bestT = h.t;
-                bestPrim = prim;
-                bestB1 = h.b1;
-                bestB2 = h.b2;
-            }
-        }
-    };
-
-    for (;;) {
-        ++nodeVisits;
-        const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
-        const int4 r = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
-        const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
-        const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
-        float tl = 0.f, tr = 0.f;
-        bool hl = r.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
-        bool hr = r.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
-        if (hl && r.x < 0) { leaf(r.x); hl = false; if (ANY && done) break; }
-        if (hr && r.y < 0) { leaf(r.y); hr = false; if (ANY && done) break; }
-        if (hl && hr) {
-            const bool leftNear = tl <= tr;
-            if (sp < kStackDepth) stack[sp++] = make_int2(leftNear ? r.y : r.x, __float_as_int(leftNear ? tr : tl));
-            else overflow = 1;
-            node = leftNear ? r.x : r.y;
-            continue;
-        }
-        if (hl) { node = r.x; continue; }
-        if (hr) { node = r.y; continue; }
-        // pop the nearest pending node that can still hold a closer hit
-        bool found = false;
-        while (sp > 0) {
-            const int2 e = stack[--sp];
-            if (__int_as_float(e.y) <= bestT * kTfarScale) { node = e.x; found = true; break; }
-        }
-        if (!found) break;
-    }
+    const TraceResult h = traverse<ANY>(reinterpret_cast<const float4*>(P.nodes), P.tris, ox, oy, oz, dx, dy, dz, tmin, tmax,
+                                        nodeVisits, triTests, overflow);
     if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     if (ANY) {
-        P.occluded[i] = bestPrim != 0xFFFFFFFFu ? 1u : 0u;
+        P.occluded[i] = h.prim != 0xFFFFFFFFu ? 1u : 0u;
     } else {
-        P.prim[i] = bestPrim;
-        if (P.t) P.t[i] = bestPrim != 0xFFFFFFFFu ? bestT : -1.f;
-        if (P.bary) { P.bary[i] = bestB1; P.bary[n + i] = bestB2; }
+        P.prim[i] = h.prim;
+        if (P.t) P.t[i] = h.prim != 0xFFFFFFFFu ? h.t : -1.f;
+        if (P.bary) { P.bary[i] = h.b1; P.bary[n + i] = h.b2; }
     }
 }
 

@@ -85,4 +85,98 @@ __device__ __forceinline__ bool slab(const float* mn, const float* mx, float ox,
     return tn <= tf;
 }
 
+constexpr int kStackDepth = 64;
+
+__device__ __forceinline__ float safeRcp(float d) { return d != 0.f ? __fdiv_rn(1.f, d) : copysignf(INFINITY, d); }
+
+// Result of one BVH query.
+struct TraceResult {
+    uint32_t prim;      // triangle id, 0xFFFFFFFF on a miss
+    float t, b1, b2;
+};
+
+// Stack traversal of the two-wide BVH for one ray: closest hit with tmin <= t <= tmax (ties to
+// the lowest triangle id), or, with ANY, the first hit found (TraceRay with
+// ACCEPT_FIRST_HIT_AND_END_SEARCH).  Counts node visits and triangle tests; sets `overflow` when
+// the fixed-depth stack overflowed (the result is then possibly not the closest).
+template <bool ANY>
+__device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, float ox, float oy,
+                                                float oz, float dx, float dy, float dz, float tmin, float tmax,
+                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow) {
+    TraceResult res;
+    res.prim = 0xFFFFFFFFu;
+    res.t = tmax;
+    res.b1 = res.b2 = 0.f;
+    // A zero or non-finite direction (e.g. the zero vector a grating returns for an evanescent
+    // diffraction order) makes every watertight test yield t = NaN, so nothing can be hit; the
+    // slab test would not cull anything for it (fminf/fmaxf drop NaNs), so return the miss here.
+    const float dsum = fabsf(dx) + fabsf(dy) + fabsf(dz);
+    if (!(dsum > 0.f) || !(dsum < INFINITY)) return res;
+    const float ix = safeRcp(dx), iy = safeRcp(dy), iz = safeRcp(dz);
+    float bestT = tmax, bestB1 = 0.f, bestB2 = 0.f;
+    uint32_t bestPrim = 0xFFFFFFFFu;
+    bool done = false;
+    int2 stack[kStackDepth];
+    int sp = 0;
+    int32_t node = 0;
+
+    auto leaf = [&](int32_t ref) {
+        const uint32_t v = (uint32_t)~ref;
+        const uint32_t first = v >> 4, count = (v & 15u) + 1u;
+        for (uint32_t k = first; k < first + count; ++k) {
+            const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
+            ++triTests;
+            const TriHit h = watertight(ox, oy, oz, dx, dy, dz, v0, v1, v2);
+            if (!h.hit || !(h.t >= tmin) || !(h.t <= bestT)) continue;
+            const uint32_t prim = __float_as_uint(v0.w);
+            if (ANY) {
+                bestT = h.t;
+                bestPrim = prim;
+                done = true;
+                return;
+            }
+            if (h.t < bestT || prim < bestPrim) {
+                bestT = h.t;
+                bestPrim = prim;
+                bestB1 = h.b1;
+                bestB2 = h.b2;
+            }
+        }
+    };
+
+    for (;;) {
+        ++nodeVisits;
+        const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
+        const int4 r = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
+        const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
+        const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
+        float tl = 0.f, tr = 0.f;
+        bool hl = r.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
+        bool hr = r.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
+        if (hl && r.x < 0) { leaf(r.x); hl = false; if (ANY && done) break; }
+        if (hr && r.y < 0) { leaf(r.y); hr = false; if (ANY && done) break; }
+        if (hl && hr) {
+            const bool leftNear = tl <= tr;
+            if (sp < kStackDepth) stack[sp++] = make_int2(leftNear ? r.y : r.x, __float_as_int(leftNear ? tr : tl));
+            else overflow = 1;
+            node = leftNear ? r.x : r.y;
+            continue;
+        }
+        if (hl) { node = r.x; continue; }
+        if (hr) { node = r.y; continue; }
+        // pop the nearest pending node that can still hold a closer hit
+        bool found = false;
+        while (sp > 0) {
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= bestT * kTfarScale) { node = e.x; found = true; break; }
+        }
+        if (!found) break;
+    }
+    res.prim = bestPrim;
+    res.t = bestT;
+    res.b1 = bestB1;
+    res.b2 = bestB2;
+    return res;
+}
+
 }  // namespace pltdev

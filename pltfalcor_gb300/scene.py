@@ -53,8 +53,11 @@ def grid_quad(corner, e1, e2, n):
 class Scene:
     """Triangle soup with per-triangle material indices, material records and light data."""
 
-    def __init__(self, vertices, indices, tri_material, records, emissive_tris, light_material, mnee_material, bounds):
+    def __init__(self, vertices, indices, tri_material, records, emissive_tris, light_material, mnee_material, bounds,
+                 normals=None):
         self.vertices = np.ascontiguousarray(vertices, np.float32)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        self.tangents = None
         self.indices = np.ascontiguousarray(indices, np.uint32)
         self.tri_material = np.ascontiguousarray(tri_material, np.uint32)
         self.records = records
@@ -83,14 +86,15 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
     wall = M.opaque_dielectric(1, 0.3, albedo=(0.7, 0.7, 0.7))
     records = np.concatenate([recs, light, glass, wall])
     light_mat, glass_mat, wall_mat = len(recs), len(recs) + 1, len(recs) + 2
-    verts, faces, mats = [], [], []
+    verts, faces, mats, norms = [], [], [], []
     nv = 0
 
-    def add(v, f, m):
+    def add(v, f, m, n):
         nonlocal nv
         verts.append(v)
         faces.append(f + nv)
         mats.append(np.full(len(f), m, np.uint32))
+        norms.append(np.broadcast_to(np.asarray(n, np.float64), v.shape))
         nv += len(v)
 
     # room: six subdivided faces of [-room, room]^3
@@ -103,22 +107,23 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
                (np.array([R, -R, -R]), np.array([0, 0, 2 * R]), np.array([0, 2 * R, 0]))]
     for c, e1, e2 in corners:
         v, f = grid_quad(c, e1, e2, box_subdiv)
-        add(v, f, wall_mat)
-    # area light under the ceiling (z = +R is the ceiling)
-    v, f = grid_quad(np.array([-1.5, -1.5, R - 0.05]), np.array([3.0, 0, 0]), np.array([0, 3.0, 0]), 1)
+        add(v, f, wall_mat, _unit(np.cross(e1, e2)))
+    # area light under the ceiling (z = +R is the ceiling), emitting downwards
+    e1, e2 = np.array([0, 3.0, 0]), np.array([3.0, 0, 0])
+    v, f = grid_quad(np.array([-1.5, -1.5, R - 0.05]), e1, e2, 1)
     first_emissive = sum(len(x) for x in faces)
-    add(v, f, light_mat)
+    add(v, f, light_mat, _unit(np.cross(e1, e2)))
     emissive = np.arange(first_emissive, first_emissive + len(f))
     # smooth dielectric sphere below the light (manifold NEE occluder)
     sv, sf = icosphere(min(sphere_level, 4))
-    add(sv * 1.2 + np.array([0.0, 0.0, R - 4.0]), sf, glass_mat)
+    add(sv * 1.2 + np.array([0.0, 0.0, R - 4.0]), sf, glass_mat, sv)
     # random icospheres
     cx, cy, cz, rad, mt, mi = u(), u(), u(), u(), u(), u()
     for s in range(n_spheres):
         r = 0.25 + 0.75 * rad[s]
         c = np.array([(2 * cx[s] - 1) * (R - 1.5), (2 * cy[s] - 1) * (R - 1.5), (2 * cz[s] - 1) * (R - 6.0) - 1.0])
         t = min(int(mt[s] * 8), 7)
-        add(sv * r + c, sf, t * per_type + min(int(mi[s] * per_type), per_type - 1))
+        add(sv * r + c, sf, t * per_type + min(int(mi[s] * per_type), per_type - 1), sv)
     # random quads
     qx, qy, qz, qa, qb, qs, qt, qm = u(), u(), u(), u(), u(), u(), u(), u()
     for q in range(n_quads):
@@ -131,11 +136,48 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
         size = 0.5 + 1.5 * qs[q]
         v, f = grid_quad(c - 0.5 * size * (e1 + e2), size * e1, size * e2, 1)
         t = min(int(qt[q] * 8), 7)
-        add(v, f, t * per_type + min(int(qm[q] * per_type), per_type - 1))
+        add(v, f, t * per_type + min(int(qm[q] * per_type), per_type - 1), _unit(np.cross(size * e1, size * e2)))
     V = np.concatenate(verts).astype(np.float32)
     F = np.concatenate(faces).astype(np.uint32)
     Mt = np.concatenate(mats)
-    return Scene(V, F, Mt, records, emissive, light_mat, glass_mat, (-R, R))
+    Nv = np.concatenate(norms)
+    Nv = (Nv / np.linalg.norm(Nv, axis=1, keepdims=True)).astype(np.float32)
+    return Scene(V, F, Mt, records, emissive, light_mat, glass_mat, (-R, R), normals=Nv)
+
+
+def small_scene(seed=3):
+    """The procedural room at test size (about 8 K triangles): 12 level-2 icospheres, 40 quads,
+    4x4 box faces, the light and the glass sphere."""
+    return procedural_scene(seed=seed, n_spheres=12, sphere_level=2, n_quads=40, box_subdiv=4)
+
+
+def _unit(v):
+    v = np.asarray(v, np.float64)
+    return v / np.linalg.norm(v)
+
+
+def look_at_camera(pos, target, up, fovy_deg, aspect, focal_distance=1.0):
+    """plt_camera with Falcor's CameraData construction (Scene/Camera/Camera.cpp, calculateCameraParameters):
+    W = normalize(target - pos) * focal distance, U/V orthonormal scaled by the image-plane half extents."""
+    from . import capi
+    pos = np.asarray(pos, np.float64)
+    W = _unit(np.asarray(target, np.float64) - pos) * focal_distance
+    U = _unit(np.cross(W, np.asarray(up, np.float64)))
+    V = _unit(np.cross(U, W))
+    vlen = focal_distance * np.tan(np.radians(fovy_deg) * 0.5)
+    U = U * vlen * aspect
+    V = V * vlen
+    cam = capi.Camera()
+    for name, val in (("pos", pos), ("u", U), ("v", V), ("w", W)):
+        arr = getattr(cam, name)
+        for i in range(3):
+            arr[i] = float(val[i])
+    return cam
+
+
+def room_camera(width, height, room=10.0):
+    """The benchmark view: from near the front wall towards the room centre, light and glass sphere in view."""
+    return look_at_camera((0.0, -(room - 1.0), -1.0), (0.0, 0.0, 2.0), (0.0, 0.0, 1.0), 75.0, width / height)
 
 
 def random_rays(n, seed, bounds, scene_tris=None):
