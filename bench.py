@@ -174,6 +174,84 @@ def trace_bench(ctx, dev, stream, steps, warmup):
     return out
 
 
+def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
+    """PLTPT render pass (sample + solve) on the 1.04 M-triangle procedural room: 1024^2 paths per
+    frame, max depth 8, HWSS 4 with spectral MIS, NEE + MIS, Russian roulette, power-sampled
+    emissive light; one frame per launch sequence, `frames` frames timed with CUDA events.  e2e
+    adds the device-to-host read of the accumulated image.  The CPU figure is the oracle's
+    restatement of both passes (OpenMP, its own BVH) on a 128^2 image of the same view."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from pltfalcor_gb300 import scene as S, spectra
+    from pltfalcor_gb300.bsdf import PLTContext
+    prof, _ = spectra.standard_profiles()
+    sc = S.procedural_scene()
+    opts = {"max_bounces": 8, "hwss": 4, "do_mnee": 0}
+    ctx = PLTContext(opts)
+    ctx.load_scene(sc, prof)
+    W = H = 1024
+    cam = S.room_camera(W, H)
+    out = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+    ctx.render(cam, W, H, out, 0, max(1, warmup), stream)
+    torch.cuda.synchronize()
+    st = ctx.check_status(stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.render(cam, W, H, out, 1000, frames, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / frames
+    stats = ctx.render_stats()
+    host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for f in range(frames):
+        ctx.render(cam, W, H, out, 2000 + f, 1, stream)
+        host.copy_(out, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1) / frames
+    res = {"workload": "procedural room 1.04 M triangles, 1024x1024 paths/frame, max depth 8, HWSS 4 + spectral MIS, NEE + MIS, RR "
+                       "(manifold NEE not yet in the GPU path)",
+           "status": int(st), "frames": frames, "ms_per_frame": ms, "paths_per_s": W * H / (ms * 1e-3),
+           "e2e": {"paths_per_s": W * H / (ms_e2e * 1e-3), "d2h_bytes_per_frame": W * H * 16, "h2d_bytes_per_frame": 0},
+           "bounces_per_path": stats["bounces"] / (W * H), "shadow_rays_per_path": stats["shadow_rays"] / (W * H),
+           "bsdf_evals_per_path": stats["bsdf_evals"] / (W * H), "gpu_launches_per_frame": 8 + 1 + 2 + 1}
+    ctx.close()
+    if cpu_seconds > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        opt = capi_options(opts)
+        w = h = 256
+        ccam = S.room_camera(w, h)
+        setups = []
+        for _ in range(2):   # set-up alone (scene copy, BVH, light table): a 1-pixel render
+            t0 = time.perf_counter()
+            oracle.render(sc, prof, ccam, opt, 1, 1, frame=0)
+            setups.append(time.perf_counter() - t0)
+        setup = min(setups)
+        calls, frames, t0 = 0, 2, time.perf_counter()
+        while calls == 0 or time.perf_counter() - t0 < cpu_seconds + calls * setup:
+            oracle.render(sc, prof, ccam, opt, w, h, frame=calls * frames, frames=frames)
+            calls += 1
+        dt = max(1e-6, time.perf_counter() - t0 - calls * setup)
+        res["cpu_baseline"] = {"value": calls * frames * w * h / dt, "unit": "paths/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "%d frames of a 256x256 image of the same view and options, %.1f s of rendering "
+                                         "(per-call set-up of %.2f s excluded)" % (calls * frames, dt, setup)}
+    return res
+
+
+def capi_options(overrides):
+    import ctypes as C
+    from pltfalcor_gb300 import capi
+    o = capi.Options()
+    capi.load_library().plt_options_default(C.byref(o))
+    for k, v in overrides.items():
+        setattr(o, k, v)
+    return o
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -344,6 +422,9 @@ def run_ours(args):
                 "gpu_launches": 2 * args.steps, "roofline": roof, "clocks": clocks}
         if not args.no_trace:
             line["trace"] = trace_bench(ctx, dev, stream, max(3, min(args.steps, 50)), max(1, args.warmup))
+        if not args.no_render:
+            line["render"] = render_bench(dev, stream, max(3, min(args.steps // 10, 16)), 1,
+                                          cpu_seconds=0.0 if (world > 1 or args.no_cpu_baseline) else min(args.cpu_seconds, 10.0))
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         print(json.dumps(line))
@@ -361,6 +442,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-trace", action="store_true")
+    ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

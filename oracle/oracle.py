@@ -38,6 +38,8 @@ def load():
         lib.plto_bsdf_batch_range.argtypes = [i32, i32, vp, u32, vp, u32, vp, vp, u32, i32, C.c_uint64, C.c_uint64]
         lib.plto_trace_brute.restype = None
         lib.plto_trace_brute.argtypes = [vp, u32, vp, vp, vp, vp, u32, i32, vp, vp, vp, vp, i32]
+        lib.plto_trace_bvh.restype = None
+        lib.plto_trace_bvh.argtypes = [vp, u32, vp, vp, vp, vp, u32, i32, vp, vp, vp, vp, i32]
         lib.plto_set_sr_seed.restype = None
         lib.plto_set_sr_seed.argtypes = [C.c_uint64]
         lib.plto_count_ops.restype = i32
@@ -136,9 +138,11 @@ def count_ops(wl, ops=None):
     return {t: {"fp": a[t, 0], "sfu": a[t, 1], "div": a[t, 2], "count": int(a[t, 3])} for t in range(12) if a[t, 3] > 0}
 
 
-def trace_brute(tri_verts, origin, direction, tmin=None, tmax=None, any_hit=False, threads=0):
-    """Brute-force closest hit (prim, t, bary) or occlusion over all triangles ([n_tri][9] vertices)."""
+def trace_brute(tri_verts, origin, direction, tmin=None, tmax=None, any_hit=False, threads=0, bvh=False):
+    """Brute-force closest hit (prim, t, bary) or occlusion over all triangles ([n_tri][9] vertices);
+    bvh=True runs the same query through the oracle's BVH (identical results)."""
     lib = load()
+    fn = lib.plto_trace_bvh if bvh else lib.plto_trace_brute
     tv = np.ascontiguousarray(tri_verts, np.float32)
     o = np.ascontiguousarray(origin, np.float32)
     d = np.ascontiguousarray(direction, np.float32)
@@ -148,15 +152,15 @@ def trace_brute(tri_verts, origin, direction, tmin=None, tmax=None, any_hit=Fals
     t1 = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
     if any_hit:
         occ = np.zeros(n, np.uint32)
-        lib.plto_trace_brute(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
-                             n, 1, None, None, None, C.c_void_p(occ.ctypes.data), threads or os.cpu_count())
+        fn(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
+           n, 1, None, None, None, C.c_void_p(occ.ctypes.data), threads or os.cpu_count())
         return occ
     prim = np.zeros(n, np.uint32)
     t = np.zeros(n, np.float32)
     bary = np.zeros(2 * n, np.float32)
-    lib.plto_trace_brute(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
-                         n, 0, C.c_void_p(prim.ctypes.data), C.c_void_p(t.ctypes.data), C.c_void_p(bary.ctypes.data), None,
-                         threads or os.cpu_count())
+    fn(C.c_void_p(tv.ctypes.data), len(tv), C.c_void_p(o.ctypes.data), C.c_void_p(d.ctypes.data), p(t0), p(t1),
+       n, 0, C.c_void_p(prim.ctypes.data), C.c_void_p(t.ctypes.data), C.c_void_p(bary.ctypes.data), None,
+       threads or os.cpu_count())
     return prim, t, bary
 
 
@@ -183,7 +187,7 @@ def _scene_struct(scene, profiles):
     return s, (keep, tan, profiles)
 
 
-def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False):
+def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1):
     """FP32 oracle render of one frame: rgb [height][width][3]; with records=True also per-path bounce
     records (prim, lobe, flags) [height*width][max_bounces+1] and stats (paths, shadow rays, evals).
     `profiles` is a ctypes array of plt_spectral_profile, `camera`/`options` the ctypes structs of
@@ -191,7 +195,7 @@ def render(scene, profiles, camera, options, width, height, frame=0, threads=0, 
     lib = load()
     if not hasattr(lib, "_render_sig"):
         lib.plto_render.restype = C.c_int
-        lib.plto_render.argtypes = [C.c_void_p] * 3 + [C.c_uint32] * 3 + [C.c_int] + [C.c_void_p] * 5
+        lib.plto_render.argtypes = [C.c_void_p] * 3 + [C.c_uint32] * 4 + [C.c_int] + [C.c_void_p] * 5
         lib.plto_light_table.restype = C.c_uint32
         lib.plto_light_table.argtypes = [C.c_void_p] * 4
         lib._render_sig = True
@@ -200,7 +204,7 @@ def render(scene, profiles, camera, options, width, height, frame=0, threads=0, 
     nb = options.max_bounces + 1
     recs = [np.zeros((height * width, nb), np.uint32) for _ in range(3)] if records else [None] * 3
     stats = np.zeros(3, np.uint64)
-    st = lib.plto_render(C.addressof(s), C.addressof(camera), C.addressof(options), width, height, frame,
+    st = lib.plto_render(C.addressof(s), C.addressof(camera), C.addressof(options), width, height, frame, frames,
                          threads or os.cpu_count(), rgb.ctypes.data, *[None if r is None else r.ctypes.data for r in recs],
                          stats.ctypes.data)
     if st != 0:

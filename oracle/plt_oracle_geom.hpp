@@ -11,6 +11,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <algorithm>
+#include <vector>
 
 namespace plt_oracle {
 namespace geom {
@@ -178,6 +180,125 @@ inline uint16_t floatToHalfRne(float f) {
     if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
     return (uint16_t)(sign | h);
 }
+
+
+// Bounding-volume hierarchy over tri[ntri][9] for the oracle's ray casts: median splits on the
+// longest centroid axis, up to 4 triangles per leaf, boxes padded by 2^-18 of their extent plus
+// 2^-20 of the coordinate magnitude so no box that holds a hit can be culled.  The query returns
+// exactly what traceBrute returns (lowest t in [t0, t1], ties to the lowest index).
+struct OracleBvh {
+    struct Node { float lo[3], hi[3]; int32_t left, right, first, count; };
+    std::vector<Node> nodes;
+    std::vector<uint32_t> order;
+    const float* tri = nullptr;
+
+    void build(const float* t, uint32_t n) {
+        tri = t;
+        order.resize(n);
+        for (uint32_t i = 0; i < n; ++i) order[i] = i;
+        nodes.clear();
+        nodes.reserve(2 * (size_t)n + 1);
+        if (n) buildRec(0, n);
+    }
+    int32_t buildRec(uint32_t b, uint32_t e) {
+        Node nd;
+        for (int c = 0; c < 3; ++c) { nd.lo[c] = INFINITY; nd.hi[c] = -INFINITY; }
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t i = b; i < e; ++i) {
+            const float* v = tri + 9 * (size_t)order[i];
+            for (int c = 0; c < 3; ++c) {
+                const float mn = std::fmin(v[c], std::fmin(v[3 + c], v[6 + c]));
+                const float mx = std::fmax(v[c], std::fmax(v[3 + c], v[6 + c]));
+                nd.lo[c] = std::fmin(nd.lo[c], mn);
+                nd.hi[c] = std::fmax(nd.hi[c], mx);
+                const float ce = 0.5f * (mn + mx);
+                clo[c] = std::fmin(clo[c], ce);
+                chi[c] = std::fmax(chi[c], ce);
+            }
+        }
+        for (int c = 0; c < 3; ++c) {
+            const float pad = (nd.hi[c] - nd.lo[c]) * 0x1p-18f + std::fmax(std::fabs(nd.lo[c]), std::fabs(nd.hi[c])) * 0x1p-20f + 1e-30f;
+            nd.lo[c] -= pad;
+            nd.hi[c] += pad;
+        }
+        const int32_t id = (int32_t)nodes.size();
+        nodes.push_back(nd);
+        if (e - b <= 4) {
+            nodes[id].left = nodes[id].right = -1;
+            nodes[id].first = (int32_t)b;
+            nodes[id].count = (int32_t)(e - b);
+            return id;
+        }
+        int axis = 0;
+        for (int c = 1; c < 3; ++c) if (chi[c] - clo[c] > chi[axis] - clo[axis]) axis = c;
+        const uint32_t mid = b + (e - b) / 2;
+        auto key = [&](uint32_t t) {
+            const float* v = tri + 9 * (size_t)t;
+            return std::fmin(v[axis], std::fmin(v[3 + axis], v[6 + axis])) + std::fmax(v[axis], std::fmax(v[3 + axis], v[6 + axis]));
+        };
+        std::nth_element(order.begin() + b, order.begin() + mid, order.begin() + e,
+                         [&](uint32_t x, uint32_t y) { const float kx = key(x), ky = key(y); return kx < ky || (kx == ky && x < y); });
+        const int32_t l = buildRec(b, mid);
+        const int32_t r = buildRec(mid, e);
+        nodes[id].left = l;
+        nodes[id].right = r;
+        nodes[id].first = nodes[id].count = 0;
+        return id;
+    }
+    static bool slab(const Node& n, const float o[3], const float inv[3], float t0, float t1) {
+        float tn = t0, tf = t1;
+        for (int c = 0; c < 3; ++c) {
+            float a = (n.lo[c] - o[c]) * inv[c], b = (n.hi[c] - o[c]) * inv[c];
+            if (std::isnan(a) || std::isnan(b)) { a = -INFINITY; b = INFINITY; }
+            if (a > b) std::swap(a, b);
+            tn = std::fmax(tn, a);
+            tf = std::fmin(tf, b);
+        }
+        return tn <= tf * 1.0000005f;
+    }
+    uint32_t trace(const float o[3], const float d[3], float t0, float t1, bool any, float& tHit, float& b1, float& b2) const {
+        float bestT = t1, bb1 = 0.f, bb2 = 0.f;
+        uint32_t best = 0xFFFFFFFFu;
+        tHit = bestT;
+        b1 = b2 = 0.f;
+        const float dsum = std::fabs(d[0]) + std::fabs(d[1]) + std::fabs(d[2]);
+        if (nodes.empty() || !(dsum > 0.f) || !(dsum < INFINITY)) return best;
+        const float inv[3] = {1.f / d[0], 1.f / d[1], 1.f / d[2]};
+        int32_t stack[128];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const Node& n = nodes[(size_t)stack[--sp]];
+            if (!slab(n, o, inv, t0 - std::fabs(t0) * 1e-6f, bestT)) continue;
+            if (n.left < 0) {
+                for (int32_t i = n.first; i < n.first + n.count; ++i) {
+                    const uint32_t k = order[(size_t)i];
+                    float t, u, v;
+                    if (!intersectRayTriangle(o, d, tri + 9 * (size_t)k, t, u, v)) continue;
+                    if (!(t >= t0) || !(t <= bestT)) continue;
+                    if (t < bestT || k < best) {
+                        bestT = t;
+                        best = k;
+                        bb1 = u;
+                        bb2 = v;
+                        if (any) { tHit = bestT; b1 = bb1; b2 = bb2; return best; }
+                    }
+                }
+            } else {
+                if (sp + 2 > 128) return traceFallback(o, d, t0, t1, any, tHit, b1, b2);
+                stack[sp++] = n.right;
+                stack[sp++] = n.left;
+            }
+        }
+        tHit = bestT;
+        b1 = bb1;
+        b2 = bb2;
+        return best;
+    }
+    uint32_t traceFallback(const float o[3], const float d[3], float t0, float t1, bool any, float& tHit, float& b1, float& b2) const {
+        return traceBrute(tri, (uint32_t)order.size(), o, d, t0, t1, any, tHit, b1, b2);
+    }
+};
 
 }  // namespace geom
 }  // namespace plt_oracle

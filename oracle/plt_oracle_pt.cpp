@@ -53,6 +53,7 @@ struct Scene {
     std::vector<uint32_t> matFlags;
     SceneTables tables;
     std::vector<float> triVerts;       // [nt][9]
+    geom::OracleBvh bvh;
     // light collection (LightCollection.cpp, EmissivePowerSampler.cpp)
     std::vector<uint32_t> lightTri;    // light triangle -> primitive
     std::vector<uint32_t> primToLight; // primitive -> light triangle or kNone
@@ -495,12 +496,12 @@ struct Renderer {
 
     uint32_t trace(F3 org, F3 dir, float t0, float t1, float& t, float& b1, float& b2) const {
         const float O[3] = {org.x, org.y, org.z}, D[3] = {dir.x, dir.y, dir.z};
-        return geom::traceBrute(s.triVerts.data(), s.nt, O, D, t0, t1, false, t, b1, b2);
+        return s.bvh.trace(O, D, t0, t1, false, t, b1, b2);
     }
     bool visible(F3 org, F3 dir, float t0, float t1) const {
         const float O[3] = {org.x, org.y, org.z}, D[3] = {dir.x, dir.y, dir.z};
         float t, b1, b2;
-        return geom::traceBrute(s.triVerts.data(), s.nt, O, D, t0, t1, true, t, b1, b2) == kNone;
+        return s.bvh.trace(O, D, t0, t1, true, t, b1, b2) == kNone;
     }
 
     // Camera.computeRayPinhole, Camera.slang:46-78
@@ -865,13 +866,15 @@ typedef struct plto_scene {
     const plt_spectral_profile* profiles;
 } plto_scene;
 
-// Renders frame `frame` of a width x height image into rgb [height][width][3].  Optional per-path
-// records [height*width][max_bounces+1] of bounce primitive (0xFFFFFFFF when absent), lobe and flags.
+// Renders frames frame .. frame + frames - 1 of a width x height image into rgb [height][width][3]
+// (their mean).  Optional per-path records [height*width][max_bounces+1] of bounce primitive
+// (0xFFFFFFFF when absent), lobe and flags, of the last frame.
 // stats (optional, 3 values): paths, shadow rays, forward BSDF evaluations.  MNEE is not restated
 // yet: do_mnee must be 0.
 int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* opt, uint32_t width, uint32_t height,
-                uint32_t frame, int threads, float* rgb, uint32_t* rec_prim, uint32_t* rec_lobe, uint32_t* rec_flags,
-                uint64_t* stats) {
+                uint32_t frame, uint32_t frames, int threads, float* rgb, uint32_t* rec_prim, uint32_t* rec_lobe,
+                uint32_t* rec_flags, uint64_t* stats) {
+    if (frames == 0) return PLT_INVALID_ARG;
     if (!sc || !cam || !opt || !rgb) return PLT_INVALID_ARG;
     if (opt->hwss < 1 || opt->hwss > 4 || opt->do_mnee) return PLT_NOT_SUPPORTED;
     Scene s;
@@ -896,6 +899,7 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
         for (int k = 0; k < 3; ++k)
             for (int c = 0; c < 3; ++c) s.triVerts[9 * (size_t)t + 3 * k + c] = s.pos[3 * (size_t)s.idx[3 * (size_t)t + k] + c];
     buildLights(s);
+    s.bvh.build(s.triVerts.data(), s.nt);
 
     Options o;
     o.maxBounces = opt->max_bounces;
@@ -912,10 +916,12 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.sourcingArea = opt->sourcing_area_from_emissive_geometry;
     o.maxBeamOmega = opt->sourcing_max_beam_omega;
 
-    Renderer R{s, *cam, o, width, height, frame};
     const uint32_t nb = o.maxBounces + 1;
     const int64_t npix = (int64_t)width * height;
     uint64_t shadow = 0, evals = 0;
+    std::vector<double> acc(frames > 1 ? 3 * (size_t)npix : 0, 0.0);
+    for (uint32_t f = 0; f < frames; ++f) {
+    Renderer R{s, *cam, o, width, height, frame + f};
 #ifdef _OPENMP
 #pragma omp parallel num_threads(threads > 0 ? threads : 1) if (threads != 1) reduction(+ : shadow, evals)
 #endif
@@ -941,6 +947,9 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
         shadow += st[0];
         evals += st[1];
     }
+    if (frames > 1) for (size_t k = 0; k < acc.size(); ++k) acc[k] += rgb[k];
+    }
+    if (frames > 1) for (size_t k = 0; k < acc.size(); ++k) rgb[k] = (float)(acc[k] / frames);
     if (stats) {
         stats[0] = (uint64_t)npix;
         stats[1] = shadow;

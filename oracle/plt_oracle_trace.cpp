@@ -6,55 +6,9 @@
 #include <cstdint>
 #include <cstring>
 
-namespace {
+#include "plt_oracle_geom.hpp"
 
-bool intersectRayTriangle(const float o[3], const float d[3], const float* v, float& t, float& b1, float& b2) {
-    const float absDir[3] = {std::fabs(d[0]), std::fabs(d[1]), std::fabs(d[2])};
-    unsigned axis = 0;
-    if (absDir[1] > absDir[0] && absDir[1] > absDir[2]) axis = 1;
-    if (absDir[2] > absDir[0] && absDir[2] > absDir[1]) axis = 2;
-    unsigned kz = axis;
-    unsigned kx = (kz + 1) % 3;
-    unsigned ky = (kx + 1) % 3;
-    if (d[kz] < 0.f) { const unsigned s = kx; kx = ky; ky = s; }
-    const float Sx = d[kx] / d[kz];
-    const float Sy = d[ky] / d[kz];
-    const float Sz = 1.f / d[kz];
-    const float A[3] = {v[0] - o[0], v[1] - o[1], v[2] - o[2]};
-    const float B[3] = {v[3] - o[0], v[4] - o[1], v[5] - o[2]};
-    const float C[3] = {v[6] - o[0], v[7] - o[1], v[8] - o[2]};
-    const float Ax = A[kx] - Sx * A[kz];
-    const float Ay = A[ky] - Sy * A[kz];
-    const float Bx = B[kx] - Sx * B[kz];
-    const float By = B[ky] - Sy * B[kz];
-    const float Cx = C[kx] - Sx * C[kz];
-    const float Cy = C[ky] - Sy * C[kz];
-    float U = Cx * By - Cy * Bx;
-    float V = Ax * Cy - Ay * Cx;
-    float W = Bx * Ay - By * Ax;
-    if (U == 0.f || V == 0.f || W == 0.f) {
-        const double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
-        U = (float)(CxBy - CyBx);
-        const double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
-        V = (float)(AxCy - AyCx);
-        const double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
-        W = (float)(BxAy - ByAx);
-    }
-    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
-    const float det = U + V + W;
-    if (det == 0.f) return false;
-    const float Az = Sz * A[kz];
-    const float Bz = Sz * B[kz];
-    const float Cz = Sz * C[kz];
-    const float T = U * Az + V * Bz + W * Cz;
-    const float rcpDet = 1.f / det;
-    t = T * rcpDet;
-    b1 = V * rcpDet;
-    b2 = W * rcpDet;
-    return true;
-}
-
-}  // namespace
+using plt_oracle::geom::intersectRayTriangle;
 
 extern "C" {
 
@@ -92,6 +46,34 @@ void plto_trace_brute(const float* tri, uint32_t ntri, const float* origin, cons
             prim[i] = best;
             if (tout) tout[i] = best != 0xFFFFFFFFu ? bestT : -1.f;
             if (bary) { bary[i] = bb1; bary[n + i] = bb2; }
+        }
+    }
+}
+
+// Same query through the oracle's own BVH (plt_oracle_geom.hpp); must return what the brute force
+// returns (hit ids, distances, barycentrics) -- the path-tracing oracle casts its rays this way.
+void plto_trace_bvh(const float* tri, uint32_t ntri, const float* origin, const float* dir, const float* tmin,
+                    const float* tmax, uint32_t n, int any, uint32_t* prim, float* tout, float* bary, uint32_t* occluded,
+                    int threads) {
+    plt_oracle::geom::OracleBvh bvh;
+    bvh.build(tri, ntri);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(threads > 0 ? threads : 1) if (threads != 1)
+#endif
+    for (long long ii = 0; ii < (long long)n; ++ii) {
+        const uint32_t i = (uint32_t)ii;
+        const float o[3] = {origin[i], origin[n + i], origin[2 * (size_t)n + i]};
+        const float d[3] = {dir[i], dir[n + i], dir[2 * (size_t)n + i]};
+        const float t0 = tmin ? tmin[i] : 0.f;
+        const float t1 = tmax ? tmax[i] : 3.402823466e+38f;
+        float t, b1, b2;
+        const uint32_t best = bvh.trace(o, d, t0, t1, any != 0, t, b1, b2);
+        if (any) {
+            occluded[i] = best != 0xFFFFFFFFu ? 1u : 0u;
+        } else {
+            prim[i] = best;
+            if (tout) tout[i] = best != 0xFFFFFFFFu ? t : -1.f;
+            if (bary) { bary[i] = b1; bary[n + i] = b2; }
         }
     }
 }

@@ -34,3 +34,27 @@ def test_known_distance_and_barycentrics(oracle_lib):
     prim, t, b = oracle.trace_brute(tv, o, d)
     assert prim[0] == 0 and t[0] == 2.0
     assert abs(b[0] - 0.25) < 1e-6 and abs(b[1] - 0.5) < 1e-6
+
+
+def test_oracle_bvh_equals_brute_force(oracle_lib):
+    """The path-tracing oracle casts rays through its own BVH; on the small room (random rays, a
+    fifth aimed exactly at vertices and edge midpoints, plus zero and degenerate directions) it
+    returns exactly the brute-force hits, distances and barycentrics, and the same occlusion."""
+    sc = S.small_scene()
+    tv = sc.triangle_vertices()
+    o, d = S.random_rays(20000, 11, sc.bounds, tv)
+    d = d.reshape(3, -1)
+    d[:, :50] = 0.0                      # zero direction: no hit
+    d[0, 50:100] = 0.0                   # axis-aligned components
+    d = d.reshape(-1)
+    tmax = np.full(20000, 3.0e38, np.float32)
+    tmax[::7] = 2.5
+    pb, tb, bb = oracle.trace_brute(tv, o, d, tmax=tmax)
+    pv, tv2, bv = oracle.trace_brute(tv, o, d, tmax=tmax, bvh=True)
+    assert (pb == pv).all()
+    assert (pb[:50] == 0xFFFFFFFF).all()
+    hit = pb != 0xFFFFFFFF
+    assert (tb[hit] == tv2[hit]).all() and (bb.reshape(2, -1)[:, hit] == bv.reshape(2, -1)[:, hit]).all()
+    ob = oracle.trace_brute(tv, o, d, tmax=tmax, any_hit=True)
+    ov = oracle.trace_brute(tv, o, d, tmax=tmax, any_hit=True, bvh=True)
+    assert (ob == ov).all()
