@@ -176,8 +176,8 @@ def trace_bench(ctx, dev, stream, steps, warmup):
 
 def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
     """PLTPT render pass (sample + solve) on the 1.04 M-triangle procedural room: 1024^2 paths per
-    frame, max depth 8, HWSS 4 with spectral MIS, NEE + MIS, Russian roulette, power-sampled
-    emissive light; one frame per launch sequence, `frames` frames timed with CUDA events.  e2e
+    frame, max depth 8, HWSS 4 with spectral MIS, NEE + MIS with manifold walks, Russian roulette,
+    power-sampled emissive light; one frame per launch sequence, `frames` frames timed with CUDA events.  e2e
     adds the device-to-host read of the accumulated image.  The CPU figure is the oracle's
     restatement of both passes (OpenMP, its own BVH) on a 128^2 image of the same view."""
     import ctypes as C
@@ -187,7 +187,8 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
     from pltfalcor_gb300.bsdf import PLTContext
     prof, _ = spectra.standard_profiles()
     sc = S.procedural_scene()
-    opts = {"max_bounces": 8, "hwss": 4, "do_mnee": 0}
+    opts = {"max_bounces": 8, "hwss": 4, "do_mnee": 1, "mnee_max_occluders": 2, "mnee_max_iterations": 60,
+            "mnee_solver_threshold": 5e-5}
     ctx = PLTContext(opts)
     ctx.load_scene(sc, prof)
     W = H = 1024
@@ -212,8 +213,8 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
     f1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = f0.elapsed_time(f1) / frames
-    res = {"workload": "procedural room 1.04 M triangles, 1024x1024 paths/frame, max depth 8, HWSS 4 + spectral MIS, NEE + MIS, RR "
-                       "(manifold NEE not yet in the GPU path)",
+    res = {"workload": "procedural room 1.04 M triangles, 1024x1024 paths/frame, max depth 8, HWSS 4 + spectral MIS, NEE + MIS, RR, "
+                       "manifold NEE (2 occluders, 60 iterations, threshold 5e-5)",
            "status": int(st), "frames": frames, "ms_per_frame": ms, "paths_per_s": W * H / (ms * 1e-3),
            "e2e": {"paths_per_s": W * H / (ms_e2e * 1e-3), "d2h_bytes_per_frame": W * H * 16, "h2d_bytes_per_frame": 0},
            "bounces_per_path": stats["bounces"] / (W * H), "shadow_rays_per_path": stats["shadow_rays"] / (W * H),

@@ -268,10 +268,13 @@ plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4);
  * (Scene/SceneTypes.slang) in world space (the scene has identity instance transforms): normals
  * [n_vertices][3] (required before plt_render), tangents [n_vertices][4] (xyz + handedness sign w;
  * NULL = no tangent space, the shading frame is then built with perp_stark as in
- * ShadingUtils.slang:126-153).  Host arrays, copied.  Also builds the emissive-triangle list and
- * the power sampler's alias table from the materials set with plt_set_materials, so call it after
- * both plt_set_scene and plt_set_materials (and again when either changes). */
-plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices);
+ * ShadingUtils.slang:126-153), tri_instance [n_triangles] the geometry instance (mesh) of each
+ * triangle, which manifold walks re-project onto (Manifolds.slangh:246-248; NULL = one instance).
+ * Host arrays, copied.  Also builds the emissive-triangle list and the power sampler's alias table
+ * from the materials set with plt_set_materials, so call it after both plt_set_scene and
+ * plt_set_materials (and again when either changes). */
+plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices,
+                                 const uint32_t* tri_instance);
 
 /* Material double-sidedness, MaterialHeader::isDoubleSided (Scene/Material/MaterialData.slang:126-130),
  * carried in plt_material_record.flags; transmissive records are double-sided regardless

@@ -173,7 +173,7 @@ def rng_stream(px, py, frame, count):
 class _Scene(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("n_materials", C.c_uint32), ("n_profiles", C.c_uint32),
                 ("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("indices", C.c_void_p),
-                ("tri_material", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p)]
+                ("tri_material", C.c_void_p), ("tri_instance", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p)]
 
 
 def _scene_struct(scene, profiles):
@@ -181,10 +181,12 @@ def _scene_struct(scene, profiles):
             np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
             np.ascontiguousarray(scene.records)]
     tan = None if getattr(scene, "tangents", None) is None else np.ascontiguousarray(scene.tangents, np.float32)
+    inst = None if getattr(scene, "tri_instance", None) is None else np.ascontiguousarray(scene.tri_instance, np.uint32)
     s = _Scene(len(keep[0]), len(keep[2]), len(keep[4]), len(profiles) if profiles is not None else 0,
                keep[0].ctypes.data, keep[1].ctypes.data, None if tan is None else tan.ctypes.data, keep[2].ctypes.data,
-               keep[3].ctypes.data, keep[4].ctypes.data, C.cast(profiles, C.c_void_p) if profiles is not None else None)
-    return s, (keep, tan, profiles)
+               keep[3].ctypes.data, None if inst is None else inst.ctypes.data, keep[4].ctypes.data,
+               C.cast(profiles, C.c_void_p) if profiles is not None else None)
+    return s, (keep, tan, inst, profiles)
 
 
 def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1):

@@ -541,6 +541,32 @@ template <class R> struct DiffractionGrating {
         }
         return intensityMultiplier * ix * iy;
     }
+    // closestLobeHint, DiffractionGrating.slang:92-107: the diffraction order whose direction is
+    // closest to -woHint (manifold walks pass the direction towards the next path vertex)
+    void closestLobeHint(V3<R> wi, V3<R> woHint, R alpha, R lambda, int& lx, int& ly) const {
+        lx = ly = 0;
+        if (alpha == R(1)) return;
+        const R li2x = sqr(wi.x) + sqr(wi.z), li2y = sqr(wi.y) + sqr(wi.z);
+        const R lo2x = sqr(woHint.x) + sqr(woHint.z), lo2y = sqr(woHint.y) + sqr(woHint.z);
+        const R six = li2x > R(K_FLT_EPSILON) ? wi.x / o_sqrt(li2x) : R(0);
+        const R siy = li2y > R(K_FLT_EPSILON) ? wi.y / o_sqrt(li2y) : R(0);
+        const R sox = lo2x > R(K_FLT_EPSILON) ? -woHint.x / o_sqrt(lo2x) : R(0);
+        const R soy = lo2y > R(K_FLT_EPSILON) ? -woHint.y / o_sqrt(lo2y) : R(0);
+        auto toLobe = [&](R l) {
+            const R v = l + o_sign(l) * R(0.5);
+            const double dv = (double)o_fval(v);
+            int li = std::isfinite(dv) ? (int)std::max(-1e9, std::min(1e9, dv)) : 0;
+            return std::max(-(int)lobeCount, std::min((int)lobeCount, li));
+        };
+        const R l0 = (six - sox) / (invPitch.x * lambda);
+        lx = toLobe(l0);
+        if (alpha == R(0) && lx == 0) lx = (int)o_fval(o_sign(l0));
+        if (!is1D()) {
+            const R l1 = (siy - soy) / (invPitch.y * lambda);
+            ly = toLobe(l1);
+            if (alpha == R(0) && ly == 0) ly = (int)o_fval(o_sign(l1));
+        }
+    }
     // sampleLobe, :109-140
     void sampleLobe(V3<R> wi, int& lx, int& ly, V2<R>& pdf, R lambda, SampleGen& sg) const {
         R intensity[16];

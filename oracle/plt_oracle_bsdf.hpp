@@ -600,6 +600,43 @@ template <class R, bool CONDUCTOR> struct Grated {
         pdf = pdf * (lobePdf.x * lobePdf.y);
         return true;
     }
+    // sample with a direction hint (manifold walks), PLTDiffractionGrated*BSDF.slang:109-161
+    bool sampleHint(V3<R> wi, V3<R>& wo, R& pdf, R& weight, uint32_t& bsdfLobe, SampleGen& sg, R wavelength, uint32_t lobeMask,
+                    V3<R> woHint) const {
+        const bool hasReflection = (lobeMask & LOBE_REFLECTION) != 0;
+        const bool hasDirect = (lobeMask & LOBE_DELTA) != 0;
+        const bool hasScatter = (lobeMask & LOBE_NON_DELTA) != 0;
+        if (!hasReflection || (!hasDirect && !hasScatter)) return false;
+        const R lambda = R(1e-3) * wavelength;
+        const R k = R(K_2PI) / lambda;
+        const R a = grating.alpha(wi, k);
+        const bool hasHint = hasDirect && (woHint.x != R(0) || woHint.y != R(0) || woHint.z != R(0));
+        int lx = 0, ly = 0;
+        if (hasHint && a < R(1)) grating.closestLobeHint(wi, woHint, a, lambda, lx, ly);
+        bool isDirect = hasDirect;
+        if (hasHint) {
+            isDirect = lx == 0 && ly == 0;
+            pdf = R(1);
+        } else if (hasDirect && hasScatter) {
+            isDirect = a == R(1) || next1D<R>(sg) < a;
+            pdf = isDirect ? a : R(1) - a;
+        }
+        if (isDirect) {
+            R basePdf;
+            if (CONDUCTOR) baseC.sample(wi, wo, basePdf, weight, bsdfLobe, sg, wavelength, lobeMask);
+            else baseD.sample(wi, wo, basePdf, weight, bsdfLobe, sg, wavelength, lobeMask);
+            pdf = pdf * basePdf;
+            return true;
+        }
+        weight = CONDUCTOR ? baseC.weight(wavelength) : baseD.weight(wavelength);
+        V2<R> lobePdf = {R(1), R(1)};
+        if (!hasHint) grating.sampleLobe(wi, lx, ly, lobePdf, lambda, sg);
+        wo = grating.diffract(wi, lx, ly, lambda);
+        bsdfLobe = LOBE_DISPERSIVE_DELTA_REFLECTION;
+        encodeGratingLobe(lx, ly, bsdfLobe);
+        pdf = pdf * (lobePdf.x * lobePdf.y);
+        return true;
+    }
     R pdf(V3<R> wi, V3<R> wo, R wavelength) const {
         const R k = R(K_2PI) / (R(1e-3) * wavelength);
         const R a = grating.alpha(wi, k);

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <random>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -49,6 +50,7 @@ struct Scene {
     const float* tan = nullptr;
     const uint32_t* idx = nullptr;
     const uint32_t* triMat = nullptr;
+    const uint32_t* triInst = nullptr;   // geometry instance of each triangle (MNEE re-projection), or null = 0
     std::vector<Material<float>> mats;
     std::vector<uint32_t> matFlags;
     SceneTables tables;
@@ -68,6 +70,9 @@ struct Options {
     uint32_t maxBounces, tileSize, hwss;
     bool hwssMis, useDirect, useEmissive, doNee, doMis, doRR, perTileSg, importanceSampleEmitters;
     float sourcingArea, maxBeamOmega;
+    bool doMnee;
+    uint32_t mneeMaxOccluders, mneeMaxIterations;
+    float mneeThreshold;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -306,15 +311,270 @@ void bsdfEval(const Scene& s, const ShadingData& sd, F3 toEye, uint32_t lobe, Be
         beam.t = F.fromLocal(beam.t);
     });
 }
+bool bsdfSampleHint(const Scene& s, const ShadingData& sd, SampleGen& sg, BSDFSample& out, float wavelength, uint32_t lobeMask, F3 woHint);
+// sample(sd, sg, result, wavelength): lobe mask All, no hint (the sample pass)
 bool bsdfSample(const Scene& s, const ShadingData& sd, SampleGen& sg, BSDFSample& out, float wavelength) {
+    return bsdfSampleHint(s, sd, sg, out, wavelength, LOBE_ALL, F3{0.f, 0.f, 0.f});
+}
+// sample(sd, sg, result, wavelength, lobeMask, woHint) of the wrappers: the dielectric and the thin
+// dielectric restrict the lobes to the hint's side (PLTDielectricBSDF.slang:310-321,
+// PLTThinDielectricBSDF.slang:230-243), the grated materials pick the diffraction order closest to
+// the hint, the others ignore it.
+bool bsdfSampleHint(const Scene& s, const ShadingData& sd, SampleGen& sg, BSDFSample& out, float wavelength, uint32_t lobeMask, F3 woHint) {
     bool valid = false;
-    withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool grated, V2<float> gx) {
+    const Material<float>& m = s.mats[sd.materialID];
+    withBx(m, s.tables, [&](auto& bx, bool grated, V2<float> gx) {
         const Frame<float> F = grated ? gratingSdFrame(sd, gx) : sdFrame(sd);
-        valid = bx.sample(F.toLocal(sd.V), out.wo, out.pdf, out.weight, out.lobe, sg, wavelength, LOBE_ALL);
-        if (valid || !grated) out.wo = F.fromLocal(out.wo);
+        if (m.type == PLT_MATERIAL_DIELECTRIC || m.type == PLT_MATERIAL_THIN_DIELECTRIC) {
+            const float dh = dot(sd.V, woHint);
+            const uint32_t lobes = (dh > 0.f ? LOBE_REFLECTION : dh < 0.f ? LOBE_TRANSMISSION : LOBE_ALL) & lobeMask;
+            valid = bx.sample(F.toLocal(sd.V), out.wo, out.pdf, out.weight, out.lobe, sg, wavelength, lobes);
+            if (valid || m.type == PLT_MATERIAL_DIELECTRIC) out.wo = F.fromLocal(out.wo);
+            return;
+        }
+        if constexpr (std::is_same_v<std::decay_t<decltype(bx)>, Grated<float, true>> ||
+                      std::is_same_v<std::decay_t<decltype(bx)>, Grated<float, false>>) {
+            valid = bx.sampleHint(F.toLocal(sd.V), out.wo, out.pdf, out.weight, out.lobe, sg, wavelength, lobeMask, F.toLocal(woHint));
+        } else {
+            valid = bx.sample(F.toLocal(sd.V), out.wo, out.pdf, out.weight, out.lobe, sg, wavelength, lobeMask);
+        }
+        if (valid) out.wo = F.fromLocal(out.wo);
     });
     return valid;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Differential shading geometry and scattering derivatives for manifold walks,
+// Rendering/Utils/DifferentialShadingGeometry.slang:28-222
+// ---------------------------------------------------------------------------------------------
+struct F3pdv { F3 v, ddu, ddv; };
+struct F3kpdv { F3 v, ddu, ddv, ddl; };
+struct DSG {
+    F3pdv p, n, s, t;
+    F3 fromLocal(F3 v) const { return s.v * v.x + t.v * v.y + n.v * v.z; }
+    // pdw: direction from the surface point to dst and its derivatives
+    F3pdv pdw(F3 dst) const {
+        F3pdv w;
+        w.v = dst - p.v;
+        const float ilo = 1.f / length(w.v);
+        w.v = w.v * ilo;
+        w.ddu = (p.ddu - w.v * dot(w.v, p.ddu)) * -ilo;
+        w.ddv = (p.ddv - w.v * dot(w.v, p.ddv)) * -ilo;
+        return w;
+    }
+};
+F3 zero3() { return {0.f, 0.f, 0.f}; }
+// differentialShadingGeometry (untextured: the (1,0), (0,1) triangle parameterisation)
+DSG differentialShadingGeometry(const Scene& s, uint32_t prim, float b1, float b2) {
+    const float bary[3] = {1.f - b1 - b2, b1, b2};
+    const uint32_t* I = s.idx + 3 * (size_t)prim;
+    const F3 p0 = f3(s.pos + 3 * (size_t)I[0]), p1 = f3(s.pos + 3 * (size_t)I[1]), p2 = f3(s.pos + 3 * (size_t)I[2]);
+    const F3 n0 = f3(s.nrm + 3 * (size_t)I[0]), n1 = f3(s.nrm + 3 * (size_t)I[1]), n2 = f3(s.nrm + 3 * (size_t)I[2]);
+    DSG g;
+    g.p.v = p0 * bary[0] + p1 * bary[1] + p2 * bary[2];
+    g.n.v = n0 * bary[0] + n1 * bary[1] + n2 * bary[2];
+    const float il = 1.0f / length(g.n.v);
+    g.n.v = g.n.v * il;
+    g.p.ddu = perp_stark(g.n.v);
+    g.p.ddv = cross(g.n.v, g.p.ddu);
+    const float duv0x = 1.f, duv0y = 0.f, duv1x = 0.f, duv1y = 1.f;
+    const F3 dp0 = p1 - p0, dp1 = p2 - p0;
+    g.n.ddu = (n1 - n0) * il;
+    g.n.ddv = (n2 - n0) * il;
+    g.n.ddu = g.n.ddu - g.n.v * dot(g.n.v, g.n.ddu);
+    g.n.ddv = g.n.ddv - g.n.v * dot(g.n.v, g.n.ddv);
+    const float det = duv0x * duv1y - duv0y * duv1x;
+    if (std::fabs(det) > K_FLT_EPSILON) {
+        const float invDet = 1.0f / det;
+        g.p.ddu = (dp0 * duv1y - dp1 * duv0y) * invDet;
+        g.p.ddv = (dp0 * -duv1x + dp1 * duv0x) * invDet;
+        const F3 nddu = (g.n.ddu * duv1y - g.n.ddv * duv0y) * invDet;
+        const F3 nddv = (g.n.ddu * -duv1x + g.n.ddv * duv0x) * invDet;
+        g.n.ddu = nddu;
+        g.n.ddv = nddv;
+    } else {
+        g.n.ddu = zero3();
+        g.n.ddv = zero3();
+    }
+    g.s.v = g.p.ddu - g.n.v * dot(g.n.v, g.p.ddu);
+    float ils = 1.0f / length(g.s.v);
+    g.s.v = g.s.v * ils;
+    if (g.p.ddu.x == 0.f && g.p.ddu.y == 0.f && g.p.ddu.z == 0.f) {
+        g.s.v = perp_stark(g.n.v);
+        ils = 1.0f;
+    }
+    g.t.v = cross(g.n.v, g.s.v);
+    g.s.ddu = ((-g.n.ddu) * dot(g.n.v, g.p.ddu) - g.n.v * dot(g.n.ddu, g.p.ddu)) * ils;
+    g.s.ddv = ((-g.n.ddv) * dot(g.n.v, g.p.ddu) - g.n.v * dot(g.n.ddv, g.p.ddu)) * ils;
+    g.s.ddu = g.s.ddu - g.s.v * dot(g.s.ddu, g.s.v);
+    g.s.ddv = g.s.ddv - g.s.v * dot(g.s.ddv, g.s.v);
+    g.t.ddu = cross(g.n.ddu, g.s.v) + cross(g.n.v, g.s.ddu);
+    g.t.ddv = cross(g.n.ddv, g.s.v) + cross(g.n.v, g.s.ddv);
+    return g;
+}
+F3kpdv reflectDerivatives(const F3pdv& wi, const F3pdv& n) {
+    const float wn = dot(wi.v, n.v);
+    const float dwdun = dot(wi.ddu, n.v), dwdvn = dot(wi.ddv, n.v);
+    const float dnduw = dot(n.ddu, wi.v), dndvw = dot(n.ddv, wi.v);
+    F3kpdv r;
+    r.v = n.v * (2.f * wn) - wi.v;
+    r.ddu = (n.v * (dwdun + dnduw) + n.ddu * wn) * 2.f - wi.ddu;
+    r.ddv = (n.v * (dwdvn + dndvw) + n.ddv * wn) * 2.f - wi.ddv;
+    r.ddl = zero3();
+    return r;
+}
+F3kpdv refractDerivatives(const F3pdv& wi, F3pdv n, float eta) {
+    const float wn = dot(wi.v, n.v);
+    eta = wn < 0.f ? eta : 1.f / eta;
+    const float dEdl = 0.f;
+    if (wn < 0.f) { n.v = -n.v; n.ddu = -n.ddu; n.ddv = -n.ddv; }
+    const float eta2 = sqr(eta);
+    const float dwdun = dot(wi.ddu, n.v), dwdvn = dot(wi.ddv, n.v);
+    const float dnduw = dot(n.ddu, wi.v), dndvw = dot(n.ddv, wi.v);
+    const float root = std::sqrt(std::max(0.f, 1.f - eta2 * (1.0f - sqr(wn))));
+    F3kpdv r;
+    if (root == 0.f) { r.v = r.ddu = r.ddv = r.ddl = zero3(); return r; }
+    const float dRoot = -(1.0f - sqr(wn)) * eta * dEdl / root;
+    const float a = eta - eta2 * wn / root;
+    r.v = (wi.v - n.v * wn) * -eta - n.v * root;
+    r.ddu = n.v * (a * (dnduw + dwdun)) + n.ddu * (eta * wn - root) - wi.ddu * eta;
+    r.ddv = n.v * (a * (dndvw + dwdvn)) + n.ddv * (eta * wn - root) - wi.ddv * eta;
+    r.ddl = (wi.v - n.v * wn) * -dEdl - n.v * dRoot;
+    return r;
+}
+// DiffractionGrating.partialDerivatives, DiffractionGrating.slang:188-265
+F3kpdv gratingDerivatives(const DSG& g, const F3pdv& wi, V2<float> gx, V2<float> invPitch, int lx, int ly, float wavelength) {
+    F3kpdv ret;
+    ret.v = ret.ddu = ret.ddv = ret.ddl = zero3();
+    const F3pdv& n = g.n;
+    F3pdv X;
+    X.v = g.fromLocal(F3{gx.x, gx.y, 0.f});
+    X.ddu = g.s.ddu * gx.x + g.t.ddu * gx.y;
+    X.ddv = g.s.ddv * gx.x + g.t.ddv * gx.y;
+    if (lx == 0 && ly == 0) return reflectDerivatives(wi, n);
+    const float lambda = 1e-3f * wavelength;
+    const float lpx = (float)lx * invPitch.x, lpy = (float)ly * invPitch.y;
+    const F3 Y = cross(n.v, X.v);
+    const float x = dot(wi.v, X.v), y = dot(wi.v, Y), z = dot(wi.v, n.v);
+    const float px = std::sqrt(sqr(x) + sqr(z)), py = std::sqrt(sqr(y) + sqr(z));
+    const float ipx = px > K_FLT_EPSILON ? 1.f / px : 0.f, ipy = py > K_FLT_EPSILON ? 1.f / py : 0.f;
+    const float sinix = x * ipx, siniy = y * ipy;
+    const float a = lambda * lpx - sinix, b = lambda * lpy - siniy;
+    const float oneMinusA2 = std::max(0.f, 1 - sqr(a));
+    const float m = -oneMinusA2 / (sqr(a * b) - 1);
+    const float q = 1 - sqr(b) * m;
+    if (a > 1.f || a < -1.f || b > 1.f || b < -1.f || q < 0.f || !(m >= 0.f)) return ret;
+    const float sqrtOneM = std::sqrt(q), sqrtM = std::sqrt(m);
+    const float c = .5f / (sqrtOneM * std::sqrt(oneMinusA2));
+    const float dxdu = dot(wi.v, X.ddu) + dot(wi.ddu, X.v), dxdv = dot(wi.v, X.ddv) + dot(wi.ddv, X.v);
+    const float dzdu = dot(wi.v, n.ddu) + dot(wi.ddu, n.v), dzdv = dot(wi.v, n.ddv) + dot(wi.ddv, n.v);
+    const float dadu = z * (x * dzdu - z * dxdu) * (sqr(ipx) * ipx);
+    const float dbdu = z * (y * dzdu - z * dxdu) * (sqr(ipy) * ipy);
+    const float dadv = z * (x * dzdv - z * dxdv) * (sqr(ipx) * ipx);
+    const float dbdv = z * (y * dzdv - z * dxdv) * (sqr(ipy) * ipy);
+    const float dadl = lpx, dbdl = lpy;
+    const float den = sqr(sqr(a * b) - 1);
+    const float dmdu = 2 * a * (a * b * oneMinusA2 * dbdu - dadu * (1 - sqr(b))) / den;
+    const float dmdv = 2 * a * (a * b * oneMinusA2 * dbdv - dadv * (1 - sqr(b))) / den;
+    const float dmdl = 2 * a * (a * b * oneMinusA2 * dbdl - dadl * (1 - sqr(b))) / den;
+    ret.v = X.v * (a * sqrtOneM) + Y * (b * sqrtM) + n.v * std::sqrt(std::max(0.f, 1 - sqr(a) * q - sqr(b) * m));
+    auto d = [&](float da, float db, float dm) {
+        return X.v * ((q * da - a * b * (b * dm / 2.f + m * db)) / sqrtOneM) + Y * ((b * dm / 2.f + m * db) / sqrtM) +
+               n.v * ((-2 * a * da * q - b * (b * dm + 2.f * m * db) + sqr(a) * b * (b * dm + 2.f * m * db)) * c);
+    };
+    ret.ddu = d(dadu, dbdu, dmdu);
+    ret.ddv = d(dadv, dbdv, dmdv);
+    ret.ddl = d(dadl, dbdl, dmdl);
+    return ret;
+}
+// IMaterialInstance.partialDerivatives of each PLT*BSDF.slang (world space)
+F3kpdv bsdfPartialDerivatives(const Scene& s, uint32_t mid, const F3pdv& wi, const DSG& g, uint32_t lobe, float wavelength) {
+    const Material<float>& m = s.mats[mid];
+    switch (m.type) {
+    case PLT_MATERIAL_DIELECTRIC: {
+        Dielectric<float> b(m);
+        if (lobe & LOBE_TRANSMISSION) {
+            const float k = (float)K_2PI / (1e-3f * wavelength);
+            return refractDerivatives(wi, g.n, b.ior(k));
+        }
+        return reflectDerivatives(wi, g.n);
+    }
+    case PLT_MATERIAL_THIN_DIELECTRIC:
+        if (lobe & LOBE_TRANSMISSION) {
+            F3kpdv r;
+            r.v = -wi.v; r.ddu = -wi.ddu; r.ddv = -wi.ddv; r.ddl = zero3();
+            return r;
+        }
+        return reflectDerivatives(wi, g.n);
+    case PLT_MATERIAL_GRATED_CONDUCTOR:
+    case PLT_MATERIAL_GRATED_OPAQUE_DIELECTRIC: {
+        int lx, ly;
+        decodeGratingLobe(lobe, lx, ly);
+        if (lx == 0 && ly == 0) return reflectDerivatives(wi, g.n);
+        const DiffractionGrating<float> gr = makeGrating(m);
+        return gratingDerivatives(g, wi, gr.gratingX, gr.invPitch, lx, ly, wavelength);
+    }
+    case PLT_MATERIAL_DIFFUSE: {
+        F3kpdv r;
+        r.v = r.ddu = r.ddv = r.ddl = zero3();
+        return r;
+    }
+    default: return reflectDerivatives(wi, g.n);
+    }
+}
+
+// sphcoords / derivatives and one Newton step on the angle constraint, Manifolds.slangh:283-347
+void sphcoords(F3 w, float& theta, float& phi) {
+    theta = std::acos(std::min(std::max(w.z, -1.f), 1.f));
+    phi = std::atan2(w.y, w.x);
+    phi += phi < 0.f ? (float)K_2PI : 0.f;
+}
+bool manifoldOneStep(const F3pdv& w, const F3kpdv& ws, const F3pdv& p, float& lenC, F3& stepDir) {
+    float t0, p0, t1, p1;
+    sphcoords(w.v, t0, p0);
+    sphcoords(ws.v, t1, p1);
+    const float dt = t0 - t1;
+    float dp = p0 - p1;
+    dp = std::fabs(dp) > (float)K_PI ? dp - o_sign(dp) * (float)K_2PI : dp;
+    lenC = std::sqrt(dt * dt + dp * dp);
+    auto der = [](F3 v, F3 du, F3 dv, float out[2][2]) {
+        const float dAcos = -1.f / std::sqrt(std::max(0.f, 1.f - sqr(v.z)));
+        const float invNorm = 1.f / (v.x * v.x + v.y * v.y);
+        out[0][0] = dAcos * du.z;
+        out[0][1] = dAcos * dv.z;
+        out[1][0] = invNorm * (v.x * du.y - v.y * du.x);
+        out[1][1] = invNorm * (v.x * dv.y - v.y * dv.x);
+    };
+    float dO[2][2], dI[2][2];
+    der(w.v, w.ddu, w.ddv, dO);
+    der(ws.v, ws.ddu, ws.ddv, dI);
+    const float A = dO[0][0] - dI[0][0], B = dO[0][1] - dI[0][1], C = dO[1][0] - dI[1][0], D = dO[1][1] - dI[1][1];
+    // tryInvert with the reference's determinant threshold, MathHelpers.slang:484-498
+    const float det = A * D - B * C;
+    if (std::fabs(det) < 4e-6f) return false;
+    const float id = 1.f / det;
+    const float i00 = D * id, i01 = -B * id, i10 = -C * id, i11 = A * id;
+    const float dx = i00 * dt + i01 * dp, dy = i10 * dt + i11 * dp;
+    stepDir = p.ddu * dx + p.ddv * dy;
+    return true;
+}
+
+struct MSHit {
+    uint32_t prim;
+    float b1, b2;
+    F3 posW;
+    uint32_t lobe;
+};
+struct ManifoldSample {
+    MSHit hits[4];
+    F3 woLastHitToLight = {0.f, 0.f, 0.f};
+    int hitCount = 0;
+    uint32_t iterations = 0;
+    float wavelength = 0.f;
+    float pdf = 1.f;
+    bool dispersive = false;
+};
+
 float bsdfPdf(const Scene& s, const ShadingData& sd, F3 toLight, float wavelength) {
     float p = 0.f;
     withBx(s.mats[sd.materialID], s.tables, [&](auto& bx, bool grated, V2<float> gx) {
@@ -604,8 +864,10 @@ struct Renderer {
         uint64_t shadowRays = 0, unwindEvals = 0;
     };
 
+    // wasNEEAvailable, pltpt_solve.rt.slang:204-210
     bool wasNEEAvailable(int p, uint32_t flags) const {
-        return o.doNee && p > 0 && (flags & FLAG_LAST_DELTA) == 0;   // MNEE off
+        return o.doNee && p > 0 &&
+               ((flags & FLAG_LAST_DELTA) == 0 || (o.doMnee && (flags >> 16) <= o.mneeMaxOccluders && p > 1));
     }
 
     void forwardUnwindStep(uint32_t prim, const VertexData& v, F3 wo, uint32_t lobe, Beam<float>& beam, Solve& sv) const {
@@ -760,11 +1022,137 @@ struct Renderer {
         return valid && ls.pdf > 1e-6f && !(!sampleRefl && isReflection) && !(!sampleTrans && !isReflection);
     }
 
-    // NEE without manifold walks, pltpt_solve.rt.slang:245-366
+    // closest-hit shadow ray, ShadowRays.slangh:96-135 (a hit needs dist > 0)
+    bool shadowRay(F3 org, F3 dir, float tmin, float tmax, uint32_t& prim, float& t, float& b1, float& b2) const {
+        const float O[3] = {org.x, org.y, org.z}, D[3] = {dir.x, dir.y, dir.z};
+        prim = s.bvh.trace(O, D, tmin, tmax, false, t, b1, b2);
+        return prim != kNone && t > 0.f;
+    }
+    uint32_t instanceOf(uint32_t prim) const { return s.triInst ? s.triInst[prim] : 0u; }
+
+    // manifoldSampleVertex, Manifolds.slangh:84-108: sample a delta lobe towards the light
+    bool manifoldSampleVertex(uint32_t prim, float b1, float b2, const ShadingData& sd, F3 lightDir, SampleGen& sg,
+                              ManifoldSample& d) const {
+        BSDFSample smp;
+        if (!bsdfSampleHint(s, sd, sg, smp, d.wavelength, LOBE_DELTA, lightDir)) return false;
+        d.pdf *= smp.pdf;
+        d.hits[d.hitCount] = MSHit{prim, b1, b2, sd.posW, smp.lobe};
+        d.dispersive = d.dispersive || (smp.lobe & (LOBE_DISPERSIVE_DELTA_REFLECTION | LOBE_DISPERSIVE_DELTA_TRANSMISSION)) != 0;
+        ++d.hitCount;
+        return true;
+    }
+
+    // traceMNEEOccluders, Manifolds.slangh:110-156
+    bool traceMNEEOccluders(F3 rayO, F3 rayD, float tmin, float tmax, SampleGen& sg, int maxMS, ManifoldSample& d, Solve& sv) const {
+        const F3 wi = -rayD;
+        for (;;) {
+            uint32_t prim;
+            float t, b1, b2;
+            ++sv.shadowRays;
+            if (!shadowRay(rayO, rayD, tmin, tmax, prim, t, b1, b2)) return true;
+            if (d.hitCount >= (int)o.mneeMaxOccluders || d.hitCount >= maxMS) return false;
+            VertexData v = vertexData(s, prim, b1, b2);
+            v.posW = rayO + rayD * t;
+            const uint32_t mid = s.triMat[prim];
+            const ShadingData sd = prepareShadingData(s, v, mid, wi);
+            if (!(bsdfProps(s, mid).flags & PROP_MW_TRANSMISSIVE)) return false;
+            if (!manifoldSampleVertex(prim, b1, b2, sd, -wi, sg, d) || (d.hits[d.hitCount - 1].lobe & LOBE_TRANSMISSION) == 0)
+                return false;
+            rayO = newRayOriginToward(sd, rayD);
+            tmax -= t;
+        }
+    }
+
+    // manifoldNEESample, Manifolds.slangh:171-281: Newton walk of the occluder chain on the
+    // spherical-angle constraint, re-projected onto the same geometry instance by shadow rays,
+    // then a visibility test from the last occluder to the light.
+    bool manifoldNEESample(F3 visO, F3 visD, float visTmin, float visTmax, F3 origin, F3 lightPos, F3 lightDir, bool distant,
+                           int maxMS, SampleGen& sg, ManifoldSample& d, Solve& sv) const {
+        if (!traceMNEEOccluders(visO, visD, visTmin, visTmax, sg, maxMS, d, sv)) return false;
+        if (d.hitCount == 0) return true;
+        float beta[4] = {1.f, 1.f, 1.f, 1.f};
+        bool success = false;
+        while (!success) {
+            success = true;
+            for (int idx = 0; idx < d.hitCount; ++idx) {
+                MSHit& h = d.hits[idx];
+                const uint32_t mid = s.triMat[h.prim];
+                const DSG g = differentialShadingGeometry(s, h.prim, h.b1, h.b2);
+                const F3 p0 = idx == 0 ? origin : d.hits[idx - 1].posW;
+                const F3pdv pdv0 = g.pdw(p0);
+                const F3 p2 = idx + 1 == d.hitCount ? lightPos : d.hits[idx + 1].posW;
+                F3pdv pdv2 = {lightDir, zero3(), zero3()};
+                if (!distant) pdv2 = g.pdw(p2);
+                const bool woIsIn = dot(pdv2.v, g.n.v) < 0.f;
+                const F3pdv wi = woIsIn ? pdv0 : pdv2;
+                const F3pdv wo = woIsIn ? pdv2 : pdv0;
+                const F3kpdv wos = bsdfPartialDerivatives(s, mid, wi, g, h.lobe, d.wavelength);
+                if (wos.v.x == 0.f && wos.v.y == 0.f && wos.v.z == 0.f) return false;
+                float lenC;
+                F3 stepDir;
+                if (!manifoldOneStep(wo, wos, g.p, lenC, stepDir)) return false;
+                if (lenC < o.mneeThreshold) continue;
+                success = false;
+                for (;;) {
+                    if (++d.iterations > o.mneeMaxIterations) return false;
+                    const F3 proposal = h.posW - stepDir * beta[idx];
+                    F3 dirTo = proposal - p0;
+                    const float dist = length(dirTo);
+                    dirTo = dirTo / dist;
+                    uint32_t prim;
+                    float t, b1, b2;
+                    ++sv.shadowRays;
+                    const bool hit = shadowRay(p0, dirTo, std::max(1e-4f, .99f * dist), 1.01f * dist, prim, t, b1, b2);
+                    if (!hit || instanceOf(h.prim) != instanceOf(prim)) {
+                        beta[idx] /= 4.f;
+                        continue;
+                    }
+                    h.prim = prim;
+                    h.b1 = b1;
+                    h.b2 = b2;
+                    h.posW = p0 + dirTo * t;
+                    beta[idx] = std::min(1.0f, 2.f * beta[idx]);
+                    break;
+                }
+            }
+        }
+        const F3 pl = d.hits[d.hitCount - 1].posW;
+        F3 dir;
+        float dist;
+        if (!distant) {
+            dir = lightPos - pl;
+            dist = length(dir);
+            dir = dir / dist;
+        } else {
+            dir = lightDir;
+            dist = FLT_MAX;
+        }
+        ++sv.shadowRays;
+        const bool vis = visible(pl, dir, 1e-4f, dist);
+        d.woLastHitToLight = dir;
+        return vis;
+    }
+
+    // manifoldForwardUnwind, pltpt_solve.rt.slang:80-93
+    void manifoldForwardUnwind(const ManifoldSample& ms, F3 origin, Beam<float>& beam, Solve& sv) const {
+        for (int idx = ms.hitCount - 1; idx >= 0; --idx) {
+            const MSHit& h = ms.hits[idx];
+            VertexData v = vertexData(s, h.prim, h.b1, h.b2);
+            v.posW = h.posW;
+            const F3 p2 = idx == 0 ? origin : ms.hits[idx - 1].posW;
+            const F3 wo = normalize(p2 - v.posW);
+            forwardUnwindStep(h.prim, v, wo, h.lobe, beam, sv);
+        }
+    }
+
+    // NEE, pltpt_solve.rt.slang:245-366
     void NEE(Solve& sv, int p, const Bounce* bounces, const ShadingData& sd, const VertexData& V, uint32_t mid) const {
+        const Bounce& bounce = bounces[p];
         const Props props = bsdfProps(s, mid);
         const uint32_t lobes = props.lobes;
-        const bool sampleRefl = (lobes & 0x03u) != 0;
+        const bool allowMSOnCurrentVertex =
+            o.doMnee && p > 0 && (bounce.flags & FLAG_LAST_DELTA) == 0 && (props.flags & PROP_MW_REFLECTIVE) != 0;
+        const bool sampleRefl = (lobes & 0x03u) != 0 || allowMSOnCurrentVertex;
         const bool sampleTrans = (lobes & 0x30u) != 0;
         if (!sampleRefl && !sampleTrans) return;
         LightSample ls;
@@ -772,28 +1160,63 @@ struct Renderer {
         bool anyL = false;
         for (int j = 0; j < ls.beam.H; ++j) anyL = anyL || ls.beam.L[0][j] > 0.f;
         if (!anyL) return;
-        if (!o.hwssMis && (bounces[p].flags & FLAG_DISPERSIVE)) ls.beam.H = 1;
+        if (!o.hwssMis && (bounce.flags & FLAG_DISPERSIVE)) ls.beam.H = 1;
         const bool doMis = o.doMis;
-        ++sv.shadowRays;
-        if (!visible(ls.origin, ls.dir, 0.f, ls.distance)) return;
-        if (doMis) {
-            const float bsdfPdfV = bsdfPdf(s, sd, ls.dir, ls.beam.wl[0]);
-            scaleBeam(ls.beam, MISWeight(ls.pdf, bsdfPdfV));
+        bool evalCurrentVertex = true;
+        const int maxMSBounces = (int)o.maxBounces - p;
+        if (!o.doMnee || maxMSBounces <= 0) {
+            ++sv.shadowRays;
+            if (!visible(ls.origin, ls.dir, 0.f, ls.distance)) return;
+            if (doMis) scaleBeam(ls.beam, MISWeight(ls.pdf, bsdfPdf(s, sd, ls.dir, ls.beam.wl[0])));
+        } else {
+            const F3 lightDir = -ls.beam.r;
+            float misBsdfPdf = 0.f;
+            ManifoldSample ms;
+            ms.wavelength = ls.beam.wl[0];
+            const bool isReflection = dot(sd.N, lightDir) * dot(sd.N, sd.V) > 0.f;
+            const bool currentVertexMS = isReflection && allowMSOnCurrentVertex;
+            if (currentVertexMS) {
+                if (!manifoldSampleVertex(bounce.prim, bounce.b1, bounce.b2, sd, lightDir, sv.sg, ms) ||
+                    (ms.hits[0].lobe & LOBE_REFLECTION) == 0)
+                    return;
+            }
+            const F3 origin = !currentVertexMS ? V.posW : sv.pathOrigin;
+            const bool mneeOk = manifoldNEESample(ls.origin, ls.dir, 0.f, ls.distance, origin, ls.beam.posW, lightDir, false,
+                                                  maxMSBounces, sv.sg, ms, sv);
+            if (!mneeOk || ms.pdf < 1e-6f) return;
+            if (ms.hitCount > 0) {
+                if (!o.hwssMis && ms.dispersive) ls.beam.H = 1;
+                ls.dir = ms.woLastHitToLight;
+                ls.beam.r = -ms.woLastHitToLight;
+                ls.beam.t = perp_stark(ls.beam.r);
+                scaleBeam(ls.beam, 1.f / ms.pdf);
+                manifoldForwardUnwind(ms, origin, ls.beam, sv);
+                if (currentVertexMS) {
+                    evalCurrentVertex = false;
+                    misBsdfPdf = bounce.lastNonDeltaPdf;
+                }
+            }
+            if (doMis) {
+                if (ms.hitCount == 0 || !currentVertexMS) misBsdfPdf = bsdfPdf(s, sd, ls.dir, ls.beam.wl[0]);
+                scaleBeam(ls.beam, MISWeight(ls.pdf, misBsdfPdf * ms.pdf));
+            }
         }
-        // evalNEE with the current vertex
-        const ShadingData fsd = prepareShadingData(s, V, mid, -ls.beam.r);
-        propagate(ls.beam, fsd.posW);
-        const F3 wi = bounces[p].wi();
-        bsdfEval(s, fsd, wi, LOBE_NON_DELTA, ls.beam);
-        ++sv.unwindEvals;
-        if (o.hwssMis) {
-            float pdfs[MAXH];
-            for (int j = 0; j < MAXH; ++j) pdfs[j] = 1.f;
-            bsdfLambdaPdf(s, fsd, wi, LOBE_NON_DELTA, ls.beam, pdfs);
-            for (uint32_t j = 0; j < o.hwss; ++j) ls.beam.spdf[j] *= pdfs[j];
+        // evalNEE, pltpt_solve.rt.slang:219-243
+        if (evalCurrentVertex) {
+            const ShadingData fsd = prepareShadingData(s, V, mid, -ls.beam.r);
+            propagate(ls.beam, fsd.posW);
+            const F3 wi = bounce.wi();
+            bsdfEval(s, fsd, wi, LOBE_NON_DELTA, ls.beam);
+            ++sv.unwindEvals;
+            if (o.hwssMis) {
+                float pdfs[MAXH];
+                for (int j = 0; j < MAXH; ++j) pdfs[j] = 1.f;
+                bsdfLambdaPdf(s, fsd, wi, LOBE_NON_DELTA, ls.beam, pdfs);
+                for (uint32_t j = 0; j < o.hwss; ++j) ls.beam.spdf[j] *= pdfs[j];
+            }
         }
         forwardUnwind(p, bounces, ls.beam, sv);
-        measure(sv, p, bounces[p].pathContribution, ls.beam);
+        measure(sv, p, bounce.pathContribution, ls.beam);
     }
 
     // evalEmissive, pltpt_solve.rt.slang:152-200
@@ -862,6 +1285,7 @@ typedef struct plto_scene {
     const float* tangents;               // [n_vertices][4] or NULL
     const uint32_t* indices;             // [n_triangles][3]
     const uint32_t* tri_material;        // [n_triangles]
+    const uint32_t* tri_instance;        // [n_triangles] geometry instance (mesh) of each triangle, or NULL
     const plt_material_record* materials;
     const plt_spectral_profile* profiles;
 } plto_scene;
@@ -869,14 +1293,13 @@ typedef struct plto_scene {
 // Renders frames frame .. frame + frames - 1 of a width x height image into rgb [height][width][3]
 // (their mean).  Optional per-path records [height*width][max_bounces+1] of bounce primitive
 // (0xFFFFFFFF when absent), lobe and flags, of the last frame.
-// stats (optional, 3 values): paths, shadow rays, forward BSDF evaluations.  MNEE is not restated
-// yet: do_mnee must be 0.
+// stats (optional, 3 values): paths, shadow rays, forward BSDF evaluations.
 int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* opt, uint32_t width, uint32_t height,
                 uint32_t frame, uint32_t frames, int threads, float* rgb, uint32_t* rec_prim, uint32_t* rec_lobe,
                 uint32_t* rec_flags, uint64_t* stats) {
     if (frames == 0) return PLT_INVALID_ARG;
     if (!sc || !cam || !opt || !rgb) return PLT_INVALID_ARG;
-    if (opt->hwss < 1 || opt->hwss > 4 || opt->do_mnee) return PLT_NOT_SUPPORTED;
+    if (opt->hwss < 1 || opt->hwss > 4 || opt->mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     Scene s;
     s.nv = sc->n_vertices;
     s.nt = sc->n_triangles;
@@ -885,6 +1308,7 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     s.tan = sc->tangents;
     s.idx = sc->indices;
     s.triMat = sc->tri_material;
+    s.triInst = sc->tri_instance;
     s.tables.profiles = sc->profiles;
     s.tables.count = sc->n_profiles;
     s.mats.reserve(sc->n_materials);
@@ -915,6 +1339,10 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.importanceSampleEmitters = opt->do_importance_sample_emitters != 0;
     o.sourcingArea = opt->sourcing_area_from_emissive_geometry;
     o.maxBeamOmega = opt->sourcing_max_beam_omega;
+    o.doMnee = opt->do_nee != 0 && opt->do_mnee != 0;
+    o.mneeMaxOccluders = std::min<uint32_t>(opt->mnee_max_occluders, 4u);
+    o.mneeMaxIterations = opt->mnee_max_iterations;
+    o.mneeThreshold = opt->mnee_solver_threshold;
 
     const uint32_t nb = o.maxBounces + 1;
     const int64_t npix = (int64_t)width * height;

@@ -182,18 +182,19 @@ class PLTContext:
         return self.lib.plt_check_status(self.handle, s)
 
     # ---- PLTPT render pass ----
-    def set_scene_shading(self, normals, tangents=None):
+    def set_scene_shading(self, normals, tangents=None, tri_instance=None):
         n = np.ascontiguousarray(normals, np.float32)
         t = None if tangents is None else np.ascontiguousarray(tangents, np.float32)
+        g = None if tri_instance is None else np.ascontiguousarray(tri_instance, np.uint32)
         capi.check(self.lib.plt_set_scene_shading(self.handle, C.c_void_p(n.ctypes.data), None if t is None else C.c_void_p(t.ctypes.data),
-                                                  len(n)), "plt_set_scene_shading")
+                                                  len(n), None if g is None else C.c_void_p(g.ctypes.data)), "plt_set_scene_shading")
 
     def load_scene(self, scene, profiles):
         """Spectral profiles, materials, geometry and shading attributes of a scene.Scene."""
         self.set_spectral_profiles(profiles)
         self.set_materials(scene.records)
         self.set_scene(scene.vertices, scene.indices, scene.tri_material)
-        self.set_scene_shading(scene.normals, scene.tangents)
+        self.set_scene_shading(scene.normals, scene.tangents, getattr(scene, "tri_instance", None))
 
     def render(self, camera, width, height, out_rgba, frame_begin=0, frame_count=1, stream=None):
         """plt_render into the device tensor out_rgba [height][width][4] (float32)."""

@@ -127,7 +127,7 @@ def load_library(path=LIB_PATH):
         "plt_scene_stats": (i32, [vp, C.POINTER(C.c_uint32)]),
         "plt_bsdf_batch_noalloc": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
         "plt_set_timing_events": (i32, [vp, vp, vp, vp]),
-        "plt_set_scene_shading": (i32, [vp, vp, vp, u32]),
+        "plt_set_scene_shading": (i32, [vp, vp, vp, u32, vp]),
         "plt_render": (i32, [vp, C.POINTER(Camera), u32, u32, u32, u32, vp, vp]),
         "plt_render_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
         "plt_render_bounces": (i32, [vp, vp, vp, vp]),

@@ -44,6 +44,7 @@ struct plt_context {
     uint32_t* dIdx = nullptr;        // [nTris][3]
     float* dNrm = nullptr;           // [nVerts][3]
     float* dTan = nullptr;           // [nVerts][4] or null
+    uint32_t* dTriInst = nullptr;    // [nTris] geometry instance
     bool shadingReady = false;
     // light collection + power sampler
     float* dLightPos = nullptr;

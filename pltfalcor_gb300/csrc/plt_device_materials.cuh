@@ -72,21 +72,30 @@ PLT_DI void dielEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
     }
 }
 PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0, hasT = (lobeMask & kLobeTransmission) != 0;
+    const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
+    if ((!hasR && !hasT) || (!hasD && !hasS)) return false;
     const float* p = m->p;
     const float k = kOfWl(wl);
     const Alpha a = gaussAlpha(p, wi, wi, k);
     const float eta = dielIor(p, k);
-    // lobe mask All: pdfDirect = a
-    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
-    pdf = isDirect ? a.a : a.om;
+    bool isDirect;
+    if (hasD && hasS) {
+        isDirect = a.a == 1.f || sg.next1D() < a.a;
+        pdf = isDirect ? a.a : a.om;
+    } else {
+        isDirect = hasD || sg.next1D() < 0.f;   // pdfDirect 1 (delta only) or 0 (scatter only: one draw)
+        pdf = 1.f;
+    }
+    const bool both = hasR && hasT;
     bool isReflection;
     if (isDirect) {
         const FresnelD f = fresnel_dielectric(wi.z, eta);
         const float Fd = fresnelR(f);
-        isReflection = Fd > 0.f && sg.next1D() <= Fd;
+        isReflection = hasR ? (Fd > 0.f && sg.next1D() <= Fd) : false;
         wo = isReflection ? reflectL(wi) : dielRefract(wi, f.cosT, eta);
-        pdf *= isReflection ? Fd : 1.f - Fd;
+        pdf *= both ? (isReflection ? Fd : 1.f - Fd) : 1.f;
         lobe = isReflection ? kLobeDeltaR : (__ldg(p + PG_B) != 0.f ? kLobeDispDeltaT : kLobeDeltaT);
     } else {
         float surfPdf;
@@ -94,9 +103,9 @@ PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
         pdf *= surfPdf;
         const f3 mh = normalize(wi + wo);
         const float F = fresnelR(fresnel_dielectric(signf(wi.z) * dot(wi, mh), eta));
-        isReflection = F > 0.f && sg.next1D() <= F;
+        isReflection = hasR ? (F > 0.f && sg.next1D() <= F) : false;
         if (!isReflection) wo = dielScatteredWo(wo, eta);
-        pdf *= isReflection ? F : 1.f - F;
+        pdf *= both ? (isReflection ? F : 1.f - F) : 1.f;
         lobe = isReflection ? kLobeScatterR : kLobeScatterT;
     }
     weight = m00Of(isReflection ? m->m00a : m->m00b, wl);
@@ -179,12 +188,19 @@ PLT_DI void condEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
     }
 }
 PLT_DI bool condSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0;
+    const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
+    if (!hasR || (!hasD && !hasS)) return false;
     const float* p = m->p;
     const float k = kOfWl(wl);
-    const Alpha a = fracAlpha(p, wi, wi, k);
-    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
-    pdf = isDirect ? a.a : a.om;
+    bool isDirect = hasD;
+    pdf = 1.f;
+    if (hasD && hasS) {
+        const Alpha a = fracAlpha(p, wi, wi, k);
+        isDirect = a.a == 1.f || sg.next1D() < a.a;
+        pdf = isDirect ? a.a : a.om;
+    }
     weight = m00Of(m->m00a, wl);
     if (isDirect) {
         wo = reflectL(wi);
@@ -221,12 +237,19 @@ PLT_DI void opaqEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
     for (int j = 0; j < H; ++j) b.setSP(j, (M * m00Of(m->m00a, b.wl[j])) * b.getSP(j));
 }
 PLT_DI bool opaqSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0;
+    const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
+    if (!hasR || (!hasD && !hasS)) return false;
     const float* p = m->p;
     const float mk = meank();
-    const Alpha a = fracAlpha(p, wi, wi, mk);
-    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
-    pdf = isDirect ? a.a : a.om;
+    bool isDirect = hasD;
+    pdf = 1.f;
+    if (hasD && hasS) {
+        const Alpha a = fracAlpha(p, wi, wi, mk);
+        isDirect = a.a == 1.f || sg.next1D() < a.a;
+        pdf = isDirect ? a.a : a.om;
+    }
     weight = m00Of(m->m00a, wl);
     if (isDirect) {
         wo = reflectL(wi);
@@ -321,7 +344,10 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
     }
 }
 PLT_DI bool coatSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0;
+    const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
+    if (!hasR || (!hasD && !hasS)) return false;
     const float* p = m->p;
     if (wi.z <= 0.f) return false;
     const float k = kOfWl(wl);
@@ -340,9 +366,14 @@ PLT_DI bool coatSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
     const f3 wiIn = -coatRefract(wi, eta1, f.cosT);
     if (wiIn.z == 0.f) return false;
     weight = m00Of(m->m00a, wl);
-    const Alpha a = fracAlpha(p, wiIn, wiIn, k);
-    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
-    pdf *= isDirect ? a.a : a.om;
+    bool isDirect;
+    if (hasD && hasS) {
+        const Alpha a = fracAlpha(p, wiIn, wiIn, k);
+        isDirect = a.a == 1.f || sg.next1D() < a.a;
+        pdf *= isDirect ? a.a : a.om;
+    } else {
+        isDirect = hasD || sg.next1D() < 0.f;
+    }
     if (isDirect) {
         wo = reflectL(wi);
         lobe = kLobeDeltaR;
@@ -504,25 +535,60 @@ PLT_DI void gratSampleLobe(const DevMaterial* __restrict__ m, f3 wi, int& lx, in
     if (ry < 0.f) ly = -ly;
     if (__ldg(m->p + PD_IPY) == 0.f) { ly = 0; py = 1.f; }
 }
+// closestLobeHint, DiffractionGrating.slang:92-107: the order whose direction is closest to -woHint
+PLT_DI void gratClosestLobeHint(const DevMaterial* __restrict__ m, f3 wi, f3 woHint, float alpha, float lambda, int& lx, int& ly) {
+    lx = ly = 0;
+    if (alpha == 1.f) return;
+    const float* p = m->p;
+    const int lobeCount = (int)(m->aux & 0xFFu);
+    const float li2x = wi.x * wi.x + wi.z * wi.z, li2y = wi.y * wi.y + wi.z * wi.z;
+    const float lo2x = woHint.x * woHint.x + woHint.z * woHint.z, lo2y = woHint.y * woHint.y + woHint.z * woHint.z;
+    const float six = li2x > kFltEps ? wi.x / sqrtf(li2x) : 0.f, siy = li2y > kFltEps ? wi.y / sqrtf(li2y) : 0.f;
+    const float sox = lo2x > kFltEps ? -woHint.x / sqrtf(lo2x) : 0.f, soy = lo2y > kFltEps ? -woHint.y / sqrtf(lo2y) : 0.f;
+    auto toLobe = [&](float l) {
+        const float v = l + signf(l) * .5f;
+        const int li = isfinite(v) ? (int)fmaxf(-1e9f, fminf(1e9f, v)) : 0;
+        return max(-lobeCount, min(lobeCount, li));
+    };
+    const float l0 = (six - sox) / (__ldg(p + PD_IPX) * lambda);
+    lx = toLobe(l0);
+    if (alpha == 0.f && lx == 0) lx = (int)signf(l0);
+    if (__ldg(p + PD_IPY) != 0.f) {
+        const float l1 = (siy - soy) / (__ldg(p + PD_IPY) * lambda);
+        ly = toLobe(l1);
+        if (alpha == 0.f && ly == 0) ly = (int)signf(l1);
+    }
+}
 template <bool CONDUCTOR>
 PLT_DI bool gratSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0;
+    const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
+    if (!hasR || (!hasD && !hasS)) return false;
     const float* p = m->p;
     const float lambda = 1e-3f * wl;
     const Alpha a = gratAlphaFull(p, wi, k2Pi / lambda);
-    const bool isDirect = a.a == 1.f || sg.next1D() < a.a;
-    pdf = isDirect ? a.a : a.om;
+    const bool hasHint = hasD && (woHint.x != 0.f || woHint.y != 0.f || woHint.z != 0.f);
+    int lx = 0, ly = 0;
+    if (hasHint && a.a < 1.f) gratClosestLobeHint(m, wi, woHint, a.a, lambda, lx, ly);
+    bool isDirect = hasD;
+    if (hasHint) {
+        isDirect = lx == 0 && ly == 0;
+        pdf = 1.f;
+    } else if (hasD && hasS) {
+        isDirect = a.a == 1.f || sg.next1D() < a.a;
+        pdf = isDirect ? a.a : a.om;
+    }
     if (isDirect) {
         float bp = 0.f;
-        if (CONDUCTOR) condSample(m, wi, wo, bp, weight, lobe, sg, wl);
-        else opaqSample(m, wi, wo, bp, weight, lobe, sg, wl);
+        if (CONDUCTOR) condSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask);
+        else opaqSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask);
         pdf *= bp;
         return true;
     }
     weight = m00Of(m->m00a, wl);
-    int lx, ly;
-    float px, py;
-    gratSampleLobe(m, wi, lx, ly, px, py, lambda, sg);
+    float px = 1.f, py = 1.f;
+    if (!hasHint) gratSampleLobe(m, wi, lx, ly, px, py, lambda, sg);
     wo = gratDiffract(p, wi, lx, ly, lambda);
     lobe = encodeGratingLobe(lx, ly, kLobeDispDeltaR);
     pdf *= px * py;
@@ -701,13 +767,16 @@ PLT_DI void thinEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
 #pragma unroll
     for (int j = 0; j < H; ++j) b.setSP(j, mapply(M, b.getSP(j)));
 }
-PLT_DI bool thinSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe, SampleGen& sg) {
+PLT_DI bool thinSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe, SampleGen& sg,
+                       uint32_t lobeMask = kLobeAll) {
+    const bool hasR = (lobeMask & kLobeReflection) != 0, hasT = (lobeMask & kLobeTransmission) != 0;
+    if (!hasR && !hasT) return false;
     const float eta = __ldg(m->p + PT_ETA) / 1.f;
     const float Fd = fresnelR(fresnel_dielectric(fabsf(wi.z), eta));
-    const bool isReflection = Fd > 0.f && sg.next1D() <= Fd;
+    const bool isReflection = hasR ? (Fd > 0.f && sg.next1D() <= Fd) : false;
     wo = isReflection ? reflectL(wi) : -wi;
     weight = 1.f;
-    pdf = isReflection ? Fd : 1.f - Fd;
+    pdf = hasR && hasT ? (isReflection ? Fd : 1.f - Fd) : 1.f;
     lobe = isReflection ? kLobeDeltaR : kLobeDeltaT;
     return true;
 }

@@ -63,7 +63,7 @@ constexpr uint32_t kPropEmissive = 0x1u, kPropTransmissive = 0x2u, kPropMwReflec
 constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 // option bits of PtParams.opt
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
-                   kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u;
+                   kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u;
 
 struct PtParams {
     // scene
@@ -74,6 +74,7 @@ struct PtParams {
     const float* tan;             // [nv][4] or null
     const uint32_t* idx;          // [nt][3]
     const uint32_t* triMat;       // [nt]
+    const uint32_t* triInst;      // [nt] geometry instance (manifold re-projection)
     uint32_t nTris;
     const pltdev::DevMaterial* mats;
     const uint2* matProps;
@@ -94,6 +95,8 @@ struct PtParams {
     // options
     uint32_t maxBounces, tileSize, hwss, opt, flags;
     float sourcingArea, maxBeamOmega;
+    uint32_t mneeMaxOccluders, mneeMaxIterations;
+    float mneeThreshold;
     plt_camera cam;
     uint32_t width, height, npix, frame;
     // path state of the sample pass

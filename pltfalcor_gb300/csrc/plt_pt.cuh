@@ -176,32 +176,41 @@ PLT_DI void ptEval(const DevMaterial* __restrict__ m, uint32_t type, const Ctx& 
     b.t = F.fromLocal(b.t);
 }
 
+// sample(sd, sg, result, wavelength, lobeMask, woHint): the dielectric and thin dielectric
+// restrict the lobes to the hint's side (PLTDielectricBSDF.slang:310-321,
+// PLTThinDielectricBSDF.slang:230-243), the grated materials take the diffraction order closest to
+// the hint; the sample pass uses lobeMask All and no hint.
 PLT_DI bool ptSample(const DevMaterial* __restrict__ m, uint32_t type, const SD& sd, SampleGen& sg, float wl, f3& wo, float& pdf,
-                     float& weight, uint32_t& lobe) {
+                     float& weight, uint32_t& lobe, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}) {
     const WFrame F = bsdfFrame(sd, type, m);
     const f3 V = F.toLocal(sd.V);
+    uint32_t sideMask = lobeMask;
+    if (type == kMatDielectric || type == kMatThin) {
+        const float dh = dot(sd.V, woHint);
+        sideMask = (dh > 0.f ? kLobeReflection : dh < 0.f ? kLobeTransmission : kLobeAll) & lobeMask;
+    }
     bool ok;
     switch (type) {
-    case kMatDielectric: ok = dielSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
-    case kMatConductor: ok = condSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
-    case kMatOpaqueDielectric: ok = opaqSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatDielectric: ok = dielSample(m, V, wo, pdf, weight, lobe, sg, wl, sideMask); break;
+    case kMatConductor: ok = condSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
+    case kMatOpaqueDielectric: ok = opaqSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
     case kMatCoatedConductor:
-    case kMatCoatedOpaque: ok = coatSample(m, V, wo, pdf, weight, lobe, sg, wl); break;
-    case kMatGratedConductor: ok = gratSample<true>(m, V, wo, pdf, weight, lobe, sg, wl); break;
-    case kMatGratedOpaque: ok = gratSample<false>(m, V, wo, pdf, weight, lobe, sg, wl); break;
-    case kMatThin: ok = thinSample(m, V, wo, pdf, weight, lobe, sg); break;
+    case kMatCoatedOpaque: ok = coatSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
+    case kMatGratedConductor: ok = gratSample<true>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint)); break;
+    case kMatGratedOpaque: ok = gratSample<false>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint)); break;
+    case kMatThin: ok = thinSample(m, V, wo, pdf, weight, lobe, sg, sideMask); break;
     case kMatMultilayer:
-        if (V.z <= 0.f) { ok = false; break; }
+        if ((lobeMask & kLobeReflection) == 0 || (lobeMask & kLobeDelta) == 0 || V.z <= 0.f) { ok = false; break; }
         pdf = 1.f;
         wo = reflectL(V);
         lobe = kLobeDeltaR;
         weight = m00Of(m->m00a, wl);
         ok = V.z * wo.z > 0.f;
         break;
-    case kMatDiffuse: ok = diffSample(m, wo, pdf, weight, lobe, sg, wl); break;
+    case kMatDiffuse: ok = diffSample(m, wo, pdf, weight, lobe, sg, wl) && (lobeMask & kLobeDiffuseR) != 0; break;
     default: ok = false; break;
     }
-    if (ok || !isGrated(type)) wo = F.fromLocal(wo);
+    if (ok || type == kMatDielectric) wo = F.fromLocal(wo);
     return ok;
 }
 
@@ -528,6 +537,303 @@ __global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t
 
 #endif  // PLT_PT_SAMPLE_PASS
 
+// ---- manifold NEE (Manifolds.slangh, DifferentialShadingGeometry.slang) ---------------------
+struct F3pdv { f3 v, ddu, ddv; };
+struct F3kpdv { f3 v, ddu, ddv, ddl; };
+struct DSG {
+    F3pdv p, n, s, t;
+    PLT_DI f3 fromLocal(f3 v) const { return s.v * v.x + t.v * v.y + n.v * v.z; }
+    PLT_DI F3pdv pdw(f3 dst) const {
+        F3pdv w;
+        w.v = dst - p.v;
+        const float ilo = 1.f / sqrtf(dot(w.v, w.v));
+        w.v = w.v * ilo;
+        w.ddu = (p.ddu - w.v * dot(w.v, p.ddu)) * -ilo;
+        w.ddv = (p.ddv - w.v * dot(w.v, p.ddv)) * -ilo;
+        return w;
+    }
+};
+PLT_DI f3 zero3() { return mk3(0.f, 0.f, 0.f); }
+// differentialShadingGeometry, DifferentialShadingGeometry.slang:94-178 (untextured meshes: the
+// (1,0), (0,1) triangle parameterisation, so dp/du = p1 - p0 and dp/dv = p2 - p0)
+PLT_NI DSG differentialShadingGeometry(const PtParams& P, uint32_t prim, float b1, float b2) {
+    const float w0 = 1.f - b1 - b2;
+    const uint32_t i0 = __ldg(P.idx + 3 * prim), i1 = __ldg(P.idx + 3 * prim + 1), i2 = __ldg(P.idx + 3 * prim + 2);
+    const f3 p0 = ld3s(P.pos, i0), p1 = ld3s(P.pos, i1), p2 = ld3s(P.pos, i2);
+    const f3 n0 = ld3s(P.nrm, i0), n1 = ld3s(P.nrm, i1), n2 = ld3s(P.nrm, i2);
+    DSG g;
+    g.p.v = p0 * w0 + p1 * b1 + p2 * b2;
+    g.n.v = n0 * w0 + n1 * b1 + n2 * b2;
+    const float il = 1.0f / sqrtf(dot(g.n.v, g.n.v));
+    g.n.v = g.n.v * il;
+    g.n.ddu = (n1 - n0) * il;
+    g.n.ddv = (n2 - n0) * il;
+    g.n.ddu = g.n.ddu - g.n.v * dot(g.n.v, g.n.ddu);
+    g.n.ddv = g.n.ddv - g.n.v * dot(g.n.v, g.n.ddv);
+    g.p.ddu = p1 - p0;
+    g.p.ddv = p2 - p0;
+    g.s.v = g.p.ddu - g.n.v * dot(g.n.v, g.p.ddu);
+    float ils = 1.0f / sqrtf(dot(g.s.v, g.s.v));
+    g.s.v = g.s.v * ils;
+    if (g.p.ddu.x == 0.f && g.p.ddu.y == 0.f && g.p.ddu.z == 0.f) {
+        g.s.v = perp_stark(g.n.v);
+        ils = 1.0f;
+    }
+    g.t.v = cross(g.n.v, g.s.v);
+    g.s.ddu = ((-g.n.ddu) * dot(g.n.v, g.p.ddu) - g.n.v * dot(g.n.ddu, g.p.ddu)) * ils;
+    g.s.ddv = ((-g.n.ddv) * dot(g.n.v, g.p.ddu) - g.n.v * dot(g.n.ddv, g.p.ddu)) * ils;
+    g.s.ddu = g.s.ddu - g.s.v * dot(g.s.ddu, g.s.v);
+    g.s.ddv = g.s.ddv - g.s.v * dot(g.s.ddv, g.s.v);
+    g.t.ddu = cross(g.n.ddu, g.s.v) + cross(g.n.v, g.s.ddu);
+    g.t.ddv = cross(g.n.ddv, g.s.v) + cross(g.n.v, g.s.ddv);
+    return g;
+}
+// reflectDerivatives / refractDerivatives, DifferentialShadingGeometry.slang:180-222
+PLT_DI F3kpdv reflectDerivatives(const F3pdv& wi, const F3pdv& n) {
+    const float wn = dot(wi.v, n.v);
+    const float dwdun = dot(wi.ddu, n.v), dwdvn = dot(wi.ddv, n.v);
+    const float dnduw = dot(n.ddu, wi.v), dndvw = dot(n.ddv, wi.v);
+    F3kpdv r;
+    r.v = n.v * (2.f * wn) - wi.v;
+    r.ddu = (n.v * (dwdun + dnduw) + n.ddu * wn) * 2.f - wi.ddu;
+    r.ddv = (n.v * (dwdvn + dndvw) + n.ddv * wn) * 2.f - wi.ddv;
+    r.ddl = zero3();
+    return r;
+}
+PLT_DI F3kpdv refractDerivatives(const F3pdv& wi, F3pdv n, float eta) {
+    const float wn = dot(wi.v, n.v);
+    eta = wn < 0.f ? eta : 1.f / eta;
+    if (wn < 0.f) { n.v = -n.v; n.ddu = -n.ddu; n.ddv = -n.ddv; }
+    const float eta2 = eta * eta;
+    const float dwdun = dot(wi.ddu, n.v), dwdvn = dot(wi.ddv, n.v);
+    const float dnduw = dot(n.ddu, wi.v), dndvw = dot(n.ddv, wi.v);
+    const float root = sqrtf(fmaxf(0.f, 1.f - eta2 * (1.0f - wn * wn)));
+    F3kpdv r;
+    if (root == 0.f) { r.v = r.ddu = r.ddv = r.ddl = zero3(); return r; }
+    const float a = eta - eta2 * wn / root;
+    r.v = (wi.v - n.v * wn) * -eta - n.v * root;
+    r.ddu = n.v * (a * (dnduw + dwdun)) + n.ddu * (eta * wn - root) - wi.ddu * eta;
+    r.ddv = n.v * (a * (dndvw + dwdvn)) + n.ddv * (eta * wn - root) - wi.ddv * eta;
+    r.ddl = zero3();
+    return r;
+}
+// DiffractionGrating.partialDerivatives, DiffractionGrating.slang:188-265
+PLT_NI F3kpdv gratingDerivatives(const DSG& g, const F3pdv& wi, float gx, float gy, float ipx, float ipy, int lx, int ly, float wavelength) {
+    F3kpdv ret;
+    ret.v = ret.ddu = ret.ddv = ret.ddl = zero3();
+    const F3pdv& n = g.n;
+    const f3 Xv = g.fromLocal(mk3(gx, gy, 0.f));
+    const f3 Xdu = g.s.ddu * gx + g.t.ddu * gy, Xdv = g.s.ddv * gx + g.t.ddv * gy;
+    const float lambda = 1e-3f * wavelength;
+    const float lpx = (float)lx * ipx, lpy = (float)ly * ipy;
+    const f3 Y = cross(n.v, Xv);
+    const float x = dot(wi.v, Xv), y = dot(wi.v, Y), z = dot(wi.v, n.v);
+    const float px = sqrtf(x * x + z * z), py = sqrtf(y * y + z * z);
+    const float iqx = px > kFltEps ? 1.f / px : 0.f, iqy = py > kFltEps ? 1.f / py : 0.f;
+    const float a = lambda * lpx - x * iqx, b = lambda * lpy - y * iqy;
+    const float oneMinusA2 = fmaxf(0.f, 1 - a * a);
+    const float m = -oneMinusA2 / ((a * b) * (a * b) - 1);
+    const float q = 1 - b * b * m;
+    if (a > 1.f || a < -1.f || b > 1.f || b < -1.f || q < 0.f || !(m >= 0.f)) return ret;
+    const float sqrtOneM = sqrtf(q), sqrtM = sqrtf(m);
+    const float c = .5f / (sqrtOneM * sqrtf(oneMinusA2));
+    const float dxdu = dot(wi.v, Xdu) + dot(wi.ddu, Xv), dxdv = dot(wi.v, Xdv) + dot(wi.ddv, Xv);
+    const float dzdu = dot(wi.v, n.ddu) + dot(wi.ddu, n.v), dzdv = dot(wi.v, n.ddv) + dot(wi.ddv, n.v);
+    const float iqx3 = iqx * iqx * iqx, iqy3 = iqy * iqy * iqy;
+    const float dadu = z * (x * dzdu - z * dxdu) * iqx3, dbdu = z * (y * dzdu - z * dxdu) * iqy3;
+    const float dadv = z * (x * dzdv - z * dxdv) * iqx3, dbdv = z * (y * dzdv - z * dxdv) * iqy3;
+    const float den = ((a * b) * (a * b) - 1) * ((a * b) * (a * b) - 1);
+    const float dmdu = 2 * a * (a * b * oneMinusA2 * dbdu - dadu * (1 - b * b)) / den;
+    const float dmdv = 2 * a * (a * b * oneMinusA2 * dbdv - dadv * (1 - b * b)) / den;
+    const float dmdl = 2 * a * (a * b * oneMinusA2 * lpy - lpx * (1 - b * b)) / den;
+    ret.v = Xv * (a * sqrtOneM) + Y * (b * sqrtM) + n.v * sqrtf(fmaxf(0.f, 1 - a * a * q - b * b * m));
+    auto d = [&](float da, float db, float dm) {
+        return Xv * ((q * da - a * b * (b * dm / 2.f + m * db)) / sqrtOneM) + Y * ((b * dm / 2.f + m * db) / sqrtM) +
+               n.v * ((-2 * a * da * q - b * (b * dm + 2.f * m * db) + a * a * b * (b * dm + 2.f * m * db)) * c);
+    };
+    ret.ddu = d(dadu, dbdu, dmdu);
+    ret.ddv = d(dadv, dbdv, dmdv);
+    ret.ddl = d(lpx, lpy, dmdl);
+    return ret;
+}
+// IMaterialInstance.partialDerivatives of the PLT*BSDF.slang wrappers (world space)
+PLT_DI F3kpdv ptPartialDerivatives(const DevMaterial* __restrict__ m, uint32_t type, const F3pdv& wi, const DSG& g, uint32_t lobe,
+                                   float wavelength) {
+    switch (type) {
+    case kMatDielectric:
+        if (lobe & kLobeTransmission) return refractDerivatives(wi, g.n, dielIor(m->p, kOfWl(wavelength)));
+        return reflectDerivatives(wi, g.n);
+    case kMatThin:
+        if (lobe & kLobeTransmission) {
+            F3kpdv r;
+            r.v = -wi.v; r.ddu = -wi.ddu; r.ddv = -wi.ddv; r.ddl = zero3();
+            return r;
+        }
+        return reflectDerivatives(wi, g.n);
+    case kMatGratedConductor:
+    case kMatGratedOpaque: {
+        int lx, ly;
+        decodeGratingLobe(lobe, lx, ly);
+        if (lx == 0 && ly == 0) return reflectDerivatives(wi, g.n);
+        return gratingDerivatives(g, wi, __ldg(m->p + PD_GX), __ldg(m->p + PD_GY), __ldg(m->p + PD_IPX), __ldg(m->p + PD_IPY), lx, ly,
+                                  wavelength);
+    }
+    case kMatDiffuse: {
+        F3kpdv r;
+        r.v = r.ddu = r.ddv = r.ddl = zero3();
+        return r;
+    }
+    default: return reflectDerivatives(wi, g.n);
+    }
+}
+// manifoldOneStep with sphcoords and their derivatives, Manifolds.slangh:283-347
+PLT_DI void sphcoords(f3 w, float& theta, float& phi) {
+    theta = acosf(fminf(fmaxf(w.z, -1.f), 1.f));
+    phi = atan2f(w.y, w.x);
+    phi += phi < 0.f ? k2Pi : 0.f;
+}
+PLT_DI bool manifoldOneStep(const F3pdv& w, const F3kpdv& ws, const F3pdv& p, float& lenC, f3& stepDir) {
+    float t0, p0, t1, p1;
+    sphcoords(w.v, t0, p0);
+    sphcoords(ws.v, t1, p1);
+    const float dt = t0 - t1;
+    float dp = p0 - p1;
+    dp = fabsf(dp) > kPi ? dp - signf(dp) * k2Pi : dp;
+    lenC = sqrtf(dt * dt + dp * dp);
+    const float aO = -1.f / sqrtf(fmaxf(0.f, 1.f - w.v.z * w.v.z)), iO = 1.f / (w.v.x * w.v.x + w.v.y * w.v.y);
+    const float aI = -1.f / sqrtf(fmaxf(0.f, 1.f - ws.v.z * ws.v.z)), iI = 1.f / (ws.v.x * ws.v.x + ws.v.y * ws.v.y);
+    const float A = aO * w.ddu.z - aI * ws.ddu.z;
+    const float B = aO * w.ddv.z - aI * ws.ddv.z;
+    const float C = iO * (w.v.x * w.ddu.y - w.v.y * w.ddu.x) - iI * (ws.v.x * ws.ddu.y - ws.v.y * ws.ddu.x);
+    const float D = iO * (w.v.x * w.ddv.y - w.v.y * w.ddv.x) - iI * (ws.v.x * ws.ddv.y - ws.v.y * ws.ddv.x);
+    const float det = A * D - B * C;
+    if (fabsf(det) < 4e-6f) return false;      // tryInvert, MathHelpers.slang:484-498
+    const float id = 1.0f / det;
+    const float dx = (D * id) * dt + (-B * id) * dp, dy = (-C * id) * dt + (A * id) * dp;
+    stepDir = p.ddu * dx + p.ddv * dy;
+    return true;
+}
+
+constexpr int kMaxMsOccluders = 4;
+struct MSHit {
+    uint32_t prim, lobe;
+    float b1, b2;
+    f3 posW;
+};
+struct MSData {
+    MSHit hits[kMaxMsOccluders];
+    f3 woLastHitToLight;
+    int hitCount;
+    uint32_t iterations;
+    float wavelength, pdf;
+    bool dispersive;
+};
+struct TraceCounters {
+    uint32_t nv, tt, overflow, shadowRays;
+};
+// closest-hit shadow ray (ShadowRays.slangh:96-135): a hit needs dist > 0
+PLT_DI bool shadowRayClosest(const PtParams& P, f3 o, f3 d, float tmin, float tmax, TraceResult& h, TraceCounters& tc) {
+    ++tc.shadowRays;
+    h = traverse<false>(reinterpret_cast<const float4*>(P.nodes), P.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, tc.nv, tc.tt, tc.overflow);
+    return h.prim != kNoHit && h.t > 0.f;
+}
+// manifoldSampleVertex, Manifolds.slangh:84-108
+PLT_DI bool manifoldSampleVertex(const PtParams& P, uint32_t prim, float b1, float b2, const SD& sd, uint32_t mid, f3 lightDir,
+                                 SampleGen& sg, MSData& d) {
+    const DevMaterial* __restrict__ m = P.mats + mid;
+    f3 wo;
+    float pdf = 0.f, weight = 0.f;
+    uint32_t lobe = 0;
+    if (!ptSample(m, __ldg(&m->type), sd, sg, d.wavelength, wo, pdf, weight, lobe, kLobeDelta, lightDir)) return false;
+    d.pdf *= pdf;
+    MSHit& h = d.hits[d.hitCount];
+    h.prim = prim;
+    h.b1 = b1;
+    h.b2 = b2;
+    h.posW = sd.posW;
+    h.lobe = lobe;
+    d.dispersive = d.dispersive || (lobe & (kLobeDispDeltaR | kLobeDispDeltaT)) != 0;
+    ++d.hitCount;
+    return true;
+}
+// traceMNEEOccluders + manifoldNEESample, Manifolds.slangh:110-281
+PLT_NI bool manifoldNEESample(const PtParams& P, f3 rayO, f3 rayD, float tmax, f3 origin, f3 lightPos, f3 lightDir, int maxMS,
+                              SampleGen& sg, MSData& d, TraceCounters& tc) {
+    const int maxOcc = (int)min(P.mneeMaxOccluders, (uint32_t)kMaxMsOccluders);
+    const f3 wi = -rayD;
+    for (int guard = 0; guard <= kMaxMsOccluders; ++guard) {
+        TraceResult h;
+        if (!shadowRayClosest(P, rayO, rayD, 0.f, tmax, h, tc)) break;
+        if (d.hitCount >= maxOcc || d.hitCount >= maxMS) return false;
+        VData v = vertexData(P, h.prim, h.b1, h.b2);
+        v.posW = rayO + rayD * h.t;
+        const uint32_t mid = __ldg(P.triMat + h.prim);
+        const uint2 props = __ldg(P.matProps + mid);
+        const SD sd = prepareSD(v, props.x, wi);
+        if (!(props.x & plt::kPropMwTransmissive)) return false;
+        if (!manifoldSampleVertex(P, h.prim, h.b1, h.b2, sd, mid, -wi, sg, d) || (d.hits[d.hitCount - 1].lobe & kLobeTransmission) == 0)
+            return false;
+        rayO = newRayOriginToward(sd, rayD);
+        tmax -= h.t;
+    }
+    if (d.hitCount == 0) return true;
+    float beta[kMaxMsOccluders];
+#pragma unroll
+    for (int i = 0; i < kMaxMsOccluders; ++i) beta[i] = 1.f;
+    bool success = false;
+    while (!success) {
+        success = true;
+        for (int idx = 0; idx < d.hitCount; ++idx) {
+            MSHit& h = d.hits[idx];
+            const uint32_t mid = __ldg(P.triMat + h.prim);
+            const DSG g = differentialShadingGeometry(P, h.prim, h.b1, h.b2);
+            const f3 p0 = idx == 0 ? origin : d.hits[idx - 1].posW;
+            const F3pdv pdv0 = g.pdw(p0);
+            const f3 p2 = idx + 1 == d.hitCount ? lightPos : d.hits[idx + 1].posW;
+            const F3pdv pdv2 = g.pdw(p2);
+            const bool woIsIn = dot(pdv2.v, g.n.v) < 0.f;
+            const F3pdv wiP = woIsIn ? pdv0 : pdv2;
+            const F3pdv woP = woIsIn ? pdv2 : pdv0;
+            const DevMaterial* __restrict__ m = P.mats + mid;
+            const F3kpdv wos = ptPartialDerivatives(m, __ldg(&m->type), wiP, g, h.lobe, d.wavelength);
+            if (wos.v.x == 0.f && wos.v.y == 0.f && wos.v.z == 0.f) return false;
+            float lenC;
+            f3 stepDir;
+            if (!manifoldOneStep(woP, wos, g.p, lenC, stepDir)) return false;
+            if (lenC < P.mneeThreshold) continue;
+            success = false;
+            for (;;) {
+                if (++d.iterations > P.mneeMaxIterations) return false;
+                const f3 proposal = h.posW - stepDir * beta[idx];
+                f3 dirTo = proposal - p0;
+                const float dist = sqrtf(dot(dirTo, dirTo));
+                dirTo = dirTo / dist;
+                TraceResult hp;
+                const bool hit = shadowRayClosest(P, p0, dirTo, fmaxf(1e-4f, .99f * dist), 1.01f * dist, hp, tc);
+                if (!hit || __ldg(P.triInst + h.prim) != __ldg(P.triInst + hp.prim)) {
+                    beta[idx] /= 4.f;
+                    continue;
+                }
+                h.prim = hp.prim;
+                h.b1 = hp.b1;
+                h.b2 = hp.b2;
+                h.posW = p0 + dirTo * hp.t;
+                beta[idx] = fminf(1.0f, 2.f * beta[idx]);
+                break;
+            }
+        }
+    }
+    const f3 pl = d.hits[d.hitCount - 1].posW;
+    f3 dir = lightPos - pl;
+    const float dist = sqrtf(dot(dir, dir));
+    dir = dir / dist;
+    ++tc.shadowRays;
+    const TraceResult vis = traverse<true>(reinterpret_cast<const float4*>(P.nodes), P.tris, pl.x, pl.y, pl.z, dir.x, dir.y, dir.z, 1e-4f,
+                                           dist, tc.nv, tc.tt, tc.overflow);
+    d.woLastHitToLight = dir;
+    return vis.prim == kNoHit;
+}
+
 // ---- solve pass -----------------------------------------------------------------------------
 template <int H> struct Bnc {
     uint32_t prim, lobe, flags;
@@ -573,7 +879,10 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
     const bool doNee = (P.opt & plt::kPtDoNee) != 0, doMis = (P.opt & plt::kPtDoMis) != 0;
     const bool useEmissive = (P.opt & plt::kPtUseEmissive) != 0;
     const bool importance = (P.opt & plt::kPtImportanceEmit) != 0;
-    uint32_t nv = 0, tt = 0, overflow = 0, shadowRays = 0, evals = 0;
+    const bool doMnee = (P.opt & plt::kPtDoMnee) != 0;
+    TraceCounters tc{0u, 0u, 0u, 0u};
+    uint32_t evals = 0;
+    MSData ms;
     for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x) {
         const uint32_t px = pid % P.width, py = pid / P.width;
         SampleGen sg, tilesg;
@@ -593,16 +902,21 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
             const DevMaterial* __restrict__ m = P.mats + mid;
             const uint32_t type = __ldg(&m->type);
             const uint32_t lobes = (props.x >> 8) & 0xFFu;
-            const bool didNEE = doNee && p > 0 && (bounce.flags & kFlagLastDelta) == 0;
+            // wasNEEAvailable, pltpt_solve.rt.slang:204-210
+            const bool didNEE = doNee && p > 0 &&
+                                ((bounce.flags & kFlagLastDelta) == 0 || (doMnee && (bounce.flags >> 16) <= P.mneeMaxOccluders && p > 1));
             // two beam sources per vertex: NEE (pltpt_solve.rt.slang:245-366) and emission
             // (evalEmissive, :152-200); each is replayed through vertices p (NEE: non-delta lobes)
             // and p-1 .. 0 (forwardUnwind, :48-79), then measured (:96-147).
             for (int src = 0; src < 2; ++src) {
                 PBeam<H> pb;
                 bool evalCurrent = false;
+                int nMs = 0;            // manifold vertices to replay first (NEE with manifold walks)
+                f3 msOrigin = pathOrigin;
                 if (src == 0) {
                     if (!doNee) continue;
-                    const bool sampleRefl = (lobes & 0x03u) != 0, sampleTrans = (lobes & 0x30u) != 0;
+                    const bool allowMS = doMnee && p > 0 && (bounce.flags & kFlagLastDelta) == 0 && (props.x & plt::kPropMwReflective) != 0;
+                    const bool sampleRefl = (lobes & 0x03u) != 0 || allowMS, sampleTrans = (lobes & 0x30u) != 0;
                     if (!sampleRefl && !sampleTrans) continue;
                     // generateLightSample: selectLightType (one draw), emissive power sampler
                     SampleGen& selSg = (P.opt & plt::kPtPerTileSg) ? tilesg : sg;
@@ -647,11 +961,50 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
                     const bool isRefl = dot(sd.faceN, ldir) * dot(sd.faceN, sd.V) > 0.f;
                     if (!(anyPos && tpdf > 1e-6f && !(!sampleRefl && isRefl) && !(!sampleTrans && !isRefl))) continue;
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
-                    ++shadowRays;
-                    const TraceResult vis = traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, nv, tt, overflow);
-                    if (vis.prim != kNoHit) continue;
-                    if (doMis) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
+                    const int maxMS = (int)P.maxBounces - p;
                     evalCurrent = true;
+                    if (!doMnee || maxMS <= 0) {
+                        ++tc.shadowRays;
+                        const TraceResult vis =
+                            traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, tc.nv, tc.tt, tc.overflow);
+                        if (vis.prim != kNoHit) continue;
+                        if (doMis) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
+                    } else {
+                        // manifold sampling on NEE, pltpt_solve.rt.slang:293-353
+                        const f3 lightDir = ldir;
+                        ms.hitCount = 0;
+                        ms.iterations = 0;
+                        ms.wavelength = pb.b.wl[0];
+                        ms.pdf = 1.f;
+                        ms.dispersive = false;
+                        const bool isRefl = dot(sd.N, lightDir) * dot(sd.N, sd.V) > 0.f;
+                        const bool curMS = isRefl && allowMS;
+                        if (curMS) {
+                            if (!manifoldSampleVertex(P, bounce.prim, bounce.b1, bounce.b2, sd, mid, lightDir, sg, ms) ||
+                                (ms.hits[0].lobe & kLobeReflection) == 0)
+                                continue;
+                        }
+                        msOrigin = !curMS ? V.posW : pathOrigin;
+                        if (!manifoldNEESample(P, lorg, ldir, ldist, msOrigin, tposW, lightDir, maxMS, sg, ms, tc) || ms.pdf < 1e-6f) continue;
+                        float misBsdfPdf = 0.f;
+                        f3 lsDir = ldir;
+                        if (ms.hitCount > 0) {
+                            if (!hwssMis && ms.dispersive) pb.comps = 1;
+                            lsDir = ms.woLastHitToLight;
+                            pb.b.r = -ms.woLastHitToLight;
+                            pb.b.t = perp_stark(pb.b.r);
+                            scaleBeam(pb, 1.f / ms.pdf);
+                            nMs = ms.hitCount;
+                            if (curMS) {
+                                evalCurrent = false;
+                                misBsdfPdf = bounce.lndp;
+                            }
+                        }
+                        if (doMis) {
+                            if (ms.hitCount == 0 || !curMS) misBsdfPdf = ptPdf(m, type, sd, lsDir, pb.b.wl[0]);
+                            scaleBeam(pb, misWeight(tpdf, misBsdfPdf * ms.pdf));
+                        }
+                    }
                 } else {
                     if (!(useEmissive && (props.x & plt::kPropEmissive) && (doMis || !didNEE))) continue;
                     const bool needMIS = doMis && didNEE;
@@ -672,18 +1025,32 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
                     sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
                 }
-                // forward replay: the current vertex (NEE, non-delta lobes), then p-1 .. 0
-                for (int q = evalCurrent ? p : p - 1; q >= 0; --q) {
+                // forward replay: the manifold vertices (last to first, manifoldForwardUnwind,
+                // pltpt_solve.rt.slang:80-93), the current vertex (NEE, non-delta lobes), then p-1 .. 0
+                const int total = nMs + (evalCurrent ? 1 : 0) + p;
+                for (int k = 0; k < total; ++k) {
                     uint32_t qprim, qlobe;
                     float qb1, qb2;
                     f3 qwo;
-                    if (q == p) {
+                    bool msVertex = false;
+                    f3 msPos;
+                    if (k < nMs) {
+                        const int idx = nMs - 1 - k;
+                        const MSHit& h = ms.hits[idx];
+                        qprim = h.prim; qlobe = h.lobe; qb1 = h.b1; qb2 = h.b2;
+                        msPos = h.posW;
+                        msVertex = true;
+                        const f3 p2 = idx == 0 ? msOrigin : ms.hits[idx - 1].posW;
+                        qwo = normalize(p2 - h.posW);
+                    } else if (evalCurrent && k == nMs) {
                         qprim = bounce.prim; qlobe = kLobeNonDelta; qb1 = bounce.b1; qb2 = bounce.b2; qwo = bounce.wi;
                     } else {
+                        const int q = p - 1 - (k - nMs - (evalCurrent ? 1 : 0));
                         const Bnc<H> bq = readBounce<H>(P, pid, q);
                         qprim = bq.prim; qlobe = bq.lobe; qb1 = bq.b1; qb2 = bq.b2; qwo = bq.wi;
                     }
-                    const VData qv = vertexData(P, qprim, qb1, qb2);
+                    VData qv = vertexData(P, qprim, qb1, qb2);
+                    if (msVertex) qv.posW = msPos;
                     const uint32_t qmid = __ldg(P.triMat + qprim);
                     const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
                     propagate(pb, qsd.posW);
@@ -745,8 +1112,8 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
         P.accum[3 * (size_t)pid + 1] += (double)Lg;
         P.accum[3 * (size_t)pid + 2] += (double)Lb;
     }
-    if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
-    unsigned long long s1 = shadowRays, s2 = evals;
+    if (tc.overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    unsigned long long s1 = tc.shadowRays, s2 = evals;
     for (int o = 16; o > 0; o >>= 1) {
         s1 += __shfl_down_sync(0xFFFFFFFFu, s1, o);
         s2 += __shfl_down_sync(0xFFFFFFFFu, s2, o);

@@ -290,14 +290,15 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 }
 
 void pltReleaseRenderState(plt_context* ctx) {
-    void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dLightPos, ctx->dLightNrm,
+    void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
                     ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats};
     for (void* p : ptrs) cudaFree(p);
 }
 
 extern "C" {
 
-plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices) {
+plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices,
+                                 const uint32_t* tri_instance) {
     if (!ctx || !normals) return PLT_INVALID_ARG;
     if (n_vertices != ctx->nVerts || ctx->nTris == 0) return PLT_INVALID_ARG;
     for (size_t i = 0; i < 3 * (size_t)n_vertices; ++i)
@@ -307,6 +308,11 @@ plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const f
     cudaFree(ctx->dTan);
     ctx->dTan = nullptr;
     if (tangents && (s = upload(ctx, ctx->dTan, tangents, 4 * (size_t)n_vertices)) != PLT_OK) return s;
+    {
+        std::vector<uint32_t> inst(ctx->nTris, 0u);
+        if (tri_instance) std::memcpy(inst.data(), tri_instance, sizeof(uint32_t) * ctx->nTris);
+        if ((s = upload(ctx, ctx->dTriInst, inst.data(), inst.size())) != PLT_OK) return s;
+    }
     if ((s = buildLights(ctx)) != PLT_OK) return s;
     ctx->shadingReady = true;
     return PLT_OK;
@@ -319,7 +325,7 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     if (!ctx->shadingReady || ctx->nTris == 0 || ctx->nMats == 0) return PLT_INVALID_ARG;
     const plt_options& o = ctx->opt;
     if (o.hwss < 1 || o.hwss > 4) return PLT_NOT_SUPPORTED;
-    if (o.do_mnee) return PLT_NOT_SUPPORTED;       // manifold NEE is not implemented yet
+    if (o.mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     if (o.max_bounces > 64) return PLT_NOT_SUPPORTED;
     const uint64_t npix64 = (uint64_t)width * height;
     if (npix64 == 0) return PLT_OK;
@@ -337,6 +343,7 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     P.tan = ctx->dTan;
     P.idx = ctx->dIdx;
     P.triMat = ctx->dTriMaterial;
+    P.triInst = ctx->dTriInst;
     P.nTris = ctx->nTris;
     P.mats = ctx->dMats;
     P.matProps = ctx->dMatProps;
@@ -362,7 +369,11 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     P.opt = (o.hwss_do_mis ? plt::kPtHwssMis : 0u) | (o.use_direct_light ? plt::kPtUseDirect : 0u) |
             (o.use_emissive_lights && ctx->nLights ? plt::kPtUseEmissive : 0u) | (nee ? plt::kPtDoNee : 0u) |
             (nee && o.do_mis ? plt::kPtDoMis : 0u) | (o.do_russian_roulette ? plt::kPtDoRR : 0u) |
-            (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u);
+            (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u) |
+            (nee && o.do_mnee ? plt::kPtDoMnee : 0u);
+    P.mneeMaxOccluders = o.mnee_max_occluders;
+    P.mneeMaxIterations = o.mnee_max_iterations;
+    P.mneeThreshold = o.mnee_solver_threshold;
     P.sourcingArea = o.sourcing_area_from_emissive_geometry;
     P.maxBeamOmega = o.sourcing_max_beam_omega;
     P.cam = *camera;

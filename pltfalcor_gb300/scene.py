@@ -54,10 +54,12 @@ class Scene:
     """Triangle soup with per-triangle material indices, material records and light data."""
 
     def __init__(self, vertices, indices, tri_material, records, emissive_tris, light_material, mnee_material, bounds,
-                 normals=None):
+                 normals=None, tri_instance=None):
         self.vertices = np.ascontiguousarray(vertices, np.float32)
         self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32)
         self.tangents = None
+        # geometry instance (mesh) of each triangle: manifold walks re-project onto the same instance
+        self.tri_instance = None if tri_instance is None else np.ascontiguousarray(tri_instance, np.uint32)
         self.indices = np.ascontiguousarray(indices, np.uint32)
         self.tri_material = np.ascontiguousarray(tri_material, np.uint32)
         self.records = records
@@ -86,7 +88,7 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
     wall = M.opaque_dielectric(1, 0.3, albedo=(0.7, 0.7, 0.7))
     records = np.concatenate([recs, light, glass, wall])
     light_mat, glass_mat, wall_mat = len(recs), len(recs) + 1, len(recs) + 2
-    verts, faces, mats, norms = [], [], [], []
+    verts, faces, mats, norms, insts = [], [], [], [], []
     nv = 0
 
     def add(v, f, m, n):
@@ -95,6 +97,7 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
         faces.append(f + nv)
         mats.append(np.full(len(f), m, np.uint32))
         norms.append(np.broadcast_to(np.asarray(n, np.float64), v.shape))
+        insts.append(np.full(len(f), len(insts), np.uint32))
         nv += len(v)
 
     # room: six subdivided faces of [-room, room]^3
@@ -142,7 +145,7 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
     Mt = np.concatenate(mats)
     Nv = np.concatenate(norms)
     Nv = (Nv / np.linalg.norm(Nv, axis=1, keepdims=True)).astype(np.float32)
-    return Scene(V, F, Mt, records, emissive, light_mat, glass_mat, (-R, R), normals=Nv)
+    return Scene(V, F, Mt, records, emissive, light_mat, glass_mat, (-R, R), normals=Nv, tri_instance=np.concatenate(insts))
 
 
 def small_scene(seed=3):

@@ -46,7 +46,6 @@ def _options(**kw):
     lib.plt_options_default(C.byref(o))
     o.max_bounces = 8
     o.hwss = 4
-    o.do_mnee = 0
     for k, v in kw.items():
         setattr(o, k, v)
     return o
@@ -88,18 +87,19 @@ def _compare(gpu, orc, grecs, orecs, label):
     return same
 
 
-@pytest.mark.parametrize("hwss", [4, 1])
-def test_render_matches_oracle(torch_cuda, oracle_lib, product_lib, profiles, room, hwss):
+@pytest.mark.parametrize("hwss,mnee", [(4, 1), (4, 0), (1, 1)])
+def test_render_matches_oracle(torch_cuda, oracle_lib, product_lib, profiles, room, hwss, mnee):
+    """Default PLTPT options (manifold NEE on) and without manifold walks."""
     import oracle
     prof = profiles[0]
     w, h = 64, 48
     cam = S.room_camera(w, h)
-    opt = _options(hwss=hwss)
+    opt = _options(hwss=hwss, do_mnee=mnee)
     gpu, grecs, stats = _render_gpu(torch_cuda, room, prof, opt, cam, w, h, frame=0)
     orc, orecs, ostats = oracle.render(room, prof, cam, opt, w, h, frame=0, records=True)
     assert np.isfinite(gpu).all()
     assert (gpu[..., 3] == 1.0).all()
-    _compare(gpu, orc, grecs, orecs, "hwss %d" % hwss)
+    _compare(gpu, orc, grecs, orecs, "hwss %d mnee %d" % (hwss, mnee))
     # work counters agree with the oracle's to within the diverged paths
     assert abs(stats["shadow_rays"] - int(ostats[1])) <= 0.05 * int(ostats[1]) + 10
     assert stats["paths"] == w * h
@@ -112,7 +112,8 @@ def test_render_options_and_frames(torch_cuda, oracle_lib, product_lib, profiles
     w, h = 48, 32
     cam = S.room_camera(w, h)
     for kw in ({"do_mis": 0}, {"do_nee": 0}, {"do_russian_roulette": 0, "do_importance_sample_emitters": 0},
-               {"hwss_do_mis": 0, "hwss": 2}):
+               {"hwss_do_mis": 0, "hwss": 2}, {"mnee_max_occluders": 1, "mnee_max_iterations": 8},
+               {"do_mnee": 0, "max_bounces": 3}):
         opt = _options(**kw)
         gpu, grecs, _ = _render_gpu(torch_cuda, room, prof, opt, cam, w, h, frame=7)
         orc, orecs, _ = oracle.render(room, prof, cam, opt, w, h, frame=7, records=True)
@@ -143,7 +144,7 @@ def test_light_table_matches_oracle(torch_cuda, oracle_lib, product_lib, profile
 def test_render_rejects_bad_calls(torch_cuda, product_lib, profiles, room):
     from pltfalcor_gb300.bsdf import PLTContext
     import ctypes as C
-    ctx = PLTContext({"do_mnee": 0})
+    ctx = PLTContext()
     out = torch_cuda.zeros((4, 4, 4), dtype=torch_cuda.float32, device="cuda")
     cam = S.room_camera(4, 4)
     lib = capi.load_library()
@@ -153,7 +154,7 @@ def test_render_rejects_bad_calls(torch_cuda, product_lib, profiles, room):
     assert lib.plt_render(ctx.handle, C.byref(cam), 4, 4, 0, 0, C.c_void_p(out.data_ptr()), None) == capi.PLT_INVALID_ARG
     assert lib.plt_render(ctx.handle, C.byref(cam), 4, 4, 0, 1, C.c_void_p(out.data_ptr() + 4), None) == capi.PLT_INVALID_ARG
     ctx.close()
-    ctx2 = PLTContext({"do_mnee": 1})
+    ctx2 = PLTContext({"mnee_max_occluders": 5})
     ctx2.load_scene(room, profiles[0])
     assert lib.plt_render(ctx2.handle, C.byref(cam), 4, 4, 0, 1, C.c_void_p(out.data_ptr()), None) == capi.PLT_NOT_SUPPORTED
     ctx2.close()
