@@ -317,6 +317,36 @@ plt_status plt_render_bounces(plt_context* ctx, uint32_t* prim, uint32_t* lobe, 
  * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
 plt_status plt_check_status(plt_context* ctx, void* stream);
 
+/* Learned MIS proposal (no counterpart in the reference, whose PLTPT samples only the analytic
+ * BSDF samplers).  A conditional MLP 16 -> 64 -> 64 -> 64 -> 32 with SiLU maps the features of a
+ * query -- wi (3, shading frame, z >= 0), (wavelength - 550) / 170, roughness, grating pitch / 5 um,
+ * material class one-hot (8), two zero pads -- to 8 x (logit, mu_x, mu_y, log sigma): a mixture of
+ * isotropic Gaussians over the projected hemisphere (wo.xy on the unit disk).  BF16 weights and
+ * activations, FP32 accumulation on the tensor cores.  The render pass uses it as an extra
+ * one-sample MIS technique for the non-delta lobes (plt_options.learned_proposal).  Parameters
+ * are FP32 on the host side of these calls, in the order W1 [64][16], W2 [64][64], W3 [64][64],
+ * W4 [32][64], b1, b2, b3, b4.  Training samples come from the exact non-delta samplers of the
+ * context's materials (set them first). */
+#define PLT_PROPOSAL_PARAMS 11488u
+#define PLT_PROPOSAL_FEATURES 16u
+#define PLT_PROPOSAL_OUTPUTS 32u
+plt_status plt_proposal_init(plt_context* ctx, uint64_t seed);
+plt_status plt_proposal_set_params(plt_context* ctx, const float* params);   /* host [PLT_PROPOSAL_PARAMS] */
+plt_status plt_proposal_get_params(plt_context* ctx, float* params);         /* host [PLT_PROPOSAL_PARAMS] */
+/* n training samples (device): x [n][16] bf16 bits, target [n][2] (wo.xy), weight [n] (0 = no sample). */
+plt_status plt_proposal_generate(plt_context* ctx, uint32_t n, uint32_t seed, uint16_t* x, float* target, float* weight, void* stream);
+/* grad [PLT_PROPOSAL_PARAMS] (device, overwritten) and loss [1] (device) of the mean weighted
+ * negative log-likelihood of the batch under the current parameters. */
+plt_status plt_proposal_gradient(plt_context* ctx, uint32_t n, const uint16_t* x, const float* target, const float* weight, float* grad,
+                                 float* loss, void* stream);
+/* out [n][32] (device, fp32): the network outputs for feature rows x. */
+plt_status plt_proposal_forward(plt_context* ctx, uint32_t n, const uint16_t* x, float* out, void* stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) with a device gradient. */
+plt_status plt_proposal_adam_step(plt_context* ctx, const float* grad, float lr, void* stream);
+/* steps x (generate batch, gradient, Adam); loss_history (host [steps]) may be NULL.  Initialises
+ * the parameters from `seed` when none are set. */
+plt_status plt_proposal_train(plt_context* ctx, uint32_t steps, uint32_t batch, float lr, uint32_t seed, float* loss_history, void* stream);
+
 /* Per-kernel timing of plt_bsdf_batch (a profiling aid; no counterpart in the reference, whose
  * shaders are timed only as a whole render pass).  Each later plt_bsdf_batch
  * on this context records the given cudaEvent_t handles (any may be NULL) on its stream: before the

@@ -227,3 +227,40 @@ def light_table(scene, profiles):
     inv = C.c_float(0)
     lib.plto_light_table(C.addressof(s), alias.ctypes.data, tris.ctypes.data, C.byref(inv))
     return alias, tris, inv.value
+
+
+def _mlp_sig(lib):
+    if not hasattr(lib, "_mlp_sig"):
+        lib.plto_mlp_forward.restype = None
+        lib.plto_mlp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]
+        lib.plto_mlp_gradient.restype = C.c_double
+        lib.plto_mlp_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]
+        lib._mlp_sig = True
+
+
+def mlp_forward(params, x_bits, round_bf16=True):
+    """Proposal network outputs [n][32] for bf16 feature rows x_bits [n][16] (uint16)."""
+    lib = load()
+    _mlp_sig(lib)
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x_bits, np.uint16)
+    n = len(x)
+    out = np.zeros((n, 32), np.float32)
+    lib.plto_mlp_forward(p.ctypes.data, x.ctypes.data, n, int(round_bf16), out.ctypes.data)
+    return out
+
+
+def mlp_gradient(params, target, weight, x_bits=None, x_f64=None, round_bf16=True):
+    """(mean weighted mixture NLL, gradient [11488]) of a batch; features as bf16 bits or float64."""
+    lib = load()
+    _mlp_sig(lib)
+    p = np.ascontiguousarray(params, np.float32)
+    t = np.ascontiguousarray(target, np.float32)
+    w = np.ascontiguousarray(weight, np.float32)
+    xb = None if x_bits is None else np.ascontiguousarray(x_bits, np.uint16)
+    xf = None if x_f64 is None else np.ascontiguousarray(x_f64, np.float64)
+    n = len(w)
+    g = np.zeros(11488, np.float64)
+    loss = lib.plto_mlp_gradient(p.ctypes.data, None if xb is None else xb.ctypes.data, None if xf is None else xf.ctypes.data,
+                                 t.ctypes.data, w.ctypes.data, n, int(round_bf16), g.ctypes.data)
+    return loss, g

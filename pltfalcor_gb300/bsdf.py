@@ -208,6 +208,48 @@ class PLTContext:
         capi.check(self.lib.plt_render_bounces(self.handle, *[C.c_void_p(a.ctypes.data) for a in out]), "plt_render_bounces")
         return out
 
+    # ---- learned MIS proposal ----
+    def proposal_init(self, seed=0):
+        capi.check(self.lib.plt_proposal_init(self.handle, seed), "plt_proposal_init")
+
+    def proposal_params(self):
+        out = np.zeros(capi.PROPOSAL_PARAMS, np.float32)
+        capi.check(self.lib.plt_proposal_get_params(self.handle, out.ctypes.data_as(C.POINTER(C.c_float))), "plt_proposal_get_params")
+        return out
+
+    def proposal_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        capi.check(self.lib.plt_proposal_set_params(self.handle, p.ctypes.data_as(C.POINTER(C.c_float))), "plt_proposal_set_params")
+
+    def proposal_generate(self, n, seed, device="cuda"):
+        """Training batch from the exact samplers: (x bf16 bits as int16 [n][16], target [n][2], weight [n])."""
+        import torch
+        x = torch.zeros((n, 16), dtype=torch.int16, device=device)
+        t = torch.zeros((n, 2), dtype=torch.float32, device=device)
+        w = torch.zeros(n, dtype=torch.float32, device=device)
+        capi.check(self.lib.plt_proposal_generate(self.handle, n, seed, _ptr(x), _ptr(t), _ptr(w), None), "plt_proposal_generate")
+        return x, t, w
+
+    def proposal_gradient(self, x, t, w):
+        import torch
+        g = torch.zeros(capi.PROPOSAL_PARAMS, dtype=torch.float32, device=x.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=x.device)
+        capi.check(self.lib.plt_proposal_gradient(self.handle, len(w), _ptr(x), _ptr(t), _ptr(w), _ptr(g), _ptr(loss), None),
+                   "plt_proposal_gradient")
+        return float(loss.item()), g
+
+    def proposal_forward(self, x):
+        import torch
+        out = torch.zeros((x.shape[0], 32), dtype=torch.float32, device=x.device)
+        capi.check(self.lib.plt_proposal_forward(self.handle, x.shape[0], _ptr(x), _ptr(out), None), "plt_proposal_forward")
+        return out
+
+    def proposal_train(self, steps, batch=65536, lr=1e-3, seed=1):
+        hist = np.zeros(steps, np.float32)
+        capi.check(self.lib.plt_proposal_train(self.handle, steps, batch, lr, seed, hist.ctypes.data_as(C.POINTER(C.c_float)), None),
+                   "plt_proposal_train")
+        return hist
+
     def render_stats(self):
         out = (C.c_uint64 * 4)()
         capi.check(self.lib.plt_render_stats(self.handle, out), "plt_render_stats")

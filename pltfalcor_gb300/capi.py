@@ -87,8 +87,11 @@ EXPORTED_SYMBOLS = [
     "plt_bsdf_batch", "plt_check_status", "plt_bsdf_eval", "plt_bsdf_pdf", "plt_bsdf_sample", "plt_bsdf_lambda_pdf",
     "plt_set_scene", "plt_trace_closest", "plt_trace_any", "plt_scene_stats", "plt_bsdf_batch_noalloc",
     "plt_set_timing_events", "plt_set_scene_shading", "plt_render", "plt_render_stats", "plt_render_bounces",
+    "plt_proposal_init", "plt_proposal_set_params", "plt_proposal_get_params", "plt_proposal_generate",
+    "plt_proposal_gradient", "plt_proposal_forward", "plt_proposal_adam_step", "plt_proposal_train",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
+PROPOSAL_PARAMS = 11488
 PLT_TOO_LARGE = 8
 STATUS_NAMES[PLT_TOO_LARGE] = "PLT_TOO_LARGE"
 
@@ -131,6 +134,14 @@ def load_library(path=LIB_PATH):
         "plt_render": (i32, [vp, C.POINTER(Camera), u32, u32, u32, u32, vp, vp]),
         "plt_render_stats": (i32, [vp, C.POINTER(C.c_uint64)]),
         "plt_render_bounces": (i32, [vp, vp, vp, vp]),
+        "plt_proposal_init": (i32, [vp, C.c_uint64]),
+        "plt_proposal_set_params": (i32, [vp, C.POINTER(C.c_float)]),
+        "plt_proposal_get_params": (i32, [vp, C.POINTER(C.c_float)]),
+        "plt_proposal_generate": (i32, [vp, u32, u32, vp, vp, vp, vp]),
+        "plt_proposal_gradient": (i32, [vp, u32, vp, vp, vp, vp, vp, vp]),
+        "plt_proposal_forward": (i32, [vp, u32, vp, vp, vp]),
+        "plt_proposal_adam_step": (i32, [vp, vp, C.c_float, vp]),
+        "plt_proposal_train": (i32, [vp, u32, u32, C.c_float, u32, C.POINTER(C.c_float), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -107,6 +107,7 @@ plt_status plt_destroy(plt_context* ctx) {
     cudaFree(ctx->dTris);
     cudaFree(ctx->dTriMaterial);
     pltReleaseRenderState(ctx);
+    pltReleaseProposal(ctx);
     delete ctx;
     return PLT_OK;
 }
@@ -181,6 +182,27 @@ plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, 
         for (uint32_t i = 0; i < count; ++i) props[i] = pltMaterialProps(mats[i], h[i]);
         PLT_CUDA(ctx, cudaMalloc(&ctx->dMatProps, sizeof(uint2) * count));
         PLT_CUDA(ctx, cudaMemcpy(ctx->dMatProps, props.data(), sizeof(uint2) * count, cudaMemcpyHostToDevice));
+    }
+    // learned-proposal features and the list of materials it serves
+    cudaFree(ctx->dMatFeat);
+    cudaFree(ctx->dPropEnabled);
+    ctx->dMatFeat = nullptr;
+    ctx->dPropEnabled = nullptr;
+    ctx->nPropEnabled = 0;
+    if (count) {
+        std::vector<float4> feat(count);
+        std::vector<uint32_t> enabled;
+        for (uint32_t i = 0; i < count; ++i) {
+            feat[i] = pltProposalFeatures(mats[i], h[i]);
+            if (feat[i].w != 0.f) enabled.push_back(i);
+        }
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dMatFeat, sizeof(float4) * count));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dMatFeat, feat.data(), sizeof(float4) * count, cudaMemcpyHostToDevice));
+        if (!enabled.empty()) {
+            PLT_CUDA(ctx, cudaMalloc(&ctx->dPropEnabled, sizeof(uint32_t) * enabled.size()));
+            PLT_CUDA(ctx, cudaMemcpy(ctx->dPropEnabled, enabled.data(), sizeof(uint32_t) * enabled.size(), cudaMemcpyHostToDevice));
+        }
+        ctx->nPropEnabled = (uint32_t)enabled.size();
     }
     ctx->hMats.assign(mats, mats + count);
     ctx->hDevMats = h;

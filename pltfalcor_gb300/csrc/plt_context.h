@@ -62,9 +62,28 @@ struct plt_context {
     uint32_t ptNpix = 0, ptMaxB = 0;
     plt::PtParams pt{};
     unsigned long long* dPtStats = nullptr;
+    // learned MIS proposal: FP32 master weights, Adam moments, BF16 copy, gradient, loss;
+    // per-material features (roughness, pitch, class, enabled) and the enabled-material list
+    float* dPropParams = nullptr;
+    float* dPropM = nullptr;
+    float* dPropV = nullptr;
+    void* dPropBf16 = nullptr;
+    float* dPropGrad = nullptr;
+    float* dPropLoss = nullptr;
+    uint32_t propStep = 0;
+    bool propReady = false;
+    float4* dMatFeat = nullptr;
+    uint32_t* dPropEnabled = nullptr;
+    uint32_t nPropEnabled = 0;
+    void* dPropBatch = nullptr;      // training batch (features, targets, weights)
+    uint32_t propBatchCap = 0;
 };
 
 // Frees the render-pass state of a context (plt_render.cpp).
 void pltReleaseRenderState(plt_context* ctx);
 // Material property word for the render pass (plt_render.cpp).
 uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& d);
+// Learned-proposal features of a material: (roughness, pitch feature, class, enabled) (plt_proposal.cpp).
+float4 pltProposalFeatures(const plt_material_record& r, const pltdev::DevMaterial& d);
+// Frees the learned-proposal state (plt_proposal.cpp).
+void pltReleaseProposal(plt_context* ctx);

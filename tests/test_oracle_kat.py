@@ -187,3 +187,26 @@ def test_op_counting_build(profiles):
     assert set(c) == set(M.BENCH_TYPES)
     for t, v in c.items():
         assert 50 < v["fp"] < 5000 and 5 < v["sfu"] < 500
+
+
+def test_proposal_oracle_backprop_matches_finite_differences(oracle_lib):
+    """The CPU network oracle's back-propagation (double precision, no BF16 rounding) against
+    central differences of its own loss, on random parameters and a small batch."""
+    import oracle as O
+    rng = np.random.default_rng(0)
+    p = (rng.standard_normal(11488) * 0.2).astype(np.float32)
+    n = 16
+    xf = rng.standard_normal((n, 16))
+    xf[:, 14:] = 0
+    t = rng.uniform(-0.7, 0.7, (n, 2)).astype(np.float32)
+    w = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    _, g = O.mlp_gradient(p, t, w, x_f64=xf, round_bf16=False)
+    for idx in list(rng.integers(0, 11488, 30)) + [11456 + 3, 11456 + 1, 9216 + 5]:
+        eps = 1e-3 * max(1.0, abs(float(p[idx])))
+        pp, pm = p.copy(), p.copy()
+        pp[idx] = np.float32(p[idx] + eps)
+        pm[idx] = np.float32(p[idx] - eps)
+        lp, _ = O.mlp_gradient(pp, t, w, x_f64=xf, round_bf16=False)
+        lm, _ = O.mlp_gradient(pm, t, w, x_f64=xf, round_bf16=False)
+        fd = (lp - lm) / (float(pp[idx]) - float(pm[idx]))
+        assert abs(fd - g[idx]) <= 1e-3 * max(abs(fd), abs(g[idx]), 1e-4), (idx, fd, g[idx])
