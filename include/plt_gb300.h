@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define PLT_ABI_VERSION 1u
+#define PLT_ABI_VERSION 2u
 #define PLT_MAX_HWSS 8u                 /* hero wavelengths per beam (reference: <= 4, Utils/HWSS.slang:4-9) */
 #define PLT_SPECTRAL_MAX_BINS 128u      /* SpectralProfile::kMaxBins */
 #define PLT_NO_SPECTRAL_PROFILE 0xFFFFFFFFu
@@ -209,6 +209,13 @@ typedef struct plt_options {
     uint32_t mnee_max_iterations;       /* default 60 */
     float mnee_solver_threshold;        /* default 5e-5 */
     uint32_t flags;                     /* PLT_OPTION_* */
+    /* Learned MIS proposal (no counterpart in the reference): when non-zero, plt_render samples
+     * every proposal vertex (a material with non-delta lobes other than PLTDiffuse, hit from the
+     * front) with the context's proposal network with probability learned_proposal_prob and with
+     * the analytic sampler otherwise (one-sample MIS; the exact BSDF is always evaluated).
+     * Requires plt_proposal_init or plt_proposal_set_params first. */
+    uint32_t learned_proposal;          /* default 0 */
+    float learned_proposal_prob;        /* in (0, 1), default 0.5 */
 } plt_options;
 
 #define PLT_OPTION_FP64_MULTILAYER 0x1u /* multilayer recursion in FP64 instead of the reference FP32 */
@@ -321,9 +328,11 @@ plt_status plt_check_status(plt_context* ctx, void* stream);
  * BSDF samplers).  A conditional MLP 16 -> 64 -> 64 -> 64 -> 32 with SiLU maps the features of a
  * query -- wi (3, shading frame, z >= 0), (wavelength - 550) / 170, roughness, grating pitch / 5 um,
  * material class one-hot (8), two zero pads -- to 8 x (logit, mu_x, mu_y, log sigma): a mixture of
- * isotropic Gaussians over the projected hemisphere (wo.xy on the unit disk).  BF16 weights and
- * activations, FP32 accumulation on the tensor cores.  The render pass uses it as an extra
- * one-sample MIS technique for the non-delta lobes (plt_options.learned_proposal).  Parameters
+ * isotropic Gaussians over the primary sample (u0, u1) in [0,1)^2 that the material's surface model
+ * (Gaussian or fractal) maps to a non-delta direction.  BF16 weights and activations, FP32
+ * accumulation on the tensor cores.  The render pass uses it as an extra one-sample MIS technique
+ * in primary sample space (plt_options.learned_proposal): the path weight is divided by the
+ * primary sample's mixture density, so the estimate has the analytic tracer's expectation.  Parameters
  * are FP32 on the host side of these calls, in the order W1 [64][16], W2 [64][64], W3 [64][64],
  * W4 [32][64], b1, b2, b3, b4.  Training samples come from the exact non-delta samplers of the
  * context's materials (set them first). */
@@ -333,7 +342,9 @@ plt_status plt_check_status(plt_context* ctx, void* stream);
 plt_status plt_proposal_init(plt_context* ctx, uint64_t seed);
 plt_status plt_proposal_set_params(plt_context* ctx, const float* params);   /* host [PLT_PROPOSAL_PARAMS] */
 plt_status plt_proposal_get_params(plt_context* ctx, float* params);         /* host [PLT_PROPOSAL_PARAMS] */
-/* n training samples (device): x [n][16] bf16 bits, target [n][2] (wo.xy), weight [n] (0 = no sample). */
+/* n training samples (device): x [n][16] bf16 bits, target [n][2] (the uniform primary sample the
+ * surface model turned into a non-delta direction), weight [n] (that direction's BSDF value over the
+ * sampler's pdf for an unpolarised beam, clamped to 4; 0 = no sample). */
 plt_status plt_proposal_generate(plt_context* ctx, uint32_t n, uint32_t seed, uint16_t* x, float* target, float* weight, void* stream);
 /* grad [PLT_PROPOSAL_PARAMS] (device, overwritten) and loss [1] (device) of the mean weighted
  * negative log-likelihood of the batch under the current parameters. */

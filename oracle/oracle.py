@@ -173,10 +173,11 @@ def rng_stream(px, py, frame, count):
 class _Scene(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("n_materials", C.c_uint32), ("n_profiles", C.c_uint32),
                 ("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("indices", C.c_void_p),
-                ("tri_material", C.c_void_p), ("tri_instance", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p)]
+                ("tri_material", C.c_void_p), ("tri_instance", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p),
+                ("proposal_params", C.c_void_p)]
 
 
-def _scene_struct(scene, profiles):
+def _scene_struct(scene, profiles, proposal_params=None):
     keep = [np.ascontiguousarray(scene.vertices, np.float32), np.ascontiguousarray(scene.normals, np.float32),
             np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
             np.ascontiguousarray(scene.records)]
@@ -186,14 +187,16 @@ def _scene_struct(scene, profiles):
                keep[0].ctypes.data, keep[1].ctypes.data, None if tan is None else tan.ctypes.data, keep[2].ctypes.data,
                keep[3].ctypes.data, None if inst is None else inst.ctypes.data, keep[4].ctypes.data,
                C.cast(profiles, C.c_void_p) if profiles is not None else None)
-    return s, (keep, tan, inst, profiles)
+    pp = None if proposal_params is None else np.ascontiguousarray(proposal_params, np.float32)
+    s.proposal_params = None if pp is None else pp.ctypes.data
+    return s, (keep, tan, inst, profiles, pp)
 
 
-def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1):
+def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1, proposal_params=None):
     """FP32 oracle render of one frame: rgb [height][width][3]; with records=True also per-path bounce
     records (prim, lobe, flags) [height*width][max_bounces+1] and stats (paths, shadow rays, evals).
     `profiles` is a ctypes array of plt_spectral_profile, `camera`/`options` the ctypes structs of
-    include/plt_gb300.h."""
+    include/plt_gb300.h; `proposal_params` (11488 floats) the network of learned_proposal renders."""
     lib = load()
     if not hasattr(lib, "_render_sig"):
         lib.plto_render.restype = C.c_int
@@ -201,7 +204,7 @@ def render(scene, profiles, camera, options, width, height, frame=0, threads=0, 
         lib.plto_light_table.restype = C.c_uint32
         lib.plto_light_table.argtypes = [C.c_void_p] * 4
         lib._render_sig = True
-    s, keep = _scene_struct(scene, profiles)
+    s, keep = _scene_struct(scene, profiles, proposal_params)
     rgb = np.zeros((height, width, 3), np.float32)
     nb = options.max_bounces + 1
     recs = [np.zeros((height * width, nb), np.uint32) for _ in range(3)] if records else [None] * 3

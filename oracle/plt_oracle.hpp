@@ -83,6 +83,15 @@ struct SampleGen {
 };
 template <class R> inline R next1D(SampleGen& sg) { return R((double)sg.next1D()); }
 template <class R> inline V2<R> next2D(SampleGen& sg) { V2<R> u; u.x = next1D<R>(sg); u.y = next1D<R>(sg); return u; }
+// Primary-sample warp of the surface models' direction samplers (the learned proposal of the
+// path-tracing oracle): when set, the Gaussian and fractal surface samplers draw their pair as usual
+// and then use this one instead.  Set and cleared around one sample call by the caller.
+inline thread_local const float* g_directionWarp = nullptr;
+template <class R> inline V2<R> nextDirection2D(SampleGen& sg) {
+    V2<R> u = next2D<R>(sg);
+    if (g_directionWarp) { u.x = R(g_directionWarp[0]); u.y = R(g_directionWarp[1]); }
+    return u;
+}
 
 // ---------------------------------------------------------------------------------------------
 // Spectra.  rgbToSpectrum: Utils/Color/SpectrumUtils.slang:106-198 (11-bin Smits-style basis over
@@ -449,7 +458,7 @@ template <class R> struct GaussianSurface {
         const R w = R(1) / sigma2;
         const R s2 = w / sqr(k);
         const V2<R> mean = {-wi.x, -wi.y};
-        const V2<R> wo = sample_boxmueller_truncated(next2D<R>(sg), mean, s2, pdf);
+        const V2<R> wo = sample_boxmueller_truncated(nextDirection2D<R>(sg), mean, s2, pdf);
         const R z = o_sqrt(o_max(R(0), R(1) - dot(wo, wo)));
         return {wo.x, wo.y, o_sign(wi.z) * z};
     }
@@ -496,7 +505,7 @@ template <class R> struct FractalSurface {
         const R s = o_sqrt(o_max(R(0), R(1) - sqr(wi.z)));
         const R phi_i = s > R(0) ? o_atan2(wi.y, wi.x) : R(0);
         const R sqrtT = o_sqrt(T);
-        const V2<R> u1 = next2D<R>(sg);
+        const V2<R> u1 = nextDirection2D<R>(sg);
         const V2<R> u2 = next2D<R>(sg);
         (void)u2;
         const R M = R(1) - o_pow(R(1) + sqr(k) * T * sqr(R(1) + s), -(gamma - R(1)) / R(2));

@@ -10,74 +10,12 @@
 #include <cstring>
 #include <vector>
 
+
+#include "plt_oracle_mlp.hpp"
+
 namespace {
 
-constexpr int kIn = 16, kHid = 64, kOut = 32, kComp = 8;
-constexpr int kW1 = 0, kW2 = kW1 + kHid * kIn, kW3 = kW2 + kHid * kHid, kW4 = kW3 + kHid * kHid;
-constexpr int kB1 = kW4 + kOut * kHid, kB2 = kB1 + kHid, kB3 = kB2 + kHid, kB4 = kB3 + kHid;
-constexpr int kParams = kB4 + kOut;
-constexpr double kLogSigmaMin = -6.0, kLogSigmaMax = 2.0;
-
-float bf16Round(float f) {
-    uint32_t u;
-    std::memcpy(&u, &f, 4);
-    if ((u & 0x7F800000u) == 0x7F800000u) return f;
-    u += 0x7FFFu + ((u >> 16) & 1u);
-    u &= 0xFFFF0000u;
-    std::memcpy(&f, &u, 4);
-    return f;
-}
-float bf16Bits(uint16_t h) {
-    const uint32_t u = (uint32_t)h << 16;
-    float f;
-    std::memcpy(&f, &u, 4);
-    return f;
-}
-
-struct Net {
-    bool round;
-    std::vector<double> p;
-    double q(double v) const { return round ? (double)bf16Round((float)v) : v; }
-    double silu(double z) const { return round ? (double)((float)z / (1.f + std::exp(-(float)z))) : z / (1.0 + std::exp(-z)); }
-    double siluGrad(double z) const {
-        if (round) {
-            const float s = 1.f / (1.f + std::exp(-(float)z));
-            return (double)(s * (1.f + (float)z * (1.f - s)));
-        }
-        const double s = 1.0 / (1.0 + std::exp(-z));
-        return s * (1.0 + z * (1.0 - s));
-    }
-    explicit Net(const float* params, bool r) : round(r), p(kParams) {
-        for (int i = 0; i < kParams; ++i) p[i] = round ? (double)bf16Round(params[i]) : (double)params[i];
-    }
-    // forward of one row: Z1..Z3 (stored values) and outputs
-    void forward(const double* x, double* z1, double* z2, double* z3, double* out) const {
-        for (int o = 0; o < kHid; ++o) {
-            double a = 0.0;
-            for (int i = 0; i < kIn; ++i) a += x[i] * p[kW1 + o * kIn + i];
-            z1[o] = q(a + p[kB1 + o]);
-        }
-        double h[kHid];
-        for (int i = 0; i < kHid; ++i) h[i] = q(silu(z1[i]));
-        for (int o = 0; o < kHid; ++o) {
-            double a = 0.0;
-            for (int i = 0; i < kHid; ++i) a += h[i] * p[kW2 + o * kHid + i];
-            z2[o] = q(a + p[kB2 + o]);
-        }
-        for (int i = 0; i < kHid; ++i) h[i] = q(silu(z2[i]));
-        for (int o = 0; o < kHid; ++o) {
-            double a = 0.0;
-            for (int i = 0; i < kHid; ++i) a += h[i] * p[kW3 + o * kHid + i];
-            z3[o] = q(a + p[kB3 + o]);
-        }
-        for (int i = 0; i < kHid; ++i) h[i] = q(silu(z3[i]));
-        for (int o = 0; o < kOut; ++o) {
-            double a = 0.0;
-            for (int i = 0; i < kHid; ++i) a += h[i] * p[kW4 + o * kHid + i];
-            out[o] = round ? (double)(float)(a + p[kB4 + o]) : a + p[kB4 + o];
-        }
-    }
-};
+using namespace plt_oracle_mlp;
 
 // mixture NLL of one sample and d(loss)/d(out)
 double nllGrad(const double* out, double tx, double ty, double w, double* d) {

@@ -8,9 +8,11 @@
 #include "plt_oracle.hpp"
 #include "plt_oracle_bsdf.hpp"
 #include "plt_oracle_geom.hpp"
+#include "plt_oracle_mlp.hpp"
 
 #include <algorithm>
 #include <cfloat>
+#include <memory>
 #include <random>
 #include <type_traits>
 #include <vector>
@@ -29,6 +31,8 @@ inline void put(F3 v, float* p) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t FLAG_LAST_DELTA = 0x1u, FLAG_DISPERSIVE = 0x2u, FLAG_ONLY_DELTA = 0x4u, FLAG_MISS = 0x10u,
                    FLAG_TERMINATED = 0x20u;
+// a vertex where the learned proposal was a sampling technique (no counterpart in the reference)
+constexpr uint32_t FLAG_LEARNED = 0x40u;
 constexpr float kQcutoffForMS = .15f;               // IMaterialInstance.slang:44
 constexpr uint32_t PROP_EMISSIVE = 0x1u, PROP_TRANSMISSIVE = 0x2u, PROP_MW_REFLECTIVE = 0x4u, PROP_MW_TRANSMISSIVE = 0x8u;
 
@@ -64,6 +68,9 @@ struct Scene {
     std::vector<float> lightArea, lightFlux;
     std::vector<uint32_t> alias;       // [nl][2]
     float invWeightsSum = 0.f;
+    // learned proposal: network (bf16-rounded) and per-material (roughness, pitch, class, enabled)
+    std::unique_ptr<plt_oracle_mlp::Net> net;
+    std::vector<float> matFeat;        // [nmat][4]
 };
 
 struct Options {
@@ -73,6 +80,8 @@ struct Options {
     bool doMnee;
     uint32_t mneeMaxOccluders, mneeMaxIterations;
     float mneeThreshold;
+    bool learned = false;
+    float learnedProb = 0.5f;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -592,6 +601,38 @@ void bsdfLambdaPdf(const Scene& s, const ShadingData& sd, F3 wo, uint32_t lobe, 
     });
 }
 
+// Learned proposal features of a material (roughness, pitch feature, class, enabled), as the
+// library's material upload derives them: classes conductor 0, dielectric 1, opaque dielectric 2,
+// coated conductor 3, coated opaque dielectric 4, grated conductor 5, grated opaque dielectric 6,
+// diffuse 7; enabled for materials with non-delta lobes other than PLTDiffuse.  The roughness
+// feature is the surface model's q, the pitch feature the grating pitch x in um / 5.
+void proposalFeatures(const Material<float>& m, const SceneTables& t, float* f) {
+    float rough = 0.f, pitch = 0.f, cls = -1.f;
+    bool scatter = false;
+    switch (m.type) {
+    case PLT_MATERIAL_CONDUCTOR: cls = 0.f; rough = Conductor<float>(m, &t).gfs.q(); scatter = true; break;
+    case PLT_MATERIAL_DIELECTRIC: cls = 1.f; rough = Dielectric<float>(m).gfs.q; scatter = rough != 0.f; break;
+    case PLT_MATERIAL_OPAQUE_DIELECTRIC: cls = 2.f; rough = OpaqueDielectric<float>(m).gfs.q(); scatter = true; break;
+    case PLT_MATERIAL_COATED_CONDUCTOR: cls = 3.f; rough = Coated<float, true>(m, &t).gfs.q(); scatter = true; break;
+    case PLT_MATERIAL_COATED_OPAQUE_DIELECTRIC: cls = 4.f; rough = Coated<float, false>(m, &t).gfs.q(); scatter = true; break;
+    case PLT_MATERIAL_GRATED_CONDUCTOR:
+    case PLT_MATERIAL_GRATED_OPAQUE_DIELECTRIC: {
+        cls = m.type == PLT_MATERIAL_GRATED_CONDUCTOR ? 5.f : 6.f;
+        rough = OpaqueDielectric<float>(m, true).gfs.q();
+        const DiffractionGrating<float> g = makeGrating(m);
+        pitch = g.invPitch.x > 0.f ? (1.f / g.invPitch.x) / 5.f : 0.f;
+        scatter = true;
+        break;
+    }
+    case PLT_MATERIAL_DIFFUSE: cls = 7.f; rough = 1.f; break;
+    default: break;
+    }
+    f[0] = rough;
+    f[1] = pitch;
+    f[2] = cls;
+    f[3] = scatter ? 1.f : 0.f;
+}
+
 // getProperties / getLobes of each PLT*BSDF.slang
 struct Props {
     uint32_t flags = 0;
@@ -781,11 +822,12 @@ struct Renderer {
         const float wavelength = sampleOneWavelength(sg.next1D());
         F3 origin = f3(cam.pos), dir = cameraDir(px, py);
         float weight = 1.f, pdf = 1.f, thp = 1.f, lastNonDeltaPdf = 0.f;
+        float wps = 1.f;   // product of the primary-sample MIS densities (learned proposal)
         uint32_t flags = FLAG_ONLY_DELTA;
         const uint32_t maxB = o.maxBounces;
-        auto append = [&](uint32_t length, uint32_t prim, float b1, float b2, F3 wi, uint32_t lobe) {
+        auto append = [&](uint32_t length, uint32_t prim, float b1, float b2, F3 wi, uint32_t lobe, uint32_t extra = 0u) {
             Bounce& b = bounces[length];
-            b.flags = flags;
+            b.flags = flags | extra;
             b.prim = prim;
             b.b1 = b1;
             b.b2 = b2;
@@ -793,7 +835,7 @@ struct Renderer {
             geom::ndirToOctEqualArea(n, b.ewi);
             b.lobe = lobe;
             b.lastNonDeltaPdf = lastNonDeltaPdf;
-            b.pathContribution = 1.f / (pdf * thp);
+            b.pathContribution = 1.f / (pdf * thp * wps);
         };
         for (uint32_t length = 0; length < maxB + 1 && (flags & (FLAG_MISS | FLAG_TERMINATED)) == 0;) {
             float t, b1, b2;
@@ -823,9 +865,53 @@ struct Renderer {
                 rcp_thp = u < p ? 0.f : 1.f - p;
             }
             bool shouldEnd = length == maxB || (rcp_thp == 0.f && length > 0);
+            // learned proposal (plt_pt.cuh ptBounceKernel<true>): a proposal vertex is an enabled
+            // material hit from the front with wi above the shading plane; the network's mixture is
+            // a density over the surface sampler's primary sample
+            bool useNet = false;
+            plt_oracle_mlp::PackedMix mix{};
+            if (o.learned) {
+                const float* mf = &s.matFeat[4 * (size_t)mid];
+                const F3 wiL = sd.toLocal(sd.V);
+                useNet = mf[3] > 0.f && sd.frontFacing && wiL.z > 0.f;
+                if (useNet) {
+                    double x[plt_oracle_mlp::kIn], z1[plt_oracle_mlp::kHid], z2[plt_oracle_mlp::kHid], z3[plt_oracle_mlp::kHid],
+                        out[plt_oracle_mlp::kOut];
+                    plt_oracle_mlp::featureRow(wiL.x, wiL.y, wiL.z, wavelength, mf, x);
+                    s.net->forward(x, z1, z2, z3, out);
+                    mix = plt_oracle_mlp::packMixture(out);
+                }
+            }
+            const uint32_t extra = useNet ? FLAG_LEARNED : 0u;
             BSDFSample bs;
+            float warp = 1.f;
             if (!shouldEnd) {
-                const bool ok = bsdfSample(s, sd, sg, bs, wavelength);
+                // one-sample MIS in primary sample space: the surface sampler's primary sample comes
+                // from the proposal (probability c) or is uniform; a non-delta direction's path weight
+                // is divided by c q(u) + 1 - c, the analytic pdf is kept for everything else
+                float warpU[2] = {0.f, 0.f};
+                float mpss = 1.f;
+                bool inside = true;
+                if (useNet) {
+                    const float c = o.learnedProb;
+                    if (sg.next1D() < c) {
+                        const float u0 = sg.next1D(), u1 = sg.next1D(), u2 = sg.next1D();
+                        plt_oracle_mlp::sampleMixture(mix, u0, u1, u2, warpU[0], warpU[1]);
+                        inside = warpU[0] >= 0.f && warpU[0] < 1.f && warpU[1] >= 0.f && warpU[1] < 1.f;
+                    } else {
+                        warpU[0] = sg.next1D();
+                        warpU[1] = sg.next1D();
+                    }
+                    mpss = inside ? c * plt_oracle_mlp::mixtureDensity(mix, warpU[0], warpU[1]) + (1.f - c) : 0.f;
+                    if (!inside) warpU[0] = warpU[1] = .5f;
+                    g_directionWarp = warpU;
+                }
+                bool ok = bsdfSample(s, sd, sg, bs, wavelength);
+                g_directionWarp = nullptr;
+                if (useNet && ok && (bs.lobe & LOBE_DELTA) == 0) {
+                    ok = inside && mpss > 0.f;
+                    warp = mpss;
+                }
                 shouldEnd = !ok || bs.pdf == 0.f;
                 const float nc = pdf * bs.pdf * thp * rcp_thp;
                 shouldEnd = shouldEnd || nc < 1e-6f;
@@ -836,14 +922,15 @@ struct Renderer {
             const bool isMS = (isRefl && (props.flags & PROP_MW_REFLECTIVE)) || (!isRefl && (props.flags & PROP_MW_TRANSMISSIVE));
             if (shouldEnd) {
                 flags |= FLAG_TERMINATED;
-                append(length, prim, b1, b2, wi, 0);
+                append(length, prim, b1, b2, wi, 0, extra);
                 continue;
             }
             weight *= bs.weight;
             thp *= rcp_thp;
             pdf *= bs.pdf;
+            wps *= warp;
             if (isDisp) flags |= FLAG_DISPERSIVE;
-            append(length, prim, b1, b2, wi, bs.lobe);
+            append(length, prim, b1, b2, wi, bs.lobe, extra);
             ++length;
             lastNonDeltaPdf = !isDelta ? bs.pdf : lastNonDeltaPdf;
             const uint32_t msc = isMS ? (flags >> 16) + 1u : 0u;
@@ -1288,6 +1375,7 @@ typedef struct plto_scene {
     const uint32_t* tri_instance;        // [n_triangles] geometry instance (mesh) of each triangle, or NULL
     const plt_material_record* materials;
     const plt_spectral_profile* profiles;
+    const float* proposal_params;        // [11488] learned proposal parameters (learned_proposal renders), or NULL
 } plto_scene;
 
 // Renders frames frame .. frame + frames - 1 of a width x height image into rgb [height][width][3]
@@ -1343,6 +1431,14 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.mneeMaxOccluders = std::min<uint32_t>(opt->mnee_max_occluders, 4u);
     o.mneeMaxIterations = opt->mnee_max_iterations;
     o.mneeThreshold = opt->mnee_solver_threshold;
+    o.learned = opt->learned_proposal != 0;
+    o.learnedProb = opt->learned_proposal_prob;
+    if (o.learned) {
+        if (!sc->proposal_params || !(o.learnedProb > 0.f && o.learnedProb < 1.f)) return PLT_INVALID_ARG;
+        s.net.reset(new plt_oracle_mlp::Net(sc->proposal_params, true));
+        s.matFeat.resize(4 * (size_t)sc->n_materials);
+        for (uint32_t i = 0; i < sc->n_materials; ++i) proposalFeatures(s.mats[i], s.tables, &s.matFeat[4 * (size_t)i]);
+    }
 
     const uint32_t nb = o.maxBounces + 1;
     const int64_t npix = (int64_t)width * height;

@@ -67,7 +67,8 @@ class Options(C.Structure):
                 ("do_russian_roulette", C.c_uint32), ("nee_use_per_tile_sg", C.c_uint32),
                 ("do_importance_sample_emitters", C.c_uint32), ("do_mnee", C.c_uint32),
                 ("mnee_max_occluders", C.c_uint32), ("mnee_max_iterations", C.c_uint32),
-                ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32)]
+                ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32),
+                ("learned_proposal", C.c_uint32), ("learned_proposal_prob", C.c_float)]
 
 
 class Camera(C.Structure):

@@ -71,6 +71,8 @@ plt_status plt_options_default(plt_options* o) {
     o->mnee_max_iterations = 60;
     o->mnee_solver_threshold = 5e-5f;
     o->flags = 0;
+    o->learned_proposal = 0;
+    o->learned_proposal_prob = .5f;
     return PLT_OK;
 }
 

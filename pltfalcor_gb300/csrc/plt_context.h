@@ -59,6 +59,8 @@ struct plt_context {
     // render-pass buffers (one allocation, sized for ptNpix paths and ptMaxB bounces)
     void* dPt = nullptr;
     size_t ptBytes = 0;
+    void* dPtMix = nullptr;       // per-path primary-sample MIS density products (learned renders)
+    size_t ptMixBytes = 0;
     uint32_t ptNpix = 0, ptMaxB = 0;
     plt::PtParams pt{};
     unsigned long long* dPtStats = nullptr;

@@ -138,9 +138,12 @@ PLT_NI float boxMullerTruncatedPdf(f2 wo, f2 mean, float sigma2) {
     const float max_phi = (r < kFltEps || l < kFltEps) ? kPi : acosf(clampf((r * r + l * l - 1.f) / (2.f * r * l), -1.f, 1.f));
     return .5f * x / (max_phi * sigma2) * coso;
 }
-PLT_NI f3 gaussSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
+// uw: when uw.x >= 0, the primary sample (u0, u1) of the direction is replaced by uw after the
+// generator has drawn its own pair (a primary-sample-space warp; the generator's stream is unchanged).
+PLT_NI f3 gaussSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf, f2 uw) {
     const float s2 = __ldg(p + PG_INVSIGMA2) / (k * k);
-    const float u0 = sg.next1D(), u1 = sg.next1D();
+    float u0 = sg.next1D(), u1 = sg.next1D();
+    if (uw.x >= 0.f) { u0 = uw.x; u1 = uw.y; }
     const f2 wo = boxMullerTruncated(u0, u1, f2{-wi.x, -wi.y}, s2, pdf);
     const float z = sqrtf(fmaxf(0.f, 1.f - dot(wo, wo)));
     return mk3(wo.x, wo.y, signf(wi.z) * z);
@@ -181,11 +184,12 @@ PLT_NI float fracPGF(const float* __restrict__ p, float zx, float zy) {
     const float f = 1.f / powPos(1.f + __ldg(p + PF_T) * (zx * zx + zy * zy), __ldg(p + PF_EXPO));
     return __ldg(p + PF_C) * f;
 }
-PLT_NI f3 fracSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf) {
+PLT_NI f3 fracSample(const float* __restrict__ p, f3 wi, SampleGen& sg, float k, float& pdf, f2 uw) {
     const float s = sqrtf(fmaxf(0.f, 1.f - wi.z * wi.z));
     const float phi_i = s > 0.f ? atan2f(wi.y, wi.x) : 0.f;
     const float T = __ldg(p + PF_T);
-    const float u0 = sg.next1D(), u1 = sg.next1D();
+    float u0 = sg.next1D(), u1 = sg.next1D();
+    if (uw.x >= 0.f) { u0 = uw.x; u1 = uw.y; }
     sg.next(); sg.next();  // FractalSurface.sample draws a second, unused 2D sample
     const float M = 1.f - powf(1.f + k * k * T * sqr(1.f + s), __ldg(p + PF_SEXP));
     const float f = sqrtf(powf(1.f - M * u0, __ldg(p + PF_IEXP)) - 1.f) / __ldg(p + PF_SQRTT);

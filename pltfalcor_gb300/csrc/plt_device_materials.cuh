@@ -72,7 +72,7 @@ PLT_DI void dielEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
     }
 }
 PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f2 uw = kNoWarp) {
     const bool hasR = (lobeMask & kLobeReflection) != 0, hasT = (lobeMask & kLobeTransmission) != 0;
     const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
     if ((!hasR && !hasT) || (!hasD && !hasS)) return false;
@@ -99,7 +99,7 @@ PLT_DI bool dielSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
         lobe = isReflection ? kLobeDeltaR : (__ldg(p + PG_B) != 0.f ? kLobeDispDeltaT : kLobeDeltaT);
     } else {
         float surfPdf;
-        wo = gaussSample(p, wi, sg, k, surfPdf);
+        wo = gaussSample(p, wi, sg, k, surfPdf, uw);
         pdf *= surfPdf;
         const f3 mh = normalize(wi + wo);
         const float F = fresnelR(fresnel_dielectric(signf(wi.z) * dot(wi, mh), eta));
@@ -188,7 +188,7 @@ PLT_DI void condEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
     }
 }
 PLT_DI bool condSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f2 uw = kNoWarp) {
     const bool hasR = (lobeMask & kLobeReflection) != 0;
     const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
     if (!hasR || (!hasD && !hasS)) return false;
@@ -207,7 +207,7 @@ PLT_DI bool condSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
         lobe = kLobeDeltaR;
     } else {
         float sp;
-        wo = fracSample(p, wi, sg, k, sp);
+        wo = fracSample(p, wi, sg, k, sp, uw);
         pdf *= sp;
         lobe = kLobeScatterR;
     }
@@ -237,7 +237,7 @@ PLT_DI void opaqEval(const DevMaterial* __restrict__ m, f3 toLight, f3 toEye, ui
     for (int j = 0; j < H; ++j) b.setSP(j, (M * m00Of(m->m00a, b.wl[j])) * b.getSP(j));
 }
 PLT_DI bool opaqSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f2 uw = kNoWarp) {
     const bool hasR = (lobeMask & kLobeReflection) != 0;
     const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
     if (!hasR || (!hasD && !hasS)) return false;
@@ -256,7 +256,7 @@ PLT_DI bool opaqSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
         lobe = kLobeDeltaR;
     } else {
         float sp;
-        wo = fracSample(p, wi, sg, mk, sp);
+        wo = fracSample(p, wi, sg, mk, sp, uw);
         pdf *= sp;
         lobe = kLobeScatterR;
     }
@@ -344,7 +344,7 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
     }
 }
 PLT_DI bool coatSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f2 uw = kNoWarp) {
     const bool hasR = (lobeMask & kLobeReflection) != 0;
     const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
     if (!hasR || (!hasD && !hasS)) return false;
@@ -379,7 +379,7 @@ PLT_DI bool coatSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
         lobe = kLobeDeltaR;
     } else {
         float sp;
-        const f3 woIn = fracSample(p, wiIn, sg, k, sp);
+        const f3 woIn = fracSample(p, wiIn, sg, k, sp, uw);
         pdf *= sp;
         const FresnelD f1 = fresnel_dielectric(-woIn.z, eta1);
         wo = coatRefract(-woIn, eta1, f1.cosT);
@@ -561,7 +561,7 @@ PLT_DI void gratClosestLobeHint(const DevMaterial* __restrict__ m, f3 wi, f3 woH
 }
 template <bool CONDUCTOR>
 PLT_DI bool gratSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& pdf, float& weight, uint32_t& lobe,
-                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}) {
+                       SampleGen& sg, float wl, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}, f2 uw = kNoWarp) {
     const bool hasR = (lobeMask & kLobeReflection) != 0;
     const bool hasD = (lobeMask & kLobeDelta) != 0, hasS = (lobeMask & kLobeNonDelta) != 0;
     if (!hasR || (!hasD && !hasS)) return false;
@@ -581,8 +581,8 @@ PLT_DI bool gratSample(const DevMaterial* __restrict__ m, f3 wi, f3& wo, float& 
     }
     if (isDirect) {
         float bp = 0.f;
-        if (CONDUCTOR) condSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask);
-        else opaqSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask);
+        if (CONDUCTOR) condSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask, uw);
+        else opaqSample(m, wi, wo, bp, weight, lobe, sg, wl, lobeMask, uw);
         pdf *= bp;
         return true;
     }

@@ -44,6 +44,8 @@ constexpr uint32_t kLobeDiffuseR = 0x01u, kLobeScatterR = 0x02u, kLobeDeltaR = 0
 
 // ---- small vector helpers ----
 struct f2 { float x, y; };
+// "no primary-sample warp" for the surface samplers (x < 0)
+constexpr f2 kNoWarp = {-1.f, 0.f};
 struct f3 { float x, y, z; };
 struct f4 { float x, y, z, w; };
 PLT_DI f3 mk3(float x, float y, float z) { return {x, y, z}; }

@@ -63,7 +63,8 @@ constexpr uint32_t kPropEmissive = 0x1u, kPropTransmissive = 0x2u, kPropMwReflec
 constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 // option bits of PtParams.opt
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
-                   kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u;
+                   kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
+                   kPtLearned = 0x200u;
 
 struct PtParams {
     // scene
@@ -121,6 +122,11 @@ struct PtParams {
     uint32_t* bFlags;
     float* bContrib;
     float* bLndp;
+    // learned MIS proposal (kPtLearned)
+    const void* propNet;          // bf16 parameters
+    const float4* matFeat;        // [nMats] (roughness, pitch feature, class, enabled)
+    float propProb;               // probability of the learned strategy at a proposal vertex
+    float* wpss;                  // [npix] product of primary-sample MIS densities, or null
     // outputs
     double* accum;                // [npix][3]
     unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, paths

@@ -16,28 +16,20 @@ constexpr int kSX = kIn + 8, kSZ = kHid + 8, kSD4 = kOut + 8, kSO = kOut;
 
 // Feature vector of one query (wi in the z >= 0 frame): wi, wavelength, roughness, pitch,
 // material class one-hot.  mf = (roughness, pitch feature, class, enabled) of the material.
-__device__ __forceinline__ void features(f3 wi, float wl, float4 mf, float* x) {
-    x[0] = wi.x;
-    x[1] = wi.y;
-    x[2] = wi.z;
-    x[3] = (wl - 550.f) * (1.f / 170.f);
-    x[4] = mf.x;
-    x[5] = mf.y;
-    const int cls = (int)mf.z;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) x[6 + c] = cls == c ? 1.f : 0.f;
-    x[14] = x[15] = 0.f;
-}
+__device__ __forceinline__ void features(f3 wi, float wl, float4 mf, float* x) { featureRow(wi.x, wi.y, wi.z, wl, mf, x); }
 
 // One training sample per thread: a material among the enabled ones, wi uniform on the upper
-// hemisphere (cos >= 0.01), a wavelength in 380-720 nm, and wo drawn by the material's exact
-// sampler restricted to the non-delta lobes.  The target is wo.xy; the weight the sampler's
-// throughput weight (clamped to 4), 0 when no reflected direction was produced.
+// hemisphere (cos >= 0.01), a wavelength in 380-720 nm and a uniform primary sample u that the
+// material's exact sampler, restricted to the non-delta lobes, turns into wo.  The target is u; the
+// weight is what the path tracer's forward replay multiplies the path by at this vertex: the BSDF
+// value (an unpolarised unit beam of 1 mm^2 coherence area at 1 m arriving from wo, leaving towards
+// wi) over the sampler's pdf, clamped to 4; 0 when no direction was produced.  The weighted
+// likelihood then fits q(u) proportional to the expected contribution of u.
 __global__ void __launch_bounds__(128) proposalDataKernel(const DevMaterial* __restrict__ mats, const float4* __restrict__ matFeat,
-                                                          const uint32_t* __restrict__ enabled, uint32_t nEnabled,
-                                                          const DevProfile* __restrict__ profiles, uint32_t nProfiles, uint32_t flags,
-                                                          uint32_t n, uint32_t seed, bf16* __restrict__ x, float* __restrict__ target,
-                                                          float* __restrict__ weight) {
+                                                          const uint2* __restrict__ matProps, const uint32_t* __restrict__ enabled,
+                                                          uint32_t nEnabled, const DevProfile* __restrict__ profiles, uint32_t nProfiles,
+                                                          uint32_t flags, uint32_t n, uint32_t seed, bf16* __restrict__ x,
+                                                          float* __restrict__ target, float* __restrict__ weight) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     SampleGen sg;
@@ -50,6 +42,7 @@ __global__ void __launch_bounds__(128) proposalDataKernel(const DevMaterial* __r
     const float rxy = sqrtf(fmaxf(0.f, 1.f - z * z));
     const f3 wi = mk3(rxy * cp, rxy * sp, z);
     const float wl = 380.f + 340.f * sg.next1D();
+    const f2 u = {sg.next1D(), sg.next1D()};
     SD sd;
     sd.posW = mk3(0.f, 0.f, 0.f);
     sd.V = wi;
@@ -59,19 +52,39 @@ __global__ void __launch_bounds__(128) proposalDataKernel(const DevMaterial* __r
     sd.faceN = sd.N;
     sd.frontFacing = true;
     const DevMaterial* __restrict__ m = mats + mid;
+    const uint32_t type = __ldg(&m->type);
     f3 wo = mk3(0.f, 0.f, 0.f);
     float pdf = 0.f, w = 0.f;
     uint32_t lobe = 0;
-    (void)profiles; (void)nProfiles; (void)flags;
-    const bool ok = ptSample(m, __ldg(&m->type), sd, sg, wl, wo, pdf, w, lobe, kLobeNonDelta);
-    const bool valid = ok && pdf > 0.f && wo.z > 0.f && isfinite(w) && isfinite(wo.x) && isfinite(wo.y);
+    const bool ok = ptSample(m, type, sd, sg, wl, wo, pdf, w, lobe, kLobeNonDelta, mk3(0.f, 0.f, 0.f), u);
+    bool valid = ok && pdf > 0.f && isfinite(wo.x) && isfinite(wo.y) && isfinite(wo.z) && (lobe & kLobeDelta) == 0;
+    float contrib = 0.f;
+    if (valid) {
+        // the forward replay's view of the vertex (prepareSD with V towards the light side)
+        SD se = sd;
+        se.V = wo;
+        se.frontFacing = wo.z >= 0.f;
+        if (!se.frontFacing && (__ldg(matProps + mid).x & plt::kPropDoubleSided)) se.N = mk3(0.f, 0.f, -1.f);
+        DBeam<1> b;
+        b.L[0][0] = 1.f;
+        b.L[1][0] = b.L[2][0] = b.L[3][0] = 0.f;
+        b.wl[0] = wl;
+        b.D0 = 1.f; b.D1 = 0.f; b.D2 = 1.f;
+        b.r_m = 1.f;
+        b.r = -wo;
+        b.t = perp_stark(b.r);
+        const Ctx c{profiles, nProfiles, flags};
+        ptEval<1>(m, type, c, se, wi, lobe, b);
+        contrib = b.L[0][0] / pdf;
+        valid = isfinite(contrib);
+    }
     float f[16];
     features(wi, wl, __ldg(matFeat + mid), f);
 #pragma unroll
     for (int c = 0; c < 16; c += 2) *reinterpret_cast<uint32_t*>(x + (size_t)i * kIn + c) = packBf(f[c], f[c + 1]);
-    target[2 * (size_t)i] = valid ? wo.x : 0.f;
-    target[2 * (size_t)i + 1] = valid ? wo.y : 0.f;
-    weight[i] = valid ? fminf(fmaxf(w, 0.f), 4.f) : 0.f;
+    target[2 * (size_t)i] = u.x;
+    target[2 * (size_t)i + 1] = u.y;
+    weight[i] = valid ? fminf(fmaxf(contrib, 0.f), 4.f) : 0.f;
 }
 
 // Mixture negative log-likelihood of one sample and its gradient w.r.t. the 32 outputs.
@@ -341,12 +354,12 @@ static cudaError_t gradSmemAttr(const void* fn) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(pltdev::mlp::GradSmem));
 }
 
-cudaError_t launchProposalData(const pltdev::DevMaterial* mats, const float4* matFeat, const uint32_t* enabled, uint32_t nEnabled,
-                               const pltdev::DevProfile* profiles, uint32_t nProfiles, uint32_t flags, uint32_t n, uint32_t seed,
-                               void* x, float* target, float* weight, cudaStream_t stream) {
+cudaError_t launchProposalData(const pltdev::DevMaterial* mats, const float4* matFeat, const uint2* matProps, const uint32_t* enabled,
+                               uint32_t nEnabled, const pltdev::DevProfile* profiles, uint32_t nProfiles, uint32_t flags, uint32_t n,
+                               uint32_t seed, void* x, float* target, float* weight, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
-    pltdev::mlp::proposalDataKernel<<<(n + 127) / 128, 128, 0, stream>>>(mats, matFeat, enabled, nEnabled, profiles, nProfiles, flags, n,
-                                                                         seed, static_cast<bf16*>(x), target, weight);
+    pltdev::mlp::proposalDataKernel<<<(n + 127) / 128, 128, 0, stream>>>(mats, matFeat, matProps, enabled, nEnabled, profiles, nProfiles,
+                                                                         flags, n, seed, static_cast<bf16*>(x), target, weight);
     return cudaGetLastError();
 }
 

@@ -1,14 +1,16 @@
 // Learned MIS proposal for the non-delta BSDF lobes: a conditional MLP
 //   x (16 = wi 3, wavelength, roughness, grating pitch, material class one-hot 8, 2 zero pads)
 //   -> 64 -> 64 -> 64 (SiLU) -> 32 = 8 x (logit, mu_x, mu_y, log sigma)
-// giving a mixture of 8 isotropic Gaussians on the projected hemisphere (the unit disk of wo.xy in
-// the shading frame).  BF16 weights and activations, FP32 accumulation on the tensor cores
-// (warp-level mma.sync m16n8k16).  No counterpart in the reference: PLTPT samples only the
-// analytic BSDF samplers; the proposal is an additional one-sample MIS technique, so the exact
-// BSDF is still evaluated on every path and the estimate stays unbiased.
+// giving a mixture of 8 isotropic Gaussians over the primary sample (u0, u1) in [0,1)^2 that the
+// surface model's direction sampler (Gaussian or fractal surface) maps to wo.  BF16 weights and
+// activations, FP32 accumulation on the tensor cores (warp-level mma.sync m16n8k16).  No
+// counterpart in the reference: PLTPT samples only the analytic BSDF samplers; the proposal is an
+// additional one-sample MIS technique in primary sample space, so the exact BSDF is still evaluated
+// on every path and the estimate keeps the analytic tracer's expectation.
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdint>
 
 namespace pltdev {
@@ -143,7 +145,7 @@ __device__ __forceinline__ void decodeMixture(const float* out, Mixture& m) {
 #pragma unroll
     for (int k = 0; k < kComp; ++k) m.pi[k] *= inv;
 }
-// density on the disk at (x, y)
+// density at (x, y)
 __device__ __forceinline__ float mixtureDensity(const Mixture& m, float x, float y) {
     float p = 0.f;
 #pragma unroll
@@ -153,6 +155,103 @@ __device__ __forceinline__ float mixtureDensity(const Mixture& m, float x, float
         p += m.pi[k] * (0.159154943091895335769f * is2) * expf(-0.5f * (dx * dx + dy * dy) * is2);
     }
     return p;
+}
+
+// ---- inference inside the path tracer ------------------------------------------------------
+
+// Feature row of one query: wi in the shading frame (z > 0), the hero wavelength (nm) and the
+// material's (roughness, pitch feature, class, enabled).
+__device__ __forceinline__ void featureRow(float wx, float wy, float wz, float wl, float4 mf, float* x) {
+    x[0] = wx;
+    x[1] = wy;
+    x[2] = wz;
+    x[3] = (wl - 550.f) * (1.f / 170.f);
+    x[4] = mf.x;
+    x[5] = mf.y;
+    const int cls = (int)mf.z;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[6 + c] = cls == c ? 1.f : 0.f;
+    x[14] = x[15] = 0.f;
+}
+
+// Forward of the 32 rows of one warp in place in a [32][kSWH] bf16 buffer: inputs in columns
+// 0..15 on entry, the 32 fp32 outputs in the first 128 bytes of each row on exit.  Every layer
+// reads its 16-row tile completely before the warp overwrites it.
+__device__ __forceinline__ void warpForward32InPlace(bf16* buf, const SmemNet& net) {
+#pragma unroll 1
+    for (int t = 0; t < 2; ++t) {
+        const int r = 16 * t;
+        float a64[kHid / 8][4], a32[kOut / 8][4];
+        warpForwardTile<kIn, kHid>(buf, kSWH, r, false, net.w1, kSW1, a64);
+        __syncwarp();
+        storeZ<kHid>(a64, net.b, buf, kSWH, r);
+        __syncwarp();
+        warpForwardTile<kHid, kHid>(buf, kSWH, r, true, net.w2, kSWH, a64);
+        __syncwarp();
+        storeZ<kHid>(a64, net.b + kHid, buf, kSWH, r);
+        __syncwarp();
+        warpForwardTile<kHid, kHid>(buf, kSWH, r, true, net.w3, kSWH, a64);
+        __syncwarp();
+        storeZ<kHid>(a64, net.b + 2 * kHid, buf, kSWH, r);
+        __syncwarp();
+        warpForwardTile<kHid, kOut>(buf, kSWH, r, true, net.w4, kSWH, a32);
+        __syncwarp();
+        storeOut<kOut>(a32, net.b + 3 * kHid, reinterpret_cast<float*>(buf), kSWH / 2, r);
+        __syncwarp();
+    }
+}
+
+// A vertex's mixture as the path tracer keeps it: per component (weight, mu_x) and (mu_y, sigma)
+// as binary16 pairs (half the registers of the fp32 form); sampling and density use these values.
+struct PropMix {
+    uint2 c[kComp];
+};
+__device__ __forceinline__ uint32_t packHalf2(float lo, float hi) {
+    return (uint32_t)__half_as_ushort(__float2half_rn(lo)) | ((uint32_t)__half_as_ushort(__float2half_rn(hi)) << 16);
+}
+__device__ __forceinline__ float halfLo(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v & 0xFFFFu))); }
+__device__ __forceinline__ float halfHi(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v >> 16))); }
+
+__device__ __forceinline__ void packMixture(const float* out, PropMix& pm) {
+    Mixture m;
+    decodeMixture(out, m);
+#pragma unroll
+    for (int k = 0; k < kComp; ++k) pm.c[k] = make_uint2(packHalf2(m.pi[k], m.mx[k]), packHalf2(m.my[k], m.sig[k]));
+}
+// density at (x, y): sum_k (w_k / sum w) N((x, y); mu_k, sigma_k^2 I)
+__device__ __forceinline__ float mixtureDensityPacked(const PropMix& pm, float x, float y) {
+    float s = 0.f, p = 0.f;
+#pragma unroll
+    for (int k = 0; k < kComp; ++k) {
+        const float w = halfLo(pm.c[k].x), dx = x - halfHi(pm.c[k].x), dy = y - halfLo(pm.c[k].y), sg = halfHi(pm.c[k].y);
+        const float is2 = 1.f / (sg * sg);
+        s += w;
+        p += w * (0.159154943091895335769f * is2) * expf(-0.5f * (dx * dx + dy * dy) * is2);
+    }
+    return s > 0.f ? p / s : 0.f;
+}
+// Draws (x, y) from the mixture: a component by u0 over the cumulative weights, then a Box-Muller
+// Gaussian step from (u1, u2).
+__device__ __forceinline__ void sampleMixturePacked(const PropMix& pm, float u0, float u1, float u2, float& x, float& y) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kComp; ++k) s += halfLo(pm.c[k].x);
+    const float t = u0 * s;
+    float cum = 0.f, mx = 0.f, my = 0.f, sg = 0.f, lmx = 0.f, lmy = 0.f, lsg = 0.f;
+    bool found = false;
+#pragma unroll
+    for (int k = 0; k < kComp; ++k) {
+        const float w = halfLo(pm.c[k].x);
+        cum += w;
+        if (w > 0.f) { lmx = halfHi(pm.c[k].x); lmy = halfLo(pm.c[k].y); lsg = halfHi(pm.c[k].y); }
+        if (!found && t < cum) { found = true; mx = halfHi(pm.c[k].x); my = halfLo(pm.c[k].y); sg = halfHi(pm.c[k].y); }
+    }
+    if (!found) { mx = lmx; my = lmy; sg = lsg; }
+    const float r = sg * sqrtf(-2.f * logf(1.f - u1));
+    float sn, cs;
+    sincosf(6.28318530717958647692f * u2, &sn, &cs);
+    x = mx + r * cs;
+    y = my + r * sn;
 }
 
 }  // namespace mlp

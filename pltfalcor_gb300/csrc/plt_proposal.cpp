@@ -8,9 +8,9 @@
 #include "plt_context.h"
 
 namespace plt {
-cudaError_t launchProposalData(const pltdev::DevMaterial* mats, const float4* matFeat, const uint32_t* enabled, uint32_t nEnabled,
-                               const pltdev::DevProfile* profiles, uint32_t nProfiles, uint32_t flags, uint32_t n, uint32_t seed,
-                               void* x, float* target, float* weight, cudaStream_t stream);
+cudaError_t launchProposalData(const pltdev::DevMaterial* mats, const float4* matFeat, const uint2* matProps, const uint32_t* enabled,
+                               uint32_t nEnabled, const pltdev::DevProfile* profiles, uint32_t nProfiles, uint32_t flags, uint32_t n,
+                               uint32_t seed, void* x, float* target, float* weight, cudaStream_t stream);
 cudaError_t launchProposalGrad(const void* params, const void* x, const float* target, const float* weight, uint32_t n, float* grad,
                                float* loss, cudaStream_t stream);
 cudaError_t launchProposalForward(const void* params, const void* x, uint32_t n, float* out, cudaStream_t stream);
@@ -101,7 +101,8 @@ extern "C" {
 
 plt_status plt_proposal_init(plt_context* ctx, uint64_t seed) {
     if (!ctx) return PLT_INVALID_ARG;
-    // Glorot-uniform weights, zero biases except log sigma = -1 (sigma ~ 0.37 on the unit disk)
+    // Glorot-uniform weights, zero biases except the means (0.5, the centre of the primary-sample
+    // square) and log sigma = -1 (sigma ~ 0.37)
     std::vector<float> h(PLT_PROPOSAL_PARAMS, 0.f);
     uint64_t st = seed ^ 0x5EEDu;
     const int fan[4][2] = {{16, 64}, {64, 64}, {64, 64}, {64, 32}};
@@ -118,7 +119,10 @@ plt_status plt_proposal_init(plt_context* ctx, uint64_t seed) {
         off += (size_t)fan[l][0] * fan[l][1];
     }
     const size_t b4 = off + 3 * 64;
-    for (int k = 0; k < 8; ++k) h[b4 + 4 * k + 3] = -1.f;
+    for (int k = 0; k < 8; ++k) {
+        h[b4 + 4 * k + 1] = h[b4 + 4 * k + 2] = .5f;
+        h[b4 + 4 * k + 3] = -1.f;
+    }
     return uploadParams(ctx, h.data());
 }
 
@@ -139,8 +143,9 @@ plt_status plt_proposal_get_params(plt_context* ctx, float* params) {
 plt_status plt_proposal_generate(plt_context* ctx, uint32_t n, uint32_t seed, uint16_t* x, float* target, float* weight, void* stream) {
     if (!ctx || (n && (!x || !target || !weight))) return PLT_INVALID_ARG;
     if (ctx->nPropEnabled == 0) return PLT_INVALID_ARG;   // no material with non-delta scatter lobes
-    PLT_CUDA(ctx, plt::launchProposalData(ctx->dMats, ctx->dMatFeat, ctx->dPropEnabled, ctx->nPropEnabled, ctx->dProfiles, ctx->nProfiles,
-                                          ctx->opt.flags, n, seed, x, target, weight, (cudaStream_t)stream));
+    PLT_CUDA(ctx, plt::launchProposalData(ctx->dMats, ctx->dMatFeat, static_cast<const uint2*>(ctx->dMatProps), ctx->dPropEnabled,
+                                          ctx->nPropEnabled, ctx->dProfiles, ctx->nProfiles, ctx->opt.flags, n, seed, x, target, weight,
+                                          (cudaStream_t)stream));
     return PLT_OK;
 }
 

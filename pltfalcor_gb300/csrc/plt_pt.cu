@@ -12,18 +12,27 @@ cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream
     if (p.npix == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 2), stream);
     if (e != cudaSuccess) return e;
-    static int bpsInit = -1, bpsBounce = -1;
+    // shared memory of the learned variant: the network and one 32-row activation tile per warp
+    constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
+    static int bpsInit = -1, bpsBounce = -1, bpsLearned = -1;
     if (bpsBounce < 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel<false>, 128, 0);
         bpsBounce = b > 0 ? b : 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel<true>, 128, kLearnedSmem);
+        bpsLearned = b > 0 ? b : 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptInitKernel, 128, 0);
         bpsInit = b > 0 ? b : 1;
     }
     const uint32_t need = (p.npix + 127) / 128;
     pltdev::ptInitKernel<<<std::min<uint32_t>(need, (uint32_t)(numSMs * bpsInit)), 128, 0, stream>>>(p);
-    const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsBounce));
-    for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<<<gridB, 128, 0, stream>>>(p, it);
+    if (p.opt & kPtLearned) {
+        const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsLearned));
+        for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
+    } else {
+        const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsBounce));
+        for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<false><<<gridB, 128, 0, stream>>>(p, it);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     switch (p.hwss) {
     case 1: return pltdev::launchSolveH<1>(p, numSMs, stream);

@@ -10,6 +10,7 @@
 #include <cuda_fp16.h>
 
 #include "plt_bsdf_query.cuh"
+#include "plt_mlp.cuh"
 #include "plt_trace.cuh"
 
 namespace pltdev {
@@ -19,6 +20,8 @@ using plt::PtParams;
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 // RayFlags, Path.slang:46-106
 constexpr uint32_t kFlagLastDelta = 0x1u, kFlagDispersive = 0x2u, kFlagOnlyDelta = 0x4u, kFlagMiss = 0x10u, kFlagTerminated = 0x20u;
+// a vertex where the learned proposal was a sampling technique
+constexpr uint32_t kFlagLearned = 0x40u;
 constexpr float kQcutoffForMS = .15f;
 constexpr float kFltMax = 3.402823466e+38f;
 constexpr float kFltMin = 1.175494351e-38f;
@@ -180,8 +183,9 @@ PLT_DI void ptEval(const DevMaterial* __restrict__ m, uint32_t type, const Ctx& 
 // restrict the lobes to the hint's side (PLTDielectricBSDF.slang:310-321,
 // PLTThinDielectricBSDF.slang:230-243), the grated materials take the diffraction order closest to
 // the hint; the sample pass uses lobeMask All and no hint.
+// uw (x >= 0): primary sample of the surface model's direction sampler (used by the non-delta lobes)
 PLT_DI bool ptSample(const DevMaterial* __restrict__ m, uint32_t type, const SD& sd, SampleGen& sg, float wl, f3& wo, float& pdf,
-                     float& weight, uint32_t& lobe, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}) {
+                     float& weight, uint32_t& lobe, uint32_t lobeMask = kLobeAll, f3 woHint = f3{0.f, 0.f, 0.f}, f2 uw = kNoWarp) {
     const WFrame F = bsdfFrame(sd, type, m);
     const f3 V = F.toLocal(sd.V);
     uint32_t sideMask = lobeMask;
@@ -191,13 +195,13 @@ PLT_DI bool ptSample(const DevMaterial* __restrict__ m, uint32_t type, const SD&
     }
     bool ok;
     switch (type) {
-    case kMatDielectric: ok = dielSample(m, V, wo, pdf, weight, lobe, sg, wl, sideMask); break;
-    case kMatConductor: ok = condSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
-    case kMatOpaqueDielectric: ok = opaqSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
+    case kMatDielectric: ok = dielSample(m, V, wo, pdf, weight, lobe, sg, wl, sideMask, uw); break;
+    case kMatConductor: ok = condSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, uw); break;
+    case kMatOpaqueDielectric: ok = opaqSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, uw); break;
     case kMatCoatedConductor:
-    case kMatCoatedOpaque: ok = coatSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask); break;
-    case kMatGratedConductor: ok = gratSample<true>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint)); break;
-    case kMatGratedOpaque: ok = gratSample<false>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint)); break;
+    case kMatCoatedOpaque: ok = coatSample(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, uw); break;
+    case kMatGratedConductor: ok = gratSample<true>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint), uw); break;
+    case kMatGratedOpaque: ok = gratSample<false>(m, V, wo, pdf, weight, lobe, sg, wl, lobeMask, F.toLocal(woHint), uw); break;
     case kMatThin: ok = thinSample(m, V, wo, pdf, weight, lobe, sg, sideMask); break;
     case kMatMultilayer:
         if ((lobeMask & kLobeReflection) == 0 || (lobeMask & kLobeDelta) == 0 || V.z <= 0.f) { ok = false; break; }
@@ -408,13 +412,31 @@ __global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
         P.lndp[i] = 0.f;
         P.pflags[i] = kFlagOnlyDelta;
         P.plen[i] = 0;
+        if (P.wpss) P.wpss[i] = 1.f;
     }
 }
 
 // One segment of every live path: TraceRay + scatterTriangleMeshClosestHit / scatterMiss
 // (pltpt_sample.rt.slang:56-141), appendBounce (pltpt.slangh:138-154).  Live paths are compacted
 // into the next queue with one atomic per warp.
-__global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t it) {
+//
+// LEARNED adds the learned proposal at every proposal vertex (an enabled material hit from the
+// front with wi above the shading plane).  The warp runs the network on its 32 lanes' feature rows
+// (tensor cores, weights in shared memory); the network's mixture is a density q over the primary
+// sample (u0, u1) in [0,1)^2 that the surface model's direction sampler turns into wo.  The primary
+// sample comes from q with probability c and is uniform otherwise (one-sample MIS in primary sample
+// space), so a non-delta direction has the density p(wo) * (c q(u) + 1 - c): the path weight is
+// divided by that factor (kept in the path state), while the analytic pdf the reference's MIS
+// weights, Russian roulette and the path-pdf cutoff use is unchanged.  The estimate therefore has
+// the analytic tracer's expectation whatever the network outputs; the exact BSDF is evaluated as
+// before.  A primary sample of q outside the unit square ends a path that takes a non-delta lobe.
+// Residency of the analytic variant (blocks of 128 per SM; the register budget follows from it).
+#ifndef PLT_BOUNCE_MIN_BLOCKS
+#define PLT_BOUNCE_MIN_BLOCKS 7
+#endif
+template <bool LEARNED>
+__global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBounceKernel(const PtParams P, uint32_t it) {
+    extern __shared__ __align__(16) unsigned char ptSmem[];
     const uint32_t n = P.npix;
     const uint32_t count = it == 0 ? n : *((volatile uint32_t*)(P.qcount + it));
     const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
@@ -422,84 +444,162 @@ __global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
     uint32_t nv = 0, tt = 0, overflow = 0, recorded = 0;
     const Ctx c{P.profiles, P.nProfiles, P.flags};
+    (void)c;
+    mlp::bf16* wbuf = nullptr;
+    if constexpr (LEARNED) {
+        mlp::loadNet(*reinterpret_cast<mlp::SmemNet*>(ptSmem), static_cast<const mlp::bf16*>(P.propNet));
+        wbuf = reinterpret_cast<mlp::bf16*>(ptSmem + sizeof(mlp::SmemNet)) + (threadIdx.x >> 5) * 32 * mlp::kSWH;
+        __syncthreads();
+    }
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounds = (count + stride - 1) / stride;
     for (uint32_t rr = 0; rr < rounds; ++rr) {
         const uint32_t slot = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool act = slot < count;
         bool live = false;
         uint32_t pid = 0;
-        if (slot < count) {
+        SampleGen sg;
+        f3 org = mk3(0.f, 0.f, 0.f), dir = mk3(0.f, 0.f, 1.f);
+        float weight = 0.f, pdf = 0.f, thp = 0.f, lndp = 0.f, wavelength = 0.f;
+        float wps = 1.f;   // product of the primary-sample MIS densities (learned proposal)
+        uint32_t flags = 0, len = 0;
+        // the vertex this segment reaches
+        bool hit = false, shouldEnd = false;
+        TraceResult h;
+        SD sd;
+        uint32_t mid = 0;
+        uint2 props = make_uint2(0u, 0u);
+        float rcpThp = 1.f;
+        auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe, uint32_t extra) {
+            const size_t o = (size_t)len * n + pid;
+            P.bFlags[o] = flags | extra;
+            P.bPrim[o] = prim;
+            P.bBary[(size_t)len * 2 * n + pid] = b1;
+            P.bBary[(size_t)len * 2 * n + n + pid] = b2;
+            const f2 e = ndirToOctEqualArea(wi);
+            P.bEw[(size_t)len * 2 * n + pid] = e.x;
+            P.bEw[(size_t)len * 2 * n + n + pid] = e.y;
+            P.bLobe[o] = lobe;
+            P.bLndp[o] = lndp;
+            P.bContrib[o] = 1.f / (pdf * thp * wps);
+            ++recorded;
+        };
+        if (act) {
             pid = it == 0 ? slot : qin[slot];
-            SampleGen sg;
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
-            f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
-            float weight = P.weight[pid], pdf = P.pdf[pid], thp = P.thp[pid], lndp = P.lndp[pid];
-            uint32_t flags = P.pflags[pid], len = P.plen[pid];
-            const float wavelength = P.wl[pid];
-            auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe) {
-                const size_t o = (size_t)len * n + pid;
-                P.bFlags[o] = flags;
-                P.bPrim[o] = prim;
-                P.bBary[(size_t)len * 2 * n + pid] = b1;
-                P.bBary[(size_t)len * 2 * n + n + pid] = b2;
-                const f2 e = ndirToOctEqualArea(wi);
-                P.bEw[(size_t)len * 2 * n + pid] = e.x;
-                P.bEw[(size_t)len * 2 * n + n + pid] = e.y;
-                P.bLobe[o] = lobe;
-                P.bLndp[o] = lndp;
-                P.bContrib[o] = 1.f / (pdf * thp);
-                ++recorded;
-            };
+            org = ldPlane3(P.org, pid, n);
+            dir = ldPlane3(P.dir, pid, n);
+            weight = P.weight[pid]; pdf = P.pdf[pid]; thp = P.thp[pid]; lndp = P.lndp[pid];
+            flags = P.pflags[pid]; len = P.plen[pid];
+            wavelength = P.wl[pid];
+            if constexpr (LEARNED) wps = P.wpss[pid];
             for (int guard = 0; guard < 64; ++guard) {
-                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
+                h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
-                    append(kNoHit, 0.f, 0.f, wi, 0u);
+                    append(kNoHit, 0.f, 0.f, wi, 0u, 0u);
                     break;
                 }
                 const VData v = vertexData(P, h.prim, h.b1, h.b2);
-                const uint32_t mid = __ldg(P.triMat + h.prim);
-                const uint2 props = __ldg(P.matProps + mid);
-                const SD sd = prepareSD(v, props.x, wi);
+                mid = __ldg(P.triMat + h.prim);
+                props = __ldg(P.matProps + mid);
+                sd = prepareSD(v, props.x, wi);
                 if (props.x & plt::kPropAlphaZero) {   // alpha mask: continue the same ray
                     org = sd.newRayOrigin(false);
                     continue;
                 }
                 // Russian roulette RR(1 - weight, 2, u) (pltpt.slangh:170-176); pow of a negative
                 // base is NaN as in the shader
-                float rcpThp = 1.f;
                 if (P.opt & plt::kPtDoRR) {
                     const float rrVal = 1.f - weight;
                     const float p = rrVal < 0.f ? __int_as_float(0x7fffffff) : rrVal * rrVal;
                     const float u = sg.next1D();
                     rcpThp = u < p ? 0.f : 1.f - p;
                 }
-                bool shouldEnd = len == P.maxBounces || (rcpThp == 0.f && len > 0);
-                f3 wo = mk3(0.f, 0.f, 0.f);
-                float spdf = 0.f, sweight = 0.f;
-                uint32_t slobe = 0;
-                if (!shouldEnd) {
-                    const DevMaterial* __restrict__ m = P.mats + mid;
-                    const bool ok = ptSample(m, __ldg(&m->type), sd, sg, wavelength, wo, spdf, sweight, slobe);
-                    shouldEnd = !ok || spdf == 0.f;
-                    const float nc = pdf * spdf * thp * rcpThp;
-                    shouldEnd = shouldEnd || nc < 1e-6f;
+                shouldEnd = len == P.maxBounces || (rcpThp == 0.f && len > 0);
+                hit = true;
+                break;
+            }
+            if (!hit && (flags & kFlagMiss) == 0) {
+                // 64 alpha-masked hits in a row: end the path with an empty terminal record
+                flags |= kFlagTerminated;
+                append(kNoHit, 0.f, 0.f, -dir, 0u, 0u);
+            }
+        }
+        // learned proposal: the warp's network inference (all 32 lanes, uniform branch)
+        mlp::PropMix mix;
+        bool useNet = false;
+        if constexpr (LEARNED) {
+            float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
+            f3 wiL = mk3(0.f, 0.f, 0.f);
+            if (hit) {
+                mf = __ldg(P.matFeat + mid);
+                wiL = sd.toLocal(sd.V);
+                useNet = mf.w > 0.f && sd.frontFacing && wiL.z > 0.f;
+            }
+            if (__any_sync(0xFFFFFFFFu, useNet)) {
+                const int lane = threadIdx.x & 31;
+                float x[mlp::kIn];
+                mlp::featureRow(wiL.x, wiL.y, wiL.z, wavelength, mf, x);
+                uint32_t* row = reinterpret_cast<uint32_t*>(wbuf + lane * mlp::kSWH);
+#pragma unroll
+                for (int k = 0; k < mlp::kIn; k += 2) row[k / 2] = useNet ? mlp::packBf(x[k], x[k + 1]) : 0u;
+                __syncwarp();
+                mlp::warpForward32InPlace(wbuf, *reinterpret_cast<const mlp::SmemNet*>(ptSmem));
+                if (useNet) mlp::packMixture(reinterpret_cast<const float*>(wbuf) + lane * (mlp::kSWH / 2), mix);
+                __syncwarp();
+            }
+        }
+        if (hit) {
+            const f3 wi = -dir;
+            f3 wo = mk3(0.f, 0.f, 0.f);
+            float spdf = 0.f, sweight = 0.f, warp = 1.f;
+            uint32_t slobe = 0;
+            if (!shouldEnd) {
+                const DevMaterial* __restrict__ m = P.mats + mid;
+                const uint32_t type = __ldg(&m->type);
+                // primary sample of the direction: from the proposal (probability c) or uniform
+                f2 uw = kNoWarp;
+                float mpss = 1.f;
+                bool inside = true;
+                if (LEARNED && useNet) {
+                    const float cl = P.propProb;
+                    if (sg.next1D() < cl) {
+                        const float u0 = sg.next1D(), u1 = sg.next1D(), u2 = sg.next1D();
+                        mlp::sampleMixturePacked(mix, u0, u1, u2, uw.x, uw.y);
+                        inside = uw.x >= 0.f && uw.x < 1.f && uw.y >= 0.f && uw.y < 1.f;
+                    } else {
+                        uw.x = sg.next1D();
+                        uw.y = sg.next1D();
+                    }
+                    mpss = inside ? cl * mlp::mixtureDensityPacked(mix, uw.x, uw.y) + (1.f - cl) : 0.f;
+                    if (!inside) uw = f2{.5f, .5f};   // finite sampler arithmetic; a non-delta result is dropped below
                 }
-                const bool isDelta = (slobe & kLobeDelta) != 0;
-                const bool isDisp = (slobe & (kLobeDispDeltaR | kLobeDispDeltaT)) != 0;
-                const bool isRefl = (slobe & kLobeReflection) != 0;
-                const bool isMS = (isRefl && (props.x & plt::kPropMwReflective)) || (!isRefl && (props.x & plt::kPropMwTransmissive));
-                if (shouldEnd) {
-                    flags |= kFlagTerminated;
-                    append(h.prim, h.b1, h.b2, wi, 0u);
-                    break;
+                bool ok = ptSample(m, type, sd, sg, wavelength, wo, spdf, sweight, slobe, kLobeAll, mk3(0.f, 0.f, 0.f), uw);
+                if (LEARNED && useNet && ok && (slobe & kLobeDelta) == 0) {
+                    ok = inside && mpss > 0.f;
+                    warp = mpss;
                 }
+                shouldEnd = !ok || spdf == 0.f;
+                const float nc = pdf * spdf * thp * rcpThp;
+                shouldEnd = shouldEnd || nc < 1e-6f;
+            }
+            const uint32_t extra = useNet ? kFlagLearned : 0u;
+            const bool isDelta = (slobe & kLobeDelta) != 0;
+            const bool isDisp = (slobe & (kLobeDispDeltaR | kLobeDispDeltaT)) != 0;
+            const bool isRefl = (slobe & kLobeReflection) != 0;
+            const bool isMS = (isRefl && (props.x & plt::kPropMwReflective)) || (!isRefl && (props.x & plt::kPropMwTransmissive));
+            if (shouldEnd) {
+                flags |= kFlagTerminated;
+                append(h.prim, h.b1, h.b2, wi, 0u, extra);
+            } else {
                 weight *= sweight;
                 thp *= rcpThp;
                 pdf *= spdf;
+                wps *= warp;
                 if (isDisp) flags |= kFlagDispersive;
-                append(h.prim, h.b1, h.b2, wi, slobe);
+                append(h.prim, h.b1, h.b2, wi, slobe, extra);
                 ++len;
                 lndp = !isDelta ? spdf : lndp;
                 const uint32_t msc = isMS ? (flags >> 16) + 1u : 0u;
@@ -509,13 +609,9 @@ __global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t
                 org = sd.newRayOrigin(isRefl);
                 dir = wo;
                 live = len < P.maxBounces + 1;
-                break;
             }
-            if (!live && (flags & (kFlagMiss | kFlagTerminated)) == 0) {
-                // 64 alpha-masked hits in a row: end the path with an empty terminal record
-                flags |= kFlagTerminated;
-                append(kNoHit, 0.f, 0.f, -dir, 0u);
-            }
+        }
+        if (act) {
             P.sg[pid] = sg.s0; P.sg[n + pid] = sg.s1; P.sg[2 * n + pid] = sg.s2; P.sg[3 * n + pid] = sg.s3;
             stPlane3(P.org, pid, n, org);
             stPlane3(P.dir, pid, n, dir);
@@ -525,6 +621,7 @@ __global__ void __launch_bounds__(128) ptBounceKernel(const PtParams P, uint32_t
             P.lndp[pid] = lndp;
             P.pflags[pid] = flags;
             P.plen[pid] = len;
+            if constexpr (LEARNED) P.wpss[pid] = wps;
         }
         const uint32_t pos = warpAggregatedAdd(P.qcount + it + 1, live);
         if (live) qout[pos] = pid;

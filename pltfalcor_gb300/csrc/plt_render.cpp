@@ -291,7 +291,7 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 
 void pltReleaseRenderState(plt_context* ctx) {
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -327,12 +327,24 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     if (o.hwss < 1 || o.hwss > 4) return PLT_NOT_SUPPORTED;
     if (o.mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     if (o.max_bounces > 64) return PLT_NOT_SUPPORTED;
+    const bool learned = o.learned_proposal != 0;
+    if (learned && (!ctx->propReady || !ctx->dMatFeat || !(o.learned_proposal_prob > 0.f && o.learned_proposal_prob < 1.f)))
+        return PLT_INVALID_ARG;
     const uint64_t npix64 = (uint64_t)width * height;
     if (npix64 == 0) return PLT_OK;
     if (npix64 > (1u << 26)) return PLT_NOT_SUPPORTED;
     const uint32_t npix = (uint32_t)npix64;
     plt_status s = ensureRenderBuffers(ctx, npix, o.max_bounces);
     if (s != PLT_OK) return s;
+    // path state of learned renders: the product of primary-sample MIS densities per path
+    const size_t mixBytes = learned ? (size_t)npix * sizeof(float) : 0;
+    if (learned && ctx->ptMixBytes < mixBytes) {
+        cudaFree(ctx->dPtMix);
+        ctx->dPtMix = nullptr;
+        ctx->ptMixBytes = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dPtMix, mixBytes));
+        ctx->ptMixBytes = mixBytes;
+    }
     if (!ctx->dPtStats) PLT_CUDA(ctx, cudaMalloc(&ctx->dPtStats, 4 * sizeof(unsigned long long)));
     const cudaStream_t st = (cudaStream_t)stream;
     plt::PtParams& P = ctx->pt;
@@ -370,7 +382,11 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
             (o.use_emissive_lights && ctx->nLights ? plt::kPtUseEmissive : 0u) | (nee ? plt::kPtDoNee : 0u) |
             (nee && o.do_mis ? plt::kPtDoMis : 0u) | (o.do_russian_roulette ? plt::kPtDoRR : 0u) |
             (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u) |
-            (nee && o.do_mnee ? plt::kPtDoMnee : 0u);
+            (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u);
+    P.propNet = ctx->dPropBf16;
+    P.matFeat = ctx->dMatFeat;
+    P.propProb = o.learned_proposal_prob;
+    P.wpss = learned ? static_cast<float*>(ctx->dPtMix) : nullptr;
     P.mneeMaxOccluders = o.mnee_max_occluders;
     P.mneeMaxIterations = o.mnee_max_iterations;
     P.mneeThreshold = o.mnee_solver_threshold;
