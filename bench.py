@@ -243,6 +243,72 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
     return res
 
 
+def learned_bench(dev, stream, batches=16, spp=16, prob=0.25, width=256):
+    """Learned proposal against the analytic tracer on the 1.04 M-triangle procedural room (the render
+    leg's scene and options at width^2): the proposal is trained on 2^24 samples drawn from the exact
+    samplers of the scene's materials (256 Adam steps x 65536, lr 1e-3), then both tracers render
+    `batches` independent batches of `spp` frames.  Per-batch relMSE (eps 1e-2) is taken against the
+    mean of both tracers' batches (both are unbiased for the same image); relMSE falls as 1/spp, so the
+    time to relMSE <= 1e-3 is relMSE(spp) * spp / 1e-3 frames at the measured time per frame (CUDA
+    events), plus the training time for the learned tracer."""
+    import numpy as np
+    import torch
+    from pltfalcor_gb300 import scene as S, spectra
+    from pltfalcor_gb300.bsdf import PLTContext
+    prof, _ = spectra.standard_profiles()
+    sc = S.procedural_scene()
+    base = {"max_bounces": 8, "hwss": 4, "do_mnee": 1, "mnee_max_occluders": 2, "mnee_max_iterations": 60,
+            "mnee_solver_threshold": 5e-5}
+    W = H = width
+    cam = S.room_camera(W, H)
+    out = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
+
+    def run(ctx):
+        imgs, ms = [], []
+        ctx.render(cam, W, H, out, 1 << 24, 1, stream)
+        for b in range(batches):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.render(cam, W, H, out, b * spp, spp, stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1) / spp)
+            imgs.append(out[..., :3].double().cpu().numpy())
+        return np.stack(imgs), float(np.median(ms))
+
+    ctx = PLTContext(base)
+    ctx.load_scene(sc, prof)
+    a, ms_a = run(ctx)
+    ctx.close()
+    ctx = PLTContext(dict(base, learned_proposal=1, learned_proposal_prob=prob))
+    ctx.load_scene(sc, prof)
+    ctx.proposal_init(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = ctx.proposal_train(256, batch=65536, lr=1e-3, seed=1)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    b, ms_b = run(ctx)
+    st = ctx.check_status(stream)
+    ctx.close()
+    ref = 0.5 * (a.mean(0) + b.mean(0))
+    rel = lambda x: np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2), axis=(1, 2, 3))
+    ra, rb = rel(a), rel(b)
+    ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
+    se = float(np.sqrt(ma.var(ddof=1) / batches + mb.var(ddof=1) / batches))
+    t_a = float(ra.mean()) * spp / 1e-3 * ms_a * 1e-3
+    t_b = float(rb.mean()) * spp / 1e-3 * ms_b * 1e-3 + train_s
+    return {"workload": "procedural room 1.04 M triangles, %dx%d, max depth 8, HWSS 4 + spectral MIS, NEE + MIS + manifold NEE, "
+                        "RR; learned proposal probability %.2f, trained on 2^24 exact-sampler samples" % (W, H, prob),
+            "status": int(st), "spp_per_batch": spp, "batches": batches,
+            "relmse_plain": float(ra.mean()), "relmse_learned": float(rb.mean()),
+            "relmse_plain_median": float(np.median(ra)), "relmse_learned_median": float(np.median(rb)),
+            "image_mean_plain": float(ma.mean()), "image_mean_learned": float(mb.mean()), "image_mean_se": se,
+            "ms_per_spp_plain": ms_a, "ms_per_spp_learned": ms_b, "train_s": train_s,
+            "train_loss_first_last": [float(hist[:8].mean()), float(hist[-8:].mean())],
+            "time_to_relmse_1e-3_plain_s": t_a, "time_to_relmse_1e-3_learned_s": t_b, "speedup": t_a / t_b}
+
+
 def capi_options(overrides):
     import ctypes as C
     from pltfalcor_gb300 import capi
@@ -426,6 +492,8 @@ def run_ours(args):
         if not args.no_render:
             line["render"] = render_bench(dev, stream, max(3, min(args.steps // 10, 16)), 1,
                                           cpu_seconds=0.0 if (world > 1 or args.no_cpu_baseline) else min(args.cpu_seconds, 10.0))
+        if not args.no_learned:
+            line["learned"] = learned_bench(dev, stream)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         print(json.dumps(line))
@@ -444,6 +512,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-trace", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

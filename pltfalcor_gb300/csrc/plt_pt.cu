@@ -8,6 +8,14 @@
 
 namespace plt {
 
+// the analytic tracer's segment kernel (PLT_BOUNCE_PHASED selects the learned kernel's phased
+// structure without the network, for comparison)
+#ifdef PLT_BOUNCE_PHASED
+static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceKernel<false>;
+#else
+static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAnalyticKernel;
+#endif
+
 cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream) {
     if (p.npix == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 2), stream);
@@ -17,7 +25,7 @@ cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream
     static int bpsInit = -1, bpsBounce = -1, bpsLearned = -1;
     if (bpsBounce < 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel<false>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kPlainBounce, 128, 0);
         bpsBounce = b > 0 ? b : 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel<true>, 128, kLearnedSmem);
         bpsLearned = b > 0 ? b : 1;
@@ -31,7 +39,7 @@ cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream
         for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
     } else {
         const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsBounce));
-        for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<false><<<gridB, 128, 0, stream>>>(p, it);
+        for (uint32_t it = 0; it <= p.maxBounces; ++it) kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     switch (p.hwss) {

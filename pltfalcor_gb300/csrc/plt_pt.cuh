@@ -632,6 +632,129 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
     if ((threadIdx.x & 31u) == 0 && r) atomicAdd(P.stats, r);
 }
 
+// The analytic tracer's segment kernel: trace, Russian roulette and the sample in one pass per
+// lane (no warp-uniform phase for the network), which keeps its register allocation lean.
+__global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKernel(const PtParams P, uint32_t it) {
+    const uint32_t n = P.npix;
+    const uint32_t count = it == 0 ? n : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
+    uint32_t* qout = (it & 1u) ? P.queue1 : P.queue0;
+    const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
+    uint32_t nv = 0, tt = 0, overflow = 0, recorded = 0;
+    const Ctx c{P.profiles, P.nProfiles, P.flags};
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (count + stride - 1) / stride;
+    for (uint32_t rr = 0; rr < rounds; ++rr) {
+        const uint32_t slot = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool live = false;
+        uint32_t pid = 0;
+        if (slot < count) {
+            pid = it == 0 ? slot : qin[slot];
+            SampleGen sg;
+            sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
+            f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
+            float weight = P.weight[pid], pdf = P.pdf[pid], thp = P.thp[pid], lndp = P.lndp[pid];
+            uint32_t flags = P.pflags[pid], len = P.plen[pid];
+            const float wavelength = P.wl[pid];
+            auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe) {
+                const size_t o = (size_t)len * n + pid;
+                P.bFlags[o] = flags;
+                P.bPrim[o] = prim;
+                P.bBary[(size_t)len * 2 * n + pid] = b1;
+                P.bBary[(size_t)len * 2 * n + n + pid] = b2;
+                const f2 e = ndirToOctEqualArea(wi);
+                P.bEw[(size_t)len * 2 * n + pid] = e.x;
+                P.bEw[(size_t)len * 2 * n + n + pid] = e.y;
+                P.bLobe[o] = lobe;
+                P.bLndp[o] = lndp;
+                P.bContrib[o] = 1.f / (pdf * thp);
+                ++recorded;
+            };
+            for (int guard = 0; guard < 64; ++guard) {
+                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
+                const f3 wi = -dir;
+                if (h.prim == kNoHit) {
+                    flags |= kFlagMiss;
+                    append(kNoHit, 0.f, 0.f, wi, 0u);
+                    break;
+                }
+                const VData v = vertexData(P, h.prim, h.b1, h.b2);
+                const uint32_t mid = __ldg(P.triMat + h.prim);
+                const uint2 props = __ldg(P.matProps + mid);
+                const SD sd = prepareSD(v, props.x, wi);
+                if (props.x & plt::kPropAlphaZero) {   // alpha mask: continue the same ray
+                    org = sd.newRayOrigin(false);
+                    continue;
+                }
+                // Russian roulette RR(1 - weight, 2, u) (pltpt.slangh:170-176); pow of a negative
+                // base is NaN as in the shader
+                float rcpThp = 1.f;
+                if (P.opt & plt::kPtDoRR) {
+                    const float rrVal = 1.f - weight;
+                    const float p = rrVal < 0.f ? __int_as_float(0x7fffffff) : rrVal * rrVal;
+                    const float u = sg.next1D();
+                    rcpThp = u < p ? 0.f : 1.f - p;
+                }
+                bool shouldEnd = len == P.maxBounces || (rcpThp == 0.f && len > 0);
+                f3 wo = mk3(0.f, 0.f, 0.f);
+                float spdf = 0.f, sweight = 0.f;
+                uint32_t slobe = 0;
+                if (!shouldEnd) {
+                    const DevMaterial* __restrict__ m = P.mats + mid;
+                    const bool ok = ptSample(m, __ldg(&m->type), sd, sg, wavelength, wo, spdf, sweight, slobe);
+                    shouldEnd = !ok || spdf == 0.f;
+                    const float nc = pdf * spdf * thp * rcpThp;
+                    shouldEnd = shouldEnd || nc < 1e-6f;
+                }
+                const bool isDelta = (slobe & kLobeDelta) != 0;
+                const bool isDisp = (slobe & (kLobeDispDeltaR | kLobeDispDeltaT)) != 0;
+                const bool isRefl = (slobe & kLobeReflection) != 0;
+                const bool isMS = (isRefl && (props.x & plt::kPropMwReflective)) || (!isRefl && (props.x & plt::kPropMwTransmissive));
+                if (shouldEnd) {
+                    flags |= kFlagTerminated;
+                    append(h.prim, h.b1, h.b2, wi, 0u);
+                    break;
+                }
+                weight *= sweight;
+                thp *= rcpThp;
+                pdf *= spdf;
+                if (isDisp) flags |= kFlagDispersive;
+                append(h.prim, h.b1, h.b2, wi, slobe);
+                ++len;
+                lndp = !isDelta ? spdf : lndp;
+                const uint32_t msc = isMS ? (flags >> 16) + 1u : 0u;
+                flags = (flags & 0xFFFFu) | (msc << 16);
+                flags = isDelta ? (flags | kFlagLastDelta) : (flags & ~kFlagLastDelta);
+                if (!isDelta) flags &= ~kFlagOnlyDelta;
+                org = sd.newRayOrigin(isRefl);
+                dir = wo;
+                live = len < P.maxBounces + 1;
+                break;
+            }
+            if (!live && (flags & (kFlagMiss | kFlagTerminated)) == 0) {
+                // 64 alpha-masked hits in a row: end the path with an empty terminal record
+                flags |= kFlagTerminated;
+                append(kNoHit, 0.f, 0.f, -dir, 0u);
+            }
+            P.sg[pid] = sg.s0; P.sg[n + pid] = sg.s1; P.sg[2 * n + pid] = sg.s2; P.sg[3 * n + pid] = sg.s3;
+            stPlane3(P.org, pid, n, org);
+            stPlane3(P.dir, pid, n, dir);
+            P.weight[pid] = weight;
+            P.pdf[pid] = pdf;
+            P.thp[pid] = thp;
+            P.lndp[pid] = lndp;
+            P.pflags[pid] = flags;
+            P.plen[pid] = len;
+        }
+        const uint32_t pos = warpAggregatedAdd(P.qcount + it + 1, live);
+        if (live) qout[pos] = pid;
+    }
+    if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    unsigned long long r = recorded;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, o);
+    if ((threadIdx.x & 31u) == 0 && r) atomicAdd(P.stats, r);
+}
+
 #endif  // PLT_PT_SAMPLE_PASS
 
 // ---- manifold NEE (Manifolds.slangh, DifferentialShadingGeometry.slang) ---------------------

@@ -8,10 +8,9 @@
 - unbiasedness: the proposal draws the surface sampler's primary sample and divides the path weight
   by its one-sample MIS density, so the learned and the analytic tracer converge to the same image:
   image means agree within the Monte Carlo error estimated from independent batches of frames;
-- gain: after training on the scene's materials, the per-pixel error against a high-spp analytic
-  render at equal spp and the time per spp of both tracers are measured and printed (variance ratio
-  and time-to-equal-error ratio); the trained tracer must stay unbiased and its error must stay within
-  a stated factor of the analytic tracer's.
+- gain: after training on the scene's materials, the per-pixel error at equal spp and the time per
+  spp of both tracers are measured and printed (error ratio and time-to-equal-error ratio); the
+  trained tracer's error must stay within a stated factor of the analytic tracer's.
 """
 import time
 
@@ -135,38 +134,35 @@ def test_learned_render_unbiased(torch_cuda, product_lib, profiles, room):
     assert z <= Z_BOUND
 
 
-def _rel_mse(img, ref):
-    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
-
-
 def test_learned_gain_reported(torch_cuda, product_lib, profiles, room):
-    """Trained proposal against the analytic tracer at equal spp: relMSE against a 2048-spp analytic
-    reference, time per spp, and the resulting time to equal error."""
+    """Trained proposal against the analytic tracer at equal spp: per-batch relMSE against the mean of
+    both tracers' batches (both are unbiased for the same image), its median over the batches, the
+    time per spp, and the resulting time-to-equal-error ratio (relMSE falls as 1/spp)."""
     prof = profiles[0]
     w, h = 64, 48
     cam = S.room_camera(w, h)
-    plain, _ = _context(room, prof, False)
-    ref = _render(torch_cuda, plain, cam, w, h, 1 << 20, 2048)
-    spp, reps = 16, 12
+    spp, reps = 16, 16
 
-    def measure(ctx, base):
-        errs, times = [], []
+    def measure(ctx):
+        imgs, times = [], []
+        _render(torch_cuda, ctx, cam, w, h, 1 << 20, 1)
         for r in range(reps):
-            torch_cuda.cuda.synchronize()
             t0 = time.perf_counter()
-            img = _render(torch_cuda, ctx, cam, w, h, base + r * spp, spp)
+            imgs.append(_render(torch_cuda, ctx, cam, w, h, r * spp, spp))
             times.append(time.perf_counter() - t0)
-            errs.append(_rel_mse(img, ref))
-        return float(np.mean(errs)), float(np.median(times[1:]))
+        return np.stack(imgs), float(np.median(times))
 
-    e_plain, t_plain = measure(plain, 0)
+    plain, _ = _context(room, prof, False)
+    a, t_plain = measure(plain)
     plain.close()
     learned, _ = _context(room, prof, True, train_steps=256)
-    e_learned, t_learned = measure(learned, 0)
+    b, t_learned = measure(learned)
     learned.close()
-    # relMSE falls as 1/spp: time to equal error scales with error x time per spp
+    ref = 0.5 * (a.mean(0) + b.mean(0))
+    rel = lambda x: np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2), axis=(1, 2, 3))
+    e_plain, e_learned = float(np.median(rel(a))), float(np.median(rel(b)))
     speedup = (e_plain * t_plain) / (e_learned * t_learned)
-    print("gain: relMSE at %d spp plain %.4g learned %.4g (variance ratio %.3f); time per %d spp plain %.4f s learned %.4f s; "
+    print("gain: median relMSE at %d spp plain %.4g learned %.4g (ratio %.3f); time per %d spp plain %.4f s learned %.4f s; "
           "time-to-equal-error speed-up %.3f" % (spp, e_plain, e_learned, e_plain / e_learned, spp, t_plain, t_learned, speedup))
-    assert np.isfinite(e_learned)
+    assert np.isfinite(b).all()
     assert e_learned <= MAX_ERROR_FACTOR * e_plain
