@@ -174,7 +174,7 @@ def trace_bench(ctx, dev, stream, steps, warmup):
     return out
 
 
-def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
+def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0, size=1024):
     """PLTPT render pass (sample + solve) on the 1.04 M-triangle procedural room: 1024^2 paths per
     frame, max depth 8, HWSS 4 with spectral MIS, NEE + MIS with manifold walks, Russian roulette,
     power-sampled emissive light; one frame per launch sequence, `frames` frames timed with CUDA events.  e2e
@@ -191,7 +191,7 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
             "mnee_solver_threshold": 5e-5}
     ctx = PLTContext(opts)
     ctx.load_scene(sc, prof)
-    W = H = 1024
+    W = H = size
     cam = S.room_camera(W, H)
     out = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
     ctx.render(cam, W, H, out, 0, max(1, warmup), stream)
@@ -213,8 +213,8 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0):
     f1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = f0.elapsed_time(f1) / frames
-    res = {"workload": "procedural room 1.04 M triangles, 1024x1024 paths/frame, max depth 8, HWSS 4 + spectral MIS, NEE + MIS, RR, "
-                       "manifold NEE (2 occluders, 60 iterations, threshold 5e-5)",
+    res = {"workload": "procedural room 1.04 M triangles, %dx%d paths/frame, max depth 8, HWSS 4 + spectral MIS, NEE + MIS, RR, "
+                       "manifold NEE (2 occluders, 60 iterations, threshold 5e-5)" % (W, H),
            "status": int(st), "frames": frames, "ms_per_frame": ms, "paths_per_s": W * H / (ms * 1e-3),
            "e2e": {"paths_per_s": W * H / (ms_e2e * 1e-3), "d2h_bytes_per_frame": W * H * 16, "h2d_bytes_per_frame": 0},
            "bounces_per_path": stats["bounces"] / (W * H), "shadow_rays_per_path": stats["shadow_rays"] / (W * H),
@@ -491,7 +491,8 @@ def run_ours(args):
             line["trace"] = trace_bench(ctx, dev, stream, max(3, min(args.steps, 50)), max(1, args.warmup))
         if not args.no_render:
             line["render"] = render_bench(dev, stream, max(3, min(args.steps // 10, 16)), 1,
-                                          cpu_seconds=0.0 if (world > 1 or args.no_cpu_baseline) else min(args.cpu_seconds, 10.0))
+                                          cpu_seconds=0.0 if (world > 1 or args.no_cpu_baseline) else min(args.cpu_seconds, 10.0),
+                                          size=args.render_size)
         if not args.no_learned:
             line["learned"] = learned_bench(dev, stream)
         if world == 1 and not args.no_cpu_baseline:
@@ -513,6 +514,7 @@ def main():
     ap.add_argument("--no-trace", action="store_true")
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--render-size", type=int, default=1024, help="render leg image width = height (profiling uses small sizes)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -61,6 +61,8 @@ struct plt_context {
     size_t ptBytes = 0;
     void* dPtMix = nullptr;       // per-path primary-sample MIS density products (learned renders)
     size_t ptMixBytes = 0;
+    void* dMneeTasks = nullptr;   // deferred manifold walks of the solve pass
+    size_t mneeBytes = 0;
     uint32_t ptNpix = 0, ptMaxB = 0;
     plt::PtParams pt{};
     unsigned long long* dPtStats = nullptr;

@@ -65,6 +65,8 @@ constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
                    kPtLearned = 0x200u;
+// bytes reserved per deferred manifold walk (the device task structure is checked against it)
+constexpr size_t kMneeTaskBytes = 320;
 
 struct PtParams {
     // scene
@@ -127,6 +129,10 @@ struct PtParams {
     const float4* matFeat;        // [nMats] (roughness, pitch feature, class, enabled)
     float propProb;               // probability of the learned strategy at a proposal vertex
     float* wpss;                  // [npix] product of primary-sample MIS densities, or null
+    // deferred manifold walks of the solve pass (null: walks run inline)
+    void* mneeTasks;              // [mneeCap] tasks of kMneeTaskBytes
+    uint32_t mneeCap;
+    uint32_t* mneeCount;
     // outputs
     double* accum;                // [npix][3]
     unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, paths

@@ -18,7 +18,7 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 
 cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream) {
     if (p.npix == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 2), stream);
+    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 3), stream);   // + manifold-walk count
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);

@@ -976,27 +976,35 @@ PLT_DI bool manifoldSampleVertex(const PtParams& P, uint32_t prim, float b1, flo
     ++d.hitCount;
     return true;
 }
-// traceMNEEOccluders + manifoldNEESample, Manifolds.slangh:110-281
-PLT_NI bool manifoldNEESample(const PtParams& P, f3 rayO, f3 rayD, float tmax, f3 origin, f3 lightPos, f3 lightDir, int maxMS,
-                              SampleGen& sg, MSData& d, TraceCounters& tc) {
+// traceMNEEOccluders, Manifolds.slangh:110-160: the closest-hit shadow ray towards the light and a
+// hinted delta sample at every occluder (the only random draws of a manifold sample).  Returns
+// kMsFail (no contribution), kMsVisible (no occluder: the light is visible) or kMsWalk (occluders
+// recorded in d; manifoldWalk completes the sample).
+constexpr int kMsFail = 0, kMsVisible = 1, kMsWalk = 2;
+PLT_NI int manifoldOccluders(const PtParams& P, f3 rayO, f3 rayD, float tmax, int maxMS, SampleGen& sg, MSData& d, TraceCounters& tc) {
     const int maxOcc = (int)min(P.mneeMaxOccluders, (uint32_t)kMaxMsOccluders);
     const f3 wi = -rayD;
     for (int guard = 0; guard <= kMaxMsOccluders; ++guard) {
         TraceResult h;
         if (!shadowRayClosest(P, rayO, rayD, 0.f, tmax, h, tc)) break;
-        if (d.hitCount >= maxOcc || d.hitCount >= maxMS) return false;
+        if (d.hitCount >= maxOcc || d.hitCount >= maxMS) return kMsFail;
         VData v = vertexData(P, h.prim, h.b1, h.b2);
         v.posW = rayO + rayD * h.t;
         const uint32_t mid = __ldg(P.triMat + h.prim);
         const uint2 props = __ldg(P.matProps + mid);
         const SD sd = prepareSD(v, props.x, wi);
-        if (!(props.x & plt::kPropMwTransmissive)) return false;
+        if (!(props.x & plt::kPropMwTransmissive)) return kMsFail;
         if (!manifoldSampleVertex(P, h.prim, h.b1, h.b2, sd, mid, -wi, sg, d) || (d.hits[d.hitCount - 1].lobe & kLobeTransmission) == 0)
-            return false;
+            return kMsFail;
         rayO = newRayOriginToward(sd, rayD);
         tmax -= h.t;
     }
-    if (d.hitCount == 0) return true;
+    return d.hitCount == 0 ? kMsVisible : kMsWalk;
+}
+// manifoldNEESample's walk, Manifolds.slangh:162-281: Newton steps on the spherical-angle
+// constraint of every occluder with re-projection onto the same geometry instance, then the
+// visibility of the light from the last vertex.  Deterministic (no random draws).
+PLT_NI bool manifoldWalk(const PtParams& P, f3 origin, f3 lightPos, MSData& d, TraceCounters& tc) {
     float beta[kMaxMsOccluders];
 #pragma unroll
     for (int i = 0; i < kMaxMsOccluders; ++i) beta[i] = 1.f;
@@ -1055,6 +1063,17 @@ PLT_NI bool manifoldNEESample(const PtParams& P, f3 rayO, f3 rayD, float tmax, f
 }
 
 // ---- solve pass -----------------------------------------------------------------------------
+// A deferred manifold walk: everything the walk and the rest of its NEE sample need (the light
+// sample, the occluder search's result, the replay's origin).  The solve kernel records one per
+// NEE sample that found occluders; ptMneeKernel finishes them as a dense wavefront.
+template <int H> struct MneeTask {
+    MSData ms;
+    f3 tposW, ldir, msOrigin;
+    float ldist, tpdf;
+    float Le[H], swl[H];
+    uint32_t pid, p, curMS;
+};
+
 template <int H> struct Bnc {
     uint32_t prim, lobe, flags;
     float b1, b2, contrib, lndp;
@@ -1075,6 +1094,94 @@ template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p
     return b;
 }
 
+// Forward replay of one beam source of vertex p and its measurement (pltpt_solve.rt.slang:48-147):
+// the manifold vertices (last to first, manifoldForwardUnwind :80-93), the current vertex (NEE,
+// non-delta lobes), then vertices p-1 .. 0, the camera polariser and spectrumToRgb.  Adds the
+// path's contribution to (Lr, Lg, Lb).
+template <int H>
+PLT_DI void replayMeasure(const PtParams& P, uint32_t pid, int p, const Bnc<H>& bounce, PBeam<H>& pb, const MSData& ms, int nMs, f3 msOrigin,
+                          bool evalCurrent, const Ctx& c, bool hwssMis, float& Lr, float& Lg, float& Lb, uint32_t& evals) {
+    // forward replay: the manifold vertices (last to first, manifoldForwardUnwind,
+    // pltpt_solve.rt.slang:80-93), the current vertex (NEE, non-delta lobes), then p-1 .. 0
+    const int total = nMs + (evalCurrent ? 1 : 0) + p;
+    for (int k = 0; k < total; ++k) {
+        uint32_t qprim, qlobe;
+        float qb1, qb2;
+        f3 qwo;
+        bool msVertex = false;
+        f3 msPos;
+        if (k < nMs) {
+            const int idx = nMs - 1 - k;
+            const MSHit& h = ms.hits[idx];
+            qprim = h.prim; qlobe = h.lobe; qb1 = h.b1; qb2 = h.b2;
+            msPos = h.posW;
+            msVertex = true;
+            const f3 p2 = idx == 0 ? msOrigin : ms.hits[idx - 1].posW;
+            qwo = normalize(p2 - h.posW);
+        } else if (evalCurrent && k == nMs) {
+            qprim = bounce.prim; qlobe = kLobeNonDelta; qb1 = bounce.b1; qb2 = bounce.b2; qwo = bounce.wi;
+        } else {
+            const int q = p - 1 - (k - nMs - (evalCurrent ? 1 : 0));
+            const Bnc<H> bq = readBounce<H>(P, pid, q);
+            qprim = bq.prim; qlobe = bq.lobe; qb1 = bq.b1; qb2 = bq.b2; qwo = bq.wi;
+        }
+        VData qv = vertexData(P, qprim, qb1, qb2);
+        if (msVertex) qv.posW = msPos;
+        const uint32_t qmid = __ldg(P.triMat + qprim);
+        const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
+        propagate(pb, qsd.posW);
+        const DevMaterial* __restrict__ qm = P.mats + qmid;
+        const uint32_t qtype = __ldg(&qm->type);
+        ptEval<H>(qm, qtype, c, qsd, qwo, qlobe, pb.b);
+        ++evals;
+        if (hwssMis) {
+            float lp[H];
+            ptLambdaPdf<H>(qm, qtype, qsd, qwo, qlobe, pb.b, lp);
+#pragma unroll
+            for (int j = 0; j < H; ++j) pb.spdf[j] *= lp[j];
+        }
+    }
+    // measure (no camera polarizer unless set)
+    if (!(P.opt & plt::kPtUseDirect) && p <= 1) return;
+    propagate(pb, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
+    if (P.cam.polarizer > 0.f) {
+        const f3 Wc = rnormalize(mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]));
+        const f3 Uc = rnormalize(mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]));
+        pb.b.rotateFrame(Uc, -Wc);
+        const float pi = P.cam.polarizer;
+        float sth, cth;
+        sincosf(P.cam.polarizer_theta, &sth, &cth);
+        const float Pm[4][4] = {{.5f, .5f * cth, .5f * sth, 0.f}, {.5f * cth, .5f * (cth * cth), .5f * (cth * sth), 0.f},
+                                {.5f * sth, .5f * (cth * sth), .5f * (sth * sth), 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+            const float in[4] = {pb.b.L[0][j], pb.b.L[1][j], pb.b.L[2][j], pb.b.L[3][j]};
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                float acc = 0.f;
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) acc += ((1.f - pi) * (r == cc ? 1.f : 0.f) + pi * Pm[r][cc]) * in[cc];
+                pb.b.L[r][j] = acc;
+            }
+        }
+    }
+    float contrib = bounce.contrib;
+    if (hwssMis) {
+        float sum = 0.f;
+#pragma unroll
+        for (int j = 0; j < H; ++j) sum += pb.spdf[j];
+        contrib *= sum > kFltEps ? pb.spdf[0] / sum : 0.f;
+    } else {
+        contrib *= 1.f / float(pb.comps);
+    }
+    float Li[H];
+#pragma unroll
+    for (int j = 0; j < H; ++j) Li[j] = pb.b.L[0][j];
+    const f3 rgb = spectrumToRgb<H>(Li, pb.b.wl, pb.comps);
+    const float r = fmaxf(0.f, rgb.x * contrib), g = fmaxf(0.f, rgb.y * contrib), bb = fmaxf(0.f, rgb.z * contrib);
+    if (isfinite(r) && isfinite(g) && isfinite(bb)) { Lr += r; Lg += g; Lb += bb; }
+}
+
 // evalTrianglePdf x triangle-selection pdf (EmissiveLightSamplerHelpers.slang:120-151,
 // EmissivePowerSampler.slang:81-122)
 PLT_DI float emissivePdf(const PtParams& P, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
@@ -1090,8 +1197,13 @@ PLT_DI float emissivePdf(const PtParams& P, f3 posW, uint32_t light, f3 hitPos, 
     return sel * (distSqr / denom);
 }
 
-template <int H>
-__global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
+// MNEE = false compiles the solve kernel without manifold sampling (the do_mnee = 0 pass): the
+// occluder search and the task hand-off would otherwise enlarge the kernel for every option set.
+#ifndef PLT_SOLVE_MIN_BLOCKS
+#define PLT_SOLVE_MIN_BLOCKS 1
+#endif
+template <int H, bool MNEE>
+__global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const PtParams P) {
     const uint32_t n = P.npix;
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
     const Ctx c{P.profiles, P.nProfiles, P.flags};
@@ -1099,7 +1211,7 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
     const bool doNee = (P.opt & plt::kPtDoNee) != 0, doMis = (P.opt & plt::kPtDoMis) != 0;
     const bool useEmissive = (P.opt & plt::kPtUseEmissive) != 0;
     const bool importance = (P.opt & plt::kPtImportanceEmit) != 0;
-    const bool doMnee = (P.opt & plt::kPtDoMnee) != 0;
+    const bool doMnee = MNEE && (P.opt & plt::kPtDoMnee) != 0;
     TraceCounters tc{0u, 0u, 0u, 0u};
     uint32_t evals = 0;
     MSData ms;
@@ -1205,7 +1317,29 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
                                 continue;
                         }
                         msOrigin = !curMS ? V.posW : pathOrigin;
-                        if (!manifoldNEESample(P, lorg, ldir, ldist, msOrigin, tposW, lightDir, maxMS, sg, ms, tc) || ms.pdf < 1e-6f) continue;
+                        const int occ = manifoldOccluders(P, lorg, ldir, ldist, maxMS, sg, ms, tc);
+                        if (occ == kMsFail || ms.pdf < 1e-6f) continue;
+                        if (occ == kMsWalk) {
+                            // the walk and the rest of this sample draw no random numbers: hand them
+                            // to the walk wavefront (inline when its queue is full)
+                            const uint32_t slot = P.mneeTasks ? warpAggregatedAdd(P.mneeCount, true) : 0xFFFFFFFFu;
+                            if (slot < P.mneeCap) {
+                                MneeTask<H>* t = reinterpret_cast<MneeTask<H>*>(P.mneeTasks) + slot;
+                                t->ms = ms;
+                                t->tposW = tposW;
+                                t->ldir = ldir;
+                                t->msOrigin = msOrigin;
+                                t->ldist = ldist;
+                                t->tpdf = tpdf;
+#pragma unroll
+                                for (int j = 0; j < H; ++j) { t->Le[j] = Le[j]; t->swl[j] = swl[j]; }
+                                t->pid = pid;
+                                t->p = (uint32_t)p;
+                                t->curMS = curMS ? 1u : 0u;
+                                continue;
+                            }
+                            if (!manifoldWalk(P, msOrigin, tposW, ms, tc)) continue;
+                        }
                         float misBsdfPdf = 0.f;
                         f3 lsDir = ldir;
                         if (ms.hitCount > 0) {
@@ -1245,85 +1379,7 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
                     sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
                 }
-                // forward replay: the manifold vertices (last to first, manifoldForwardUnwind,
-                // pltpt_solve.rt.slang:80-93), the current vertex (NEE, non-delta lobes), then p-1 .. 0
-                const int total = nMs + (evalCurrent ? 1 : 0) + p;
-                for (int k = 0; k < total; ++k) {
-                    uint32_t qprim, qlobe;
-                    float qb1, qb2;
-                    f3 qwo;
-                    bool msVertex = false;
-                    f3 msPos;
-                    if (k < nMs) {
-                        const int idx = nMs - 1 - k;
-                        const MSHit& h = ms.hits[idx];
-                        qprim = h.prim; qlobe = h.lobe; qb1 = h.b1; qb2 = h.b2;
-                        msPos = h.posW;
-                        msVertex = true;
-                        const f3 p2 = idx == 0 ? msOrigin : ms.hits[idx - 1].posW;
-                        qwo = normalize(p2 - h.posW);
-                    } else if (evalCurrent && k == nMs) {
-                        qprim = bounce.prim; qlobe = kLobeNonDelta; qb1 = bounce.b1; qb2 = bounce.b2; qwo = bounce.wi;
-                    } else {
-                        const int q = p - 1 - (k - nMs - (evalCurrent ? 1 : 0));
-                        const Bnc<H> bq = readBounce<H>(P, pid, q);
-                        qprim = bq.prim; qlobe = bq.lobe; qb1 = bq.b1; qb2 = bq.b2; qwo = bq.wi;
-                    }
-                    VData qv = vertexData(P, qprim, qb1, qb2);
-                    if (msVertex) qv.posW = msPos;
-                    const uint32_t qmid = __ldg(P.triMat + qprim);
-                    const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
-                    propagate(pb, qsd.posW);
-                    const DevMaterial* __restrict__ qm = P.mats + qmid;
-                    const uint32_t qtype = __ldg(&qm->type);
-                    ptEval<H>(qm, qtype, c, qsd, qwo, qlobe, pb.b);
-                    ++evals;
-                    if (hwssMis) {
-                        float lp[H];
-                        ptLambdaPdf<H>(qm, qtype, qsd, qwo, qlobe, pb.b, lp);
-#pragma unroll
-                        for (int j = 0; j < H; ++j) pb.spdf[j] *= lp[j];
-                    }
-                }
-                // measure (no camera polarizer unless set)
-                if (!(P.opt & plt::kPtUseDirect) && p <= 1) continue;
-                propagate(pb, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
-                if (P.cam.polarizer > 0.f) {
-                    const f3 Wc = rnormalize(mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]));
-                    const f3 Uc = rnormalize(mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]));
-                    pb.b.rotateFrame(Uc, -Wc);
-                    const float pi = P.cam.polarizer;
-                    float sth, cth;
-                    sincosf(P.cam.polarizer_theta, &sth, &cth);
-                    const float Pm[4][4] = {{.5f, .5f * cth, .5f * sth, 0.f}, {.5f * cth, .5f * (cth * cth), .5f * (cth * sth), 0.f},
-                                            {.5f * sth, .5f * (cth * sth), .5f * (sth * sth), 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-                    for (int j = 0; j < H; ++j) {
-                        const float in[4] = {pb.b.L[0][j], pb.b.L[1][j], pb.b.L[2][j], pb.b.L[3][j]};
-#pragma unroll
-                        for (int r = 0; r < 4; ++r) {
-                            float acc = 0.f;
-#pragma unroll
-                            for (int cc = 0; cc < 4; ++cc) acc += ((1.f - pi) * (r == cc ? 1.f : 0.f) + pi * Pm[r][cc]) * in[cc];
-                            pb.b.L[r][j] = acc;
-                        }
-                    }
-                }
-                float contrib = bounce.contrib;
-                if (hwssMis) {
-                    float sum = 0.f;
-#pragma unroll
-                    for (int j = 0; j < H; ++j) sum += pb.spdf[j];
-                    contrib *= sum > kFltEps ? pb.spdf[0] / sum : 0.f;
-                } else {
-                    contrib *= 1.f / float(pb.comps);
-                }
-                float Li[H];
-#pragma unroll
-                for (int j = 0; j < H; ++j) Li[j] = pb.b.L[0][j];
-                const f3 rgb = spectrumToRgb<H>(Li, pb.b.wl, pb.comps);
-                const float r = fmaxf(0.f, rgb.x * contrib), g = fmaxf(0.f, rgb.y * contrib), bb = fmaxf(0.f, rgb.z * contrib);
-                if (isfinite(r) && isfinite(g) && isfinite(bb)) { Lr += r; Lg += g; Lb += bb; }
+                replayMeasure<H>(P, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
             }
             if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
             pathOrigin = V.posW;
@@ -1344,18 +1400,102 @@ __global__ void __launch_bounds__(128) ptSolveKernel(const PtParams P) {
     }
 }
 
+
+// The manifold-walk wavefront: one thread per deferred NEE sample (ptSolveKernel's MneeTask), dense
+// in the walking lanes that the solve kernel's warps would otherwise run one or two at a time.
+// Finishes the sample exactly as the solve kernel would (pltpt_solve.rt.slang:293-366: the walk,
+// the beam's new direction, 1 / pdf, the MIS weight, the manifold replay and the measurement) and
+// adds it to the pixel's accumulator.
+template <int H>
+__global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
+    static_assert(sizeof(MneeTask<H>) <= plt::kMneeTaskBytes, "MneeTask stride");
+    const uint32_t count = min(*((volatile uint32_t*)P.mneeCount), P.mneeCap);
+    const Ctx c{P.profiles, P.nProfiles, P.flags};
+    const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
+    const bool doMis = (P.opt & plt::kPtDoMis) != 0;
+    TraceCounters tc{0u, 0u, 0u, 0u};
+    uint32_t evals = 0;
+    const MneeTask<H>* tasks = reinterpret_cast<const MneeTask<H>*>(P.mneeTasks);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const MneeTask<H>& t = tasks[i];
+        MSData ms = t.ms;
+        const uint32_t pid = t.pid;
+        const int p = (int)t.p;
+        const bool curMS = t.curMS != 0;
+        const f3 msOrigin = t.msOrigin;
+        if (!manifoldWalk(P, msOrigin, t.tposW, ms, tc)) continue;
+        const Bnc<H> bounce = readBounce<H>(P, pid, p);
+        const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
+        const uint32_t mid = __ldg(P.triMat + bounce.prim);
+        const SD sd = prepareSD(V, __ldg(P.matProps + mid).x, bounce.wi);
+        const DevMaterial* __restrict__ m = P.mats + mid;
+        const uint32_t type = __ldg(&m->type);
+        float Le[H], swl[H];
+#pragma unroll
+        for (int j = 0; j < H; ++j) { Le[j] = t.Le[j]; swl[j] = t.swl[j]; }
+        PBeam<H> pb;
+        sourceBeamArea<H>(pb, t.tposW, -t.ldir, P.sourcingArea, t.ldist, Le, swl, P.maxBeamOmega);
+        if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
+        bool evalCurrent = true;
+        float misBsdfPdf = 0.f;
+        if (!hwssMis && ms.dispersive) pb.comps = 1;
+        const f3 lsDir = ms.woLastHitToLight;
+        pb.b.r = -ms.woLastHitToLight;
+        pb.b.t = perp_stark(pb.b.r);
+        scaleBeam(pb, 1.f / ms.pdf);
+        const int nMs = ms.hitCount;
+        if (curMS) {
+            evalCurrent = false;
+            misBsdfPdf = bounce.lndp;
+        }
+        if (doMis) {
+            if (!curMS) misBsdfPdf = ptPdf(m, type, sd, lsDir, pb.b.wl[0]);
+            scaleBeam(pb, misWeight(t.tpdf, misBsdfPdf * ms.pdf));
+        }
+        float Lr = 0.f, Lg = 0.f, Lb = 0.f;
+        replayMeasure<H>(P, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
+        if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
+            atomicAdd(P.accum + 3 * (size_t)pid, (double)Lr);
+            atomicAdd(P.accum + 3 * (size_t)pid + 1, (double)Lg);
+            atomicAdd(P.accum + 3 * (size_t)pid + 2, (double)Lb);
+        }
+    }
+    if (tc.overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    unsigned long long s1 = tc.shadowRays, s2 = evals;
+    for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_down_sync(0xFFFFFFFFu, s1, o);
+        s2 += __shfl_down_sync(0xFFFFFFFFu, s2, o);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        if (s1) atomicAdd(P.stats + 1, s1);
+        if (s2) atomicAdd(P.stats + 2, s2);
+    }
+}
+
 template <int H>
 cudaError_t launchSolve(const PtParams& p, int numSMs, cudaStream_t stream) {
-    static int bps = -1;
-    if (bps < 0) {
+    static int bps[2] = {-1, -1};
+    const bool mnee = (p.opt & plt::kPtDoMnee) != 0;
+    if (bps[mnee] < 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptSolveKernel<H>, 128, 0);
-        bps = b > 0 ? b : 1;
+        if (mnee) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptSolveKernel<H, true>, 128, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptSolveKernel<H, false>, 128, 0);
+        bps[mnee] = b > 0 ? b : 1;
     }
-    uint32_t grid = (uint32_t)(numSMs * bps);
+    uint32_t grid = (uint32_t)(numSMs * bps[mnee]);
     const uint32_t need = (p.npix + 127) / 128;
     if (grid > need) grid = need;
-    ptSolveKernel<H><<<grid, 128, 0, stream>>>(p);
+    if (mnee) ptSolveKernel<H, true><<<grid, 128, 0, stream>>>(p);
+    else ptSolveKernel<H, false><<<grid, 128, 0, stream>>>(p);
+    if (mnee && p.mneeTasks) {
+        static int bpsW = -1;
+        if (bpsW < 0) {
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptMneeKernel<H>, 128, 0);
+            bpsW = b > 0 ? b : 1;
+        }
+        ptMneeKernel<H><<<(uint32_t)(numSMs * bpsW), 128, 0, stream>>>(p);
+    }
     return cudaGetLastError();
 }
 

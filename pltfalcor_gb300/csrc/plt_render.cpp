@@ -199,7 +199,7 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     ctx->ptBytes = 0;
     const size_t n = npix, nb = (size_t)maxB + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al((nb + 1) * 4);
+    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al((nb + 2) * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t accumBytes = al(3 * n * 8);
     const size_t total = pathBytes + bounceBytes + accumBytes;
@@ -220,7 +220,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.plen = (uint32_t*)take(n * 4);
     P.queue0 = (uint32_t*)take(n * 4);
     P.queue1 = (uint32_t*)take(n * 4);
-    P.qcount = (uint32_t*)take((nb + 1) * 4);
+    P.qcount = (uint32_t*)take((nb + 2) * 4);   // per-segment queue lengths + the manifold-walk task count
+    P.mneeCount = P.qcount + nb + 1;
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
     P.bPrim = (uint32_t*)take(nb * n * 4);
@@ -291,7 +292,7 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 
 void pltReleaseRenderState(plt_context* ctx) {
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -387,6 +388,22 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     P.matFeat = ctx->dMatFeat;
     P.propProb = o.learned_proposal_prob;
     P.wpss = learned ? static_cast<float*>(ctx->dPtMix) : nullptr;
+    // deferred manifold walks: one task slot per path and frame (a fuller queue walks inline)
+    if (nee && o.do_mnee) {
+        const size_t taskBytes = (size_t)npix * plt::kMneeTaskBytes;
+        if (ctx->mneeBytes < taskBytes) {
+            cudaFree(ctx->dMneeTasks);
+            ctx->dMneeTasks = nullptr;
+            ctx->mneeBytes = 0;
+            PLT_CUDA(ctx, cudaMalloc(&ctx->dMneeTasks, taskBytes));
+            ctx->mneeBytes = taskBytes;
+        }
+        P.mneeTasks = ctx->dMneeTasks;
+        P.mneeCap = npix;
+    } else {
+        P.mneeTasks = nullptr;
+        P.mneeCap = 0;
+    }
     P.mneeMaxOccluders = o.mnee_max_occluders;
     P.mneeMaxIterations = o.mnee_max_iterations;
     P.mneeThreshold = o.mnee_solver_threshold;
