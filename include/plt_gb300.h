@@ -306,6 +306,44 @@ typedef struct plt_camera {
 plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width, uint32_t height, uint32_t frame_begin,
                       uint32_t frame_count, float* out_rgba, void* stream);
 
+/* Scene sets (no counterpart in the reference, whose PLTPT renders the one loaded scene): several
+ * independent scenes held by one context share its materials and spectral profiles, and
+ * plt_render_scenes renders any number of views of them in one wavefront per frame (all scenes'
+ * paths in the same segment, solve and manifold-walk launches; each path traverses its own scene's
+ * BVH and samples its own scene's lights).  plt_set_scene replaces the set with one scene;
+ * plt_add_scene appends a scene with its shading attributes (same meaning as plt_set_scene +
+ * plt_set_scene_shading; host arrays, copied) and returns its index; plt_clear_scenes empties the
+ * set.  plt_set_scene_shading applies to the most recently set or added scene.  The trace entry
+ * points and plt_render use scene 0. */
+#define PLT_MAX_SCENES 4096u
+typedef struct plt_scene_desc {
+    const float* positions;             /* [n_vertices][3] */
+    uint32_t n_vertices;
+    const uint32_t* indices;            /* [n_triangles][3] */
+    uint32_t n_triangles;
+    const uint32_t* tri_material;       /* [n_triangles] or NULL (material 0) */
+    const float* normals;               /* [n_vertices][3] */
+    const float* tangents;              /* [n_vertices][4] or NULL */
+    const uint32_t* tri_instance;       /* [n_triangles] or NULL */
+} plt_scene_desc;
+plt_status plt_add_scene(plt_context* ctx, const plt_scene_desc* desc, uint32_t* out_scene);
+plt_status plt_clear_scenes(plt_context* ctx);
+
+/* One view of a scene-set render: the scene index, camera, image size and the device output image
+ * [height][width][4] (16-byte aligned). */
+typedef struct plt_render_view {
+    uint32_t scene;
+    uint32_t width, height;
+    uint32_t pad;
+    plt_camera camera;
+    float* out_rgba;
+} plt_render_view;
+/* Renders frame_count frames of every view (the same frame indices for all views; each view's
+ * pixels seed the generator exactly as a plt_render of that view alone, so the results equal
+ * n separate plt_render calls).  At most 2^26 pixels over all views. */
+plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame_begin, uint32_t frame_count,
+                             void* stream);
+
 /* Path statistics of the last plt_render frame (host pointer, 4 values: paths, bounces recorded,
  * shadow rays traced, forward-unwind BSDF evaluations). */
 plt_status plt_render_stats(plt_context* ctx, uint64_t* out4);

@@ -202,6 +202,34 @@ class PLTContext:
         capi.check(self.lib.plt_render(self.handle, C.byref(camera), width, height, frame_begin, frame_count, _ptr(out_rgba), s),
                    "plt_render")
 
+    # ---- scene sets ----
+    def add_scene(self, scene, material_offset=0):
+        """Appends a scene.Scene (geometry + shading) to the context's scene set; its tri_material
+        indices are shifted by material_offset into the context's material table.  Returns the index."""
+        keep = [np.ascontiguousarray(scene.vertices, np.float32), np.ascontiguousarray(scene.indices, np.uint32),
+                np.ascontiguousarray(scene.tri_material + np.uint32(material_offset), np.uint32),
+                np.ascontiguousarray(scene.normals, np.float32)]
+        tan = None if scene.tangents is None else np.ascontiguousarray(scene.tangents, np.float32)
+        inst = None if getattr(scene, "tri_instance", None) is None else np.ascontiguousarray(scene.tri_instance, np.uint32)
+        d = capi.SceneDesc(keep[0].ctypes.data, len(keep[0]), keep[1].ctypes.data, len(keep[1]), keep[2].ctypes.data,
+                           keep[3].ctypes.data, None if tan is None else tan.ctypes.data, None if inst is None else inst.ctypes.data)
+        out = C.c_uint32(0)
+        capi.check(self.lib.plt_add_scene(self.handle, C.byref(d), C.byref(out)), "plt_add_scene")
+        return out.value
+
+    def clear_scenes(self):
+        capi.check(self.lib.plt_clear_scenes(self.handle), "plt_clear_scenes")
+
+    def render_scenes(self, views, frame_begin=0, frame_count=1, stream=None):
+        """plt_render_scenes: views is a list of (scene index, camera, width, height, out tensor [h][w][4])."""
+        arr = (capi.RenderView * len(views))()
+        for i, (sid, cam, w, h, out) in enumerate(views):
+            arr[i].scene, arr[i].width, arr[i].height = sid, w, h
+            arr[i].camera = cam
+            arr[i].out_rgba = _ptr(out)
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_render_scenes(self.handle, arr, len(views), frame_begin, frame_count, s), "plt_render_scenes")
+
     def render_bounces(self, npix, max_bounces):
         """Bounce records of the last frame: (prim, lobe, flags), each [npix][max_bounces+1] uint32."""
         out = [np.zeros((npix, max_bounces + 1), np.uint32) for _ in range(3)]

@@ -76,7 +76,18 @@ class Camera(C.Structure):
                 ("jitter_x", C.c_float), ("jitter_y", C.c_float), ("polarizer", C.c_float), ("polarizer_theta", C.c_float)]
 
 
+class SceneDesc(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("n_vertices", C.c_uint32), ("indices", C.c_void_p), ("n_triangles", C.c_uint32),
+                ("tri_material", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("tri_instance", C.c_void_p)]
+
+
+class RenderView(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("pad", C.c_uint32),
+                ("camera", Camera), ("out_rgba", C.c_void_p)]
+
+
 MATERIAL_FLAG_DOUBLE_SIDED = 0x1
+MAX_SCENES = 4096
 
 assert C.sizeof(SpectralProfile) == 1052
 assert C.sizeof(MaterialRecord) == 80
@@ -90,6 +101,7 @@ EXPORTED_SYMBOLS = [
     "plt_set_timing_events", "plt_set_scene_shading", "plt_render", "plt_render_stats", "plt_render_bounces",
     "plt_proposal_init", "plt_proposal_set_params", "plt_proposal_get_params", "plt_proposal_generate",
     "plt_proposal_gradient", "plt_proposal_forward", "plt_proposal_adam_step", "plt_proposal_train",
+    "plt_add_scene", "plt_clear_scenes", "plt_render_scenes",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -143,6 +155,9 @@ def load_library(path=LIB_PATH):
         "plt_proposal_forward": (i32, [vp, u32, vp, vp, vp]),
         "plt_proposal_adam_step": (i32, [vp, vp, C.c_float, vp]),
         "plt_proposal_train": (i32, [vp, u32, u32, C.c_float, u32, C.POINTER(C.c_float), vp]),
+        "plt_add_scene": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(C.c_uint32)]),
+        "plt_clear_scenes": (i32, [vp]),
+        "plt_render_scenes": (i32, [vp, C.POINTER(RenderView), u32, u32, u32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -149,7 +149,7 @@ plt_status plt_set_spectral_profiles(plt_context* ctx, const plt_spectral_profil
     }
     ctx->hProfiles.assign(profiles, profiles + count);
     ctx->nProfiles = count;
-    ctx->shadingReady = false;
+    ctx->shadingDirty = true;   // lights depend on materials and profiles
     return PLT_OK;
 }
 
@@ -209,7 +209,7 @@ plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, 
     ctx->hMats.assign(mats, mats + count);
     ctx->hDevMats = h;
     ctx->nMats = count;
-    ctx->shadingReady = false;
+    ctx->shadingDirty = true;   // lights depend on materials and profiles
     return PLT_OK;
 }
 
@@ -309,80 +309,12 @@ plt_status plt_bsdf_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsd
 plt_status plt_bsdf_sample(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_SAMPLE, s); }
 plt_status plt_bsdf_lambda_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_LAMBDA_PDF, s); }
 
-plt_status plt_set_scene(plt_context* ctx, const float* vertices, uint32_t nVerts, const uint32_t* indices, uint32_t nTris,
-                         const uint32_t* material) {
-    if (!ctx || (nTris > 0 && (!vertices || !indices))) return PLT_INVALID_ARG;
-    if (nTris >= (1u << 27)) return PLT_NOT_SUPPORTED;  // leaf encoding holds 27-bit triangle offsets
-    std::vector<float> tv((size_t)nTris * 9);
-    for (uint32_t t = 0; t < nTris; ++t)
-        for (int k = 0; k < 3; ++k) {
-            const uint32_t vi = indices[3 * (size_t)t + k];
-            if (vi >= nVerts) return PLT_INVALID_ARG;
-            for (int a = 0; a < 3; ++a) {
-                const float x = vertices[3 * (size_t)vi + a];
-                if (!std::isfinite(x)) return PLT_NAN_INPUT;
-                tv[9 * (size_t)t + 3 * k + a] = x;
-            }
-        }
-    std::vector<plt::BvhNode> nodes;
-    std::vector<uint32_t> order;
-    plt::BvhBuildStats st;
-    plt::buildBvh(tv.data(), nTris, nodes, order, &st);
-    std::vector<float4> tris((size_t)nTris * 3);
-    for (uint32_t s = 0; s < nTris; ++s) {
-        const uint32_t t = order[s];
-        const float* p = &tv[9 * (size_t)t];
-        float idBits;
-        std::memcpy(&idBits, &t, 4);
-        tris[3 * s] = make_float4(p[0], p[1], p[2], idBits);
-        tris[3 * s + 1] = make_float4(p[3], p[4], p[5], 0.f);
-        tris[3 * s + 2] = make_float4(p[6], p[7], p[8], 0.f);
-    }
-    cudaFree(ctx->dNodes);
-    cudaFree(ctx->dTris);
-    cudaFree(ctx->dTriMaterial);
-    ctx->dNodes = nullptr;
-    ctx->dTris = nullptr;
-    ctx->dTriMaterial = nullptr;
-    ctx->nTris = 0;
-    PLT_CUDA(ctx, cudaMalloc(&ctx->dNodes, sizeof(plt::BvhNode) * nodes.size()));
-    PLT_CUDA(ctx, cudaMemcpy(ctx->dNodes, nodes.data(), sizeof(plt::BvhNode) * nodes.size(), cudaMemcpyHostToDevice));
-    if (nTris) {
-        PLT_CUDA(ctx, cudaMalloc(&ctx->dTris, sizeof(float4) * tris.size()));
-        PLT_CUDA(ctx, cudaMemcpy(ctx->dTris, tris.data(), sizeof(float4) * tris.size(), cudaMemcpyHostToDevice));
-        std::vector<uint32_t> mat(nTris, 0u);
-        if (material) std::memcpy(mat.data(), material, sizeof(uint32_t) * nTris);
-        PLT_CUDA(ctx, cudaMalloc(&ctx->dTriMaterial, sizeof(uint32_t) * nTris));
-        PLT_CUDA(ctx, cudaMemcpy(ctx->dTriMaterial, mat.data(), sizeof(uint32_t) * nTris, cudaMemcpyHostToDevice));
-    }
-    // vertex positions and indices for shading (render pass)
-    cudaFree(ctx->dPos);
-    cudaFree(ctx->dIdx);
-    ctx->dPos = nullptr;
-    ctx->dIdx = nullptr;
-    if (nTris) {
-        PLT_CUDA(ctx, cudaMalloc(&ctx->dPos, sizeof(float) * 3 * (size_t)nVerts));
-        PLT_CUDA(ctx, cudaMemcpy(ctx->dPos, vertices, sizeof(float) * 3 * (size_t)nVerts, cudaMemcpyHostToDevice));
-        PLT_CUDA(ctx, cudaMalloc(&ctx->dIdx, sizeof(uint32_t) * 3 * (size_t)nTris));
-        PLT_CUDA(ctx, cudaMemcpy(ctx->dIdx, indices, sizeof(uint32_t) * 3 * (size_t)nTris, cudaMemcpyHostToDevice));
-        ctx->hPos.assign(vertices, vertices + 3 * (size_t)nVerts);
-        ctx->hIdx.assign(indices, indices + 3 * (size_t)nTris);
-        ctx->hTriMat.assign(nTris, 0u);
-        if (material) std::memcpy(ctx->hTriMat.data(), material, sizeof(uint32_t) * nTris);
-    } else {
-        ctx->hPos.clear();
-        ctx->hIdx.clear();
-        ctx->hTriMat.clear();
-    }
-    ctx->nVerts = nVerts;
-    ctx->nTris = nTris;
-    ctx->bvhStats = st;
-    ctx->shadingReady = false;
-    return PLT_OK;
-}
-
 static plt_status traceCommon(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, uint32_t* occluded, bool any, void* stream) {
     if (!ctx || !rays) return PLT_INVALID_ARG;
+    if (ctx->geometryDirty) {
+        const plt_status s = pltUploadScenes(ctx);
+        if (s != PLT_OK) return s;
+    }
     if (!ctx->dNodes) return PLT_INVALID_ARG;  // no scene
     if (rays->n == 0) return PLT_OK;
     if (!rays->origin || !rays->dir) return PLT_INVALID_ARG;

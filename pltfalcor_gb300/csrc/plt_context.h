@@ -10,6 +10,24 @@
 #include "plt_host.h"
 #include "plt_internal.h"
 
+// One scene of the context's scene set, kept on the host: its BVH (scene-local node and triangle
+// indices), triangles in leaf order, and its shading attributes.  The device holds all scenes
+// concatenated (pltUploadScenes).
+struct plt_scene_host {
+    std::vector<plt::BvhNode> nodes;
+    std::vector<float4> tris;          // 3 per triangle, leaf order; .w of the first = local triangle id
+    std::vector<float> pos, nrm, tan;  // tan empty: no tangents
+    std::vector<uint32_t> idx, triMat, triInst;
+    uint32_t nVerts = 0, nTris = 0;
+    plt::BvhBuildStats stats{};
+    bool shaded = false;
+};
+// A scene's place in the combined device arrays.
+struct plt_scene_slot {
+    uint32_t root = 0, triBase = 0, lightBase = 0, nLights = 0;
+    float invWeightsSum = 0.f;
+};
+
 struct plt_context {
     int device = 0;
     int numSMs = 0;
@@ -35,9 +53,12 @@ struct plt_context {
     std::vector<plt_spectral_profile> hProfiles;
     std::vector<plt_material_record> hMats;
     std::vector<pltdev::DevMaterial> hDevMats;
-    std::vector<float> hPos;
-    std::vector<uint32_t> hIdx, hTriMat;
-    uint32_t nVerts = 0;
+    std::vector<plt_scene_host> scenes;   // the scene set (plt_set_scene: one scene)
+    std::vector<plt_scene_slot> slots;    // each scene's root, triangle and light ranges on the device
+    bool geometryDirty = false, shadingDirty = false;
+    uint32_t nVerts = 0;                  // vertices of the last scene set (plt_set_scene_shading checks it)
+    plt::PtScene* dScenes = nullptr;      // per-render scene table
+    uint32_t scenesCap = 0;
     float* dProfileIcdf = nullptr;   // [nProfiles][128]
     uint2* dMatProps = nullptr;      // [nMats]
     float* dPos = nullptr;           // [nVerts][3]
@@ -91,3 +112,6 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 float4 pltProposalFeatures(const plt_material_record& r, const pltdev::DevMaterial& d);
 // Frees the learned-proposal state (plt_proposal.cpp).
 void pltReleaseProposal(plt_context* ctx);
+
+// Uploads the scene set if it changed (geometry, shading, light collections); plt_scenes.cpp.
+plt_status pltUploadScenes(plt_context* ctx);

@@ -68,6 +68,18 @@ constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
 
+// One scene of a render: its BVH root in the combined node array, its light range in the combined
+// light arrays (the power sampler's table holds scene-local indices), its camera, image size, the
+// first path of its pixels in the frame's path range, and its output image.
+struct PtScene {
+    plt_camera cam;
+    uint32_t width, height, pixelBase, root;
+    uint32_t lightBase, nLights;
+    float invWeightsSum;
+    uint32_t pad;
+    float* out;                   // [height][width][4]
+};
+
 struct PtParams {
     // scene
     const void* nodes;
@@ -93,15 +105,15 @@ struct PtParams {
     const uint2* alias;           // [nl]
     const uint32_t* primToLight;  // [nt]
     const uint32_t* lightEmission;// [nl] emission profile id
-    uint32_t nLights;
-    float invWeightsSum;
+    // scenes of this render (one for plt_render, several for plt_render_scenes)
+    const PtScene* scenes;
+    uint32_t nScenes;
     // options
     uint32_t maxBounces, tileSize, hwss, opt, flags;
     float sourcingArea, maxBeamOmega;
     uint32_t mneeMaxOccluders, mneeMaxIterations;
     float mneeThreshold;
-    plt_camera cam;
-    uint32_t width, height, npix, frame;
+    uint32_t npix, frame;         // paths of all scenes, frame index
     // path state of the sample pass
     uint32_t* sg;                 // [4][npix]
     float* org;                   // [3][npix]

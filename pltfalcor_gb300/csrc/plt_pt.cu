@@ -55,12 +55,15 @@ cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream
 
 namespace pltdev {
 
-__global__ void ptResolveKernel(const double* __restrict__ accum, uint32_t npix, double inv, float* __restrict__ out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += gridDim.x * blockDim.x) {
-        out[4 * (size_t)i] = (float)(accum[3 * (size_t)i] * inv);
-        out[4 * (size_t)i + 1] = (float)(accum[3 * (size_t)i + 1] * inv);
-        out[4 * (size_t)i + 2] = (float)(accum[3 * (size_t)i + 2] * inv);
-        out[4 * (size_t)i + 3] = 1.f;
+// The mean of the accumulated frames into each view's output image.
+__global__ void ptResolveKernel(const PtParams P, double inv) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npix; i += gridDim.x * blockDim.x) {
+        const PtScene& S = P.scenes[sceneOf(P, i)];
+        float* out = S.out + 4 * (size_t)(i - S.pixelBase);
+        out[0] = (float)(P.accum[3 * (size_t)i] * inv);
+        out[1] = (float)(P.accum[3 * (size_t)i + 1] * inv);
+        out[2] = (float)(P.accum[3 * (size_t)i + 2] * inv);
+        out[3] = 1.f;
     }
 }
 
@@ -68,10 +71,10 @@ __global__ void ptResolveKernel(const double* __restrict__ accum, uint32_t npix,
 
 namespace plt {
 
-cudaError_t launchResolve(const double* accum, uint32_t npix, uint32_t frames, float* out, int numSMs, cudaStream_t stream) {
-    if (npix == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>((npix + 255) / 256, (uint32_t)numSMs * 8u);
-    pltdev::ptResolveKernel<<<grid, 256, 0, stream>>>(accum, npix, 1.0 / (double)frames, out);
+cudaError_t launchResolve(const PtParams& p, uint32_t frames, int numSMs, cudaStream_t stream) {
+    if (p.npix == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>((p.npix + 255) / 256, (uint32_t)numSMs * 8);
+    pltdev::ptResolveKernel<<<grid, 256, 0, stream>>>(p, 1.0 / (double)frames);
     return cudaGetLastError();
 }
 

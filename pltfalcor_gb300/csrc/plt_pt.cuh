@@ -16,6 +16,7 @@
 namespace pltdev {
 
 using plt::PtParams;
+using plt::PtScene;
 
 constexpr uint32_t kNoHit = 0xFFFFFFFFu;
 // RayFlags, Path.slang:46-106
@@ -371,15 +372,27 @@ template <int H> PLT_DI void scaleBeam(PBeam<H>& pb, float s) {
 PLT_DI float misWeight(float p0, float p1) { return p0 / (p0 + p1); }
 
 // ---- sample pass ----------------------------------------------------------------------------
+// The scene of path pid: the last scene whose first path is <= pid (scenes in path order).
+PLT_DI uint32_t sceneOf(const PtParams& P, uint32_t pid) {
+    uint32_t lo = 0, hi = P.nScenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&P.scenes[mid].pixelBase) <= pid) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+PLT_DI f3 camPos(const PtScene& S) { return mk3(S.cam.pos[0], S.cam.pos[1], S.cam.pos[2]); }
+
 // Camera.computeRayPinhole, Scene/Camera/Camera.slang:46-78
-PLT_DI f3 cameraDir(const PtParams& P, uint32_t px, uint32_t py) {
-    float p0 = (float(px) + 0.5f) / float(P.width);
-    float p1 = (float(py) + 0.5f) / float(P.height);
-    p0 += -P.cam.jitter_x;
-    p1 += P.cam.jitter_y;
+PLT_DI f3 cameraDir(const PtScene& S, uint32_t px, uint32_t py) {
+    float p0 = (float(px) + 0.5f) / float(S.width);
+    float p1 = (float(py) + 0.5f) / float(S.height);
+    p0 += -S.cam.jitter_x;
+    p1 += S.cam.jitter_y;
     const float ndcx = 2.f * p0 + -1.f, ndcy = -2.f * p1 + 1.f;
-    const f3 U = mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]), V = mk3(P.cam.v[0], P.cam.v[1], P.cam.v[2]);
-    const f3 W = mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]);
+    const f3 U = mk3(S.cam.u[0], S.cam.u[1], S.cam.u[2]), V = mk3(S.cam.v[0], S.cam.v[1], S.cam.v[2]);
+    const f3 W = mk3(S.cam.w[0], S.cam.w[1], S.cam.w[2]);
     return rnormalize(U * ndcx + V * ndcy + W);
 }
 
@@ -396,14 +409,16 @@ PLT_DI uint32_t warpAggregatedAdd(uint32_t* counter, bool pred) {
 #ifdef PLT_PT_SAMPLE_PASS   // defined by plt_pt.cu only: one copy of the sample-pass kernels
 __global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npix; i += gridDim.x * blockDim.x) {
-        const uint32_t px = i % P.width, py = i / P.width;
+        const PtScene& S = P.scenes[sceneOf(P, i)];
+        const uint32_t local = i - S.pixelBase;
+        const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg;
         sg.init(px, py, P.frame);
         const float wl = 380.0f + sg.next1D() * (720.0f - 380.0f);   // SpectrumSampler.sampleOne
-        const f3 d = cameraDir(P, px, py);
+        const f3 d = cameraDir(S, px, py);
         const uint32_t n = P.npix;
         P.sg[i] = sg.s0; P.sg[n + i] = sg.s1; P.sg[2 * n + i] = sg.s2; P.sg[3 * n + i] = sg.s3;
-        stPlane3(P.org, i, n, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
+        stPlane3(P.org, i, n, camPos(S));
         stPlane3(P.dir, i, n, d);
         P.wl[i] = wl;
         P.weight[i] = 1.f;
@@ -494,7 +509,8 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
             wavelength = P.wl[pid];
             if constexpr (LEARNED) wps = P.wpss[pid];
             for (int guard = 0; guard < 64; ++guard) {
-                h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
+                h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
+                                    __ldg(&P.scenes[sceneOf(P, pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
@@ -671,7 +687,8 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
                 ++recorded;
             };
             for (int guard = 0; guard < 64; ++guard) {
-                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow);
+                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
+                                                      __ldg(&P.scenes[sceneOf(P, pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
@@ -952,9 +969,10 @@ struct TraceCounters {
     uint32_t nv, tt, overflow, shadowRays;
 };
 // closest-hit shadow ray (ShadowRays.slangh:96-135): a hit needs dist > 0
-PLT_DI bool shadowRayClosest(const PtParams& P, f3 o, f3 d, float tmin, float tmax, TraceResult& h, TraceCounters& tc) {
+PLT_DI bool shadowRayClosest(const PtParams& P, int32_t root, f3 o, f3 d, float tmin, float tmax, TraceResult& h, TraceCounters& tc) {
     ++tc.shadowRays;
-    h = traverse<false>(reinterpret_cast<const float4*>(P.nodes), P.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, tc.nv, tc.tt, tc.overflow);
+    h = traverse<false>(reinterpret_cast<const float4*>(P.nodes), P.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, tc.nv, tc.tt, tc.overflow,
+                        root);
     return h.prim != kNoHit && h.t > 0.f;
 }
 // manifoldSampleVertex, Manifolds.slangh:84-108
@@ -981,12 +999,13 @@ PLT_DI bool manifoldSampleVertex(const PtParams& P, uint32_t prim, float b1, flo
 // kMsFail (no contribution), kMsVisible (no occluder: the light is visible) or kMsWalk (occluders
 // recorded in d; manifoldWalk completes the sample).
 constexpr int kMsFail = 0, kMsVisible = 1, kMsWalk = 2;
-PLT_NI int manifoldOccluders(const PtParams& P, f3 rayO, f3 rayD, float tmax, int maxMS, SampleGen& sg, MSData& d, TraceCounters& tc) {
+PLT_NI int manifoldOccluders(const PtParams& P, int32_t root, f3 rayO, f3 rayD, float tmax, int maxMS, SampleGen& sg, MSData& d,
+                             TraceCounters& tc) {
     const int maxOcc = (int)min(P.mneeMaxOccluders, (uint32_t)kMaxMsOccluders);
     const f3 wi = -rayD;
     for (int guard = 0; guard <= kMaxMsOccluders; ++guard) {
         TraceResult h;
-        if (!shadowRayClosest(P, rayO, rayD, 0.f, tmax, h, tc)) break;
+        if (!shadowRayClosest(P, root, rayO, rayD, 0.f, tmax, h, tc)) break;
         if (d.hitCount >= maxOcc || d.hitCount >= maxMS) return kMsFail;
         VData v = vertexData(P, h.prim, h.b1, h.b2);
         v.posW = rayO + rayD * h.t;
@@ -1004,7 +1023,7 @@ PLT_NI int manifoldOccluders(const PtParams& P, f3 rayO, f3 rayD, float tmax, in
 // manifoldNEESample's walk, Manifolds.slangh:162-281: Newton steps on the spherical-angle
 // constraint of every occluder with re-projection onto the same geometry instance, then the
 // visibility of the light from the last vertex.  Deterministic (no random draws).
-PLT_NI bool manifoldWalk(const PtParams& P, f3 origin, f3 lightPos, MSData& d, TraceCounters& tc) {
+PLT_NI bool manifoldWalk(const PtParams& P, int32_t root, f3 origin, f3 lightPos, MSData& d, TraceCounters& tc) {
     float beta[kMaxMsOccluders];
 #pragma unroll
     for (int i = 0; i < kMaxMsOccluders; ++i) beta[i] = 1.f;
@@ -1037,7 +1056,7 @@ PLT_NI bool manifoldWalk(const PtParams& P, f3 origin, f3 lightPos, MSData& d, T
                 const float dist = sqrtf(dot(dirTo, dirTo));
                 dirTo = dirTo / dist;
                 TraceResult hp;
-                const bool hit = shadowRayClosest(P, p0, dirTo, fmaxf(1e-4f, .99f * dist), 1.01f * dist, hp, tc);
+                const bool hit = shadowRayClosest(P, root, p0, dirTo, fmaxf(1e-4f, .99f * dist), 1.01f * dist, hp, tc);
                 if (!hit || __ldg(P.triInst + h.prim) != __ldg(P.triInst + hp.prim)) {
                     beta[idx] /= 4.f;
                     continue;
@@ -1057,7 +1076,7 @@ PLT_NI bool manifoldWalk(const PtParams& P, f3 origin, f3 lightPos, MSData& d, T
     dir = dir / dist;
     ++tc.shadowRays;
     const TraceResult vis = traverse<true>(reinterpret_cast<const float4*>(P.nodes), P.tris, pl.x, pl.y, pl.z, dir.x, dir.y, dir.z, 1e-4f,
-                                           dist, tc.nv, tc.tt, tc.overflow);
+                                           dist, tc.nv, tc.tt, tc.overflow, root);
     d.woLastHitToLight = dir;
     return vis.prim == kNoHit;
 }
@@ -1099,8 +1118,9 @@ template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p
 // non-delta lobes), then vertices p-1 .. 0, the camera polariser and spectrumToRgb.  Adds the
 // path's contribution to (Lr, Lg, Lb).
 template <int H>
-PLT_DI void replayMeasure(const PtParams& P, uint32_t pid, int p, const Bnc<H>& bounce, PBeam<H>& pb, const MSData& ms, int nMs, f3 msOrigin,
-                          bool evalCurrent, const Ctx& c, bool hwssMis, float& Lr, float& Lg, float& Lb, uint32_t& evals) {
+PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int p, const Bnc<H>& bounce, PBeam<H>& pb, const MSData& ms,
+                          int nMs, f3 msOrigin, bool evalCurrent, const Ctx& c, bool hwssMis, float& Lr, float& Lg, float& Lb,
+                          uint32_t& evals) {
     // forward replay: the manifold vertices (last to first, manifoldForwardUnwind,
     // pltpt_solve.rt.slang:80-93), the current vertex (NEE, non-delta lobes), then p-1 .. 0
     const int total = nMs + (evalCurrent ? 1 : 0) + p;
@@ -1143,14 +1163,14 @@ PLT_DI void replayMeasure(const PtParams& P, uint32_t pid, int p, const Bnc<H>& 
     }
     // measure (no camera polarizer unless set)
     if (!(P.opt & plt::kPtUseDirect) && p <= 1) return;
-    propagate(pb, mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]));
-    if (P.cam.polarizer > 0.f) {
-        const f3 Wc = rnormalize(mk3(P.cam.w[0], P.cam.w[1], P.cam.w[2]));
-        const f3 Uc = rnormalize(mk3(P.cam.u[0], P.cam.u[1], P.cam.u[2]));
+    propagate(pb, camPos(S));
+    if (S.cam.polarizer > 0.f) {
+        const f3 Wc = rnormalize(mk3(S.cam.w[0], S.cam.w[1], S.cam.w[2]));
+        const f3 Uc = rnormalize(mk3(S.cam.u[0], S.cam.u[1], S.cam.u[2]));
         pb.b.rotateFrame(Uc, -Wc);
-        const float pi = P.cam.polarizer;
+        const float pi = S.cam.polarizer;
         float sth, cth;
-        sincosf(P.cam.polarizer_theta, &sth, &cth);
+        sincosf(S.cam.polarizer_theta, &sth, &cth);
         const float Pm[4][4] = {{.5f, .5f * cth, .5f * sth, 0.f}, {.5f * cth, .5f * (cth * cth), .5f * (cth * sth), 0.f},
                                 {.5f * sth, .5f * (cth * sth), .5f * (sth * sth), 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
@@ -1184,9 +1204,9 @@ PLT_DI void replayMeasure(const PtParams& P, uint32_t pid, int p, const Bnc<H>& 
 
 // evalTrianglePdf x triangle-selection pdf (EmissiveLightSamplerHelpers.slang:120-151,
 // EmissivePowerSampler.slang:81-122)
-PLT_DI float emissivePdf(const PtParams& P, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
+PLT_DI float emissivePdf(const PtParams& P, const PtScene& S, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
     if (light == kNoHit) return 0.f;
-    const float sel = __ldg(P.lightFlux + light) * P.invWeightsSum;
+    const float sel = __ldg(P.lightFlux + light) * S.invWeightsSum;
     const f3 toLight = hitPos - posW;
     const float distSqr = dot(toLight, toLight);
     if (distSqr <= kFltMin) return 0.f;
@@ -1216,12 +1236,15 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     uint32_t evals = 0;
     MSData ms;
     for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x) {
-        const uint32_t px = pid % P.width, py = pid / P.width;
+        const PtScene& S = P.scenes[sceneOf(P, pid)];
+        const int32_t root = (int32_t)S.root;
+        const uint32_t local = pid - S.pixelBase;
+        const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg, tilesg;
         sg.init(px, py, P.frame);
         tilesg.init(px / P.tileSize, py / P.tileSize, P.frame << 2);
         const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
-        f3 pathOrigin = mk3(P.cam.pos[0], P.cam.pos[1], P.cam.pos[2]);
+        f3 pathOrigin = camPos(S);
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
         for (int p = 0; p <= (int)P.maxBounces; ++p) {
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
@@ -1253,15 +1276,15 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     // generateLightSample: selectLightType (one draw), emissive power sampler
                     SampleGen& selSg = (P.opt & plt::kPtPerTileSg) ? tilesg : sg;
                     const float uType = selSg.next1D();
-                    if (!useEmissive || !(uType < 1.f) || P.nLights == 0) continue;
+                    if (!useEmissive || !(uType < 1.f) || S.nLights == 0) continue;
                     const float uLight = sg.next1D();
-                    uint32_t ti = min((uint32_t)(uLight * (float)P.nLights), P.nLights - 1);
-                    const uint2 a = __ldg(P.alias + ti);
+                    uint32_t ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
+                    const uint2 a = __ldg(P.alias + S.lightBase + ti);
                     const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
                     const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
                     const uint32_t selectBelow = a.y & 0xFFFFFFu;
-                    ti = (sg.next1D() >= threshold) ? selectAbove : selectBelow;
-                    const float triSelPdf = __ldg(P.lightFlux + ti) * P.invWeightsSum;
+                    ti = S.lightBase + ((sg.next1D() >= threshold) ? selectAbove : selectBelow);
+                    const float triSelPdf = __ldg(P.lightFlux + ti) * S.invWeightsSum;
                     const float u0 = sg.next1D(), u1 = sg.next1D();
                     const float su = sqrtf(u0);
                     const float bx = 1.f - su, by = u1 * su;
@@ -1298,7 +1321,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     if (!doMnee || maxMS <= 0) {
                         ++tc.shadowRays;
                         const TraceResult vis =
-                            traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, tc.nv, tc.tt, tc.overflow);
+                            traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, tc.nv, tc.tt, tc.overflow, root);
                         if (vis.prim != kNoHit) continue;
                         if (doMis) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
                     } else {
@@ -1317,7 +1340,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 continue;
                         }
                         msOrigin = !curMS ? V.posW : pathOrigin;
-                        const int occ = manifoldOccluders(P, lorg, ldir, ldist, maxMS, sg, ms, tc);
+                        const int occ = manifoldOccluders(P, root, lorg, ldir, ldist, maxMS, sg, ms, tc);
                         if (occ == kMsFail || ms.pdf < 1e-6f) continue;
                         if (occ == kMsWalk) {
                             // the walk and the rest of this sample draw no random numbers: hand them
@@ -1338,7 +1361,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 t->curMS = curMS ? 1u : 0u;
                                 continue;
                             }
-                            if (!manifoldWalk(P, msOrigin, tposW, ms, tc)) continue;
+                            if (!manifoldWalk(P, root, msOrigin, tposW, ms, tc)) continue;
                         }
                         float misBsdfPdf = 0.f;
                         f3 lsDir = ldir;
@@ -1364,7 +1387,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     const bool needMIS = doMis && didNEE;
                     const uint32_t light = __ldg(P.primToLight + bounce.prim);
                     const f3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
-                    const float lightPdf = emissivePdf(P, pathOrigin, light, sd.posW, hn);
+                    const float lightPdf = emissivePdf(P, S, pathOrigin, light, sd.posW, hn);
                     const float mw = needMIS ? misWeight(bounce.lndp, lightPdf) : 1.f;
                     float Le[H], swl[H];
                     sampleSpectrum<H>(P, props.y, wavelength, sg, importance, Le, swl);
@@ -1379,7 +1402,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
                 }
-                replayMeasure<H>(P, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
+                replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
             }
             if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
             pathOrigin = V.posW;
@@ -1423,7 +1446,8 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         const int p = (int)t.p;
         const bool curMS = t.curMS != 0;
         const f3 msOrigin = t.msOrigin;
-        if (!manifoldWalk(P, msOrigin, t.tposW, ms, tc)) continue;
+        const PtScene& S = P.scenes[sceneOf(P, pid)];
+        if (!manifoldWalk(P, (int32_t)S.root, msOrigin, t.tposW, ms, tc)) continue;
         const Bnc<H> bounce = readBounce<H>(P, pid, p);
         const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
         const uint32_t mid = __ldg(P.triMat + bounce.prim);
@@ -1453,7 +1477,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
             scaleBeam(pb, misWeight(t.tpdf, misBsdfPdf * ms.pdf));
         }
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
-        replayMeasure<H>(P, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
+        replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
         if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
             atomicAdd(P.accum + 3 * (size_t)pid, (double)Lr);
             atomicAdd(P.accum + 3 * (size_t)pid + 1, (double)Lg);

@@ -30,167 +30,6 @@ template <class T> plt_status upload(plt_context* ctx, T*& dst, const T* src, si
     return PLT_OK;
 }
 
-struct V3 { float x, y, z; };
-V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-V3 crossv(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-float lengthv(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
-
-// snorm16 octahedral encode -> decode of a unit normal, the storage of the emissive triangles'
-// face normals (encodeNormal2x16 / decodeNormal2x16, Utils/Math/PackedFormats.slang:50-62,
-// FormatConversion.slang:216-258, MathHelpers.slang:147-185)
-void octWrap(float& x, float& y) {
-    const float nx = (1.f - std::fabs(y)) * (x >= 0.f ? 1.f : -1.f);
-    const float ny = (1.f - std::fabs(x)) * (y >= 0.f ? 1.f : -1.f);
-    x = nx;
-    y = ny;
-}
-int32_t toSnorm16(float v) {
-    v = std::isnan(v) ? 0.f : std::fmin(std::fmax(v, -1.f), 1.f);
-    return (int32_t)std::trunc(v * 32767.f + (v >= 0.f ? 0.5f : -0.5f));
-}
-V3 storedNormal(V3 n) {
-    const float s = 1.f / (std::fabs(n.x) + std::fabs(n.y) + std::fabs(n.z));
-    float px = n.x * s, py = n.y * s;
-    if (n.z < 0.f) octWrap(px, py);
-    const uint32_t packed = ((uint32_t)toSnorm16(px) & 0xFFFFu) | ((uint32_t)toSnorm16(py) << 16);
-    const int32_t bx = (int32_t)(packed << 16) >> 16, by = (int32_t)packed >> 16;
-    float x = std::fmax((float)bx / 32767.f, -1.f), y = std::fmax((float)by / 32767.f, -1.f);
-    const float z = 1.f - std::fabs(x) - std::fabs(y);
-    if (z < 0.f) octWrap(x, y);
-    const float l = std::sqrt(x * x + y * y + z * z);
-    return {x / l, y / l, z / l};
-}
-
-// binary16 of a threshold in [0, 1], round to nearest even
-uint16_t halfBits(float f) {
-    uint32_t x;
-    std::memcpy(&x, &f, 4);
-    const uint32_t sign = (x >> 16) & 0x8000u;
-    const int32_t e = (int32_t)((x >> 23) & 0xFF) - 127 + 15;
-    uint32_t m = x & 0x7FFFFFu;
-    if (((x >> 23) & 0xFF) == 0xFF) return (uint16_t)(sign | 0x7C00u | (m ? 0x200u : 0u));
-    if (e >= 31) return (uint16_t)(sign | 0x7C00u);
-    if (e <= 0) {
-        if (e < -10) return (uint16_t)sign;
-        m |= 0x800000u;
-        const int shift = 14 - e;
-        uint32_t hm = m >> shift;
-        const uint32_t rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
-        if (rem > half || (rem == half && (hm & 1u))) ++hm;
-        return (uint16_t)(sign | hm);
-    }
-    uint32_t h = ((uint32_t)e << 10) | (m >> 13);
-    const uint32_t rem = m & 0x1FFFu;
-    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
-    return (uint16_t)(sign | h);
-}
-
-// Alias table over the light weights, EmissivePowerSampler::generateAliasTable
-// (Rendering/Lights/EmissivePowerSampler.cpp:86-175): weights scaled to mean 1 and ordered
-// small to large (a stable order for equal weights), paired head/tail, entries shuffled with a
-// default-seeded mt19937 (full-range draws), packed as {binary16 threshold | alias >> 8,
-// alias & 0xFF << 24 | own index}.
-void buildAliasTable(const std::vector<float>& flux, std::vector<uint2>& table, float& invWeightsSum) {
-    const uint32_t N = (uint32_t)flux.size();
-    table.assign(N, make_uint2(0u, 0u));
-    if (N == 0) { invWeightsSum = 0.f; return; }
-    std::vector<float> w(flux);
-    double sum = 0.0;
-    for (float f : w) sum += f;
-    for (float& f : w) f *= N / float(sum);
-    std::vector<uint32_t> perm(N);
-    for (uint32_t i = 0; i < N; ++i) perm[i] = i;
-    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return w[a] < w[b]; });
-    std::vector<float> thr(N, 0.f);
-    std::vector<uint32_t> alias(N, 0u);
-    uint32_t head = 0, tail = N - 1;
-    while (head != tail) {
-        const uint32_t i = perm[head], j = perm[tail];
-        thr[i] = w[i];
-        alias[i] = j;
-        w[j] -= 1.0f - w[i];
-        if (head == tail - 1) {
-            thr[j] = 1.0f;
-            alias[j] = j;
-            break;
-        }
-        if (w[j] < 1.0f) {
-            std::swap(perm[head], perm[tail]);
-            tail--;
-        } else {
-            head++;
-        }
-    }
-    for (uint32_t i = 0; i < N; ++i) perm[i] = i;
-    std::mt19937 rng;
-    for (uint32_t i = 0; i < N; ++i) {
-        const uint32_t dst = i + ((uint32_t)rng() % (N - i));
-        std::swap(thr[i], thr[dst]);
-        std::swap(alias[i], alias[dst]);
-        std::swap(perm[i], perm[dst]);
-    }
-    for (uint32_t i = 0; i < N; ++i) {
-        const uint32_t prob = (uint32_t)halfBits(thr[i]) << 16u;
-        const uint32_t a = alias[i] & 0xFFFFFFu, own = perm[i] & 0xFFFFFFu;
-        table[i] = make_uint2(prob | ((a >> 8u) & 0xFFFFu), ((a & 0xFFu) << 24u) | own);
-    }
-    invWeightsSum = 1.0f / float(sum);
-}
-
-// Emissive triangles (materials with an emission profile, in primitive order), their face normal
-// and area (computeFaceNormalAndAreaW, Scene/Scene.slang:482-497) and luminous flux
-// luminance(profile rgb) * area * pi (Scene/Lights/FinalizeIntegration.cs.slang:60-110).
-plt_status buildLights(plt_context* ctx) {
-    const uint32_t nt = ctx->nTris;
-    std::vector<uint32_t> primToLight(nt, 0xFFFFFFFFu), lightTri;
-    for (uint32_t t = 0; t < nt; ++t) {
-        const uint32_t m = ctx->hTriMat[t];
-        if (m >= ctx->hMats.size()) return PLT_BAD_MATERIAL;
-        const plt_material_record& r = ctx->hMats[m];
-        if (r.type != PLT_MATERIAL_DIFFUSE || r.emission_spectral_id == PLT_NO_SPECTRAL_PROFILE) continue;
-        primToLight[t] = (uint32_t)lightTri.size();
-        lightTri.push_back(t);
-    }
-    const uint32_t nl = (uint32_t)lightTri.size();
-    std::vector<float> pos(9 * (size_t)nl), nrm(3 * (size_t)nl), area(nl), flux(nl);
-    std::vector<uint32_t> emission(nl);
-    for (uint32_t l = 0; l < nl; ++l) {
-        const uint32_t t = lightTri[l];
-        V3 p[3];
-        for (int k = 0; k < 3; ++k) {
-            const float* v = &ctx->hPos[3 * (size_t)ctx->hIdx[3 * (size_t)t + k]];
-            p[k] = {v[0], v[1], v[2]};
-            std::memcpy(&pos[9 * (size_t)l + 3 * k], v, 12);
-        }
-        const V3 N = crossv(sub(p[1], p[0]), sub(p[2], p[0]));
-        const float len = lengthv(N);
-        const V3 n = storedNormal({N.x / len, N.y / len, N.z / len});
-        nrm[3 * (size_t)l] = n.x;
-        nrm[3 * (size_t)l + 1] = n.y;
-        nrm[3 * (size_t)l + 2] = n.z;
-        area[l] = 0.5f * len;
-        const uint32_t em = ctx->hMats[ctx->hTriMat[t]].emission_spectral_id;
-        emission[l] = em;
-        float rgb[3] = {0.f, 0.f, 0.f};
-        if (em < ctx->hProfiles.size())
-            for (int c = 0; c < 3; ++c) rgb[c] = std::max(0.f, ctx->hProfiles[em].rgb[c]);
-        const float lum = rgb[0] * 0.2126f + rgb[1] * 0.7152f + rgb[2] * 0.0722f;
-        flux[l] = lum * area[l] * 3.14159265358979323846f;
-    }
-    std::vector<uint2> table;
-    buildAliasTable(flux, table, ctx->invWeightsSum);
-    plt_status s;
-    if ((s = upload(ctx, ctx->dLightPos, pos.data(), pos.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dLightNrm, nrm.data(), nrm.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dLightArea, area.data(), area.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dLightFlux, flux.data(), flux.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dAlias, table.data(), table.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dLightEmission, emission.data(), emission.size())) != PLT_OK) return s;
-    if ((s = upload(ctx, ctx->dPrimToLight, primToLight.data(), primToLight.size())) != PLT_OK) return s;
-    ctx->nLights = nl;
-    return PLT_OK;
-}
-
 // Render buffers for npix paths and maxB bounces: path state, queues, bounce buffer, accumulator.
 plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     if (ctx->dPt && ctx->ptNpix == npix && ctx->ptMaxB == maxB) return PLT_OK;
@@ -238,7 +77,7 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
 }  // namespace
 
 namespace plt {
-cudaError_t launchResolve(const double* accum, uint32_t npix, uint32_t frames, float* out, int numSMs, cudaStream_t stream);
+cudaError_t launchResolve(const PtParams& p, uint32_t frames, int numSMs, cudaStream_t stream);
 }
 
 // getProperties / getLobes of the PLT*BSDF.slang wrappers, double-sidedness
@@ -292,37 +131,19 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 
 void pltReleaseRenderState(plt_context* ctx) {
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes};
     for (void* p : ptrs) cudaFree(p);
 }
 
-extern "C" {
+namespace {
 
-plt_status plt_set_scene_shading(plt_context* ctx, const float* normals, const float* tangents, uint32_t n_vertices,
-                                 const uint32_t* tri_instance) {
-    if (!ctx || !normals) return PLT_INVALID_ARG;
-    if (n_vertices != ctx->nVerts || ctx->nTris == 0) return PLT_INVALID_ARG;
-    for (size_t i = 0; i < 3 * (size_t)n_vertices; ++i)
-        if (!std::isfinite(normals[i])) return PLT_NAN_INPUT;
-    plt_status s;
-    if ((s = upload(ctx, ctx->dNrm, normals, 3 * (size_t)n_vertices)) != PLT_OK) return s;
-    cudaFree(ctx->dTan);
-    ctx->dTan = nullptr;
-    if (tangents && (s = upload(ctx, ctx->dTan, tangents, 4 * (size_t)n_vertices)) != PLT_OK) return s;
-    {
-        std::vector<uint32_t> inst(ctx->nTris, 0u);
-        if (tri_instance) std::memcpy(inst.data(), tri_instance, sizeof(uint32_t) * ctx->nTris);
-        if ((s = upload(ctx, ctx->dTriInst, inst.data(), inst.size())) != PLT_OK) return s;
-    }
-    if ((s = buildLights(ctx)) != PLT_OK) return s;
-    ctx->shadingReady = true;
-    return PLT_OK;
-}
-
-plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width, uint32_t height, uint32_t frame_begin,
-                      uint32_t frame_count, float* out_rgba, void* stream) {
-    if (!ctx || !camera || !out_rgba || frame_count == 0) return PLT_INVALID_ARG;
-    if (((uintptr_t)out_rgba & 15u) != 0) return PLT_INVALID_ARG;
+// One render of a set of views: per-view validation, the scene table, buffers for all views'
+// paths, the frame loop and the per-view resolve.
+plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t nViews, uint32_t frame_begin, uint32_t frame_count,
+                       void* stream) {
+    if (!ctx || !views || nViews == 0 || frame_count == 0) return PLT_INVALID_ARG;
+    plt_status s = pltUploadScenes(ctx);
+    if (s != PLT_OK) return s;
     if (!ctx->shadingReady || ctx->nTris == 0 || ctx->nMats == 0) return PLT_INVALID_ARG;
     const plt_options& o = ctx->opt;
     if (o.hwss < 1 || o.hwss > 4) return PLT_NOT_SUPPORTED;
@@ -331,12 +152,42 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     const bool learned = o.learned_proposal != 0;
     if (learned && (!ctx->propReady || !ctx->dMatFeat || !(o.learned_proposal_prob > 0.f && o.learned_proposal_prob < 1.f)))
         return PLT_INVALID_ARG;
-    const uint64_t npix64 = (uint64_t)width * height;
+    std::vector<plt::PtScene> table(nViews);
+    uint64_t npix64 = 0;
+    for (uint32_t v = 0; v < nViews; ++v) {
+        const plt_render_view& rv = views[v];
+        if (rv.scene >= ctx->scenes.size() || !rv.out_rgba || ((uintptr_t)rv.out_rgba & 15u) != 0) return PLT_INVALID_ARG;
+        const plt_scene_slot& sl = ctx->slots[rv.scene];
+        plt::PtScene& S = table[v];
+        std::memset(&S, 0, sizeof(S));
+        S.cam = rv.camera;
+        S.width = rv.width;
+        S.height = rv.height;
+        S.pixelBase = (uint32_t)npix64;
+        S.root = sl.root;
+        S.lightBase = sl.lightBase;
+        S.nLights = sl.nLights;
+        S.invWeightsSum = sl.invWeightsSum;
+        S.out = rv.out_rgba;
+        npix64 += (uint64_t)rv.width * rv.height;
+        if (npix64 > (1u << 26)) return PLT_NOT_SUPPORTED;
+    }
     if (npix64 == 0) return PLT_OK;
-    if (npix64 > (1u << 26)) return PLT_NOT_SUPPORTED;
+    // views without pixels take no path range: drop them from the lookup table
+    table.erase(std::remove_if(table.begin(), table.end(), [](const plt::PtScene& S) { return S.width == 0 || S.height == 0; }),
+                table.end());
     const uint32_t npix = (uint32_t)npix64;
-    plt_status s = ensureRenderBuffers(ctx, npix, o.max_bounces);
+    s = ensureRenderBuffers(ctx, npix, o.max_bounces);
     if (s != PLT_OK) return s;
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (ctx->scenesCap < table.size()) {
+        cudaFree(ctx->dScenes);
+        ctx->dScenes = nullptr;
+        ctx->scenesCap = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dScenes, sizeof(plt::PtScene) * table.size()));
+        ctx->scenesCap = (uint32_t)table.size();
+    }
+    PLT_CUDA(ctx, cudaMemcpyAsync(ctx->dScenes, table.data(), sizeof(plt::PtScene) * table.size(), cudaMemcpyHostToDevice, st));
     // path state of learned renders: the product of primary-sample MIS densities per path
     const size_t mixBytes = learned ? (size_t)npix * sizeof(float) : 0;
     if (learned && ctx->ptMixBytes < mixBytes) {
@@ -347,8 +198,9 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
         ctx->ptMixBytes = mixBytes;
     }
     if (!ctx->dPtStats) PLT_CUDA(ctx, cudaMalloc(&ctx->dPtStats, 4 * sizeof(unsigned long long)));
-    const cudaStream_t st = (cudaStream_t)stream;
     plt::PtParams& P = ctx->pt;
+    P.scenes = ctx->dScenes;
+    P.nScenes = (uint32_t)table.size();
     P.nodes = ctx->dNodes;
     P.tris = ctx->dTris;
     P.pos = ctx->dPos;
@@ -371,8 +223,6 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     P.alias = ctx->dAlias;
     P.primToLight = ctx->dPrimToLight;
     P.lightEmission = ctx->dLightEmission;
-    P.nLights = ctx->nLights;
-    P.invWeightsSum = ctx->invWeightsSum;
     P.maxBounces = o.max_bounces;
     P.tileSize = o.tile_size ? o.tile_size : 512;
     P.hwss = o.hwss;
@@ -409,9 +259,6 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     P.mneeThreshold = o.mnee_solver_threshold;
     P.sourcingArea = o.sourcing_area_from_emissive_geometry;
     P.maxBeamOmega = o.sourcing_max_beam_omega;
-    P.cam = *camera;
-    P.width = width;
-    P.height = height;
     P.npix = npix;
     P.stats = ctx->dPtStats;
     P.status = ctx->dStatus;
@@ -421,9 +268,34 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
         P.frame = frame_begin + f;
         PLT_CUDA(ctx, plt::launchRenderFrame(P, ctx->numSMs, st));
     }
-    PLT_CUDA(ctx, plt::launchResolve(P.accum, npix, frame_count, out_rgba, ctx->numSMs, st));
+    PLT_CUDA(ctx, plt::launchResolve(P, frame_count, ctx->numSMs, st));
     return PLT_OK;
 }
+
+}  // namespace
+
+extern "C" {
+
+plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width, uint32_t height, uint32_t frame_begin,
+                      uint32_t frame_count, float* out_rgba, void* stream) {
+    if (!ctx || !camera || !out_rgba || frame_count == 0) return PLT_INVALID_ARG;
+    if (((uintptr_t)out_rgba & 15u) != 0) return PLT_INVALID_ARG;
+    if ((uint64_t)width * height == 0) return PLT_OK;
+    plt_render_view v;
+    std::memset(&v, 0, sizeof(v));
+    v.scene = 0;
+    v.width = width;
+    v.height = height;
+    v.camera = *camera;
+    v.out_rgba = out_rgba;
+    return renderViews(ctx, &v, 1, frame_begin, frame_count, stream);
+}
+
+plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame_begin, uint32_t frame_count,
+                             void* stream) {
+    return renderViews(ctx, views, n_views, frame_begin, frame_count, stream);
+}
+
 
 plt_status plt_render_stats(plt_context* ctx, uint64_t* out4) {
     if (!ctx || !out4) return PLT_INVALID_ARG;

@@ -102,7 +102,7 @@ struct TraceResult {
 template <bool ANY>
 __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, float ox, float oy,
                                                 float oz, float dx, float dy, float dz, float tmin, float tmax,
-                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow) {
+                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow, int32_t root = 0) {
     TraceResult res;
     res.prim = 0xFFFFFFFFu;
     res.t = tmax;
@@ -118,7 +118,7 @@ __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes
     bool done = false;
     int2 stack[kStackDepth];
     int sp = 0;
-    int32_t node = 0;
+    int32_t node = root;   // a scene's root in a combined node array (0 for a single scene)
 
     auto leaf = [&](int32_t ref) {
         const uint32_t v = (uint32_t)~ref;

@@ -206,3 +206,36 @@ def random_rays(n, seed, bounds, scene_tris=None):
         dd /= np.maximum(np.linalg.norm(dd, axis=0, keepdims=True), 1e-12)
         d = np.where(sel[None, :], dd, d)
     return np.ascontiguousarray(o.astype(np.float32).reshape(-1)), np.ascontiguousarray(d.astype(np.float32).reshape(-1))
+
+
+def merged_materials(scenes):
+    """One material table for a scene set: the scenes' records concatenated, and the offset of each
+    scene's records (its tri_material indices shift by it)."""
+    offsets, recs, n = [], [], 0
+    for sc in scenes:
+        offsets.append(n)
+        recs.append(sc.records)
+        n += len(sc.records)
+    return np.concatenate(recs), offsets
+
+
+def scene_set(seed=4, count=64, tris=(10_000, 500_000), rays=(4096, 1 << 20), sphere_level=3):
+    """`count` independent procedural rooms of uneven size: triangle counts and primary-ray counts
+    log-uniform in the given ranges (seeded), each room with its own materials over all eight PLT
+    types (gratings and up to 32-layer stacks included), light and glass sphere.  Returns a list of
+    (scene, width, height); width = height, a multiple of 8."""
+    rng = CounterRNG(seed, count)
+    ut, ur = rng.uniform().astype(np.float64), rng.uniform().astype(np.float64)
+    per_sphere = 20 * 4 ** sphere_level
+    box, quads = 16, 200
+    base = 12 * box * box + 2 + 20 * 4 ** min(sphere_level, 4) + 2 * quads
+    out = []
+    for i in range(count):
+        target = np.exp(np.log(tris[0]) + ut[i] * (np.log(tris[1]) - np.log(tris[0])))
+        n_spheres = max(0, int(round((target - base) / per_sphere)))
+        r = np.exp(np.log(rays[0]) + ur[i] * (np.log(rays[1]) - np.log(rays[0])))
+        side = max(8, int(round(np.sqrt(r) / 8.0)) * 8)
+        sc = procedural_scene(seed=1000 + seed * 131 + i, n_spheres=n_spheres, sphere_level=sphere_level, n_quads=quads,
+                              box_subdiv=box)
+        out.append((sc, side, side))
+    return out
