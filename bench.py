@@ -309,6 +309,79 @@ def learned_bench(dev, stream, batches=16, spp=16, prob=0.25, width=256):
             "time_to_relmse_1e-3_plain_s": t_a, "time_to_relmse_1e-3_learned_s": t_b, "speedup": t_a / t_b}
 
 
+def scene_set_bench(dev, stream, count=64, frames=2):
+    """Heterogeneous batched render: `count` seeded procedural rooms of uneven size (10 K-500 K
+    triangles, 4 K-1 M primary rays each, log-uniform; every room with its own materials over the
+    eight PLT types, gratings and up to 32-layer stacks included), HWSS 8, max depth 8, manifold
+    NEE, learned proposal on (probability 0.25, trained on 2^24 exact-sampler samples).  Batched:
+    all views in one plt_render_scenes wavefront per frame, replayed as a recorded CUDA graph, launch
+    shape from plt_render_tune.  Against: the same views as `count` separate plt_render_scenes calls
+    of one view each, launched directly (PLT_OPTION_NO_GRAPH) with the default launch shape.  Rays
+    = closest-hit segments + shadow and manifold rays (the render statistics)."""
+    import torch
+    from pltfalcor_gb300 import capi, scene as S, spectra
+    from pltfalcor_gb300.bsdf import PLTContext
+    prof, _ = spectra.standard_profiles()
+    t0 = time.perf_counter()
+    rooms = S.scene_set(seed=4, count=count)
+    gen_s = time.perf_counter() - t0
+    recs, offs = S.merged_materials([r for r, _, _ in rooms])
+    base = {"max_bounces": 8, "hwss": 8, "do_mnee": 1, "mnee_max_occluders": 2, "mnee_max_iterations": 60,
+            "mnee_solver_threshold": 5e-5, "learned_proposal": 1, "learned_proposal_prob": 0.25}
+
+    def context(flags):
+        ctx = PLTContext(dict(base, flags=flags))
+        ctx.set_spectral_profiles(prof)
+        ctx.set_materials(recs)
+        for (r, _, _), o in zip(rooms, offs):
+            ctx.add_scene(r, o)
+        ctx.proposal_init(3)
+        ctx.proposal_train(256, batch=65536, lr=1e-3, seed=1)
+        return ctx
+
+    outs = [torch.zeros((h, w, 4), dtype=torch.float32, device=dev) for _, w, h in rooms]
+    views = [(i, S.room_camera(w, h), w, h, o) for i, ((_, w, h), o) in enumerate(zip(rooms, outs))]
+    paths = sum(w * h for _, w, h in rooms)
+    t0 = time.perf_counter()
+    ctx = context(0)
+    ctx.render_scenes(views, 0, 1, stream)      # scene upload, light tables, buffers
+    torch.cuda.synchronize()
+    load_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    shape, tuned_ms = ctx.render_tune(views, 100, 1, stream)
+    tune_s = time.perf_counter() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.render_scenes(views, 1000, frames, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_batched = e0.elapsed_time(e1) / frames
+    st = ctx.check_status(stream)
+    stats = ctx.render_stats()
+    rays = stats["bounces"] + stats["shadow_rays"]
+    ctx.close()
+    ctx = context(capi.OPTION_NO_GRAPH)
+    for v in views:
+        ctx.render_scenes([v], 0, 1, stream)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for v in views:
+        ctx.render_scenes([v], 1000, frames, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_separate = e0.elapsed_time(e1) / frames
+    ctx.close()
+    tris = [r.n_tris for r, _, _ in rooms]
+    return {"workload": "%d procedural rooms, %d-%d triangles (%d total), %d-%d primary rays (%d total), HWSS 8, depth 8, "
+                        "manifold NEE, learned proposal on" % (count, min(tris), max(tris), sum(tris), min(w * h for _, w, h in rooms),
+                                                               max(w * h for _, w, h in rooms), paths),
+            "status": int(st), "frames": frames, "paths_per_frame": paths,
+            "ms_per_frame_batched": ms_batched, "ms_per_frame_separate": ms_separate, "speedup": ms_separate / ms_batched,
+            "paths_per_s_batched": paths / (ms_batched * 1e-3), "rays_per_s_batched": rays / (ms_batched * 1e-3),
+            "rays_per_frame": int(rays), "launch_shape": shape, "tuned_ms_per_frame": tuned_ms,
+            "scene_gen_s": gen_s, "load_s": load_s, "tune_s": tune_s}
+
+
 def capi_options(overrides):
     import ctypes as C
     from pltfalcor_gb300 import capi
@@ -495,6 +568,8 @@ def run_ours(args):
                                           size=args.render_size)
         if not args.no_learned:
             line["learned"] = learned_bench(dev, stream)
+        if not args.no_scene_set:
+            line["scene_set"] = scene_set_bench(dev, stream)
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         print(json.dumps(line))
@@ -514,6 +589,7 @@ def main():
     ap.add_argument("--no-trace", action="store_true")
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-scene-set", action="store_true")
     ap.add_argument("--render-size", type=int, default=1024, help="render leg image width = height (profiling uses small sizes)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()

@@ -219,6 +219,7 @@ typedef struct plt_options {
 } plt_options;
 
 #define PLT_OPTION_FP64_MULTILAYER 0x1u /* multilayer recursion in FP64 instead of the reference FP32 */
+#define PLT_OPTION_NO_GRAPH 0x2u        /* plt_render*: launch each frame directly instead of replaying its recorded CUDA graph */
 
 typedef struct plt_context plt_context;
 
@@ -343,6 +344,22 @@ typedef struct plt_render_view {
  * n separate plt_render calls).  At most 2^26 pixels over all views. */
 plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame_begin, uint32_t frame_count,
                              void* stream);
+
+/* Launch shape of the render pass (no counterpart in the reference): the frame's paths of all views
+ * are processed in waves of at most wave_paths paths (0 = one wave; smaller waves bound the path
+ * state and bounce records and keep them cache-resident between the sample and solve passes), and
+ * the segment, solve and manifold-walk kernels run with the given blocks of 128 per SM (0 = the
+ * occupancy limit).  Results do not depend on the shape.  plt_render_tune times a coordinate
+ * search over the shape on the caller's views (frames frame, frame + 1, ...; the views' outputs are
+ * overwritten), keeps the fastest for later renders and returns it with its time per frame. */
+typedef struct plt_launch_shape {
+    uint32_t wave_paths;
+    uint32_t segment_blocks_per_sm, solve_blocks_per_sm, walk_blocks_per_sm;
+} plt_launch_shape;
+plt_status plt_set_launch_shape(plt_context* ctx, const plt_launch_shape* shape);   /* NULL = defaults */
+plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape);
+plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame, uint32_t frames,
+                           plt_launch_shape* best, float* best_ms, void* stream);
 
 /* Path statistics of the last plt_render frame (host pointer, 4 values: paths, bounces recorded,
  * shadow rays traced, forward-unwind BSDF evaluations). */

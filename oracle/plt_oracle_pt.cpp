@@ -722,8 +722,10 @@ void sampleSpectrum(const Scene& s, uint32_t id, float hero, SampleGen& sg, bool
         const plt_spectral_profile& sp = s.tables.profiles[id];
         wl[0] = hero;
         le[0] = evalSpectrum<float>(s.tables, id, hero);
-        float x[3];
-        for (int c = 0; c < 3; ++c) x[c] = float(sp.bins) * sg.next1D();
+        // three draws (sampleNext3D) for at most three companions; beyond HWSS 4 one per companion
+        const uint32_t draws = H - 1 > 3 ? H - 1 : 3;
+        float x[MAXH];
+        for (uint32_t c = 0; c < draws; ++c) x[c] = float(sp.bins) * sg.next1D();
         for (uint32_t j = 1; j < H; ++j) {
             const uint32_t i = (uint32_t)x[j - 1];
             const float a = i < sp.bins ? sp.icdf[i] : 1.f;
@@ -1387,7 +1389,7 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
                 uint32_t* rec_flags, uint64_t* stats) {
     if (frames == 0) return PLT_INVALID_ARG;
     if (!sc || !cam || !opt || !rgb) return PLT_INVALID_ARG;
-    if (opt->hwss < 1 || opt->hwss > 4 || opt->mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
+    if (opt->hwss < 1 || (opt->hwss > 4 && opt->hwss != 8) || opt->mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     Scene s;
     s.nv = sc->n_vertices;
     s.nt = sc->n_triangles;

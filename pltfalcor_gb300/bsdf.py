@@ -222,13 +222,35 @@ class PLTContext:
 
     def render_scenes(self, views, frame_begin=0, frame_count=1, stream=None):
         """plt_render_scenes: views is a list of (scene index, camera, width, height, out tensor [h][w][4])."""
+        arr = self._views(views)
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_render_scenes(self.handle, arr, len(views), frame_begin, frame_count, s), "plt_render_scenes")
+
+    def _views(self, views):
         arr = (capi.RenderView * len(views))()
         for i, (sid, cam, w, h, out) in enumerate(views):
             arr[i].scene, arr[i].width, arr[i].height = sid, w, h
             arr[i].camera = cam
             arr[i].out_rgba = _ptr(out)
+        return arr
+
+    def set_launch_shape(self, wave_paths=0, segment=0, solve=0, walk=0):
+        sh = capi.LaunchShape(wave_paths, segment, solve, walk)
+        capi.check(self.lib.plt_set_launch_shape(self.handle, C.byref(sh)), "plt_set_launch_shape")
+
+    def launch_shape(self):
+        sh = capi.LaunchShape()
+        capi.check(self.lib.plt_get_launch_shape(self.handle, C.byref(sh)), "plt_get_launch_shape")
+        return {"wave_paths": sh.wave_paths, "segment": sh.segment_blocks_per_sm, "solve": sh.solve_blocks_per_sm,
+                "walk": sh.walk_blocks_per_sm}
+
+    def render_tune(self, views, frame=0, frames=1, stream=None):
+        """plt_render_tune over views (as render_scenes); returns (shape dict, ms per frame)."""
+        arr = self._views(views)
+        sh, ms = capi.LaunchShape(), C.c_float(0)
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
-        capi.check(self.lib.plt_render_scenes(self.handle, arr, len(views), frame_begin, frame_count, s), "plt_render_scenes")
+        capi.check(self.lib.plt_render_tune(self.handle, arr, len(views), frame, frames, C.byref(sh), C.byref(ms), s), "plt_render_tune")
+        return self.launch_shape(), ms.value
 
     def render_bounces(self, npix, max_bounces):
         """Bounce records of the last frame: (prim, lobe, flags), each [npix][max_bounces+1] uint32."""

@@ -86,8 +86,14 @@ class RenderView(C.Structure):
                 ("camera", Camera), ("out_rgba", C.c_void_p)]
 
 
+class LaunchShape(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("segment_blocks_per_sm", C.c_uint32), ("solve_blocks_per_sm", C.c_uint32),
+                ("walk_blocks_per_sm", C.c_uint32)]
+
+
 MATERIAL_FLAG_DOUBLE_SIDED = 0x1
 MAX_SCENES = 4096
+OPTION_NO_GRAPH = 0x2
 
 assert C.sizeof(SpectralProfile) == 1052
 assert C.sizeof(MaterialRecord) == 80
@@ -101,7 +107,7 @@ EXPORTED_SYMBOLS = [
     "plt_set_timing_events", "plt_set_scene_shading", "plt_render", "plt_render_stats", "plt_render_bounces",
     "plt_proposal_init", "plt_proposal_set_params", "plt_proposal_get_params", "plt_proposal_generate",
     "plt_proposal_gradient", "plt_proposal_forward", "plt_proposal_adam_step", "plt_proposal_train",
-    "plt_add_scene", "plt_clear_scenes", "plt_render_scenes",
+    "plt_add_scene", "plt_clear_scenes", "plt_render_scenes", "plt_set_launch_shape", "plt_get_launch_shape", "plt_render_tune",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -158,6 +164,9 @@ def load_library(path=LIB_PATH):
         "plt_add_scene": (i32, [vp, C.POINTER(SceneDesc), C.POINTER(C.c_uint32)]),
         "plt_clear_scenes": (i32, [vp]),
         "plt_render_scenes": (i32, [vp, C.POINTER(RenderView), u32, u32, u32, vp]),
+        "plt_set_launch_shape": (i32, [vp, C.POINTER(LaunchShape)]),
+        "plt_get_launch_shape": (i32, [vp, C.POINTER(LaunchShape)]),
+        "plt_render_tune": (i32, [vp, C.POINTER(RenderView), u32, u32, u32, C.POINTER(LaunchShape), C.POINTER(C.c_float), vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

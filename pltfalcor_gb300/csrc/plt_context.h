@@ -85,6 +85,13 @@ struct plt_context {
     void* dMneeTasks = nullptr;   // deferred manifold walks of the solve pass
     size_t mneeBytes = 0;
     uint32_t ptNpix = 0, ptMaxB = 0;
+    double* dAccum = nullptr;     // [paths of all views][3] frame accumulation
+    uint32_t accumCap = 0;
+    plt::PtLaunch launch{};       // launch shape (plt_render_tune; zeros = defaults)
+    uint32_t* dFrame = nullptr;   // frame index word of the render kernels
+    void* capStream = nullptr;    // cudaStream_t the frame graph is recorded on
+    void* graphExec = nullptr;    // cudaGraphExec_t of one frame's launch sequence
+    std::vector<unsigned char> graphKey;   // the parameters it was recorded with
     plt::PtParams pt{};
     unsigned long long* dPtStats = nullptr;
     // learned MIS proposal: FP32 master weights, Adam moments, BF16 copy, gradient, loss;

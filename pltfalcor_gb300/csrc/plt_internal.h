@@ -80,6 +80,14 @@ struct PtScene {
     float* out;                   // [height][width][4]
 };
 
+// Launch shape of a render (chosen by plt_render_tune; zeros: defaults): paths per wave (0 = all
+// paths of the frame in one wave) and blocks of 128 per SM for the segment, solve and
+// manifold-walk kernels (0 = the occupancy limit).
+struct PtLaunch {
+    uint32_t waveCap;
+    uint32_t segBlocksPerSM, solveBlocksPerSM, walkBlocksPerSM;
+};
+
 struct PtParams {
     // scene
     const void* nodes;
@@ -113,7 +121,11 @@ struct PtParams {
     float sourcingArea, maxBeamOmega;
     uint32_t mneeMaxOccluders, mneeMaxIterations;
     float mneeThreshold;
-    uint32_t npix, frame;         // paths of all scenes, frame index
+    // paths: the frame's paths of all views are processed in waves of at most `npix` paths (the
+    // plane stride of the path state and bounce records); this wave holds paths
+    // [pidBase, pidBase + nWave) of the frame's nTotal
+    uint32_t npix, nWave, pidBase, nTotal;
+    const uint32_t* frameDev;     // the frame index (device word: one recorded launch sequence serves every frame)
     // path state of the sample pass
     uint32_t* sg;                 // [4][npix]
     float* org;                   // [3][npix]
@@ -150,7 +162,8 @@ struct PtParams {
     unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, paths
     uint32_t* status;
 };
-cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream);
+cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream);
+cudaError_t launchSetFrame(uint32_t* frameDev, uint32_t frame, bool advance, cudaStream_t stream);
 
 constexpr int kBatchThreads = 256;     // classify CTA
 constexpr int kBatchItems = 8;

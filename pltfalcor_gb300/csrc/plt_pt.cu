@@ -16,8 +16,10 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceKe
 static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAnalyticKernel;
 #endif
 
-cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream) {
-    if (p.npix == 0) return cudaSuccess;
+// One wave of one frame: the queue counters, the path initialisation, maxBounces + 1 segment
+// launches over the compacted queues, then the solve pass and its manifold-walk wavefront.
+cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
+    if (p.nWave == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 3), stream);   // + manifold-walk count
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
@@ -32,21 +34,23 @@ cudaError_t launchRenderFrame(const PtParams& p, int numSMs, cudaStream_t stream
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptInitKernel, 128, 0);
         bpsInit = b > 0 ? b : 1;
     }
-    const uint32_t need = (p.npix + 127) / 128;
-    pltdev::ptInitKernel<<<std::min<uint32_t>(need, (uint32_t)(numSMs * bpsInit)), 128, 0, stream>>>(p);
+    auto blocks = [&](int occ, uint32_t want) { return (uint32_t)numSMs * (want ? std::min<uint32_t>(want, (uint32_t)occ) : (uint32_t)occ); };
+    const uint32_t need = (p.nWave + 127) / 128;
+    pltdev::ptInitKernel<<<std::min<uint32_t>(need, blocks(bpsInit, 0)), 128, 0, stream>>>(p);
     if (p.opt & kPtLearned) {
-        const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsLearned));
+        const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsLearned, L.segBlocksPerSM));
         for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
     } else {
-        const uint32_t gridB = std::min<uint32_t>(need, (uint32_t)(numSMs * bpsBounce));
+        const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsBounce, L.segBlocksPerSM));
         for (uint32_t it = 0; it <= p.maxBounces; ++it) kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     switch (p.hwss) {
-    case 1: return pltdev::launchSolveH<1>(p, numSMs, stream);
-    case 2: return pltdev::launchSolveH<2>(p, numSMs, stream);
-    case 3: return pltdev::launchSolveH<3>(p, numSMs, stream);
-    case 4: return pltdev::launchSolveH<4>(p, numSMs, stream);
+    case 1: return pltdev::launchSolveH<1>(p, L, numSMs, stream);
+    case 2: return pltdev::launchSolveH<2>(p, L, numSMs, stream);
+    case 3: return pltdev::launchSolveH<3>(p, L, numSMs, stream);
+    case 4: return pltdev::launchSolveH<4>(p, L, numSMs, stream);
+    case 8: return pltdev::launchSolveH<8>(p, L, numSMs, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -57,7 +61,7 @@ namespace pltdev {
 
 // The mean of the accumulated frames into each view's output image.
 __global__ void ptResolveKernel(const PtParams P, double inv) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npix; i += gridDim.x * blockDim.x) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nTotal; i += gridDim.x * blockDim.x) {
         const PtScene& S = P.scenes[sceneOf(P, i)];
         float* out = S.out + 4 * (size_t)(i - S.pixelBase);
         out[0] = (float)(P.accum[3 * (size_t)i] * inv);
@@ -67,13 +71,21 @@ __global__ void ptResolveKernel(const PtParams P, double inv) {
     }
 }
 
+// The frame index word: set before the first frame, advanced after every frame.
+__global__ void ptFrameKernel(uint32_t* frameDev, uint32_t frame, int advance) { *frameDev = advance ? *frameDev + 1u : frame; }
+
 }  // namespace pltdev
 
 namespace plt {
 
+cudaError_t launchSetFrame(uint32_t* frameDev, uint32_t frame, bool advance, cudaStream_t stream) {
+    pltdev::ptFrameKernel<<<1, 1, 0, stream>>>(frameDev, frame, advance ? 1 : 0);
+    return cudaGetLastError();
+}
+
 cudaError_t launchResolve(const PtParams& p, uint32_t frames, int numSMs, cudaStream_t stream) {
-    if (p.npix == 0) return cudaSuccess;
-    const uint32_t grid = std::min<uint32_t>((p.npix + 255) / 256, (uint32_t)numSMs * 8);
+    if (p.nTotal == 0) return cudaSuccess;
+    const uint32_t grid = std::min<uint32_t>((p.nTotal + 255) / 256, (uint32_t)numSMs * 8);
     pltdev::ptResolveKernel<<<grid, 256, 0, stream>>>(p, 1.0 / (double)frames);
     return cudaGetLastError();
 }

@@ -274,9 +274,12 @@ PLT_DI void sampleSpectrum(const PtParams& P, uint32_t id, float hero, SampleGen
         const DevProfile& sp = P.profiles[id];
         wl[0] = hero;
         le[0] = evalSpectrum(P.profiles, P.nProfiles, id, hero);
-        float x[3];
+        // the reference draws three numbers (sampleNext3D) for its at most three companion
+        // wavelengths; beyond HWSS 4 one number per companion
+        constexpr int kDraws = H - 1 > 3 ? H - 1 : 3;
+        float x[kDraws];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) x[c] = float(sp.bins) * sg.next1D();
+        for (int c = 0; c < kDraws; ++c) x[c] = float(sp.bins) * sg.next1D();
         const float* icdf = P.profileIcdf + 128 * id;
 #pragma unroll
         for (int j = 1; j < H; ++j) {
@@ -408,12 +411,13 @@ PLT_DI uint32_t warpAggregatedAdd(uint32_t* counter, bool pred) {
 
 #ifdef PLT_PT_SAMPLE_PASS   // defined by plt_pt.cu only: one copy of the sample-pass kernels
 __global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.npix; i += gridDim.x * blockDim.x) {
-        const PtScene& S = P.scenes[sceneOf(P, i)];
-        const uint32_t local = i - S.pixelBase;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nWave; i += gridDim.x * blockDim.x) {
+        const uint32_t gp = P.pidBase + i;
+        const PtScene& S = P.scenes[sceneOf(P, gp)];
+        const uint32_t local = gp - S.pixelBase;
         const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg;
-        sg.init(px, py, P.frame);
+        sg.init(px, py, *P.frameDev);
         const float wl = 380.0f + sg.next1D() * (720.0f - 380.0f);   // SpectrumSampler.sampleOne
         const f3 d = cameraDir(S, px, py);
         const uint32_t n = P.npix;
@@ -453,7 +457,7 @@ template <bool LEARNED>
 __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBounceKernel(const PtParams P, uint32_t it) {
     extern __shared__ __align__(16) unsigned char ptSmem[];
     const uint32_t n = P.npix;
-    const uint32_t count = it == 0 ? n : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t count = it == 0 ? P.nWave : *((volatile uint32_t*)(P.qcount + it));
     const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
     uint32_t* qout = (it & 1u) ? P.queue1 : P.queue0;
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
@@ -510,7 +514,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
             if constexpr (LEARNED) wps = P.wpss[pid];
             for (int guard = 0; guard < 64; ++guard) {
                 h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
-                                    __ldg(&P.scenes[sceneOf(P, pid)].root));
+                                    __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
@@ -652,7 +656,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
 // lane (no warp-uniform phase for the network), which keeps its register allocation lean.
 __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKernel(const PtParams P, uint32_t it) {
     const uint32_t n = P.npix;
-    const uint32_t count = it == 0 ? n : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t count = it == 0 ? P.nWave : *((volatile uint32_t*)(P.qcount + it));
     const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
     uint32_t* qout = (it & 1u) ? P.queue1 : P.queue0;
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
@@ -688,7 +692,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
             };
             for (int guard = 0; guard < 64; ++guard) {
                 const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
-                                                      __ldg(&P.scenes[sceneOf(P, pid)].root));
+                                                      __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
@@ -1235,14 +1239,16 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     TraceCounters tc{0u, 0u, 0u, 0u};
     uint32_t evals = 0;
     MSData ms;
-    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x) {
-        const PtScene& S = P.scenes[sceneOf(P, pid)];
+    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < P.nWave; pid += gridDim.x * blockDim.x) {
+        const uint32_t gp = P.pidBase + pid;
+        const PtScene& S = P.scenes[sceneOf(P, gp)];
         const int32_t root = (int32_t)S.root;
-        const uint32_t local = pid - S.pixelBase;
+        const uint32_t local = gp - S.pixelBase;
         const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg, tilesg;
-        sg.init(px, py, P.frame);
-        tilesg.init(px / P.tileSize, py / P.tileSize, P.frame << 2);
+        const uint32_t frame = *P.frameDev;
+        sg.init(px, py, frame);
+        tilesg.init(px / P.tileSize, py / P.tileSize, frame << 2);
         const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
         f3 pathOrigin = camPos(S);
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
@@ -1407,9 +1413,9 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
             if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
             pathOrigin = V.posW;
         }
-        P.accum[3 * (size_t)pid] += (double)Lr;
-        P.accum[3 * (size_t)pid + 1] += (double)Lg;
-        P.accum[3 * (size_t)pid + 2] += (double)Lb;
+        P.accum[3 * (size_t)gp] += (double)Lr;
+        P.accum[3 * (size_t)gp + 1] += (double)Lg;
+        P.accum[3 * (size_t)gp + 2] += (double)Lb;
     }
     if (tc.overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     unsigned long long s1 = tc.shadowRays, s2 = evals;
@@ -1446,7 +1452,8 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         const int p = (int)t.p;
         const bool curMS = t.curMS != 0;
         const f3 msOrigin = t.msOrigin;
-        const PtScene& S = P.scenes[sceneOf(P, pid)];
+        const uint32_t gp = P.pidBase + pid;
+        const PtScene& S = P.scenes[sceneOf(P, gp)];
         if (!manifoldWalk(P, (int32_t)S.root, msOrigin, t.tposW, ms, tc)) continue;
         const Bnc<H> bounce = readBounce<H>(P, pid, p);
         const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
@@ -1479,9 +1486,9 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
         replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
         if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
-            atomicAdd(P.accum + 3 * (size_t)pid, (double)Lr);
-            atomicAdd(P.accum + 3 * (size_t)pid + 1, (double)Lg);
-            atomicAdd(P.accum + 3 * (size_t)pid + 2, (double)Lb);
+            atomicAdd(P.accum + 3 * (size_t)gp, (double)Lr);
+            atomicAdd(P.accum + 3 * (size_t)gp + 1, (double)Lg);
+            atomicAdd(P.accum + 3 * (size_t)gp + 2, (double)Lb);
         }
     }
     if (tc.overflow) atomicOr(P.status, plt::kStatusStackOverflow);
@@ -1497,7 +1504,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
 }
 
 template <int H>
-cudaError_t launchSolve(const PtParams& p, int numSMs, cudaStream_t stream) {
+cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, cudaStream_t stream) {
     static int bps[2] = {-1, -1};
     const bool mnee = (p.opt & plt::kPtDoMnee) != 0;
     if (bps[mnee] < 0) {
@@ -1506,8 +1513,8 @@ cudaError_t launchSolve(const PtParams& p, int numSMs, cudaStream_t stream) {
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptSolveKernel<H, false>, 128, 0);
         bps[mnee] = b > 0 ? b : 1;
     }
-    uint32_t grid = (uint32_t)(numSMs * bps[mnee]);
-    const uint32_t need = (p.npix + 127) / 128;
+    uint32_t grid = (uint32_t)numSMs * (L.solveBlocksPerSM ? min((uint32_t)bps[mnee], L.solveBlocksPerSM) : (uint32_t)bps[mnee]);
+    const uint32_t need = (p.nWave + 127) / 128;
     if (grid > need) grid = need;
     if (mnee) ptSolveKernel<H, true><<<grid, 128, 0, stream>>>(p);
     else ptSolveKernel<H, false><<<grid, 128, 0, stream>>>(p);
@@ -1518,12 +1525,13 @@ cudaError_t launchSolve(const PtParams& p, int numSMs, cudaStream_t stream) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptMneeKernel<H>, 128, 0);
             bpsW = b > 0 ? b : 1;
         }
-        ptMneeKernel<H><<<(uint32_t)(numSMs * bpsW), 128, 0, stream>>>(p);
+        const uint32_t gw = (uint32_t)numSMs * (L.walkBlocksPerSM ? min((uint32_t)bpsW, L.walkBlocksPerSM) : (uint32_t)bpsW);
+        ptMneeKernel<H><<<gw, 128, 0, stream>>>(p);
     }
     return cudaGetLastError();
 }
 
 // per-H solve launchers, one translation unit each (plt_pt_h{1,2,3,4}.cu)
-template <int H> cudaError_t launchSolveH(const PtParams& p, int numSMs, cudaStream_t stream);
+template <int H> cudaError_t launchSolveH(const PtParams& p, const plt::PtLaunch& L, int numSMs, cudaStream_t stream);
 
 }  // namespace pltdev

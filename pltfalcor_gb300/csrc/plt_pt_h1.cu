@@ -2,5 +2,7 @@
 #include "plt_pt.cuh"
 
 namespace pltdev {
-template <> cudaError_t launchSolveH<1>(const PtParams& p, int numSMs, cudaStream_t stream) { return launchSolve<1>(p, numSMs, stream); }
+template <> cudaError_t launchSolveH<1>(const PtParams& p, const plt::PtLaunch& L, int numSMs, cudaStream_t stream) {
+    return launchSolve<1>(p, L, numSMs, stream);
+}
 }  // namespace pltdev

@@ -40,8 +40,7 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al((nb + 2) * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
-    const size_t accumBytes = al(3 * n * 8);
-    const size_t total = pathBytes + bounceBytes + accumBytes;
+    const size_t total = pathBytes + bounceBytes;
     PLT_CUDA(ctx, cudaMalloc(&ctx->dPt, total));
     ctx->ptBytes = total;
     char* p = static_cast<char*>(ctx->dPt);
@@ -68,7 +67,6 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.bFlags = (uint32_t*)take(nb * n * 4);
     P.bContrib = (float*)take(nb * n * 4);
     P.bLndp = (float*)take(nb * n * 4);
-    P.accum = (double*)take(3 * n * 8);
     ctx->ptNpix = npix;
     ctx->ptMaxB = maxB;
     return PLT_OK;
@@ -130,8 +128,11 @@ uint2 pltMaterialProps(const plt_material_record& r, const pltdev::DevMaterial& 
 }
 
 void pltReleaseRenderState(plt_context* ctx) {
+    if (ctx->graphExec) cudaGraphExecDestroy((cudaGraphExec_t)ctx->graphExec);
+    if (ctx->capStream) cudaStreamDestroy((cudaStream_t)ctx->capStream);
+    cudaFree(ctx->dFrame);
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes, ctx->dAccum};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -146,7 +147,7 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     if (s != PLT_OK) return s;
     if (!ctx->shadingReady || ctx->nTris == 0 || ctx->nMats == 0) return PLT_INVALID_ARG;
     const plt_options& o = ctx->opt;
-    if (o.hwss < 1 || o.hwss > 4) return PLT_NOT_SUPPORTED;
+    if (o.hwss < 1 || (o.hwss > 4 && o.hwss != 8)) return PLT_NOT_SUPPORTED;   // 8: beyond the reference's 1-4
     if (o.mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     if (o.max_bounces > 64) return PLT_NOT_SUPPORTED;
     const bool learned = o.learned_proposal != 0;
@@ -176,9 +177,19 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     // views without pixels take no path range: drop them from the lookup table
     table.erase(std::remove_if(table.begin(), table.end(), [](const plt::PtScene& S) { return S.width == 0 || S.height == 0; }),
                 table.end());
-    const uint32_t npix = (uint32_t)npix64;
+    const uint32_t total = (uint32_t)npix64;
+    // paths per wave: the tuned cap, else the whole frame
+    const plt::PtLaunch L = ctx->launch;
+    const uint32_t npix = L.waveCap ? std::min(L.waveCap, total) : total;
     s = ensureRenderBuffers(ctx, npix, o.max_bounces);
     if (s != PLT_OK) return s;
+    if (ctx->accumCap < total) {
+        cudaFree(ctx->dAccum);
+        ctx->dAccum = nullptr;
+        ctx->accumCap = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dAccum, sizeof(double) * 3 * (size_t)total));
+        ctx->accumCap = total;
+    }
     const cudaStream_t st = (cudaStream_t)stream;
     if (ctx->scenesCap < table.size()) {
         cudaFree(ctx->dScenes);
@@ -260,14 +271,60 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.sourcingArea = o.sourcing_area_from_emissive_geometry;
     P.maxBeamOmega = o.sourcing_max_beam_omega;
     P.npix = npix;
+    P.nTotal = total;
+    P.accum = ctx->dAccum;
     P.stats = ctx->dPtStats;
     P.status = ctx->dStatus;
-    PLT_CUDA(ctx, cudaMemsetAsync(P.accum, 0, sizeof(double) * 3 * (size_t)npix, st));
-    for (uint32_t f = 0; f < frame_count; ++f) {
-        PLT_CUDA(ctx, cudaMemsetAsync(ctx->dPtStats, 0, 4 * sizeof(unsigned long long), st));
-        P.frame = frame_begin + f;
-        PLT_CUDA(ctx, plt::launchRenderFrame(P, ctx->numSMs, st));
+    if (!ctx->dFrame) PLT_CUDA(ctx, cudaMalloc(&ctx->dFrame, sizeof(uint32_t)));
+    P.frameDev = ctx->dFrame;
+    P.pidBase = 0;
+    P.nWave = 0;
+    PLT_CUDA(ctx, cudaMemsetAsync(P.accum, 0, sizeof(double) * 3 * (size_t)total, st));
+    PLT_CUDA(ctx, plt::launchSetFrame(ctx->dFrame, frame_begin, false, st));
+    // one frame: the statistics reset, every wave's launch sequence, the frame-index advance
+    auto enqueueFrame = [&](cudaStream_t s2) -> cudaError_t {
+        plt::PtParams W = P;
+        cudaError_t e = cudaMemsetAsync(ctx->dPtStats, 0, 4 * sizeof(unsigned long long), s2);
+        for (uint32_t base = 0; e == cudaSuccess && base < total; base += npix) {
+            W.pidBase = base;
+            W.nWave = std::min(npix, total - base);
+            e = plt::launchRenderFrame(W, L, ctx->numSMs, s2);
+        }
+        return e == cudaSuccess ? plt::launchSetFrame(ctx->dFrame, 0, true, s2) : e;
+    };
+    // The frame is recorded once per launch configuration as a CUDA graph and replayed per frame
+    // (PLT_OPTION_NO_GRAPH launches it directly).
+    bool replayed = false;
+    if (!(o.flags & PLT_OPTION_NO_GRAPH)) {
+        std::vector<unsigned char> key(sizeof(P) + sizeof(L) + sizeof(total));
+        std::memcpy(key.data(), &P, sizeof(P));
+        std::memcpy(key.data() + sizeof(P), &L, sizeof(L));
+        std::memcpy(key.data() + sizeof(P) + sizeof(L), &total, sizeof(total));
+        if (!ctx->graphExec || key != ctx->graphKey) {
+            if (ctx->graphExec) cudaGraphExecDestroy((cudaGraphExec_t)ctx->graphExec);
+            ctx->graphExec = nullptr;
+            if (!ctx->capStream) PLT_CUDA(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&ctx->capStream, cudaStreamNonBlocking));
+            const cudaStream_t cs = (cudaStream_t)ctx->capStream;
+            PLT_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed));
+            const cudaError_t e1 = enqueueFrame(cs);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+            cudaGraphExec_t x = nullptr;
+            if (e1 == cudaSuccess && e2 == cudaSuccess && g && cudaGraphInstantiate(&x, g, 0) == cudaSuccess) {
+                ctx->graphExec = x;
+                ctx->graphKey = key;
+            }
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();   // a failed recording falls back to direct launches
+        }
+        if (ctx->graphExec) {
+            for (uint32_t f = 0; f < frame_count; ++f) PLT_CUDA(ctx, cudaGraphLaunch((cudaGraphExec_t)ctx->graphExec, st));
+            replayed = true;
+        }
     }
+    if (!replayed)
+        for (uint32_t f = 0; f < frame_count; ++f) PLT_CUDA(ctx, enqueueFrame(st));
+    P.nWave = std::min(npix, total);
     PLT_CUDA(ctx, plt::launchResolve(P, frame_count, ctx->numSMs, st));
     return PLT_OK;
 }
@@ -294,6 +351,70 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
 plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame_begin, uint32_t frame_count,
                              void* stream) {
     return renderViews(ctx, views, n_views, frame_begin, frame_count, stream);
+}
+
+plt_status plt_set_launch_shape(plt_context* ctx, const plt_launch_shape* shape) {
+    if (!ctx) return PLT_INVALID_ARG;
+    ctx->launch = shape ? plt::PtLaunch{shape->wave_paths, shape->segment_blocks_per_sm, shape->solve_blocks_per_sm, shape->walk_blocks_per_sm}
+                        : plt::PtLaunch{};
+    return PLT_OK;
+}
+
+plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape) {
+    if (!ctx || !shape) return PLT_INVALID_ARG;
+    *shape = plt_launch_shape{ctx->launch.waveCap, ctx->launch.segBlocksPerSM, ctx->launch.solveBlocksPerSM, ctx->launch.walkBlocksPerSM};
+    return PLT_OK;
+}
+
+// Coordinate search over the launch shape on the caller's views: wave size first, then the
+// blocks per SM of the segment, solve and manifold-walk kernels, each candidate timed (CUDA events
+// on the caller's stream) over `frames` frames after one untimed frame that records its graph.
+plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame, uint32_t frames,
+                           plt_launch_shape* best, float* best_ms, void* stream) {
+    if (!ctx || !views || n_views == 0 || frames == 0) return PLT_INVALID_ARG;
+    uint64_t total = 0;
+    for (uint32_t v = 0; v < n_views; ++v) total += (uint64_t)views[v].width * views[v].height;
+    if (total == 0) return PLT_INVALID_ARG;
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    PLT_CUDA(ctx, cudaEventCreate(&e0));
+    PLT_CUDA(ctx, cudaEventCreate(&e1));
+    uint32_t f = frame;
+    auto timeShape = [&](const plt::PtLaunch& L, float& ms) -> plt_status {
+        ctx->launch = L;
+        plt_status s = renderViews(ctx, views, n_views, f, 1, stream);
+        if (s != PLT_OK) return s;
+        f += 1;
+        if (cudaEventRecord(e0, st) != cudaSuccess) return PLT_CUDA_ERROR;
+        if ((s = renderViews(ctx, views, n_views, f, frames, stream)) != PLT_OK) return s;
+        f += frames;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return PLT_CUDA_ERROR;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)frames;
+        return PLT_OK;
+    };
+    plt::PtLaunch bestL{};
+    float bestMs = 0.f;
+    plt_status s = timeShape(bestL, bestMs);
+    auto tryShape = [&](plt::PtLaunch L) {
+        float ms = 0.f;
+        if (s == PLT_OK && (s = timeShape(L, ms)) == PLT_OK && ms < bestMs) {
+            bestMs = ms;
+            bestL = L;
+        }
+    };
+    for (uint32_t w : {1u << 22, 1u << 21, 1u << 20, 1u << 19, 1u << 18})
+        if (w < total) tryShape(plt::PtLaunch{w, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
+    for (uint32_t b : {2u, 4u}) tryShape(plt::PtLaunch{bestL.waveCap, b, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
+    for (uint32_t b : {1u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, b, bestL.walkBlocksPerSM});
+    for (uint32_t b : {1u, 2u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, b});
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->launch = bestL;
+    if (s != PLT_OK) return s;
+    if (best) *best = plt_launch_shape{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM};
+    if (best_ms) *best_ms = bestMs;
+    return PLT_OK;
 }
 
 

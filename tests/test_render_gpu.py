@@ -87,7 +87,7 @@ def _compare(gpu, orc, grecs, orecs, label):
     return same
 
 
-@pytest.mark.parametrize("hwss,mnee", [(4, 1), (4, 0), (1, 1)])
+@pytest.mark.parametrize("hwss,mnee", [(4, 1), (4, 0), (1, 1), (8, 1)])
 def test_render_matches_oracle(torch_cuda, oracle_lib, product_lib, profiles, room, hwss, mnee):
     """Default PLTPT options (manifold NEE on) and without manifold walks."""
     import oracle

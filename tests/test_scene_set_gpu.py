@@ -127,3 +127,44 @@ def test_scene_set_rejects_bad_views(torch_cuda, product_lib, profiles, rooms):
     v[0].out_rgba = out.data_ptr()
     assert lib.plt_render_scenes(ctx.handle, v, 1, 0, 1, None) == capi.PLT_INVALID_ARG
     ctx.close()
+
+
+def _render_set(torch, rooms, prof, views, frame, frames, opts, shape=None, tune=False):
+    from pltfalcor_gb300.bsdf import PLTContext
+    ctx = PLTContext(opts)
+    recs, offs = S.merged_materials(rooms)
+    ctx.set_spectral_profiles(prof)
+    ctx.set_materials(recs)
+    for r, o in zip(rooms, offs):
+        ctx.add_scene(r, o)
+    if opts.get("learned_proposal"):
+        ctx.proposal_init(5)
+    if shape is not None:
+        ctx.set_launch_shape(*shape)
+    outs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for (_, _, w, h) in views]
+    vv = [(sid, cam, w, h, o) for (sid, cam, w, h), o in zip(views, outs)]
+    tuned = ctx.render_tune(vv, 1000, 1) if tune else None
+    ctx.render_scenes(vv, frame, frames)
+    torch.cuda.synchronize()
+    assert ctx.check_status() == capi.PLT_OK
+    ctx.close()
+    return [o.cpu().numpy() for o in outs], tuned
+
+
+@pytest.mark.parametrize("learned", [0, 1])
+def test_waves_graphs_and_shapes_do_not_change_results(torch_cuda, product_lib, profiles, rooms, learned):
+    """Waves of 700 paths, small grids, direct launches instead of the recorded frame graph, and the
+    autotuner's choice all give the default render's image."""
+    prof = profiles[0]
+    views = _views()
+    opts = dict(OPTS, learned_proposal=learned, learned_proposal_prob=0.5)
+    ref, _ = _render_set(torch_cuda, rooms, prof, views, 2, 2, opts)
+    variants = [dict(shape=(700, 1, 1, 1)), dict(shape=(0, 2, 1, 2)), dict(tune=True)]
+    nograph = dict(opts, flags=capi.OPTION_NO_GRAPH)
+    outs = [_render_set(torch_cuda, rooms, prof, views, 2, 2, opts, **v) for v in variants]
+    outs.append(_render_set(torch_cuda, rooms, prof, views, 2, 2, nograph))
+    for (imgs, tuned) in outs:
+        if tuned is not None:
+            print("tuned shape", tuned)
+        for a, b in zip(imgs, ref):
+            np.testing.assert_allclose(a, b, rtol=RTOL, atol=ATOL * max(1.0, np.abs(b).mean()))
