@@ -380,11 +380,17 @@ plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint3
     PLT_CUDA(ctx, cudaEventCreate(&e0));
     PLT_CUDA(ctx, cudaEventCreate(&e1));
     uint32_t f = frame;
+    // a candidate with a new wave size first renders one untimed frame (its buffers are sized
+    // then); other candidates only re-record the frame graph, which the timed frames absorb
+    uint32_t warmedWave = 0xFFFFFFFFu;
     auto timeShape = [&](const plt::PtLaunch& L, float& ms) -> plt_status {
         ctx->launch = L;
-        plt_status s = renderViews(ctx, views, n_views, f, 1, stream);
-        if (s != PLT_OK) return s;
-        f += 1;
+        plt_status s = PLT_OK;
+        if (L.waveCap != warmedWave) {
+            if ((s = renderViews(ctx, views, n_views, f, 1, stream)) != PLT_OK) return s;
+            f += 1;
+            warmedWave = L.waveCap;
+        }
         if (cudaEventRecord(e0, st) != cudaSuccess) return PLT_CUDA_ERROR;
         if ((s = renderViews(ctx, views, n_views, f, frames, stream)) != PLT_OK) return s;
         f += frames;
@@ -405,6 +411,12 @@ plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint3
     };
     for (uint32_t w : {1u << 22, 1u << 21, 1u << 20, 1u << 19, 1u << 18})
         if (w < total) tryShape(plt::PtLaunch{w, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
+    if (s == PLT_OK && bestL.waveCap != warmedWave) {   // the remaining candidates use the best wave size
+        ctx->launch = bestL;
+        s = renderViews(ctx, views, n_views, f, 1, stream);
+        f += 1;
+        warmedWave = bestL.waveCap;
+    }
     for (uint32_t b : {2u, 4u}) tryShape(plt::PtLaunch{bestL.waveCap, b, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
     for (uint32_t b : {1u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, b, bestL.walkBlocksPerSM});
     for (uint32_t b : {1u, 2u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, b});
