@@ -294,6 +294,10 @@ class PLTContext:
         capi.check(self.lib.plt_proposal_forward(self.handle, x.shape[0], _ptr(x), _ptr(out), None), "plt_proposal_forward")
         return out
 
+    def proposal_adam_step(self, grad, lr=1e-3):
+        """One Adam step of the proposal with a device gradient [11488] (e.g. a rank-averaged one)."""
+        capi.check(self.lib.plt_proposal_adam_step(self.handle, _ptr(grad), lr, None), "plt_proposal_adam_step")
+
     def proposal_train(self, steps, batch=65536, lr=1e-3, seed=1):
         hist = np.zeros(steps, np.float32)
         capi.check(self.lib.plt_proposal_train(self.handle, steps, batch, lr, seed, hist.ctypes.data_as(C.POINTER(C.c_float)), None),

@@ -91,3 +91,28 @@ def test_training_reduces_loss(ctx):
     assert last < first - 0.05 * abs(first), (first, last)
     p = ctx.proposal_params()
     assert np.isfinite(p).all()
+
+
+def test_data_parallel_training_single_rank(torch_cuda, product_lib, profiles):
+    """The host-side data-parallel loop (pltfalcor_gb300.distributed) with one gloo rank: library
+    gradient, rank average, library Adam step; the loss falls as with plt_proposal_train."""
+    import socket
+    import torch.distributed as dist
+    from pltfalcor_gb300 import distributed as D
+    from pltfalcor_gb300 import scene as S
+    from pltfalcor_gb300.bsdf import PLTContext
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=0, world_size=1)
+    try:
+        c = PLTContext()
+        c.set_spectral_profiles(profiles[0])
+        c.set_materials(S.small_scene().records)
+        c.proposal_init(9)
+        hist = D.train_proposal_data_parallel(c, 40, 16384, 1e-3, 3, dist)
+        c.close()
+    finally:
+        dist.destroy_process_group()
+    assert np.isfinite(hist).all()
+    assert hist[-5:].mean() < hist[:5].mean() - 0.05 * abs(hist[:5].mean())
