@@ -349,12 +349,14 @@ plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uin
  * are processed in waves of at most wave_paths paths (0 = one wave; smaller waves bound the path
  * state and bounce records and keep them cache-resident between the sample and solve passes), and
  * the segment, solve and manifold-walk kernels run with the given blocks of 128 per SM (0 = the
- * occupancy limit).  Results do not depend on the shape.  plt_render_tune times a coordinate
+ * occupancy limit).  The solve pass takes a large wave's paths sorted by length, longest first, so a
+ * warp's paths need similar work (path_order selects: see the field).  Results do not depend on the shape.  plt_render_tune times a coordinate
  * search over the shape on the caller's views (frames frame, frame + 1, ...; the views' outputs are
  * overwritten), keeps the fastest for later renders and returns it with its time per frame. */
 typedef struct plt_launch_shape {
     uint32_t wave_paths;
     uint32_t segment_blocks_per_sm, solve_blocks_per_sm, walk_blocks_per_sm;
+    uint32_t path_order;                /* 0: longest first for waves of >= 2^18 paths; 1: path order; 2: always longest first */
 } plt_launch_shape;
 plt_status plt_set_launch_shape(plt_context* ctx, const plt_launch_shape* shape);   /* NULL = defaults */
 plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape);

@@ -234,15 +234,15 @@ class PLTContext:
             arr[i].out_rgba = _ptr(out)
         return arr
 
-    def set_launch_shape(self, wave_paths=0, segment=0, solve=0, walk=0):
-        sh = capi.LaunchShape(wave_paths, segment, solve, walk)
+    def set_launch_shape(self, wave_paths=0, segment=0, solve=0, walk=0, path_order=0):
+        sh = capi.LaunchShape(wave_paths, segment, solve, walk, path_order)
         capi.check(self.lib.plt_set_launch_shape(self.handle, C.byref(sh)), "plt_set_launch_shape")
 
     def launch_shape(self):
         sh = capi.LaunchShape()
         capi.check(self.lib.plt_get_launch_shape(self.handle, C.byref(sh)), "plt_get_launch_shape")
         return {"wave_paths": sh.wave_paths, "segment": sh.segment_blocks_per_sm, "solve": sh.solve_blocks_per_sm,
-                "walk": sh.walk_blocks_per_sm}
+                "walk": sh.walk_blocks_per_sm, "path_order": sh.path_order}
 
     def render_tune(self, views, frame=0, frames=1, stream=None):
         """plt_render_tune over views (as render_scenes); returns (shape dict, ms per frame)."""

@@ -88,7 +88,7 @@ class RenderView(C.Structure):
 
 class LaunchShape(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("segment_blocks_per_sm", C.c_uint32), ("solve_blocks_per_sm", C.c_uint32),
-                ("walk_blocks_per_sm", C.c_uint32)]
+                ("walk_blocks_per_sm", C.c_uint32), ("path_order", C.c_uint32)]
 
 
 MATERIAL_FLAG_DOUBLE_SIDED = 0x1

@@ -86,6 +86,7 @@ struct PtScene {
 struct PtLaunch {
     uint32_t waveCap;
     uint32_t segBlocksPerSM, solveBlocksPerSM, walkBlocksPerSM;
+    uint32_t noLengthSort;        // solve-pass order: 0 sorted by length for waves >= 2^18 paths, 1 path order, 2 always sorted
 };
 
 struct PtParams {
@@ -140,6 +141,9 @@ struct PtParams {
     uint32_t* queue0;             // [npix]
     uint32_t* queue1;             // [npix]
     uint32_t* qcount;             // [maxBounces + 2]
+    uint32_t* lenCount;           // [maxBounces + 1] paths per length (solve-pass order)
+    uint32_t* lenCursor;          // [maxBounces + 1]
+    const uint32_t* order;        // solve-pass path order (longest paths first), or null = path order
     // bounce buffer, planes [maxBounces + 1][npix] (two planes per bounce for bary / encoded wi)
     uint32_t* bPrim;
     float* bBary;

@@ -6,6 +6,11 @@
 #define PLT_PT_SAMPLE_PASS
 #include "plt_pt.cuh"
 
+namespace pltdev {
+__global__ void ptLenCountKernel(const PtParams P);
+__global__ void ptLenScatterKernel(const PtParams P, uint32_t* __restrict__ order);
+}  // namespace pltdev
+
 namespace plt {
 
 // the analytic tracer's segment kernel (PLT_BOUNCE_PHASED selects the learned kernel's phased
@@ -20,7 +25,8 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 // launches over the compacted queues, then the solve pass and its manifold-walk wavefront.
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
     if (p.nWave == 0) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (p.maxBounces + 3), stream);   // + manifold-walk count
+    // queue lengths, the manifold-walk count, the length histogram and its cursors
+    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (3 * (p.maxBounces + 1) + 2), stream);
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
@@ -45,12 +51,23 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
         for (uint32_t it = 0; it <= p.maxBounces; ++it) kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    PtParams q = p;
+    q.order = nullptr;
+    // path_order 0: sort waves of at least 2^18 paths (small waves are latency-bound and keep the
+    // pixel order's coherence); 1: never; 2: always
+    const bool sort = L.noLengthSort == 2u || (L.noLengthSort == 0u && p.nWave >= (1u << 18));
+    if (sort) {   // the segment queues are free again: queue0 takes the solve order
+        const uint32_t grid = std::min<uint32_t>((p.nWave + 255) / 256, (uint32_t)numSMs * 4);
+        pltdev::ptLenCountKernel<<<grid, 256, 0, stream>>>(p);
+        pltdev::ptLenScatterKernel<<<grid, 256, 0, stream>>>(p, p.queue0);
+        q.order = p.queue0;
+    }
     switch (p.hwss) {
-    case 1: return pltdev::launchSolveH<1>(p, L, numSMs, stream);
-    case 2: return pltdev::launchSolveH<2>(p, L, numSMs, stream);
-    case 3: return pltdev::launchSolveH<3>(p, L, numSMs, stream);
-    case 4: return pltdev::launchSolveH<4>(p, L, numSMs, stream);
-    case 8: return pltdev::launchSolveH<8>(p, L, numSMs, stream);
+    case 1: return pltdev::launchSolveH<1>(q, L, numSMs, stream);
+    case 2: return pltdev::launchSolveH<2>(q, L, numSMs, stream);
+    case 3: return pltdev::launchSolveH<3>(q, L, numSMs, stream);
+    case 4: return pltdev::launchSolveH<4>(q, L, numSMs, stream);
+    case 8: return pltdev::launchSolveH<8>(q, L, numSMs, stream);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -68,6 +85,43 @@ __global__ void ptResolveKernel(const PtParams P, double inv) {
         out[1] = (float)(P.accum[3 * (size_t)i + 1] * inv);
         out[2] = (float)(P.accum[3 * (size_t)i + 2] * inv);
         out[3] = 1.f;
+    }
+}
+
+// Solve-pass order of a wave's paths: a counting sort by path length, longest first, so that the
+// lanes of a warp replay paths of similar length.  Pass 1 counts lengths; pass 2 gives every
+// block a contiguous range of paths, reserves its share of each length's slots and scatters.
+constexpr uint32_t kMaxLengths = 65;   // max_bounces <= 64
+__global__ void __launch_bounds__(256) ptLenCountKernel(const PtParams P) {
+    __shared__ uint32_t h[kMaxLengths];
+    const uint32_t nb = P.maxBounces + 1;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nWave; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[min(P.plen[i], P.maxBounces)], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+        if (h[b]) atomicAdd(P.lenCount + b, h[b]);
+}
+__global__ void __launch_bounds__(256) ptLenScatterKernel(const PtParams P, uint32_t* __restrict__ order) {
+    __shared__ uint32_t h[kMaxLengths], base[kMaxLengths];
+    const uint32_t nb = P.maxBounces + 1;
+    const uint32_t per = (P.nWave + gridDim.x - 1) / gridDim.x;
+    const uint32_t begin = min(blockIdx.x * per, P.nWave), end = min(begin + per, P.nWave);
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[min(P.plen[i], P.maxBounces)], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
+        uint32_t start = 0;   // longer lengths come first
+        for (uint32_t b2 = b + 1; b2 < nb; ++b2) start += P.lenCount[b2];
+        base[b] = start + (h[b] ? atomicAdd(P.lenCursor + b, h[b]) : 0u);
+        h[b] = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t b = min(P.plen[i], P.maxBounces);
+        order[base[b] + atomicAdd(&h[b], 1u)] = i;
     }
 }
 

@@ -1258,7 +1258,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     TraceCounters tc{0u, 0u, 0u, 0u};
     uint32_t evals = 0;
     MSData ms;
-    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < P.nWave; pid += gridDim.x * blockDim.x) {
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.nWave; slot += gridDim.x * blockDim.x) {
+        const uint32_t pid = P.order ? P.order[slot] : slot;
         const uint32_t gp = P.pidBase + pid;
         const PtScene& S = P.scenes[sceneOf(P, gp)];
         const int32_t root = (int32_t)S.root;

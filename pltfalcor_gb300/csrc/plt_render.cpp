@@ -38,7 +38,7 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     ctx->ptBytes = 0;
     const size_t n = npix, nb = (size_t)maxB + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al((nb + 2) * 4);
+    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al((3 * nb + 2) * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
     PLT_CUDA(ctx, cudaMalloc(&ctx->dPt, total));
@@ -58,8 +58,11 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.plen = (uint32_t*)take(n * 4);
     P.queue0 = (uint32_t*)take(n * 4);
     P.queue1 = (uint32_t*)take(n * 4);
-    P.qcount = (uint32_t*)take((nb + 2) * 4);   // per-segment queue lengths + the manifold-walk task count
+    // per-segment queue lengths, the manifold-walk task count, the path-length histogram and cursors
+    P.qcount = (uint32_t*)take((3 * nb + 2) * 4);
     P.mneeCount = P.qcount + nb + 1;
+    P.lenCount = P.qcount + nb + 2;
+    P.lenCursor = P.lenCount + nb;
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
     P.bPrim = (uint32_t*)take(nb * n * 4);
@@ -355,14 +358,16 @@ plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uin
 
 plt_status plt_set_launch_shape(plt_context* ctx, const plt_launch_shape* shape) {
     if (!ctx) return PLT_INVALID_ARG;
-    ctx->launch = shape ? plt::PtLaunch{shape->wave_paths, shape->segment_blocks_per_sm, shape->solve_blocks_per_sm, shape->walk_blocks_per_sm}
+    ctx->launch = shape ? plt::PtLaunch{shape->wave_paths, shape->segment_blocks_per_sm, shape->solve_blocks_per_sm, shape->walk_blocks_per_sm,
+                                        shape->path_order}
                         : plt::PtLaunch{};
     return PLT_OK;
 }
 
 plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape) {
     if (!ctx || !shape) return PLT_INVALID_ARG;
-    *shape = plt_launch_shape{ctx->launch.waveCap, ctx->launch.segBlocksPerSM, ctx->launch.solveBlocksPerSM, ctx->launch.walkBlocksPerSM};
+    *shape = plt_launch_shape{ctx->launch.waveCap, ctx->launch.segBlocksPerSM, ctx->launch.solveBlocksPerSM, ctx->launch.walkBlocksPerSM,
+                              ctx->launch.noLengthSort};
     return PLT_OK;
 }
 
@@ -410,21 +415,22 @@ plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint3
         }
     };
     for (uint32_t w : {1u << 22, 1u << 21, 1u << 20, 1u << 19, 1u << 18})
-        if (w < total) tryShape(plt::PtLaunch{w, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
+        if (w < total) tryShape(plt::PtLaunch{w, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM, 0u});
     if (s == PLT_OK && bestL.waveCap != warmedWave) {   // the remaining candidates use the best wave size
         ctx->launch = bestL;
         s = renderViews(ctx, views, n_views, f, 1, stream);
         f += 1;
         warmedWave = bestL.waveCap;
     }
-    for (uint32_t b : {2u, 4u}) tryShape(plt::PtLaunch{bestL.waveCap, b, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM});
-    for (uint32_t b : {1u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, b, bestL.walkBlocksPerSM});
-    for (uint32_t b : {1u, 2u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, b});
+    for (uint32_t b : {2u, 4u}) tryShape(plt::PtLaunch{bestL.waveCap, b, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM, 0u});
+    for (uint32_t b : {1u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, b, bestL.walkBlocksPerSM, 0u});
+    for (uint32_t b : {1u, 2u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, b, 0u});
+    for (uint32_t o : {1u, 2u}) tryShape(plt::PtLaunch{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM, o});
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ctx->launch = bestL;
     if (s != PLT_OK) return s;
-    if (best) *best = plt_launch_shape{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM};
+    if (best) *best = plt_launch_shape{bestL.waveCap, bestL.segBlocksPerSM, bestL.solveBlocksPerSM, bestL.walkBlocksPerSM, bestL.noLengthSort};
     if (best_ms) *best_ms = bestMs;
     return PLT_OK;
 }

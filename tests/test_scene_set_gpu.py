@@ -159,7 +159,7 @@ def test_waves_graphs_and_shapes_do_not_change_results(torch_cuda, product_lib, 
     views = _views()
     opts = dict(OPTS, learned_proposal=learned, learned_proposal_prob=0.5)
     ref, _ = _render_set(torch_cuda, rooms, prof, views, 2, 2, opts)
-    variants = [dict(shape=(700, 1, 1, 1)), dict(shape=(0, 2, 1, 2)), dict(tune=True)]
+    variants = [dict(shape=(700, 1, 1, 1, 2)), dict(shape=(0, 2, 1, 2, 1)), dict(shape=(0, 0, 0, 0, 2)), dict(tune=True)]
     nograph = dict(opts, flags=capi.OPTION_NO_GRAPH)
     outs = [_render_set(torch_cuda, rooms, prof, views, 2, 2, opts, **v) for v in variants]
     outs.append(_render_set(torch_cuda, rooms, prof, views, 2, 2, nograph))
