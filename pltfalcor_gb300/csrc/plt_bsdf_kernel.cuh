@@ -116,20 +116,33 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
 
     const uint32_t n = P.q.n;
     const uint32_t nTiles = (n + kBatchTile - 1) / kBatchTile;
-    const uint32_t totalUnits = nTiles * kUnitsPerTile;
+    // With PLT_SHADE_SPLIT_OPS each requested operation is its own slot-major pass over a group
+    // (eval, then pdf, lambdaPdf, sample): a warp runs one operation of one material at a time,
+    // a smaller code footprint per unit for the instruction caches, at the price of re-reading the
+    // group's L2-resident inputs once per operation.
+#if PLT_SHADE_SPLIT_OPS
+    uint32_t opList[4], nOps = 0;
+    for (uint32_t o : {PLT_OP_EVAL, PLT_OP_PDF, PLT_OP_LAMBDA_PDF, PLT_OP_SAMPLE})
+        if (P.ops & o) opList[nOps++] = o;
+#else
+    const uint32_t opList[1] = {0xFFFFFFFFu}, nOps = 1;
+#endif
+    const uint32_t totalUnits = nTiles * kUnitsPerTile * nOps;
     for (;;) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(P.unitCounter, 1u);
         u = __shfl_sync(0xFFFFFFFFu, u, 0);
         if (u >= totalUnits) break;
-        const uint32_t group = u / (kUnitsPerTile * kGroupTiles);
-        const uint32_t within = u - group * (kUnitsPerTile * kGroupTiles);
+        const uint32_t group = u / (kUnitsPerTile * kGroupTiles * nOps);
+        uint32_t within = u - group * (kUnitsPerTile * kGroupTiles * nOps);
         const uint32_t gTiles = min(kGroupTiles, nTiles - group * kGroupTiles);
+        const uint32_t op = within / (gTiles * kUnitsPerTile);
+        within -= op * (gTiles * kUnitsPerTile);
         const uint32_t slot = within / gTiles;
         const uint32_t tile = group * kGroupTiles + (within - slot * gTiles);
         const uint32_t base = tile * kBatchTile;
         const uint32_t idx = base + __ldg(P.perm + base + slot * 32u + lane);
-        if (idx < n) processQuery<H>(P, c, idx);
+        if (idx < n) processQuery<H>(P, c, idx, opList[op]);
     }
 }
 

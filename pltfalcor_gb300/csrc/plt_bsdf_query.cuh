@@ -122,10 +122,10 @@ PLT_DI void lambdaPdfDispatch(uint32_t type, const DevMaterial* __restrict__ m, 
 }
 
 template <int H>
-__device__ __forceinline__ void processQuery(const BatchParams& P, const Ctx& c, uint32_t i) {
+__device__ __forceinline__ void processQuery(const BatchParams& P, const Ctx& c, uint32_t i, uint32_t opMask = 0xFFFFFFFFu) {
     const uint32_t n = P.q.n;
     const uint32_t mid = __ldg(P.q.material + i);
-    const uint32_t ops = P.ops;
+    const uint32_t ops = P.ops & opMask;
     const bool badId = mid >= P.nMats;
     const DevMaterial* __restrict__ m = P.mats + (badId ? 0u : mid);
     const uint32_t type = badId ? 0u : __ldg(&m->type);

@@ -177,6 +177,9 @@ constexpr int kShadeThreads = 128;     // shade CTA
 #define PLT_SHADE_MIN_BLOCKS 3   // 12 warps per SM, up to 170 registers: 4.15 G queries/s vs 4.05 at 4 blocks
 #endif
 constexpr int kShadeMinBlocks = PLT_SHADE_MIN_BLOCKS;
+#ifndef PLT_SHADE_SPLIT_OPS
+#define PLT_SHADE_SPLIT_OPS 0
+#endif
 
 // scratch bytes plt_bsdf_batch needs for n queries: the permutation, then the work counter
 constexpr size_t bsdfScratchBytes(uint32_t n) {
