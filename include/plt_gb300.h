@@ -252,6 +252,16 @@ plt_status plt_spectral_profile_from_samples(const float* wavelengths_nm, const 
                                              uint32_t count, float scale, int compute_icdf,
                                              plt_spectral_profile* out);
 
+/* Reads a .spd spectral table (wavelength nm, value per line; '#' and blank lines skipped; reading
+ * stops at the first other line, PiecewiseLinearSpectrum::fromFile, Utils/Color/Spectrum.cpp:89-111)
+ * and builds its SpectralProfile as plt_spectral_profile_from_samples.  Host path and pointer. */
+plt_status plt_spectral_profile_from_spd(const char* path, float scale, int compute_icdf, plt_spectral_profile* out);
+
+/* Writes an RGBA image ([height][width][4] floats, host) as an uncompressed scanline OpenEXR file,
+ * HALF channels when half != 0, else FLOAT (the reference's pass graph ends in an accumulated EXR
+ * capture, scripts/PLTPathTracer.py:19-27). */
+plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, uint32_t height, int half);
+
 /* Batched IMaterialInstance calls (see plt_bsdf_queries).  ops = PLT_OP_* mask.  One fused
  * launch serves every requested op; queries may mix materials in any order. */
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* queries,

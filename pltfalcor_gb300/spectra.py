@@ -48,3 +48,23 @@ def standard_profiles(lib=None):
 def metal_ids(metal_index):
     """(n, k) profile ids of METALS[metal_index] in standard_profiles()."""
     return 2 * metal_index, 2 * metal_index + 1
+
+
+def profile_from_spd(path, scale=1.0, compute_icdf=False, lib=None):
+    """plt_spectral_profile_from_spd: a SpectralProfile built from a .spd table file."""
+    import ctypes as C
+    lib = lib or capi.load_library()
+    out = capi.SpectralProfile()
+    capi.check(lib.plt_spectral_profile_from_spd(os.fsencode(path), scale, 1 if compute_icdf else 0, C.byref(out)),
+               "plt_spectral_profile_from_spd")
+    return out
+
+
+def write_exr(path, rgba, half=False, lib=None):
+    """plt_write_exr of a [height][width][4] float image (numpy or CPU tensor)."""
+    import ctypes as C
+    import numpy as np
+    lib = lib or capi.load_library()
+    a = np.ascontiguousarray(np.asarray(rgba, dtype=np.float32))
+    h, w = a.shape[:2]
+    capi.check(lib.plt_write_exr(os.fsencode(path), a.ctypes.data_as(C.POINTER(C.c_float)), w, h, 1 if half else 0), "plt_write_exr")
