@@ -217,6 +217,7 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0, size=1024):
                        "manifold NEE (2 occluders, 60 iterations, threshold 5e-5)" % (W, H),
            "status": int(st), "frames": frames, "ms_per_frame": ms, "paths_per_s": W * H / (ms * 1e-3),
            "e2e": {"paths_per_s": W * H / (ms_e2e * 1e-3), "d2h_bytes_per_frame": W * H * 16, "h2d_bytes_per_frame": 0},
+           "rays_per_s": (stats["bounces"] + stats["shadow_rays"]) / (ms * 1e-3),
            "bounces_per_path": stats["bounces"] / (W * H), "shadow_rays_per_path": stats["shadow_rays"] / (W * H),
            "bsdf_evals_per_path": stats["bsdf_evals"] / (W * H), "gpu_launches_per_frame": 8 + 1 + 2 + 1}
     ctx.close()
