@@ -204,6 +204,7 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0, size=1024):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / frames
     stats = ctx.render_stats()
+    counters = ctx.render_counters()
     host = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
@@ -218,6 +219,13 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0, size=1024):
            "status": int(st), "frames": frames, "ms_per_frame": ms, "paths_per_s": W * H / (ms * 1e-3),
            "e2e": {"paths_per_s": W * H / (ms_e2e * 1e-3), "d2h_bytes_per_frame": W * H * 16, "h2d_bytes_per_frame": 0},
            "rays_per_s": (stats["bounces"] + stats["shadow_rays"]) / (ms * 1e-3),
+           # traversal's algorithmic bytes per frame (64 per node visit + 48 per triangle test,
+           # counted by the kernels) over the frame time, against measured HBM bandwidth; the BVH
+           # (38 MB nodes + 50 MB triangles) is mostly L2-resident, so this is a bound, not a limit
+           "roofline": {"bound": "hbm", "achieved": counters["traversal_bytes"] / (ms * 1e-3) / 1e9,
+                        "peak": peaks()[0]["hbm_gbs"], "unit": "GB/s",
+                        "frac": counters["traversal_bytes"] / (ms * 1e-3) / 1e9 / peaks()[0]["hbm_gbs"],
+                        "traversal_bytes_per_frame": counters["traversal_bytes"], "kind": "traversal over the whole frame"},
            "bounces_per_path": stats["bounces"] / (W * H), "shadow_rays_per_path": stats["shadow_rays"] / (W * H),
            "bsdf_evals_per_path": stats["bsdf_evals"] / (W * H), "gpu_launches_per_frame": 8 + 1 + 2 + 1}
     ctx.close()
@@ -381,6 +389,65 @@ def scene_set_bench(dev, stream, count=64, frames=2):
             "paths_per_s_batched": paths / (ms_batched * 1e-3), "rays_per_s_batched": rays / (ms_batched * 1e-3),
             "rays_per_frame": int(rays), "launch_shape": shape, "tuned_ms_per_frame": tuned_ms,
             "scene_gen_s": gen_s, "load_s": load_s, "tune_s": tune_s}
+
+
+def config0_bench(dev, stream, steps=200, cpu_seconds=0.0):
+    """The reference's CPU-runnable case: the rough-dielectric eval + pdf batch, 65,536 queries,
+    seed 0 (wi, wo uniform on the upper hemisphere, IOR 1.5 with Cauchy B = 0.0042 um^2,
+    roughness 0.01-0.5, coherence area 5-50 um^2, unpolarised).  Inputs and outputs (5 MB) stay in
+    L2 between launches.  Roofline: 80 algorithmic bytes per query and the oracle-counted FP32 and
+    SFU operations (profiles/op_counts_rough_dielectric.json) against nominal rates at the clock."""
+    import torch
+    from pltfalcor_gb300 import capi, spectra
+    from pltfalcor_gb300 import workloads as W
+    from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
+    prof, _ = spectra.standard_profiles()
+    wl = W.rough_dielectric_batch(n=65536, seed=0, profiles=prof)
+    ctx = PLTContext()
+    ctx.set_spectral_profiles(prof)
+    ctx.set_materials(wl.records)
+    b = DeviceBatch(wl, device=dev)
+    ops = capi.OP_EVAL | capi.OP_PDF
+    q, r = b.queries(), b.results(ops)
+    for _ in range(10):
+        ctx.batch(q, r, ops, stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.batch(q, r, ops, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    st = ctx.check_status(stream)
+    ctx.close()
+    qps = wl.n / (ms * 1e-3)
+    out = {"workload": "rough_dielectric_batch: 65,536 eval+pdf queries, HWSS 1, seed 0", "status": int(st), "steps": steps,
+           "ms_per_batch": ms, "queries_per_s": qps, "algorithmic_bytes_per_query": 80,
+           "achieved_gbs": 80 * qps / 1e9}
+    pk, _ = peaks()
+    out["hbm_frac"] = out["achieved_gbs"] / pk["hbm_gbs"]
+    ops_path = os.path.join(ROOT, "profiles", "op_counts_rough_dielectric.json")
+    if os.path.exists(ops_path):
+        with open(ops_path) as f:
+            oc = json.load(f)
+        mhz = pk.get("sm_max_mhz", 2070.0)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak, sfu_peak = sms * 128 * 2 * mhz * 1e6 / 1e12, sms * 16 * mhz * 1e6 / 1e12
+        out["fp32_frac"] = oc["mean_fp_per_query"] * qps / 1e12 / fp32_peak
+        out["sfu_frac"] = oc["mean_sfu_per_query"] * qps / 1e12 / sfu_peak
+    if cpu_seconds > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.run(wl, ops=ops, threads=os.cpu_count())
+        done, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < cpu_seconds:
+            oracle.run(wl, ops=ops, threads=os.cpu_count())
+            done += wl.n
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done / dt, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "%d queries (the whole batch, repeated) in %.1f s, FP32 oracle, OpenMP" % (done, dt)}
+    return out
 
 
 def capi_options(overrides):
@@ -561,6 +628,7 @@ def run_ours(args):
                            "parallelism": "independent shards per GPU" if world > 1 else "1 GPU"},
                 "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": 2 * args.steps, "roofline": roof, "clocks": clocks}
+        line["config0"] = config0_bench(dev, stream, cpu_seconds=0.0 if (world > 1 or args.no_cpu_baseline) else 3.0)
         if not args.no_trace:
             line["trace"] = trace_bench(ctx, dev, stream, max(3, min(args.steps, 50)), max(1, args.warmup))
         if not args.no_render:

@@ -377,6 +377,11 @@ plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint3
  * shadow rays traced, forward-unwind BSDF evaluations). */
 plt_status plt_render_stats(plt_context* ctx, uint64_t* out4);
 
+/* Counters of the last frame of the last render (host pointer, the first n of: paths of all
+ * views, bounces recorded, shadow rays traced, forward-unwind BSDF evaluations, algorithmic
+ * traversal bytes = 64 per BVH node visited + 48 per triangle tested over all rays). */
+plt_status plt_render_counters(plt_context* ctx, uint64_t* out, uint32_t n);
+
 /* The bounce buffer of the last plt_render frame (Path.slang BounceData per path and bounce), for
  * inspection: host arrays [width*height][max_bounces+1] of the hit triangle (0xFFFFFFFF when the
  * record is absent or a miss), the sampled lobe and the RayFlags word; any may be NULL.

@@ -38,6 +38,17 @@ def main():
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)
     print(json.dumps(out, indent=1))
+    # the rough-dielectric eval + pdf batch (65,536 queries, seed 0), all of it
+    wl0 = W.rough_dielectric_batch(n=65536, seed=0, profiles=prof)
+    per0 = oracle.count_ops(wl0, ops=0x3)
+    tot0 = sum(v["count"] for v in per0.values())
+    mean0 = lambda k: sum(v[k] * v["count"] for v in per0.values()) / tot0
+    out0 = {"workload": "rough_dielectric_batch (65,536 queries, seed 0)", "ops": "eval+pdf",
+            "mean_fp_per_query": mean0("fp"), "mean_sfu_per_query": mean0("sfu"), "mean_div_per_query": mean0("div"),
+            "counting": out["counting"]}
+    with open(os.path.join(ROOT, "profiles", "op_counts_rough_dielectric.json"), "w") as f:
+        json.dump(out0, f, indent=1)
+    print(json.dumps(out0, indent=1))
 
 
 if __name__ == "__main__":

@@ -304,6 +304,11 @@ class PLTContext:
                    "plt_proposal_train")
         return hist
 
+    def render_counters(self):
+        out = (C.c_uint64 * 5)()
+        capi.check(self.lib.plt_render_counters(self.handle, out, 5), "plt_render_counters")
+        return {"paths": out[0], "bounces": out[1], "shadow_rays": out[2], "bsdf_evals": out[3], "traversal_bytes": out[4]}
+
     def render_stats(self):
         out = (C.c_uint64 * 4)()
         capi.check(self.lib.plt_render_stats(self.handle, out), "plt_render_stats")

@@ -108,7 +108,7 @@ EXPORTED_SYMBOLS = [
     "plt_proposal_init", "plt_proposal_set_params", "plt_proposal_get_params", "plt_proposal_generate",
     "plt_proposal_gradient", "plt_proposal_forward", "plt_proposal_adam_step", "plt_proposal_train",
     "plt_add_scene", "plt_clear_scenes", "plt_render_scenes", "plt_set_launch_shape", "plt_get_launch_shape", "plt_render_tune",
-    "plt_spectral_profile_from_spd", "plt_write_exr",
+    "plt_spectral_profile_from_spd", "plt_write_exr", "plt_render_counters",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -170,6 +170,7 @@ def load_library(path=LIB_PATH):
         "plt_render_tune": (i32, [vp, C.POINTER(RenderView), u32, u32, u32, C.POINTER(LaunchShape), C.POINTER(C.c_float), vp]),
         "plt_spectral_profile_from_spd": (i32, [C.c_char_p, C.c_float, i32, C.POINTER(SpectralProfile)]),
         "plt_write_exr": (i32, [C.c_char_p, C.POINTER(C.c_float), u32, u32, i32]),
+        "plt_render_counters": (i32, [vp, C.POINTER(C.c_uint64), u32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -85,6 +85,7 @@ struct plt_context {
     void* dMneeTasks = nullptr;   // deferred manifold walks of the solve pass
     size_t mneeBytes = 0;
     uint32_t ptNpix = 0, ptMaxB = 0;
+    uint64_t lastPaths = 0;       // paths of all views in the last render
     double* dAccum = nullptr;     // [paths of all views][3] frame accumulation
     uint32_t accumCap = 0;
     plt::PtLaunch launch{};       // launch shape (plt_render_tune; zeros = defaults)

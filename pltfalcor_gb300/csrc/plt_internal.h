@@ -163,7 +163,7 @@ struct PtParams {
     uint32_t* mneeCount;
     // outputs
     double* accum;                // [npix][3]
-    unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, paths
+    unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, traversal bytes
     uint32_t* status;
 };
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream);

@@ -418,6 +418,14 @@ PLT_DI f3 cameraDir(const PtScene& S, uint32_t px, uint32_t py) {
     return rnormalize(U * ndcx + V * ndcy + W);
 }
 
+// Algorithmic traversal bytes of a thread's rays (64-byte nodes visited, 48-byte triangles
+// tested), summed per warp into the frame statistics (slot 3).
+PLT_DI void addTraversalBytes(const PtParams& P, uint32_t nodeVisits, uint32_t triTests) {
+    unsigned long long b = 64ull * nodeVisits + 48ull * triTests;
+    for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xFFFFFFFFu, b, o);
+    if ((threadIdx.x & 31u) == 0 && b) atomicAdd(P.stats + 3, b);
+}
+
 PLT_DI uint32_t warpAggregatedAdd(uint32_t* counter, bool pred) {
     const uint32_t mask = __ballot_sync(__activemask(), pred);
     const uint32_t lane = threadIdx.x & 31u;
@@ -669,6 +677,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
     unsigned long long r = recorded;
     for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, o);
     if ((threadIdx.x & 31u) == 0 && r) atomicAdd(P.stats, r);
+    addTraversalBytes(P, nv, tt);
 }
 
 // The analytic tracer's segment kernel: trace, Russian roulette and the sample in one pass per
@@ -793,6 +802,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
     unsigned long long r = recorded;
     for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, o);
     if ((threadIdx.x & 31u) == 0 && r) atomicAdd(P.stats, r);
+    addTraversalBytes(P, nv, tt);
 }
 
 #endif  // PLT_PT_SAMPLE_PASS
@@ -1447,6 +1457,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         if (s1) atomicAdd(P.stats + 1, s1);
         if (s2) atomicAdd(P.stats + 2, s2);
     }
+    addTraversalBytes(P, tc.nv, tc.tt);
 }
 
 
@@ -1521,6 +1532,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         if (s1) atomicAdd(P.stats + 1, s1);
         if (s2) atomicAdd(P.stats + 2, s2);
     }
+    addTraversalBytes(P, tc.nv, tc.tt);
 }
 
 template <int H>

@@ -275,6 +275,7 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.maxBeamOmega = o.sourcing_max_beam_omega;
     P.npix = npix;
     P.nTotal = total;
+    ctx->lastPaths = total;
     P.accum = ctx->dAccum;
     P.stats = ctx->dPtStats;
     P.status = ctx->dStatus;
@@ -435,6 +436,15 @@ plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint3
     return PLT_OK;
 }
 
+
+plt_status plt_render_counters(plt_context* ctx, uint64_t* out, uint32_t n) {
+    if (!ctx || (n && !out)) return PLT_INVALID_ARG;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    if (ctx->dPtStats) PLT_CUDA(ctx, cudaMemcpy(h, ctx->dPtStats, sizeof(h), cudaMemcpyDeviceToHost));
+    const uint64_t v[5] = {ctx->lastPaths, h[0], h[1], h[2], h[3]};
+    for (uint32_t i = 0; i < n && i < 5; ++i) out[i] = v[i];
+    return PLT_OK;
+}
 
 plt_status plt_render_stats(plt_context* ctx, uint64_t* out4) {
     if (!ctx || !out4) return PLT_INVALID_ARG;
