@@ -7,11 +7,11 @@
 //     class) in shared memory and writes the tile's permutation (16-bit local indices) to the
 //     scratch buffer; block 0 resets the shade kernel's work counter.
 //  2. shade: a persistent, barrier-free grid.  Each warp takes 32-query units from one global
-//     atomic counter.  Units are issued group by group (64 tiles = 131072 queries per group) and,
+//     atomic counter.  Units are issued group by group (128 tiles = 262144 queries per group) and,
 //     inside a group, slot-major: unit slot s of every tile before slot s + 1.  Slot s covers
 //     sorted positions [32 s, 32 s + 32) of its tile, which hold the same (material, lobe) class
-//     in every tile, so at any moment the whole GPU runs one material's code path (instruction
-//     cache and SIMT coherence) while the group's inputs and outputs (~17 MB) stay L2-resident
+//     in every tile, so at any moment the GPU runs one or two materials' code paths (instruction
+//     cache and SIMT coherence) while the group's inputs and outputs (~35 MB) stay L2-resident
 //     between the eight material passes (DRAM traffic stays one read of the inputs and one write
 //     of the outputs).  The spectral tables are staged into shared memory once per CTA by a bulk
 //     asynchronous copy on an mbarrier.
@@ -22,7 +22,14 @@ namespace pltdev {
 
 constexpr uint32_t kLobeClasses = 10;                  // lowest set lobe bit (0..7), 8: none, 9: unused
 constexpr uint32_t kBuckets = 16 * kLobeClasses;        // material type x lobe class
-constexpr uint32_t kGroupTiles = 64;
+// Tiles per group: ~1,800 warps are in flight, so a group of G tiles keeps about 1800 / G slots
+// (sorted positions x 32) busy at once; 128 tiles (262 K queries, 35 MB of inputs and outputs in
+// L2) keeps them within one or two material classes.  Measured on the mixed-material batch: 64
+// tiles 4.13, 128 tiles 4.84, 256 tiles 4.66, 512 tiles 3.38 G queries/s (beyond L2).
+#ifndef PLT_GROUP_TILES
+#define PLT_GROUP_TILES 128
+#endif
+constexpr uint32_t kGroupTiles = PLT_GROUP_TILES;
 constexpr uint32_t kUnitsPerTile = plt::kBatchTile / 32;
 
 PLT_DI uint32_t lobeClass(uint32_t lobe) {
