@@ -141,8 +141,8 @@ struct PtParams {
     uint32_t* queue0;             // [npix]
     uint32_t* queue1;             // [npix]
     uint32_t* qcount;             // [maxBounces + 2]
-    uint32_t* lenCount;           // [maxBounces + 1] paths per length (solve-pass order)
-    uint32_t* lenCursor;          // [maxBounces + 1]
+    uint32_t* lenCount;           // [16 (maxBounces + 1)] paths per solve-order key (length, first-hit type)
+    uint32_t* lenCursor;          // [16 (maxBounces + 1)]
     const uint32_t* order;        // solve-pass path order (longest paths first), or null = path order
     // bounce buffer, planes [maxBounces + 1][npix] (two planes per bounce for bary / encoded wi)
     uint32_t* bPrim;

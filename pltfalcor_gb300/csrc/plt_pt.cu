@@ -8,6 +8,7 @@
 
 namespace pltdev {
 __global__ void ptLenCountKernel(const PtParams P);
+__global__ void ptLenPrefixKernel(const PtParams P);
 __global__ void ptLenScatterKernel(const PtParams P, uint32_t* __restrict__ order);
 }  // namespace pltdev
 
@@ -25,8 +26,8 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 // launches over the compacted queues, then the solve pass and its manifold-walk wavefront.
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
     if (p.nWave == 0) return cudaSuccess;
-    // queue lengths, the manifold-walk count, the length histogram and its cursors
-    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * (3 * (p.maxBounces + 1) + 2), stream);
+    // queue lengths, the manifold-walk count, the solve-order key histogram and its cursors
+    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * ((p.maxBounces + 1) * (1 + 2 * 16) + 2), stream);
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
@@ -59,6 +60,7 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
     if (sort) {   // the segment queues are free again: queue0 takes the solve order
         const uint32_t grid = std::min<uint32_t>((p.nWave + 255) / 256, (uint32_t)numSMs * 4);
         pltdev::ptLenCountKernel<<<grid, 256, 0, stream>>>(p);
+        pltdev::ptLenPrefixKernel<<<1, 32, 0, stream>>>(p);
         pltdev::ptLenScatterKernel<<<grid, 256, 0, stream>>>(p, p.queue0);
         q.order = p.queue0;
     }
@@ -88,39 +90,58 @@ __global__ void ptResolveKernel(const PtParams P, double inv) {
     }
 }
 
-// Solve-pass order of a wave's paths: a counting sort by path length, longest first, so that the
-// lanes of a warp replay paths of similar length.  Pass 1 counts lengths; pass 2 gives every
-// block a contiguous range of paths, reserves its share of each length's slots and scatters.
-constexpr uint32_t kMaxLengths = 65;   // max_bounces <= 64
+// Solve-pass order of a wave's paths: a counting sort by (path length, material type of the first
+// hit), longest first, so that the lanes of a warp replay paths of similar length whose first
+// vertex (evaluated by every replay of the path) runs the same material code.  Pass 1 counts the
+// keys; pass 2 gives every block a contiguous range of paths, reserves its share of each key's
+// slots and scatters.
+constexpr uint32_t kSortTypes = 16;
+constexpr uint32_t kMaxKeys = 65 * kSortTypes;   // max_bounces <= 64
+__device__ __forceinline__ uint32_t solveKey(const PtParams& P, uint32_t i) {
+    const uint32_t len = min(P.plen[i], P.maxBounces);
+    const uint32_t prim = P.bPrim[i];   // record 0
+    uint32_t type = 0;
+    if (prim < P.nTris) type = min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), kSortTypes - 1);
+    // keys in solve order: longer paths first, then by type
+    return (P.maxBounces - len) * kSortTypes + type;
+}
 __global__ void __launch_bounds__(256) ptLenCountKernel(const PtParams P) {
-    __shared__ uint32_t h[kMaxLengths];
-    const uint32_t nb = P.maxBounces + 1;
-    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
+    __shared__ uint32_t h[kMaxKeys];
+    const uint32_t nk = (P.maxBounces + 1) * kSortTypes;
+    for (uint32_t b = threadIdx.x; b < nk; b += blockDim.x) h[b] = 0;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nWave; i += gridDim.x * blockDim.x)
-        atomicAdd(&h[min(P.plen[i], P.maxBounces)], 1u);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < P.nWave; i += gridDim.x * blockDim.x) atomicAdd(&h[solveKey(P, i)], 1u);
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+    for (uint32_t b = threadIdx.x; b < nk; b += blockDim.x)
         if (h[b]) atomicAdd(P.lenCount + b, h[b]);
 }
+// exclusive prefix of the key counts into the cursors (one small block)
+__global__ void __launch_bounds__(32) ptLenPrefixKernel(const PtParams P) {
+    if (threadIdx.x != 0) return;
+    const uint32_t nk = (P.maxBounces + 1) * kSortTypes;
+    uint32_t run = 0;
+    for (uint32_t b = 0; b < nk; ++b) {
+        P.lenCursor[b] = run;
+        run += P.lenCount[b];
+    }
+}
 __global__ void __launch_bounds__(256) ptLenScatterKernel(const PtParams P, uint32_t* __restrict__ order) {
-    __shared__ uint32_t h[kMaxLengths], base[kMaxLengths];
-    const uint32_t nb = P.maxBounces + 1;
+    __shared__ uint32_t h[kMaxKeys], base[kMaxKeys];
+    const uint32_t nk = (P.maxBounces + 1) * kSortTypes;
     const uint32_t per = (P.nWave + gridDim.x - 1) / gridDim.x;
     const uint32_t begin = min(blockIdx.x * per, P.nWave), end = min(begin + per, P.nWave);
-    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
+    for (uint32_t b = threadIdx.x; b < nk; b += blockDim.x) h[b] = 0;
     __syncthreads();
-    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[min(P.plen[i], P.maxBounces)], 1u);
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[solveKey(P, i)], 1u);
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
-        uint32_t start = 0;   // longer lengths come first
-        for (uint32_t b2 = b + 1; b2 < nb; ++b2) start += P.lenCount[b2];
-        base[b] = start + (h[b] ? atomicAdd(P.lenCursor + b, h[b]) : 0u);
+    // each key's cursor starts at the key's first slot (ptLenPrefixKernel)
+    for (uint32_t b = threadIdx.x; b < nk; b += blockDim.x) {
+        base[b] = h[b] ? atomicAdd(P.lenCursor + b, h[b]) : 0u;
         h[b] = 0;
     }
     __syncthreads();
     for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
-        const uint32_t b = min(P.plen[i], P.maxBounces);
+        const uint32_t b = solveKey(P, i);
         order[base[b] + atomicAdd(&h[b], 1u)] = i;
     }
 }
