@@ -317,6 +317,24 @@ typedef struct plt_camera {
 plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width, uint32_t height, uint32_t frame_begin,
                       uint32_t frame_count, float* out_rgba, void* stream);
 
+/* Environment light: replaces Scene::setEnvMap / EnvMap (Scene/Lights/EnvMap.cpp:60-126,
+ * EnvMap.slang) and EnvMapSampler (Rendering/Lights/EnvMapSampler.cpp:85-120,
+ * EnvMapSampler.slang).  pixels: host [height][width][channels] linear RGB(A) lat-long map (the
+ * map is centred on -z, world_to_latlong_map), values finite and >= 0; intensity >= 0; tint (3, or
+ * NULL = white) and rotation_deg (Euler XYZ degrees, or NULL = none) as EnvMap's setTint /
+ * setRotation.  Builds the sampler's 512 x 512 importance map on the device.  With options
+ * use_env_light (default 1), plt_render and plt_render_scenes then sample the map in NEE
+ * (light-type selection between the map and emissive geometry, LightSampling.slangh:40-206) and
+ * add it on escaped paths (onMiss, pltpt_solve.rt.slang:374-395), for every scene of the context. */
+plt_status plt_set_env_map(plt_context* ctx, const float* pixels, uint32_t width, uint32_t height, uint32_t channels,
+                           float intensity, const float* tint, const float* rotation_deg);
+plt_status plt_clear_env_map(plt_context* ctx);
+/* The sampler on given inputs (device arrays; for tests): for each i, sample(u[2i], u[2i+1]) and
+ * the map's eval / evalPdf at the sampled direction and at dirs[3i..3i+2] (dirs may be NULL).
+ * out[12i..12i+11] = sampled direction (3), its pdf, eval rgb (3), evalPdf, eval rgb of dirs[i]
+ * (3), evalPdf of dirs[i].  PLT_INVALID_ARG without an environment map. */
+plt_status plt_env_map_query(plt_context* ctx, const float* u, const float* dirs, uint32_t n, float* out, void* stream);
+
 /* Scene sets (no counterpart in the reference, whose PLTPT renders the one loaded scene): several
  * independent scenes held by one context share its materials and spectral profiles, and
  * plt_render_scenes renders any number of views of them in one wavefront per frame (all scenes'

@@ -174,10 +174,41 @@ class _Scene(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("n_materials", C.c_uint32), ("n_profiles", C.c_uint32),
                 ("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("indices", C.c_void_p),
                 ("tri_material", C.c_void_p), ("tri_instance", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p),
-                ("proposal_params", C.c_void_p)]
+                ("proposal_params", C.c_void_p), ("env", C.c_void_p)]
 
 
-def _scene_struct(scene, profiles, proposal_params=None):
+class _Env(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("intensity", C.c_float),
+                ("tint", C.c_float * 3), ("rotation_deg", C.c_float * 3)]
+
+
+def _env_struct(env):
+    """env: dict(rgb=[height][width][3 or 4] array, intensity=1, tint=(1, 1, 1), rotation=(0, 0, 0))."""
+    if env is None:
+        return None, None
+    rgb = np.ascontiguousarray(np.asarray(env["rgb"], np.float32)[..., :3])
+    e = _Env(rgb.ctypes.data, rgb.shape[1], rgb.shape[0], float(env.get("intensity", 1.0)),
+             (C.c_float * 3)(*[float(x) for x in env.get("tint", (1.0, 1.0, 1.0))]),
+             (C.c_float * 3)(*[float(x) for x in env.get("rotation", (0.0, 0.0, 0.0))]))
+    return e, rgb
+
+
+def env_query(env, u, dirs=None):
+    """The oracle's environment sampler on given inputs: [n][12] as plt_env_map_query."""
+    lib = load()
+    lib.plto_env_query.restype = C.c_int
+    lib.plto_env_query.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    e, keep = _env_struct(env)
+    u = np.ascontiguousarray(u, np.float32).reshape(-1, 2)
+    d = None if dirs is None else np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    out = np.zeros((len(u), 12), np.float32)
+    st = lib.plto_env_query(C.addressof(e), u.ctypes.data, None if d is None else d.ctypes.data, len(u), out.ctypes.data)
+    if st != 0:
+        raise RuntimeError("plto_env_query failed: %d" % st)
+    return out
+
+
+def _scene_struct(scene, profiles, proposal_params=None, env=None):
     keep = [np.ascontiguousarray(scene.vertices, np.float32), np.ascontiguousarray(scene.normals, np.float32),
             np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
             np.ascontiguousarray(scene.records)]
@@ -189,14 +220,18 @@ def _scene_struct(scene, profiles, proposal_params=None):
                C.cast(profiles, C.c_void_p) if profiles is not None else None)
     pp = None if proposal_params is None else np.ascontiguousarray(proposal_params, np.float32)
     s.proposal_params = None if pp is None else pp.ctypes.data
-    return s, (keep, tan, inst, profiles, pp)
+    e, erg = _env_struct(env)
+    s.env = None if e is None else C.addressof(e)
+    return s, (keep, tan, inst, profiles, pp, e, erg)
 
 
-def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1, proposal_params=None):
+def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1, proposal_params=None,
+           env=None):
     """FP32 oracle render of one frame: rgb [height][width][3]; with records=True also per-path bounce
     records (prim, lobe, flags) [height*width][max_bounces+1] and stats (paths, shadow rays, evals).
     `profiles` is a ctypes array of plt_spectral_profile, `camera`/`options` the ctypes structs of
-    include/plt_gb300.h; `proposal_params` (11488 floats) the network of learned_proposal renders."""
+    include/plt_gb300.h; `proposal_params` (11488 floats) the network of learned_proposal renders;
+    `env` the environment light (dict of rgb, intensity, tint, rotation)."""
     lib = load()
     if not hasattr(lib, "_render_sig"):
         lib.plto_render.restype = C.c_int
@@ -204,7 +239,7 @@ def render(scene, profiles, camera, options, width, height, frame=0, threads=0, 
         lib.plto_light_table.restype = C.c_uint32
         lib.plto_light_table.argtypes = [C.c_void_p] * 4
         lib._render_sig = True
-    s, keep = _scene_struct(scene, profiles, proposal_params)
+    s, keep = _scene_struct(scene, profiles, proposal_params, env)
     rgb = np.zeros((height, width, 3), np.float32)
     nb = options.max_bounces + 1
     recs = [np.zeros((height * width, nb), np.uint32) for _ in range(3)] if records else [None] * 3

@@ -7,6 +7,7 @@
 // the light-type selection always picks emissive geometry (LightSampling.slangh:40-90).
 #include "plt_oracle.hpp"
 #include "plt_oracle_bsdf.hpp"
+#include "plt_oracle_env.hpp"
 #include "plt_oracle_geom.hpp"
 #include "plt_oracle_mlp.hpp"
 
@@ -71,6 +72,8 @@ struct Scene {
     // learned proposal: network (bf16-rounded) and per-material (roughness, pitch, class, enabled)
     std::unique_ptr<plt_oracle_mlp::Net> net;
     std::vector<float> matFeat;        // [nmat][4]
+    // environment light (EnvMap + EnvMapSampler), when present
+    plt_oracle_env::EnvMap env;
 };
 
 struct Options {
@@ -82,6 +85,7 @@ struct Options {
     float mneeThreshold;
     bool learned = false;
     float learnedProb = 0.5f;
+    bool useEnv = false;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -775,6 +779,26 @@ Beam<float> sourceBeamArea(F3 posW, F3 dir, float A, float dist, const float* Le
     b.distant = false;
     return b;
 }
+// pltSourceBeamDistant (PLT.slang:253-267): diffusivity min(solidAngle, maxOmega) I, coherence
+// radius 1 mm, distant for the beam's whole life
+Beam<float> sourceBeamDistant(F3 dir, float solidAngle, const float* Le, const float* wl, uint32_t H, float maxBeamOmega) {
+    solidAngle = std::min(solidAngle, maxBeamOmega);
+    Beam<float> b;
+    b.H = (int)H;
+    for (uint32_t j = 0; j < H; ++j) {
+        b.L[0][j] = Le[j];
+        b.L[1][j] = b.L[2][j] = b.L[3][j] = 0.f;
+        b.wl[j] = wl[j];
+        b.spdf[j] = 1.f;
+    }
+    b.D[0] = solidAngle; b.D[1] = 0.f; b.D[2] = solidAngle;
+    b.r_m = 1e-3f;
+    b.posW = {0.f, 0.f, 0.f};
+    b.r = dir;
+    b.t = perp_stark(dir);
+    b.distant = true;
+    return b;
+}
 void propagate(Beam<float>& b, F3 p) {
     if (!b.distant) b.r_m += length(p - b.posW);
     b.posW = p;
@@ -1015,6 +1039,17 @@ struct Renderer {
         if (std::isfinite(L.x) && std::isfinite(L.y) && std::isfinite(L.z)) sv.Lrgb = sv.Lrgb + L;
     }
 
+    // getLightTypeSelectionProbabilities (LightSampling.slangh:40-55): env map, emissive geometry
+    // (the scene's emissive lights when it has any), no analytic lights
+    void typeProbabilities(float& pEnv, float& pEm) const {
+        const bool useEnv = o.useEnv && s.env.present;
+        const bool useEm = o.useEmissive && !s.lightTri.empty();
+        const float sum = (useEnv ? 1.f : 0.f) + (useEm ? 1.f : 0.f);
+        const float inv = sum > 0.f ? 1.f / sum : 0.f;
+        pEnv = useEnv ? inv : 0.f;
+        pEm = useEm ? inv : 0.f;
+    }
+
     // evalTrianglePdf (EmissiveLightSamplerHelpers.slang:120-151) x triangle selection pdf
     // (EmissivePowerSampler.slang:90-122)
     float emissivePdf(F3 posW, uint32_t light, F3 hitPos, F3 hitNormal) const {
@@ -1043,11 +1078,49 @@ struct Renderer {
         ls.beam.H = (int)o.hwss;
         for (int c = 0; c < 4; ++c) for (int j = 0; j < MAXH; ++j) ls.beam.L[c][j] = 0.f;
         for (int j = 0; j < MAXH; ++j) { ls.beam.wl[j] = 0.f; ls.beam.spdf[j] = 1.f; }
-        // selectLightType: probabilities (0, 1, 0) without env map and analytic lights
+        // selectLightType (LightSampling.slangh:40-84): the environment map and emissive geometry
         SampleGen& selSg = o.perTileSg ? sv.tilesg : sv.sg;
-        const float uType = selSg.next1D();
-        if (!o.useEmissive || !(uType < 1.f)) return false;
-        const float selectionPdf = 1.f;
+        float u = selSg.next1D();
+        float pEnv, pEm;
+        typeProbabilities(pEnv, pEm);
+        float selectionPdf;
+        bool envSel;
+        if (u < pEnv) {
+            envSel = true;
+            selectionPdf = pEnv;
+        } else {
+            u -= pEnv;
+            if (!(u < pEm)) return false;
+            envSel = false;
+            selectionPdf = pEm;
+        }
+        if (envSel) {
+            // generateEnvMapSample (LightSampling.slangh:86-104)
+            const float u0 = sv.sg.next1D();
+            const float u1 = sv.sg.next1D();
+            float d[3], pdf;
+            s.env.sample(u0, u1, d, pdf);
+            float swl[MAXH], rad[3], L[MAXH];
+            for (int j = 0; j < MAXH; ++j) { swl[j] = 0.f; L[j] = 0.f; }
+            hwssWavelengths(sv.wavelength, o.hwss, swl);
+            const F3 dir = f3(d);
+            s.env.eval(d, rad);
+            bool anyPos = false;
+            for (uint32_t j = 0; j < o.hwss; ++j) {
+                const float le = rgbToSpectrum(rad, swl[j]);
+                L[j] = pdf > 0.f ? le / pdf : 0.f;
+                anyPos = anyPos || L[j] > 0.f;
+            }
+            ls.beam = sourceBeamDistant(-dir, o.maxBeamOmega, L, swl, o.hwss, o.maxBeamOmega);
+            ls.pdf = pdf;
+            ls.origin = newRayOriginToward(sd, dir);
+            ls.distance = FLT_MAX;
+            ls.dir = dir;
+            ls.pdf *= selectionPdf;
+            scaleBeam(ls.beam, 1.f / selectionPdf);
+            const bool isReflection = dot(sd.faceN, ls.dir) * dot(sd.faceN, sd.V) > 0.f;
+            return anyPos && ls.pdf > 1e-6f && !(!sampleRefl && isReflection) && !(!sampleTrans && !isReflection);
+        }
         bool valid = false;
         const uint32_t nl = (uint32_t)s.lightTri.size();
         if (nl > 0) {
@@ -1270,14 +1343,16 @@ struct Renderer {
                     return;
             }
             const F3 origin = !currentVertexMS ? V.posW : sv.pathOrigin;
-            const bool mneeOk = manifoldNEESample(ls.origin, ls.dir, 0.f, ls.distance, origin, ls.beam.posW, lightDir, false,
+            const bool mneeOk = manifoldNEESample(ls.origin, ls.dir, 0.f, ls.distance, origin, ls.beam.posW, lightDir, ls.beam.distant,
                                                   maxMSBounces, sv.sg, ms, sv);
             if (!mneeOk || ms.pdf < 1e-6f) return;
             if (ms.hitCount > 0) {
                 if (!o.hwssMis && ms.dispersive) ls.beam.H = 1;
-                ls.dir = ms.woLastHitToLight;
-                ls.beam.r = -ms.woLastHitToLight;
-                ls.beam.t = perp_stark(ls.beam.r);
+                if (!ls.beam.distant) {
+                    ls.dir = ms.woLastHitToLight;
+                    ls.beam.r = -ms.woLastHitToLight;
+                    ls.beam.t = perp_stark(ls.beam.r);
+                }
                 scaleBeam(ls.beam, 1.f / ms.pdf);
                 manifoldForwardUnwind(ms, origin, ls.beam, sv);
                 if (currentVertexMS) {
@@ -1317,7 +1392,9 @@ struct Renderer {
         const bool needMIS = o.doMis && didNEE;
         const uint32_t light = s.primToLight[bounce.prim];
         const F3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
-        const float lightPdf = 1.f * emissivePdf(sv.pathOrigin, light, sd.posW, hn);
+        float pEnv, pEm;
+        typeProbabilities(pEnv, pEm);
+        const float lightPdf = pEm * emissivePdf(sv.pathOrigin, light, sd.posW, hn);
         const float misWeight = needMIS ? MISWeight(bounce.lastNonDeltaPdf, lightPdf) : 1.f;
         float Le[MAXH], swl[MAXH];
         for (int j = 0; j < MAXH; ++j) { Le[j] = 0.f; swl[j] = 0.f; }
@@ -1336,6 +1413,29 @@ struct Renderer {
         measure(sv, p, bounce.pathContribution, beam);
     }
 
+    // onMiss, pltpt_solve.rt.slang:374-395
+    void onMiss(Solve& sv, int p, const Bounce* bounces) const {
+        const Bounce& bounce = bounces[p];
+        const F3 wo = bounce.wi();
+        const bool didNEE = wasNEEAvailable(p, bounce.flags);
+        if (!(o.useEnv && s.env.present && (o.doMis || !didNEE))) return;
+        const bool needMIS = o.doMis && didNEE;
+        float pEnv, pEm;
+        typeProbabilities(pEnv, pEm);
+        const float nwo[3] = {-wo.x, -wo.y, -wo.z};
+        const float lightPdf = pEnv * s.env.evalPdf(nwo);
+        const float misWeight = needMIS ? MISWeight(bounce.lastNonDeltaPdf, lightPdf) : 1.f;
+        float swl[MAXH], Le[MAXH], rad[3];
+        for (int j = 0; j < MAXH; ++j) { swl[j] = 0.f; Le[j] = 0.f; }
+        hwssWavelengths(sv.wavelength, o.hwss, swl);
+        s.env.eval(nwo, rad);
+        for (uint32_t j = 0; j < o.hwss; ++j) Le[j] = misWeight * rgbToSpectrum(rad, swl[j]);
+        Beam<float> beam = sourceBeamDistant(wo, o.maxBeamOmega, Le, swl, o.hwss, o.maxBeamOmega);
+        if (!o.hwssMis && (bounce.flags & FLAG_DISPERSIVE)) beam.H = 1;
+        forwardUnwind(p, bounces, beam, sv);
+        measure(sv, p, bounce.pathContribution, beam);
+    }
+
     void solvePass(uint32_t px, uint32_t py, const Bounce* bounces, float* rgb, uint64_t* stats) const {
         const uint32_t tile = o.tileSize;
         Solve sv{SampleGen(px, py, frame), SampleGen(px / tile, py / tile, frame << 2)};
@@ -1344,7 +1444,10 @@ struct Renderer {
         sv.pathNormal = normalize(f3(cam.w));
         for (int p = 0;; ++p) {
             const Bounce& b = bounces[p];
-            if (b.flags & FLAG_MISS) break;   // onMiss: no environment light
+            if (b.flags & FLAG_MISS) {
+                onMiss(sv, p, bounces);
+                break;
+            }
             const VertexData v = vertexData(s, b.prim, b.b1, b.b2);
             const uint32_t mid = s.triMat[b.prim];
             const ShadingData sd = prepareShadingData(s, v, mid, b.wi());
@@ -1378,7 +1481,51 @@ typedef struct plto_scene {
     const plt_material_record* materials;
     const plt_spectral_profile* profiles;
     const float* proposal_params;        // [11488] learned proposal parameters (learned_proposal renders), or NULL
+    const struct plto_env* env;          // environment light, or NULL
 } plto_scene;
+
+// Environment light: [height][width][3] linear RGB lat-long map, intensity, tint, Euler XYZ degrees.
+typedef struct plto_env {
+    const float* rgb;
+    uint32_t width, height;
+    float intensity, tint[3], rotation_deg[3];
+} plto_env;
+
+static bool loadEnv(const plto_env* e, plt_oracle_env::EnvMap& env) {
+    if (!e) return true;
+    if (!e->rgb || e->width == 0 || e->height == 0) return false;
+    env.width = e->width;
+    env.height = e->height;
+    env.rgb.assign(e->rgb, e->rgb + 3 * (size_t)e->width * e->height);
+    for (int k = 0; k < 3; ++k) env.scale[k] = e->intensity * e->tint[k];
+    env.setRotation(e->rotation_deg);
+    env.buildImportance();
+    env.present = true;
+    return true;
+}
+
+// The sampler on given inputs: out[12 i ..] as plt_env_map_query (sampled direction, pdf, eval,
+// evalPdf; eval and evalPdf of dirs[i], zeros when dirs is NULL).
+int plto_env_query(const plto_env* e, const float* u, const float* dirs, uint32_t n, float* out) {
+    plt_oracle_env::EnvMap env;
+    if (!e || !loadEnv(e, env)) return PLT_INVALID_ARG;
+    for (uint32_t i = 0; i < n; ++i) {
+        float d[3], pdf, c[3];
+        env.sample(u[2 * (size_t)i], u[2 * (size_t)i + 1], d, pdf);
+        env.eval(d, c);
+        float* o = out + 12 * (size_t)i;
+        o[0] = d[0]; o[1] = d[1]; o[2] = d[2]; o[3] = pdf;
+        o[4] = c[0]; o[5] = c[1]; o[6] = c[2]; o[7] = env.evalPdf(d);
+        if (dirs) {
+            const float* q = dirs + 3 * (size_t)i;
+            env.eval(q, c);
+            o[8] = c[0]; o[9] = c[1]; o[10] = c[2]; o[11] = env.evalPdf(q);
+        } else {
+            o[8] = o[9] = o[10] = o[11] = 0.f;
+        }
+    }
+    return PLT_OK;
+}
 
 // Renders frames frame .. frame + frames - 1 of a width x height image into rgb [height][width][3]
 // (their mean).  Optional per-path records [height*width][max_bounces+1] of bounce primitive
@@ -1435,6 +1582,8 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.mneeThreshold = opt->mnee_solver_threshold;
     o.learned = opt->learned_proposal != 0;
     o.learnedProb = opt->learned_proposal_prob;
+    o.useEnv = opt->use_env_light != 0;
+    if (!loadEnv(sc->env, s.env)) return PLT_INVALID_ARG;
     if (o.learned) {
         if (!sc->proposal_params || !(o.learnedProb > 0.f && o.learnedProb < 1.f)) return PLT_INVALID_ARG;
         s.net.reset(new plt_oracle_mlp::Net(sc->proposal_params, true));

@@ -220,6 +220,30 @@ class PLTContext:
     def clear_scenes(self):
         capi.check(self.lib.plt_clear_scenes(self.handle), "plt_clear_scenes")
 
+    def set_env_map(self, rgb, intensity=1.0, tint=(1.0, 1.0, 1.0), rotation=(0.0, 0.0, 0.0)):
+        """plt_set_env_map: rgb is a [height][width][3 or 4] float array (linear lat-long map)."""
+        a = np.ascontiguousarray(np.asarray(rgb, np.float32))
+        if a.ndim != 3 or a.shape[2] not in (3, 4):
+            raise ValueError("env map must be [height][width][3 or 4]")
+        t = (C.c_float * 3)(*[float(x) for x in tint])
+        r = (C.c_float * 3)(*[float(x) for x in rotation])
+        capi.check(self.lib.plt_set_env_map(self.handle, a.ctypes.data_as(C.POINTER(C.c_float)), a.shape[1], a.shape[0],
+                                            a.shape[2], float(intensity), t, r), "plt_set_env_map")
+
+    def clear_env_map(self):
+        capi.check(self.lib.plt_clear_env_map(self.handle), "plt_clear_env_map")
+
+    def env_map_query(self, u, dirs=None, stream=None):
+        """plt_env_map_query on device tensors u [n][2] (and dirs [n][3]): returns [n][12] on the device."""
+        import torch
+        n = u.shape[0]
+        out = torch.empty((n, 12), dtype=torch.float32, device=u.device)
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_env_map_query(self.handle, C.c_void_p(u.data_ptr()),
+                                              None if dirs is None else C.c_void_p(dirs.data_ptr()), n,
+                                              C.c_void_p(out.data_ptr()), s), "plt_env_map_query")
+        return out
+
     def render_scenes(self, views, frame_begin=0, frame_count=1, stream=None):
         """plt_render_scenes: views is a list of (scene index, camera, width, height, out tensor [h][w][4])."""
         arr = self._views(views)

@@ -16,7 +16,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libplt_gb300.so")
 
 CU_SOURCES = ["plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4.cu", "plt_bsdf_h8.cu", "plt_trace.cu", "plt_noalloc.cu",
-              "plt_pt.cu", "plt_pt_h1.cu", "plt_pt_h2.cu", "plt_pt_h3.cu", "plt_pt_h4.cu", "plt_pt_h8.cu", "plt_mlp.cu"]
+              "plt_pt.cu", "plt_pt_h1.cu", "plt_pt_h2.cu", "plt_pt_h3.cu", "plt_pt_h4.cu", "plt_pt_h8.cu", "plt_mlp.cu",
+              "plt_envmap.cu"]
 CPP_SOURCES = ["plt_capi.cpp", "plt_materials.cpp", "plt_bsdf_dispatch.cpp", "plt_bvh.cpp", "plt_render.cpp", "plt_proposal.cpp",
                "plt_scenes.cpp", "plt_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

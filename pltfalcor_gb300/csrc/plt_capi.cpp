@@ -110,6 +110,7 @@ plt_status plt_destroy(plt_context* ctx) {
     cudaFree(ctx->dTriMaterial);
     pltReleaseRenderState(ctx);
     pltReleaseProposal(ctx);
+    pltReleaseEnv(ctx);
     delete ctx;
     return PLT_OK;
 }

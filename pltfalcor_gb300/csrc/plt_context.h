@@ -110,6 +110,12 @@ struct plt_context {
     uint32_t nPropEnabled = 0;
     void* dPropBatch = nullptr;      // training batch (features, targets, weights)
     uint32_t propBatchCap = 0;
+    // environment light: the map (float4 texels) and the sampler's importance mip chain
+    float4* dEnvTex = nullptr;
+    size_t envTexCap = 0;
+    float* dEnvImp = nullptr;
+    plt::EnvDev env{};
+    bool hasEnv = false;
 };
 
 // Frees the render-pass state of a context (plt_render.cpp).
@@ -121,5 +127,7 @@ float4 pltProposalFeatures(const plt_material_record& r, const pltdev::DevMateri
 // Frees the learned-proposal state (plt_proposal.cpp).
 void pltReleaseProposal(plt_context* ctx);
 
+// Frees the environment light (plt_scenes.cpp).
+void pltReleaseEnv(plt_context* ctx);
 // Uploads the scene set if it changed (geometry, shading, light collections); plt_scenes.cpp.
 plt_status pltUploadScenes(plt_context* ctx);

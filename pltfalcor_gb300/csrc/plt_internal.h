@@ -64,7 +64,7 @@ constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 // option bits of PtParams.opt
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
-                   kPtLearned = 0x200u;
+                   kPtLearned = 0x200u, kPtUseEnv = 0x400u;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
 
@@ -78,6 +78,22 @@ struct PtScene {
     float invWeightsSum;
     uint32_t pad;
     float* out;                   // [height][width][4]
+};
+
+// The environment light of a render (EnvMap.slang, EnvMapSampler.slang): an RGB lat-long map
+// (float4 texels, [height][width]) filtered bilinearly with U wrapped and V clamped, scaled by
+// intensity x tint; and the sampler's hierarchical importance map over the equal-area octahedral
+// parameterisation (imp: the mip chain concatenated, level 0 of impDim x impDim first, level k at
+// mipOff[k]; level impBaseMip is the 1x1 average).  toWorld / toLocal: row-major rotations.
+constexpr uint32_t kEnvImportanceDim = 512, kEnvImportanceSpp = 64, kEnvMaxMips = 16;
+struct EnvDev {
+    const float4* tex;
+    uint32_t width, height;
+    const float* imp;
+    uint32_t impDim, impBaseMip;
+    uint32_t mipOff[kEnvMaxMips];
+    float toWorld[9], toLocal[9];
+    float scale[3];               // intensity * tint
 };
 
 // Launch shape of a render (chosen by plt_render_tune; zeros: defaults): paths per wave (0 = all
@@ -161,6 +177,8 @@ struct PtParams {
     void* mneeTasks;              // [mneeCap] tasks of kMneeTaskBytes
     uint32_t mneeCap;
     uint32_t* mneeCount;
+    // environment light (kPtUseEnv)
+    EnvDev env;
     // outputs
     double* accum;                // [npix][3]
     unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, traversal bytes
@@ -168,6 +186,11 @@ struct PtParams {
 };
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream);
 cudaError_t launchSetFrame(uint32_t* frameDev, uint32_t frame, bool advance, cudaStream_t stream);
+// Builds the environment sampler's importance map (base level, then the mips) from env.tex into
+// env.imp (plt_envmap.cu).
+cudaError_t launchEnvImportance(const EnvDev& env, cudaStream_t stream);
+// Sampler queries for tests: per query i, sample(u[i]) and eval / evalPdf of dirs[i] (plt_envmap.cu).
+cudaError_t launchEnvQuery(const EnvDev& env, const float* u, const float* dirs, uint32_t n, float* out, cudaStream_t stream);
 
 constexpr int kBatchThreads = 256;     // classify CTA
 constexpr int kBatchItems = 8;

@@ -17,6 +17,7 @@
 #include <cuda_fp16.h>
 
 #include "plt_bsdf_query.cuh"
+#include "plt_envmap.cuh"
 #include "plt_mlp.cuh"
 #include "plt_trace.cuh"
 
@@ -360,6 +361,7 @@ template <int H> struct PBeam {
     float spdf[H];
     f3 posW;
     int comps;
+    bool distant;                 // sourced by a distant light: propagation leaves the coherence alone
 };
 // pltSourceBeamArea, Rendering/PLT.slang:276-290 (unpolarised, diffusivity A * I, r = 0)
 template <int H>
@@ -379,9 +381,31 @@ PLT_DI void sourceBeamArea(PBeam<H>& pb, f3 posW, f3 dir, float A, float dist, c
     pb.b.t = perp_stark(dir);
     pb.posW = posW;
     pb.comps = H;
+    pb.distant = false;
+}
+// pltSourceBeamDistant, Rendering/PLT.slang:253-267: unpolarised, diffusivity min(solidAngle,
+// maxOmega) I, coherence radius 1 mm, flagged distant for the beam's whole life (PLT.slang:99-114,
+// 224-230)
+template <int H>
+PLT_DI void sourceBeamDistant(PBeam<H>& pb, f3 dir, float solidAngle, const float* Le, const float* wl, float maxBeamOmega) {
+    const float omega = fminf(solidAngle, maxBeamOmega);
+#pragma unroll
+    for (int j = 0; j < H; ++j) {
+        pb.b.L[0][j] = Le[j];
+        pb.b.L[1][j] = pb.b.L[2][j] = pb.b.L[3][j] = 0.f;
+        pb.b.wl[j] = wl[j];
+        pb.spdf[j] = 1.f;
+    }
+    pb.b.D0 = omega; pb.b.D1 = 0.f; pb.b.D2 = omega;
+    pb.b.r_m = 1e-3f;
+    pb.b.r = dir;
+    pb.b.t = perp_stark(dir);
+    pb.posW = mk3(0.f, 0.f, 0.f);
+    pb.comps = H;
+    pb.distant = true;
 }
 template <int H> PLT_DI void propagate(PBeam<H>& pb, f3 p) {
-    pb.b.r_m += sqrtf(dot(p - pb.posW, p - pb.posW));
+    if (!pb.distant) pb.b.r_m += sqrtf(dot(p - pb.posW, p - pb.posW));
     pb.posW = p;
 }
 template <int H> PLT_DI void scaleBeam(PBeam<H>& pb, float s) {
@@ -1056,7 +1080,8 @@ PLT_NI int manifoldOccluders(const PtParams& P, int32_t root, f3 rayO, f3 rayD, 
 // manifoldNEESample's walk, Manifolds.slangh:162-281: Newton steps on the spherical-angle
 // constraint of every occluder with re-projection onto the same geometry instance, then the
 // visibility of the light from the last vertex.  Deterministic (no random draws).
-PLT_NI bool manifoldWalk(const PtParams& P, int32_t root, f3 origin, f3 lightPos, MSData& d, TraceCounters& tc) {
+PLT_NI bool manifoldWalk(const PtParams& P, int32_t root, f3 origin, f3 lightPos, f3 lightDir, bool distant, MSData& d,
+                         TraceCounters& tc) {
     float beta[kMaxMsOccluders];
 #pragma unroll
     for (int i = 0; i < kMaxMsOccluders; ++i) beta[i] = 1.f;
@@ -1070,7 +1095,16 @@ PLT_NI bool manifoldWalk(const PtParams& P, int32_t root, f3 origin, f3 lightPos
             const f3 p0 = idx == 0 ? origin : d.hits[idx - 1].posW;
             const F3pdv pdv0 = g.pdw(p0);
             const f3 p2 = idx + 1 == d.hitCount ? lightPos : d.hits[idx + 1].posW;
-            const F3pdv pdv2 = g.pdw(p2);
+            // a distant light fixes the direction towards it at every vertex of the chain
+            // (Manifolds.slangh:199-202)
+            F3pdv pdv2;
+            if (distant) {
+                pdv2.v = lightDir;
+                pdv2.ddu = mk3(0.f, 0.f, 0.f);
+                pdv2.ddv = mk3(0.f, 0.f, 0.f);
+            } else {
+                pdv2 = g.pdw(p2);
+            }
             const bool woIsIn = dot(pdv2.v, g.n.v) < 0.f;
             const F3pdv wiP = woIsIn ? pdv0 : pdv2;
             const F3pdv woP = woIsIn ? pdv2 : pdv0;
@@ -1104,9 +1138,16 @@ PLT_NI bool manifoldWalk(const PtParams& P, int32_t root, f3 origin, f3 lightPos
         }
     }
     const f3 pl = d.hits[d.hitCount - 1].posW;
-    f3 dir = lightPos - pl;
-    const float dist = sqrtf(dot(dir, dir));
-    dir = dir / dist;
+    f3 dir;
+    float dist;
+    if (!distant) {
+        dir = lightPos - pl;
+        dist = sqrtf(dot(dir, dir));
+        dir = dir / dist;
+    } else {
+        dir = lightDir;
+        dist = kFltMax;
+    }
     ++tc.shadowRays;
     const TraceResult vis = traverse<true>(reinterpret_cast<const float4*>(P.nodes), P.tris, pl.x, pl.y, pl.z, dir.x, dir.y, dir.z, 1e-4f,
                                            dist, tc.nv, tc.tt, tc.overflow, root);
@@ -1265,6 +1306,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     const bool useEmissive = (P.opt & plt::kPtUseEmissive) != 0;
     const bool importance = (P.opt & plt::kPtImportanceEmit) != 0;
     const bool doMnee = MNEE && (P.opt & plt::kPtDoMnee) != 0;
+    const bool useEnv = (P.opt & plt::kPtUseEnv) != 0;
     TraceCounters tc{0u, 0u, 0u, 0u};
     uint32_t evals = 0;
     MSData ms;
@@ -1281,10 +1323,38 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         tilesg.init(px / P.tileSize, py / P.tileSize, frame << 2);
         const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
         f3 pathOrigin = camPos(S);
+        // light-type selection probabilities (getLightTypeSelectionProbabilities,
+        // LightSampling.slangh:40-55): the environment map and this scene's emissive geometry
+        const bool hasEm = useEmissive && S.nLights > 0;
+        const float pSum = (useEnv ? 1.f : 0.f) + (hasEm ? 1.f : 0.f);
+        const float invPSum = pSum > 0.f ? 1.f / pSum : 0.f;
+        const float pEnv = useEnv ? invPSum : 0.f, pEm = hasEm ? invPSum : 0.f;
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
         for (int p = 0; p <= (int)P.maxBounces; ++p) {
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
-            if (bounce.flags & kFlagMiss) break;   // onMiss: no environment light
+            // wasNEEAvailable, pltpt_solve.rt.slang:204-210
+            const bool didNEE = doNee && p > 0 &&
+                                ((bounce.flags & kFlagLastDelta) == 0 || (doMnee && (bounce.flags >> 16) <= P.mneeMaxOccluders && p > 1));
+            if (bounce.flags & kFlagMiss) {
+                // onMiss, pltpt_solve.rt.slang:374-395: the environment map seen along the escaped
+                // ray, a distant beam replayed through vertices p-1 .. 0
+                if (useEnv && (doMis || !didNEE)) {
+                    const f3 wo = bounce.wi;
+                    const bool needMIS = doMis && didNEE;
+                    const float lightPdf = pEnv * envEvalPdf(P.env, -wo);
+                    const float mw = needMIS ? misWeight(bounce.lndp, lightPdf) : 1.f;
+                    float Le[H], swl[H];
+                    hwssWavelengths<H>(wavelength, swl);
+                    const f3 rad = envEval(P.env, -wo);
+#pragma unroll
+                    for (int j = 0; j < H; ++j) Le[j] = mw * rgbToSpectrumAt(rad, swl[j]);
+                    PBeam<H> pb;
+                    sourceBeamDistant<H>(pb, wo, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
+                    if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
+                    replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, pathOrigin, false, c, hwssMis, Lr, Lg, Lb, evals);
+                }
+                break;
+            }
             if (bounce.prim >= P.nTris) break;     // empty terminal record
             const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
             const uint32_t mid = __ldg(P.triMat + bounce.prim);
@@ -1293,9 +1363,6 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
             const DevMaterial* __restrict__ m = P.mats + mid;
             const uint32_t type = __ldg(&m->type);
             const uint32_t lobes = (props.x >> 8) & 0xFFu;
-            // wasNEEAvailable, pltpt_solve.rt.slang:204-210
-            const bool didNEE = doNee && p > 0 &&
-                                ((bounce.flags & kFlagLastDelta) == 0 || (doMnee && (bounce.flags >> 16) <= P.mneeMaxOccluders && p > 1));
             // two beam sources per vertex: NEE (pltpt_solve.rt.slang:245-366) and emission
             // (evalEmissive, :152-200); each is replayed through vertices p (NEE: non-delta lobes)
             // and p-1 .. 0 (forwardUnwind, :48-79), then measured (:96-147).
@@ -1309,46 +1376,85 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     const bool allowMS = doMnee && p > 0 && (bounce.flags & kFlagLastDelta) == 0 && (props.x & plt::kPropMwReflective) != 0;
                     const bool sampleRefl = (lobes & 0x03u) != 0 || allowMS, sampleTrans = (lobes & 0x30u) != 0;
                     if (!sampleRefl && !sampleTrans) continue;
-                    // generateLightSample: selectLightType (one draw), emissive power sampler
+                    // generateLightSample (LightSampling.slangh:166-206): selectLightType (one
+                    // draw), then the environment map's or the emissive power sampler's sample
                     SampleGen& selSg = (P.opt & plt::kPtPerTileSg) ? tilesg : sg;
-                    const float uType = selSg.next1D();
-                    if (!useEmissive || !(uType < 1.f) || S.nLights == 0) continue;
-                    const float uLight = sg.next1D();
-                    uint32_t ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
-                    const uint2 a = __ldg(P.alias + S.lightBase + ti);
-                    const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
-                    const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
-                    const uint32_t selectBelow = a.y & 0xFFFFFFu;
-                    ti = S.lightBase + ((sg.next1D() >= threshold) ? selectAbove : selectBelow);
-                    const float triSelPdf = __ldg(P.lightFlux + ti) * S.invWeightsSum;
-                    const float u0 = sg.next1D(), u1 = sg.next1D();
-                    const float su = sqrtf(u0);
-                    const float bx = 1.f - su, by = u1 * su;
-                    const float* LP = P.lightPos + 9 * ti;
-                    const f3 tposW = ld3s(LP, 0) * (1.f - bx - by) + ld3s(LP, 1) * bx + ld3s(LP, 2) * by;
-                    const f3 toL = tposW - sd.posW;
-                    const float distSqr = fmaxf(kFltMin, dot(toL, toL));
-                    const float tdist = sqrtf(distSqr);
-                    const f3 tdir = toL / tdist;
-                    const f3 tn = ld3s(P.lightNrm, ti);
-                    const float cosTheta = dot(tn, -tdir);
-                    if (cosTheta <= 0.f) continue;
-                    float Le[H], swl[H];
-                    sampleSpectrum<H>(P, __ldg(P.lightEmission + ti), wavelength, sg, importance, Le, swl);
-                    const float tpdf = (distSqr / fmaxf(kFltMin, cosTheta * __ldg(P.lightArea + ti))) * triSelPdf;
-                    bool anyPos = false;
-#pragma unroll
-                    for (int j = 0; j < H; ++j) {
-                        Le[j] *= whiteSpectrum(swl[j]);
-                        Le[j] = tpdf > 0.f ? Le[j] / tpdf : 0.f;
-                        anyPos = anyPos || Le[j] > 0.f;
+                    float uType = selSg.next1D();
+                    float selPdf;
+                    bool distant;
+                    if (uType < pEnv) {
+                        selPdf = pEnv;
+                        distant = true;
+                    } else {
+                        uType -= pEnv;
+                        if (!(uType < pEm)) continue;
+                        selPdf = pEm;
+                        distant = false;
                     }
-                    const f3 lightPos = computeRayOrigin(tposW, tn);
-                    const f3 lorg = newRayOriginToward(sd, lightPos - sd.posW);
-                    const f3 toLight = lightPos - lorg;
-                    const float ldist = sqrtf(dot(toLight, toLight));
-                    const f3 ldir = rnormalize(toLight);
-                    sourceBeamArea<H>(pb, tposW, -ldir, P.sourcingArea, ldist, Le, swl, P.maxBeamOmega);
+                    const float invSel = 1.f / selPdf;
+                    float Le[H], swl[H];
+                    float tpdf;
+                    bool anyPos = false;
+                    f3 tposW, lorg, ldir;
+                    float ldist;
+                    if (distant) {
+                        // generateEnvMapSample (LightSampling.slangh:86-104, EnvMapSampler.slang:52-113)
+                        const float e0 = sg.next1D();
+                        const float e1 = sg.next1D();
+                        float epdf;
+                        ldir = envSampleDir(P.env, e0, e1, epdf);
+                        hwssWavelengths<H>(wavelength, swl);
+                        const f3 rad = envEval(P.env, ldir);
+#pragma unroll
+                        for (int j = 0; j < H; ++j) {
+                            const float le = rgbToSpectrumAt(rad, swl[j]);
+                            Le[j] = epdf > 0.f ? le / epdf : 0.f;
+                            anyPos = anyPos || Le[j] > 0.f;
+                            Le[j] *= invSel;
+                        }
+                        tpdf = epdf * selPdf;
+                        lorg = newRayOriginToward(sd, ldir);
+                        ldist = kFltMax;
+                        tposW = lorg;
+                        sourceBeamDistant<H>(pb, -ldir, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
+                    } else {
+                        const float uLight = sg.next1D();
+                        uint32_t ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
+                        const uint2 a = __ldg(P.alias + S.lightBase + ti);
+                        const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
+                        const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
+                        const uint32_t selectBelow = a.y & 0xFFFFFFu;
+                        ti = S.lightBase + ((sg.next1D() >= threshold) ? selectAbove : selectBelow);
+                        const float triSelPdf = __ldg(P.lightFlux + ti) * S.invWeightsSum;
+                        const float u0 = sg.next1D(), u1 = sg.next1D();
+                        const float su = sqrtf(u0);
+                        const float bx = 1.f - su, by = u1 * su;
+                        const float* LP = P.lightPos + 9 * ti;
+                        tposW = ld3s(LP, 0) * (1.f - bx - by) + ld3s(LP, 1) * bx + ld3s(LP, 2) * by;
+                        const f3 toL = tposW - sd.posW;
+                        const float distSqr = fmaxf(kFltMin, dot(toL, toL));
+                        const float tdist = sqrtf(distSqr);
+                        const f3 tdir = toL / tdist;
+                        const f3 tn = ld3s(P.lightNrm, ti);
+                        const float cosTheta = dot(tn, -tdir);
+                        if (cosTheta <= 0.f) continue;
+                        sampleSpectrum<H>(P, __ldg(P.lightEmission + ti), wavelength, sg, importance, Le, swl);
+                        const float epdf = (distSqr / fmaxf(kFltMin, cosTheta * __ldg(P.lightArea + ti))) * triSelPdf;
+#pragma unroll
+                        for (int j = 0; j < H; ++j) {
+                            Le[j] *= whiteSpectrum(swl[j]);
+                            Le[j] = epdf > 0.f ? Le[j] / epdf : 0.f;
+                            anyPos = anyPos || Le[j] > 0.f;
+                            Le[j] *= invSel;
+                        }
+                        tpdf = epdf * selPdf;
+                        const f3 lightPos = computeRayOrigin(tposW, tn);
+                        lorg = newRayOriginToward(sd, lightPos - sd.posW);
+                        const f3 toLight = lightPos - lorg;
+                        ldist = sqrtf(dot(toLight, toLight));
+                        ldir = rnormalize(toLight);
+                        sourceBeamArea<H>(pb, tposW, -ldir, P.sourcingArea, ldist, Le, swl, P.maxBeamOmega);
+                    }
                     const bool isRefl = dot(sd.faceN, ldir) * dot(sd.faceN, sd.V) > 0.f;
                     if (!(anyPos && tpdf > 1e-6f && !(!sampleRefl && isRefl) && !(!sampleTrans && !isRefl))) continue;
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
@@ -1394,14 +1500,15 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 for (int j = 0; j < H; ++j) { t->Le[j] = Le[j]; t->swl[j] = swl[j]; }
                                 t->pid = pid;
                                 t->p = (uint32_t)p;
-                                t->curMS = curMS ? 1u : 0u;
+                                t->curMS = (curMS ? 1u : 0u) | (distant ? 2u : 0u);
                                 continue;
                             }
-                            if (!manifoldWalk(P, root, msOrigin, tposW, ms, tc)) continue;
+                            if (!manifoldWalk(P, root, msOrigin, tposW, ldir, distant, ms, tc)) continue;
                         }
                         float misBsdfPdf = 0.f;
                         f3 lsDir = ldir;
                         if (ms.hitCount > 0) {
+                            // (a distant light's beam already points along -woLastHitToLight)
                             if (!hwssMis && ms.dispersive) pb.comps = 1;
                             lsDir = ms.woLastHitToLight;
                             pb.b.r = -ms.woLastHitToLight;
@@ -1423,7 +1530,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     const bool needMIS = doMis && didNEE;
                     const uint32_t light = __ldg(P.primToLight + bounce.prim);
                     const f3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
-                    const float lightPdf = emissivePdf(P, S, pathOrigin, light, sd.posW, hn);
+                    const float lightPdf = pEm * emissivePdf(P, S, pathOrigin, light, sd.posW, hn);
                     const float mw = needMIS ? misWeight(bounce.lndp, lightPdf) : 1.f;
                     float Le[H], swl[H];
                     sampleSpectrum<H>(P, props.y, wavelength, sg, importance, Le, swl);
@@ -1481,11 +1588,12 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         MSData ms = t.ms;
         const uint32_t pid = t.pid;
         const int p = (int)t.p;
-        const bool curMS = t.curMS != 0;
+        const bool curMS = (t.curMS & 1u) != 0;
+        const bool distant = (t.curMS & 2u) != 0;
         const f3 msOrigin = t.msOrigin;
         const uint32_t gp = P.pidBase + pid;
         const PtScene& S = P.scenes[sceneOf(P, gp)];
-        if (!manifoldWalk(P, (int32_t)S.root, msOrigin, t.tposW, ms, tc)) continue;
+        if (!manifoldWalk(P, (int32_t)S.root, msOrigin, t.tposW, t.ldir, distant, ms, tc)) continue;
         const Bnc<H> bounce = readBounce<H>(P, pid, p);
         const VData V = vertexData(P, bounce.prim, bounce.b1, bounce.b2);
         const uint32_t mid = __ldg(P.triMat + bounce.prim);
@@ -1496,7 +1604,8 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
 #pragma unroll
         for (int j = 0; j < H; ++j) { Le[j] = t.Le[j]; swl[j] = t.swl[j]; }
         PBeam<H> pb;
-        sourceBeamArea<H>(pb, t.tposW, -t.ldir, P.sourcingArea, t.ldist, Le, swl, P.maxBeamOmega);
+        if (distant) sourceBeamDistant<H>(pb, -t.ldir, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
+        else sourceBeamArea<H>(pb, t.tposW, -t.ldir, P.sourcingArea, t.ldist, Le, swl, P.maxBeamOmega);
         if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
         bool evalCurrent = true;
         float misBsdfPdf = 0.f;

@@ -244,12 +244,14 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.hwss = o.hwss;
     P.flags = o.flags;
     const bool nee = o.do_nee != 0;
-    // light types without an environment map or analytic lights (PLTPT.cpp:230-232)
+    // light types: emissive geometry and the environment map, no analytic lights (PLTPT.cpp:230-232)
     P.opt = (o.hwss_do_mis ? plt::kPtHwssMis : 0u) | (o.use_direct_light ? plt::kPtUseDirect : 0u) |
             (o.use_emissive_lights && ctx->nLights ? plt::kPtUseEmissive : 0u) | (nee ? plt::kPtDoNee : 0u) |
             (nee && o.do_mis ? plt::kPtDoMis : 0u) | (o.do_russian_roulette ? plt::kPtDoRR : 0u) |
             (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u) |
-            (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u);
+            (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u) |
+            (o.use_env_light && ctx->hasEnv ? plt::kPtUseEnv : 0u);
+    P.env = ctx->env;
     P.propNet = ctx->dPropBf16;
     P.matFeat = ctx->dMatFeat;
     P.propProb = o.learned_proposal_prob;

@@ -242,7 +242,33 @@ plt_status setSceneShading(plt_scene_host& sc, const float* normals, const float
     return PLT_OK;
 }
 
+// EnvMap::setRotation (Scene/Lights/EnvMap.cpp:60-71): rotation degrees (x, y, z) to
+// toWorld = Rx(x) Ry(y) Rz(z) (row-major); toLocal is its transpose.
+void envRotation(const float deg[3], float toWorld[9], float toLocal[9]) {
+    const float k = 3.14159265358979323846f / 180.f;
+    const float a = deg[0] * k, b = deg[1] * k, c = deg[2] * k;
+    const float ca = std::cos(a), sa = std::sin(a), cb = std::cos(b), sb = std::sin(b), cc = std::cos(c), sc = std::sin(c);
+    const float M[9] = {cb * cc, -cb * sc, sb,
+                        ca * sc + sa * sb * cc, ca * cc - sa * sb * sc, -sa * cb,
+                        sa * sc - ca * sb * cc, sa * cc + ca * sb * sc, ca * cb};
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) {
+            toWorld[3 * r + q] = M[3 * r + q];
+            toLocal[3 * r + q] = M[3 * q + r];
+        }
+}
+
 }  // namespace
+
+void pltReleaseEnv(plt_context* ctx) {
+    cudaFree(ctx->dEnvTex);
+    cudaFree(ctx->dEnvImp);
+    ctx->dEnvTex = nullptr;
+    ctx->dEnvImp = nullptr;
+    ctx->envTexCap = 0;
+    ctx->env = plt::EnvDev{};
+    ctx->hasEnv = false;
+}
 
 // Uploads the scene set as one set of device arrays.  Geometry: BVH nodes with child indices
 // rebased by the scene's first node and leaf triangle offsets by its first triangle, triangles with
@@ -410,6 +436,70 @@ plt_status plt_clear_scenes(plt_context* ctx) {
     ctx->scenes.clear();
     ctx->geometryDirty = true;
     return pltUploadScenes(ctx);
+}
+
+// Scene::setEnvMap + EnvMap (Scene/Lights/EnvMap.cpp) + EnvMapSampler::createImportanceMap
+// (Rendering/Lights/EnvMapSampler.cpp:85-120): uploads the lat-long map and builds the sampler's
+// 512 x 512 importance map (64 subsamples per texel) and its mips on the device.
+plt_status plt_set_env_map(plt_context* ctx, const float* pixels, uint32_t width, uint32_t height, uint32_t channels,
+                           float intensity, const float* tint, const float* rotation_deg) {
+    if (!ctx || !pixels || width == 0 || height == 0 || width > 16384 || height > 16384) return PLT_INVALID_ARG;
+    if (channels != 3 && channels != 4) return PLT_INVALID_ARG;
+    if (!std::isfinite(intensity) || intensity < 0.f) return PLT_INVALID_ARG;
+    const float one[3] = {1.f, 1.f, 1.f}, zero[3] = {0.f, 0.f, 0.f};
+    const float* tn = tint ? tint : one;
+    const float* rot = rotation_deg ? rotation_deg : zero;
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(tn[i]) || tn[i] < 0.f || !std::isfinite(rot[i])) return PLT_INVALID_ARG;
+    const size_t n = (size_t)width * height;
+    std::vector<float4> tex(n);
+    for (size_t i = 0; i < n; ++i) {
+        const float* q = pixels + channels * i;
+        if (!(std::isfinite(q[0]) && std::isfinite(q[1]) && std::isfinite(q[2])) || q[0] < 0.f || q[1] < 0.f || q[2] < 0.f)
+            return PLT_INVALID_ARG;
+        tex[i] = make_float4(q[0], q[1], q[2], channels == 4 ? q[3] : 1.f);
+    }
+    if (ctx->envTexCap < n) {
+        cudaFree(ctx->dEnvTex);
+        ctx->dEnvTex = nullptr;
+        ctx->envTexCap = 0;
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dEnvTex, sizeof(float4) * n));
+        ctx->envTexCap = n;
+    }
+    PLT_CUDA(ctx, cudaMemcpy(ctx->dEnvTex, tex.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    plt::EnvDev E{};
+    E.impDim = plt::kEnvImportanceDim;
+    uint32_t off = 0, mip = 0;
+    for (uint32_t d = E.impDim; d >= 1; d >>= 1, ++mip) {
+        E.mipOff[mip] = off;
+        off += d * d;
+        E.impBaseMip = mip;
+    }
+    if (!ctx->dEnvImp) PLT_CUDA(ctx, cudaMalloc(&ctx->dEnvImp, sizeof(float) * off));
+    E.tex = ctx->dEnvTex;
+    E.width = width;
+    E.height = height;
+    E.imp = ctx->dEnvImp;
+    envRotation(rot, E.toWorld, E.toLocal);
+    for (int i = 0; i < 3; ++i) E.scale[i] = intensity * tn[i];
+    PLT_CUDA(ctx, plt::launchEnvImportance(E, 0));
+    PLT_CUDA(ctx, cudaStreamSynchronize(0));
+    ctx->env = E;
+    ctx->hasEnv = true;
+    return PLT_OK;
+}
+
+plt_status plt_clear_env_map(plt_context* ctx) {
+    if (!ctx) return PLT_INVALID_ARG;
+    pltReleaseEnv(ctx);
+    return PLT_OK;
+}
+
+plt_status plt_env_map_query(plt_context* ctx, const float* u, const float* dirs, uint32_t n, float* out, void* stream) {
+    if (!ctx || (n > 0 && (!u || !out))) return PLT_INVALID_ARG;
+    if (!ctx->hasEnv) return PLT_INVALID_ARG;
+    PLT_CUDA(ctx, plt::launchEnvQuery(ctx->env, u, dirs, n, out, static_cast<cudaStream_t>(stream)));
+    return PLT_OK;
 }
 
 }  // extern "C"

@@ -77,7 +77,11 @@ class Scene:
         return np.ascontiguousarray(self.vertices[self.indices].reshape(-1, 9))
 
 
-def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_subdiv=32, room=10.0, emission_id=8):
+def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_subdiv=32, room=10.0, emission_id=8, walls=True,
+                     emitter=True):
+    """The procedural room: six subdivided walls (walls=False: the floor only, an open scene for an
+    environment light), an area light under the ceiling (emitter=False: none), a smooth dielectric
+    sphere below it, random icospheres and quads of the mixed PLT materials."""
     rng = CounterRNG(seed, max(n_spheres, n_quads, 1) * 16)
     u = lambda: rng.uniform().astype(np.float64)
     per_type = 512
@@ -108,15 +112,16 @@ def procedural_scene(seed=2, n_spheres=200, sphere_level=4, n_quads=500, box_sub
                (np.array([-R, R, -R]), np.array([2 * R, 0, 0]), np.array([0, 0, 2 * R])),
                (np.array([-R, -R, -R]), np.array([0, 2 * R, 0]), np.array([0, 0, 2 * R])),
                (np.array([R, -R, -R]), np.array([0, 0, 2 * R]), np.array([0, 2 * R, 0]))]
-    for c, e1, e2 in corners:
+    for c, e1, e2 in (corners if walls else corners[:1]):
         v, f = grid_quad(c, e1, e2, box_subdiv)
         add(v, f, wall_mat, _unit(np.cross(e1, e2)))
     # area light under the ceiling (z = +R is the ceiling), emitting downwards
     e1, e2 = np.array([0, 3.0, 0]), np.array([3.0, 0, 0])
     v, f = grid_quad(np.array([-1.5, -1.5, R - 0.05]), e1, e2, 1)
     first_emissive = sum(len(x) for x in faces)
-    add(v, f, light_mat, _unit(np.cross(e1, e2)))
-    emissive = np.arange(first_emissive, first_emissive + len(f))
+    if emitter:
+        add(v, f, light_mat, _unit(np.cross(e1, e2)))
+    emissive = np.arange(first_emissive, first_emissive + (len(f) if emitter else 0))
     # smooth dielectric sphere below the light (manifold NEE occluder)
     sv, sf = icosphere(min(sphere_level, 4))
     add(sv * 1.2 + np.array([0.0, 0.0, R - 4.0]), sf, glass_mat, sv)
@@ -152,6 +157,32 @@ def small_scene(seed=3):
     """The procedural room at test size (about 8 K triangles): 12 level-2 icospheres, 40 quads,
     4x4 box faces, the light and the glass sphere."""
     return procedural_scene(seed=seed, n_spheres=12, sphere_level=2, n_quads=40, box_subdiv=4)
+
+
+def open_scene(seed=5, emitter=True):
+    """An open test scene (floor, objects, optional area light, no walls) for the environment light."""
+    return procedural_scene(seed=seed, n_spheres=12, sphere_level=2, n_quads=30, box_subdiv=4, walls=False, emitter=emitter)
+
+
+def sky_env(width=256, height=128, seed=1, sun=(0.35, 0.22), sun_radiance=200.0):
+    """A synthetic HDR lat-long environment map [height][width][3]: a vertical sky gradient (map
+    top = local +y), a warm ground, coloured smooth patches and a small bright sun disc at map
+    coordinates `sun` (u, v)."""
+    rng = np.random.default_rng(seed)
+    v = (np.arange(height) + 0.5) / height
+    u = (np.arange(width) + 0.5) / width
+    U, Vv = np.meshgrid(u, v)
+    sky = np.stack([0.25 + 0.35 * Vv, 0.35 + 0.35 * Vv, 0.9 - 0.2 * Vv], -1)
+    ground = np.stack([0.3 + 0 * Vv, 0.22 + 0 * Vv, 0.15 + 0 * Vv], -1)
+    img = np.where((Vv > 0.5)[..., None], ground, sky)
+    for _ in range(6):
+        cu, cv, r = rng.uniform(0, 1), rng.uniform(0.1, 0.9), rng.uniform(0.03, 0.12)
+        col = rng.uniform(0.0, 2.0, 3)
+        d2 = np.minimum(np.abs(U - cu), 1 - np.abs(U - cu)) ** 2 + (Vv - cv) ** 2
+        img = img + col * np.exp(-d2 / (2 * r * r))[..., None]
+    d2 = np.minimum(np.abs(U - sun[0]), 1 - np.abs(U - sun[0])) ** 2 * 4 + (Vv - sun[1]) ** 2
+    img = img + np.array([1.0, 0.95, 0.85]) * sun_radiance * (d2 < (1.5 / height) ** 2)[..., None]
+    return img.astype(np.float32)
 
 
 def _unit(v):
