@@ -257,6 +257,15 @@ plt_status plt_spectral_profile_from_samples(const float* wavelengths_nm, const 
  * and builds its SpectralProfile as plt_spectral_profile_from_samples.  Host path and pointer. */
 plt_status plt_spectral_profile_from_spd(const char* path, float scale, int compute_icdf, plt_spectral_profile* out);
 
+/* The reference's spectral-table lookups by name (tables_dir = a directory laid out as the
+ * reference's Source/Tables: ior/<name>.eta.spd + ior/<name>.k.spd, emission/<name>.spd).
+ * Replaces SceneBuilder::addSpectralProfileFromMaterial ("none" = constant n 1, k 0; no inverse
+ * CDF) and SceneBuilder::addSpectralProfileForEmitterType (scaled, with inverse CDF)
+ * (Scene/SceneBuilder.cpp:967-993).  PLT_INVALID_ARG when a table is missing.  Host pointers. */
+plt_status plt_spectral_profiles_from_material(const char* tables_dir, const char* name, plt_spectral_profile* eta,
+                                               plt_spectral_profile* k);
+plt_status plt_spectral_profile_for_emitter_type(const char* tables_dir, const char* name, float scale, plt_spectral_profile* out);
+
 /* Writes an RGBA image ([height][width][4] floats, host) as an uncompressed scanline OpenEXR file,
  * HALF channels when half != 0, else FLOAT (the reference's pass graph ends in an accumulated EXR
  * capture, scripts/PLTPathTracer.py:19-27). */

@@ -110,6 +110,7 @@ EXPORTED_SYMBOLS = [
     "plt_add_scene", "plt_clear_scenes", "plt_render_scenes", "plt_set_launch_shape", "plt_get_launch_shape", "plt_render_tune",
     "plt_spectral_profile_from_spd", "plt_write_exr", "plt_render_counters",
     "plt_set_env_map", "plt_clear_env_map", "plt_env_map_query",
+    "plt_spectral_profiles_from_material", "plt_spectral_profile_for_emitter_type",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -174,6 +175,8 @@ def load_library(path=LIB_PATH):
         "plt_render_counters": (i32, [vp, C.POINTER(C.c_uint64), u32]),
         "plt_set_env_map": (i32, [vp, C.POINTER(C.c_float), u32, u32, u32, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "plt_clear_env_map": (i32, [vp]),
+        "plt_spectral_profiles_from_material": (i32, [C.c_char_p, C.c_char_p, vp, vp]),
+        "plt_spectral_profile_for_emitter_type": (i32, [C.c_char_p, C.c_char_p, C.c_float, vp]),
         "plt_env_map_query": (i32, [vp, vp, vp, u32, vp, vp]),
     }
     for name, (res, args) in sig.items():

@@ -97,6 +97,39 @@ plt_status plt_spectral_profile_from_spd(const char* path, float scale, int comp
     return plt_spectral_profile_from_samples(wl.data(), val.data(), (uint32_t)wl.size(), scale, compute_icdf, out);
 }
 
+// SceneBuilder::addSpectralProfileFromMaterial (Scene/SceneBuilder.cpp:967-976): the real and
+// imaginary IOR tables <tables>/ior/<name>.eta.spd and .k.spd, without inverse CDFs; "none" is the
+// constant one-sample spectra n = 1, k = 0 over 380-720 nm.
+plt_status plt_spectral_profiles_from_material(const char* tables_dir, const char* name, plt_spectral_profile* eta,
+                                               plt_spectral_profile* k) {
+    if (!tables_dir || !name || !eta || !k) return PLT_INVALID_ARG;
+    if (std::strcmp(name, "none") == 0) {
+        const float wl[2] = {380.0f, 720.0f};
+        for (int i = 0; i < 2; ++i) {
+            const float v[2] = {i == 0 ? 1.f : 0.f, i == 0 ? 1.f : 0.f};
+            plt_spectral_profile* out = i == 0 ? eta : k;
+            const plt_status s = plt_spectral_profile_from_samples(wl, v, 2, 1.f, 0, out);
+            if (s != PLT_OK) return s;
+            out->bins = 1;   // SampledSpectrum(value) holds one sample
+            for (uint32_t b = 1; b < PLT_SPECTRAL_MAX_BINS; ++b) out->pdf[b] = 0.f;
+            out->intensity = 1.f;
+        }
+        return PLT_OK;
+    }
+    const std::string base = std::string(tables_dir) + "/ior/" + name;
+    const plt_status s = plt_spectral_profile_from_spd((base + ".eta.spd").c_str(), 1.f, 0, eta);
+    if (s != PLT_OK) return s;
+    return plt_spectral_profile_from_spd((base + ".k.spd").c_str(), 1.f, 0, k);
+}
+
+// SceneBuilder::addSpectralProfileForEmitterType (Scene/SceneBuilder.cpp:978-993): the emission
+// table <tables>/emission/<name>.spd scaled by `scale`, with its inverse CDF.
+plt_status plt_spectral_profile_for_emitter_type(const char* tables_dir, const char* name, float scale, plt_spectral_profile* out) {
+    if (!tables_dir || !name || !out) return PLT_INVALID_ARG;
+    const std::string path = std::string(tables_dir) + "/emission/" + name + ".spd";
+    return plt_spectral_profile_from_spd(path.c_str(), scale, 1, out);
+}
+
 // OpenEXR 2 single-part scanline image, no compression, channels A, B, G, R (alphabetical, as the
 // format requires), HALF or FLOAT; rgba is [height][width][4] on the host.
 plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, uint32_t height, int half) {

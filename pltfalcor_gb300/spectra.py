@@ -60,6 +60,26 @@ def profile_from_spd(path, scale=1.0, compute_icdf=False, lib=None):
     return out
 
 
+def profiles_from_material(tables_dir, name, lib=None):
+    """plt_spectral_profiles_from_material: (eta, k) profiles of a named IOR table ("none": 1, 0)."""
+    import ctypes as C
+    lib = lib or capi.load_library()
+    eta, k = capi.SpectralProfile(), capi.SpectralProfile()
+    capi.check(lib.plt_spectral_profiles_from_material(os.fsencode(tables_dir), name.encode(), C.byref(eta), C.byref(k)),
+               "plt_spectral_profiles_from_material")
+    return eta, k
+
+
+def profile_for_emitter_type(tables_dir, name, scale=1.0, lib=None):
+    """plt_spectral_profile_for_emitter_type: the profile of a named emission table, scaled."""
+    import ctypes as C
+    lib = lib or capi.load_library()
+    out = capi.SpectralProfile()
+    capi.check(lib.plt_spectral_profile_for_emitter_type(os.fsencode(tables_dir), name.encode(), float(scale), C.byref(out)),
+               "plt_spectral_profile_for_emitter_type")
+    return out
+
+
 def write_exr(path, rgba, half=False, lib=None):
     """plt_write_exr of a [height][width][4] float image (numpy or CPU tensor)."""
     import ctypes as C

@@ -41,6 +41,36 @@ def test_spd_loader_rejects_missing_and_empty(product_lib, tmp_path):
     assert lib.plt_spectral_profile_from_spd(os.fsencode(str(p)), 1.0, 0, C.byref(out)) == capi.PLT_INVALID_ARG
 
 
+def test_named_table_lookups(product_lib, tmp_path):
+    """plt_spectral_profiles_from_material / plt_spectral_profile_for_emitter_type read the
+    reference's Tables layout (ior/<name>.eta.spd + .k.spd without inverse CDFs, emission/<name>.spd
+    scaled with one) and equal the direct .spd loads; "none" is n = 1, k = 0 in one bin."""
+    tables = spectra.load_tables()
+    (tmp_path / "ior").mkdir()
+    (tmp_path / "emission").mkdir()
+
+    def write(path, name):
+        wl, val = tables[name]["wavelength_nm"], tables[name]["value"]
+        with open(path, "w") as f:
+            for a_, b_ in zip(wl, val):
+                f.write("%r %r\n" % (float(a_), float(b_)))
+
+    write(tmp_path / "ior" / "Au.eta.spd", "Au.eta")
+    write(tmp_path / "ior" / "Au.k.spd", "Au.k")
+    write(tmp_path / "emission" / "d65.spd", "D65")
+    eta, k = spectra.profiles_from_material(str(tmp_path), "Au")
+    assert _profile_bytes(eta) == _profile_bytes(spectra.profile_from_spd(str(tmp_path / "ior" / "Au.eta.spd"), 1.0, False))
+    assert _profile_bytes(k) == _profile_bytes(spectra.profile_from_spd(str(tmp_path / "ior" / "Au.k.spd"), 1.0, False))
+    em = spectra.profile_for_emitter_type(str(tmp_path), "d65", 3.0)
+    assert _profile_bytes(em) == _profile_bytes(spectra.profile_from_spd(str(tmp_path / "emission" / "d65.spd"), 3.0, True))
+    n1, k0 = spectra.profiles_from_material(str(tmp_path), "none")
+    assert n1.bins == 1 and n1.pdf[0] == 1.0 and k0.bins == 1 and k0.pdf[0] == 0.0
+    with pytest.raises(RuntimeError):
+        spectra.profiles_from_material(str(tmp_path), "Ag")
+    with pytest.raises(RuntimeError):
+        spectra.profile_for_emitter_type(str(tmp_path), "missing")
+
+
 def _read_exr(path):
     """Minimal reader of uncompressed single-part scanline OpenEXR files."""
     data = open(path, "rb").read()
