@@ -344,6 +344,37 @@ plt_status plt_clear_env_map(plt_context* ctx);
  * (3), evalPdf of dirs[i].  PLT_INVALID_ARG without an environment map. */
 plt_status plt_env_map_query(plt_context* ctx, const float* u, const float* dirs, uint32_t n, float* out, void* stream);
 
+/* Analytic lights: LightData (Scene/Lights/LightData.slang:36-67) as the scene's light classes fill
+ * it (Scene/Lights/Light.cpp), for NEE's third light type (generateAnalyticLightSample,
+ * RenderPasses/PLTPT/LightSampling.slangh:128-164, sampleLight, Rendering/Lights/LightHelpers.slang).
+ * With options use_analytic_lights (default 1) and at least one light, light-type selection picks
+ * among the environment map, emissive geometry and these lights; a light is chosen uniformly.  As
+ * in the reference, point (spot) and directional lights have a zero pdf and their samples are
+ * rejected, analytic lights are never MIS-weighted and never hit by rays, and an area light's beam
+ * is sourced at pos (LightData.posW, left at the origin by the area-light classes).  The lights
+ * apply to every scene of the context.  Host array, copied. */
+typedef enum plt_light_type {
+    PLT_LIGHT_POINT = 0,
+    PLT_LIGHT_DIRECTIONAL = 1,
+    PLT_LIGHT_DISTANT = 2,
+    PLT_LIGHT_RECT = 3,
+    PLT_LIGHT_DISC = 4,
+    PLT_LIGHT_SPHERE = 5
+} plt_light_type;
+typedef struct plt_analytic_light {
+    uint32_t type;                      /* plt_light_type */
+    uint32_t intensity_spectral_id;     /* spectral profile of the intensity */
+    float pos[3];                       /* posW */
+    float dir[3];                       /* dirW (normalised) */
+    float opening_angle;                /* spot: half-angle, pi = full sphere */
+    float cos_opening_angle;
+    float penumbra_angle;
+    float cos_subtended_angle;          /* distant light */
+    float surface_area;                 /* area lights, as the light class's update() computes it */
+    float transform[12];                /* transMat rows 0-2 (row-major 3x4): area lights, distant light frame */
+} plt_analytic_light;
+plt_status plt_set_analytic_lights(plt_context* ctx, const plt_analytic_light* lights, uint32_t count);
+
 /* Scene sets (no counterpart in the reference, whose PLTPT renders the one loaded scene): several
  * independent scenes held by one context share its materials and spectral profiles, and
  * plt_render_scenes renders any number of views of them in one wavefront per frame (all scenes'

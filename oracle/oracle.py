@@ -174,7 +174,7 @@ class _Scene(C.Structure):
     _fields_ = [("n_vertices", C.c_uint32), ("n_triangles", C.c_uint32), ("n_materials", C.c_uint32), ("n_profiles", C.c_uint32),
                 ("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("indices", C.c_void_p),
                 ("tri_material", C.c_void_p), ("tri_instance", C.c_void_p), ("materials", C.c_void_p), ("profiles", C.c_void_p),
-                ("proposal_params", C.c_void_p), ("env", C.c_void_p)]
+                ("proposal_params", C.c_void_p), ("env", C.c_void_p), ("lights", C.c_void_p), ("n_lights", C.c_uint32)]
 
 
 class _Env(C.Structure):
@@ -208,7 +208,7 @@ def env_query(env, u, dirs=None):
     return out
 
 
-def _scene_struct(scene, profiles, proposal_params=None, env=None):
+def _scene_struct(scene, profiles, proposal_params=None, env=None, lights=None):
     keep = [np.ascontiguousarray(scene.vertices, np.float32), np.ascontiguousarray(scene.normals, np.float32),
             np.ascontiguousarray(scene.indices, np.uint32), np.ascontiguousarray(scene.tri_material, np.uint32),
             np.ascontiguousarray(scene.records)]
@@ -222,11 +222,15 @@ def _scene_struct(scene, profiles, proposal_params=None, env=None):
     s.proposal_params = None if pp is None else pp.ctypes.data
     e, erg = _env_struct(env)
     s.env = None if e is None else C.addressof(e)
-    return s, (keep, tan, inst, profiles, pp, e, erg)
+    larr = None
+    if lights:
+        larr = (type(lights[0]) * len(lights))(*lights)
+        s.lights, s.n_lights = C.addressof(larr), len(lights)
+    return s, (keep, tan, inst, profiles, pp, e, erg, larr)
 
 
 def render(scene, profiles, camera, options, width, height, frame=0, threads=0, records=False, frames=1, proposal_params=None,
-           env=None):
+           env=None, lights=None):
     """FP32 oracle render of one frame: rgb [height][width][3]; with records=True also per-path bounce
     records (prim, lobe, flags) [height*width][max_bounces+1] and stats (paths, shadow rays, evals).
     `profiles` is a ctypes array of plt_spectral_profile, `camera`/`options` the ctypes structs of
@@ -239,7 +243,7 @@ def render(scene, profiles, camera, options, width, height, frame=0, threads=0, 
         lib.plto_light_table.restype = C.c_uint32
         lib.plto_light_table.argtypes = [C.c_void_p] * 4
         lib._render_sig = True
-    s, keep = _scene_struct(scene, profiles, proposal_params, env)
+    s, keep = _scene_struct(scene, profiles, proposal_params, env, lights)
     rgb = np.zeros((height, width, 3), np.float32)
     nb = options.max_bounces + 1
     recs = [np.zeros((height * width, nb), np.uint32) for _ in range(3)] if records else [None] * 3

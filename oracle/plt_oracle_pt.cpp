@@ -12,6 +12,7 @@
 #include "plt_oracle_mlp.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <memory>
 #include <random>
@@ -74,6 +75,9 @@ struct Scene {
     std::vector<float> matFeat;        // [nmat][4]
     // environment light (EnvMap + EnvMapSampler), when present
     plt_oracle_env::EnvMap env;
+    // analytic lights (LightData) with the inverse-transpose of each transform's 3x3 part
+    std::vector<plt_analytic_light> alights;
+    std::vector<std::array<float, 9>> alightsIT;
 };
 
 struct Options {
@@ -86,6 +90,7 @@ struct Options {
     bool learned = false;
     float learnedProb = 0.5f;
     bool useEnv = false;
+    bool useAnalytic = false;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -1041,13 +1046,90 @@ struct Renderer {
 
     // getLightTypeSelectionProbabilities (LightSampling.slangh:40-55): env map, emissive geometry
     // (the scene's emissive lights when it has any), no analytic lights
-    void typeProbabilities(float& pEnv, float& pEm) const {
+    void typeProbabilities(float& pEnv, float& pEm, float& pAn) const {
         const bool useEnv = o.useEnv && s.env.present;
         const bool useEm = o.useEmissive && !s.lightTri.empty();
-        const float sum = (useEnv ? 1.f : 0.f) + (useEm ? 1.f : 0.f);
+        const bool useAn = o.useAnalytic && !s.alights.empty();
+        const float sum = (useEnv ? 1.f : 0.f) + (useEm ? 1.f : 0.f) + (useAn ? 1.f : 0.f);
         const float inv = sum > 0.f ? 1.f / sum : 0.f;
         pEnv = useEnv ? inv : 0.f;
         pEm = useEm ? inv : 0.f;
+        pAn = useAn ? inv : 0.f;
+    }
+
+    // sampleLight for analytic lights (Rendering/Lights/LightHelpers.slang:71-289)
+    bool sampleAnalytic(uint32_t li, F3 p, Solve& sv, F3& dir, float& dist, float* Li, float* wl, float& pdf) const {
+        const plt_analytic_light& L = s.alights[li];
+        const float* X = L.transform;
+        const F3 ldirW = {L.dir[0], L.dir[1], L.dir[2]};
+        if (L.type == PLT_LIGHT_POINT) {
+            const F3 toLight = F3{L.pos[0], L.pos[1], L.pos[2]} - p;
+            const float distSqr = std::max(dot(toLight, toLight), 1e-9f);
+            dist = std::sqrt(distSqr);
+            dir = toLight / dist;
+            const float cosTheta = -dot(dir, ldirW);
+            float falloff = 1.f;
+            if (cosTheta < L.cos_opening_angle) {
+                falloff = 0.f;
+            } else if (L.penumbra_angle > 0.f) {
+                const float delta = L.opening_angle - std::acos(cosTheta);
+                const float t = std::min(std::max(delta / L.penumbra_angle, 0.f), 1.f);
+                falloff = t * t * (3.f - 2.f * t);
+            }
+            sampleSpectrum(s, L.intensity_spectral_id, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Li, wl);
+            for (uint32_t j = 0; j < o.hwss; ++j) Li[j] *= falloff / distSqr;
+            pdf = 0.f;
+            return true;
+        }
+        if (L.type == PLT_LIGHT_DIRECTIONAL) {
+            dist = FLT_MAX;
+            dir = -ldirW;
+            sampleSpectrum(s, L.intensity_spectral_id, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Li, wl);
+            pdf = 0.f;
+            return true;
+        }
+        const float ux = sv.sg.next1D();
+        const float uy = sv.sg.next1D();
+        if (L.type == PLT_LIGHT_DISTANT) {
+            const float z = ux * (1.f - L.cos_subtended_angle) + L.cos_subtended_angle;
+            const float r = std::sqrt(1.f - z * z);
+            const float phi = 6.28318530717958647693f * uy;
+            const F3 d = {r * std::cos(phi), r * std::sin(phi), z};
+            dir = normalize(F3{X[0] * d.x + X[1] * d.y + X[2] * d.z, X[4] * d.x + X[5] * d.y + X[6] * d.z, X[8] * d.x + X[9] * d.y + X[10] * d.z});
+            dist = FLT_MAX;
+            const float solidAngle = 6.28318530717958647693f * (1.f - L.cos_subtended_angle);
+            sampleSpectrum(s, L.intensity_spectral_id, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Li, wl);
+            pdf = 1.f / solidAngle;
+            return true;
+        }
+        F3 lp;
+        const float phi = 6.28318530717958647693f * uy;
+        if (L.type == PLT_LIGHT_RECT) {
+            lp = {ux * 2.f - 1.f, uy * 2.f - 1.f, 0.f};
+        } else if (L.type == PLT_LIGHT_DISC) {
+            const float r = std::sqrt(ux);
+            lp = {r * std::cos(phi), r * std::sin(phi), 0.f};
+        } else {
+            const float ct = 1.0f - 2.0f * ux;
+            const float st = std::sqrt(std::max(0.0f, 1.0f - ct * ct));
+            lp = {st * std::cos(phi), st * std::sin(phi), ct};
+        }
+        const F3 posW = {X[0] * lp.x + X[1] * lp.y + X[2] * lp.z + X[3], X[4] * lp.x + X[5] * lp.y + X[6] * lp.z + X[7],
+                         X[8] * lp.x + X[9] * lp.y + X[10] * lp.z + X[11]};
+        const std::array<float, 9>& T = s.alightsIT[li];
+        const F3 nl = L.type == PLT_LIGHT_SPHERE ? lp : F3{0.f, 0.f, 1.f};
+        const F3 n = normalize(F3{T[0] * nl.x + T[1] * nl.y + T[2] * nl.z, T[3] * nl.x + T[4] * nl.y + T[5] * nl.z,
+                                  T[6] * nl.x + T[7] * nl.y + T[8] * nl.z});
+        const F3 toLight = posW - p;
+        const float distSqr = std::max(dot(toLight, toLight), 1e-9f);
+        dist = std::sqrt(distSqr);
+        dir = toLight / dist;
+        const float cosTheta = dot(n, -dir);
+        if (cosTheta <= 0.f) return false;
+        sampleSpectrum(s, L.intensity_spectral_id, sv.wavelength, sv.sg, o.importanceSampleEmitters, o.hwss, Li, wl);
+        for (uint32_t j = 0; j < o.hwss; ++j) Li[j] *= L.surface_area * cosTheta / distSqr;
+        pdf = distSqr / (cosTheta * L.surface_area);
+        return true;
     }
 
     // evalTrianglePdf (EmissiveLightSamplerHelpers.slang:120-151) x triangle selection pdf
@@ -1066,6 +1148,7 @@ struct Renderer {
     }
 
     struct LightSample {
+        bool analytic = false;
         float pdf = 0.f, distance = 0.f;
         F3 origin = {0.f, 0.f, 0.f}, dir = {0.f, 0.f, 0.f};
         Beam<float> beam;
@@ -1081,8 +1164,8 @@ struct Renderer {
         // selectLightType (LightSampling.slangh:40-84): the environment map and emissive geometry
         SampleGen& selSg = o.perTileSg ? sv.tilesg : sv.sg;
         float u = selSg.next1D();
-        float pEnv, pEm;
-        typeProbabilities(pEnv, pEm);
+        float pEnv, pEm, pAn;
+        typeProbabilities(pEnv, pEm, pAn);
         float selectionPdf;
         bool envSel;
         if (u < pEnv) {
@@ -1090,7 +1173,39 @@ struct Renderer {
             selectionPdf = pEnv;
         } else {
             u -= pEnv;
-            if (!(u < pEm)) return false;
+            if (!(u < pEm)) {
+                u -= pEm;
+                if (!(u < pAn)) return false;
+                // generateAnalyticLightSample (LightSampling.slangh:128-164)
+                ls.analytic = true;
+                const uint32_t n = (uint32_t)s.alights.size();
+                const uint32_t li = std::min((uint32_t)(sv.sg.next1D() * (float)n), n - 1);
+                const plt_analytic_light& AL = s.alights[li];
+                float Li[MAXH], swl[MAXH], apdf;
+                for (int j = 0; j < MAXH; ++j) { Li[j] = 0.f; swl[j] = 0.f; }
+                F3 dir;
+                float dist;
+                if (!sampleAnalytic(li, sd.posW, sv, dir, dist, Li, swl, apdf)) return false;
+                bool anyPos = false;
+                for (uint32_t j = 0; j < o.hwss; ++j) {
+                    Li[j] *= (float)n;
+                    anyPos = anyPos || Li[j] > 0.f;
+                }
+                ls.pdf = apdf / (float)n;
+                ls.origin = newRayOriginToward(sd, dir);
+                ls.distance = dist;
+                ls.dir = dir;
+                if (AL.type == PLT_LIGHT_DIRECTIONAL || AL.type == PLT_LIGHT_DISTANT) {
+                    const float omega = 4.f * 3.14159265358979323846f * (1.f - AL.cos_subtended_angle * AL.cos_subtended_angle);
+                    ls.beam = sourceBeamDistant(-dir, omega, Li, swl, o.hwss, o.maxBeamOmega);
+                } else {
+                    ls.beam = sourceBeamArea(F3{AL.pos[0], AL.pos[1], AL.pos[2]}, -dir, AL.surface_area, dist, Li, swl, o.hwss, o.maxBeamOmega);
+                }
+                ls.pdf *= pAn;
+                scaleBeam(ls.beam, 1.f / pAn);
+                const bool isReflection = dot(sd.faceN, ls.dir) * dot(sd.faceN, sd.V) > 0.f;
+                return anyPos && ls.pdf > 1e-6f && !(!sampleRefl && isReflection) && !(!sampleTrans && !isReflection);
+            }
             envSel = false;
             selectionPdf = pEm;
         }
@@ -1323,7 +1438,7 @@ struct Renderer {
         for (int j = 0; j < ls.beam.H; ++j) anyL = anyL || ls.beam.L[0][j] > 0.f;
         if (!anyL) return;
         if (!o.hwssMis && (bounce.flags & FLAG_DISPERSIVE)) ls.beam.H = 1;
-        const bool doMis = o.doMis;
+        const bool doMis = o.doMis && !ls.analytic;   // pltpt_solve.rt.slang:276
         bool evalCurrentVertex = true;
         const int maxMSBounces = (int)o.maxBounces - p;
         if (!o.doMnee || maxMSBounces <= 0) {
@@ -1392,8 +1507,8 @@ struct Renderer {
         const bool needMIS = o.doMis && didNEE;
         const uint32_t light = s.primToLight[bounce.prim];
         const F3 hn = sd.frontFacing ? sd.faceN : -sd.faceN;
-        float pEnv, pEm;
-        typeProbabilities(pEnv, pEm);
+        float pEnv, pEm, pAn;
+        typeProbabilities(pEnv, pEm, pAn);
         const float lightPdf = pEm * emissivePdf(sv.pathOrigin, light, sd.posW, hn);
         const float misWeight = needMIS ? MISWeight(bounce.lastNonDeltaPdf, lightPdf) : 1.f;
         float Le[MAXH], swl[MAXH];
@@ -1420,8 +1535,8 @@ struct Renderer {
         const bool didNEE = wasNEEAvailable(p, bounce.flags);
         if (!(o.useEnv && s.env.present && (o.doMis || !didNEE))) return;
         const bool needMIS = o.doMis && didNEE;
-        float pEnv, pEm;
-        typeProbabilities(pEnv, pEm);
+        float pEnv, pEm, pAn;
+        typeProbabilities(pEnv, pEm, pAn);
         const float nwo[3] = {-wo.x, -wo.y, -wo.z};
         const float lightPdf = pEnv * s.env.evalPdf(nwo);
         const float misWeight = needMIS ? MISWeight(bounce.lastNonDeltaPdf, lightPdf) : 1.f;
@@ -1482,6 +1597,8 @@ typedef struct plto_scene {
     const plt_spectral_profile* profiles;
     const float* proposal_params;        // [11488] learned proposal parameters (learned_proposal renders), or NULL
     const struct plto_env* env;          // environment light, or NULL
+    const plt_analytic_light* lights;    // analytic lights, or NULL
+    uint32_t n_lights;
 } plto_scene;
 
 // Environment light: [height][width][3] linear RGB lat-long map, intensity, tint, Euler XYZ degrees.
@@ -1583,6 +1700,20 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.learned = opt->learned_proposal != 0;
     o.learnedProb = opt->learned_proposal_prob;
     o.useEnv = opt->use_env_light != 0;
+    o.useAnalytic = opt->use_analytic_lights != 0;
+    for (uint32_t i = 0; i < sc->n_lights; ++i) {
+        const plt_analytic_light& l = sc->lights[i];
+        s.alights.push_back(l);
+        const float* t = l.transform;
+        const double a[9] = {t[0], t[1], t[2], t[4], t[5], t[6], t[8], t[9], t[10]};
+        const double cof[9] = {a[4] * a[8] - a[5] * a[7], a[5] * a[6] - a[3] * a[8], a[3] * a[7] - a[4] * a[6],
+                               a[2] * a[7] - a[1] * a[8], a[0] * a[8] - a[2] * a[6], a[1] * a[6] - a[0] * a[7],
+                               a[1] * a[5] - a[2] * a[4], a[2] * a[3] - a[0] * a[5], a[0] * a[4] - a[1] * a[3]};
+        const double det = a[0] * cof[0] + a[1] * cof[1] + a[2] * cof[2];
+        std::array<float, 9> it{};
+        for (int k = 0; k < 9; ++k) it[k] = det != 0.0 ? (float)(cof[k] / det) : 0.f;
+        s.alightsIT.push_back(it);
+    }
     if (!loadEnv(sc->env, s.env)) return PLT_INVALID_ARG;
     if (o.learned) {
         if (!sc->proposal_params || !(o.learnedProb > 0.f && o.learnedProb < 1.f)) return PLT_INVALID_ARG;

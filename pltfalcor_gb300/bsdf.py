@@ -230,6 +230,11 @@ class PLTContext:
         capi.check(self.lib.plt_set_env_map(self.handle, a.ctypes.data_as(C.POINTER(C.c_float)), a.shape[1], a.shape[0],
                                             a.shape[2], float(intensity), t, r), "plt_set_env_map")
 
+    def set_analytic_lights(self, lights):
+        """plt_set_analytic_lights from a list of capi.AnalyticLight (scene.*_light helpers)."""
+        arr = (capi.AnalyticLight * max(1, len(lights)))(*lights)
+        capi.check(self.lib.plt_set_analytic_lights(self.handle, arr if lights else None, len(lights)), "plt_set_analytic_lights")
+
     def clear_env_map(self):
         capi.check(self.lib.plt_clear_env_map(self.handle), "plt_clear_env_map")
 

@@ -81,6 +81,15 @@ class SceneDesc(C.Structure):
                 ("tri_material", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p), ("tri_instance", C.c_void_p)]
 
 
+LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_DISTANT, LIGHT_RECT, LIGHT_DISC, LIGHT_SPHERE = range(6)
+
+
+class AnalyticLight(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("intensity_spectral_id", C.c_uint32), ("pos", C.c_float * 3), ("dir", C.c_float * 3),
+                ("opening_angle", C.c_float), ("cos_opening_angle", C.c_float), ("penumbra_angle", C.c_float),
+                ("cos_subtended_angle", C.c_float), ("surface_area", C.c_float), ("transform", C.c_float * 12)]
+
+
 class RenderView(C.Structure):
     _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("pad", C.c_uint32),
                 ("camera", Camera), ("out_rgba", C.c_void_p)]
@@ -110,7 +119,7 @@ EXPORTED_SYMBOLS = [
     "plt_add_scene", "plt_clear_scenes", "plt_render_scenes", "plt_set_launch_shape", "plt_get_launch_shape", "plt_render_tune",
     "plt_spectral_profile_from_spd", "plt_write_exr", "plt_render_counters",
     "plt_set_env_map", "plt_clear_env_map", "plt_env_map_query",
-    "plt_spectral_profiles_from_material", "plt_spectral_profile_for_emitter_type",
+    "plt_spectral_profiles_from_material", "plt_spectral_profile_for_emitter_type", "plt_set_analytic_lights",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -175,6 +184,7 @@ def load_library(path=LIB_PATH):
         "plt_render_counters": (i32, [vp, C.POINTER(C.c_uint64), u32]),
         "plt_set_env_map": (i32, [vp, C.POINTER(C.c_float), u32, u32, u32, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "plt_clear_env_map": (i32, [vp]),
+        "plt_set_analytic_lights": (i32, [vp, vp, u32]),
         "plt_spectral_profiles_from_material": (i32, [C.c_char_p, C.c_char_p, vp, vp]),
         "plt_spectral_profile_for_emitter_type": (i32, [C.c_char_p, C.c_char_p, C.c_float, vp]),
         "plt_env_map_query": (i32, [vp, vp, vp, u32, vp, vp]),

@@ -116,6 +116,9 @@ struct plt_context {
     float* dEnvImp = nullptr;
     plt::EnvDev env{};
     bool hasEnv = false;
+    // analytic lights
+    plt::AnalyticLightDev* dALights = nullptr;
+    uint32_t nALights = 0;
 };
 
 // Frees the render-pass state of a context (plt_render.cpp).

@@ -64,7 +64,7 @@ constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 // option bits of PtParams.opt
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
-                   kPtLearned = 0x200u, kPtUseEnv = 0x400u;
+                   kPtLearned = 0x200u, kPtUseEnv = 0x400u, kPtUseAnalytic = 0x800u;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
 
@@ -94,6 +94,23 @@ struct EnvDev {
     uint32_t mipOff[kEnvMaxMips];
     float toWorld[9], toLocal[9];
     float scale[3];               // intensity * tint
+};
+
+// An analytic light on the device (LightData): the position, direction and spot parameters, the
+// distant light's subtended angle, the area light's surface area and model-to-world transform (rows
+// of a 3x4) with the inverse-transpose of its 3x3 part (normals), and the area lights' constant
+// world normal normalize(transMatIT (0, 0, 1)).
+struct AnalyticLightDev {
+    float pos[3];
+    uint32_t type;
+    float dir[3];
+    uint32_t spectrumId;
+    float openingAngle, cosOpeningAngle, penumbraAngle, cosSubtendedAngle;
+    float surfaceArea;
+    float nrm[3];
+    float xf[12];
+    float xfIT[9];
+    float pad[3];
 };
 
 // Launch shape of a render (chosen by plt_render_tune; zeros: defaults): paths per wave (0 = all
@@ -177,8 +194,10 @@ struct PtParams {
     void* mneeTasks;              // [mneeCap] tasks of kMneeTaskBytes
     uint32_t mneeCap;
     uint32_t* mneeCount;
-    // environment light (kPtUseEnv)
+    // environment light (kPtUseEnv) and analytic lights (kPtUseAnalytic)
     EnvDev env;
+    const AnalyticLightDev* alights;
+    uint32_t nALights;
     // outputs
     double* accum;                // [npix][3]
     unsigned long long* stats;    // [4] bounces recorded, shadow rays, forward BSDF evaluations, traversal bytes

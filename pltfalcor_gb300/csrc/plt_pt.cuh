@@ -1163,6 +1163,7 @@ template <int H> struct MneeTask {
     MSData ms;
     f3 tposW, ldir, msOrigin;
     float ldist, tpdf;
+    float srcSize;                // the sourced beam's area (area lights) or solid angle (distant lights)
     float Le[H], swl[H];
     uint32_t pid, p, curMS;
 };
@@ -1276,6 +1277,94 @@ PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int
     if (isfinite(r) && isfinite(g) && isfinite(bb)) { Lr += r; Lg += g; Lb += bb; }
 }
 
+// sampleLight for analytic lights (Rendering/Lights/LightHelpers.slang:71-289): the direction and
+// distance to the light, the incident radiance already divided by the pdf (Li, at the sampled
+// wavelengths wl) and the solid-angle pdf (0 for point and directional lights).  False when the
+// light yields no sample (an area light seen from behind).
+template <int H>
+PLT_DI bool sampleAnalytic(const PtParams& P, const plt::AnalyticLightDev& L, f3 p, float wavelength, SampleGen& sg, bool importance,
+                           f3& dir, float& dist, float* Li, float* wl, float& pdf) {
+    const uint32_t type = L.type;
+    if (type == PLT_LIGHT_POINT) {
+        const f3 toLight = mk3(L.pos[0], L.pos[1], L.pos[2]) - p;
+        const float distSqr = fmaxf(dot(toLight, toLight), 1e-9f);
+        dist = sqrtf(distSqr);
+        dir = toLight / dist;
+        const float cosTheta = -dot(dir, mk3(L.dir[0], L.dir[1], L.dir[2]));
+        float falloff = 1.f;
+        if (cosTheta < L.cosOpeningAngle) {
+            falloff = 0.f;
+        } else if (L.penumbraAngle > 0.f) {
+            const float delta = L.openingAngle - acosf(cosTheta);
+            const float t = clampf(delta / L.penumbraAngle, 0.f, 1.f);
+            falloff = t * t * (3.f - 2.f * t);
+        }
+        sampleSpectrum<H>(P, L.spectrumId, wavelength, sg, importance, Li, wl);
+#pragma unroll
+        for (int j = 0; j < H; ++j) Li[j] *= falloff / distSqr;
+        pdf = 0.f;
+        return true;
+    }
+    if (type == PLT_LIGHT_DIRECTIONAL) {
+        dist = kFltMax;
+        dir = -mk3(L.dir[0], L.dir[1], L.dir[2]);
+        sampleSpectrum<H>(P, L.spectrumId, wavelength, sg, importance, Li, wl);
+        pdf = 0.f;
+        return true;
+    }
+    const float ux = sg.next1D();
+    const float uy = sg.next1D();
+    if (type == PLT_LIGHT_DISTANT) {
+        // sample_cone (MathHelpers.slang:270-276) in the light's frame
+        const float z = ux * (1.f - L.cosSubtendedAngle) + L.cosSubtendedAngle;
+        const float r = sqrtf(1.f - z * z);
+        float sp, cp;
+        sincosf(k2Pi * uy, &sp, &cp);
+        const f3 d = mk3(r * cp, r * sp, z);
+        dir = normalize(mk3(L.xf[0] * d.x + L.xf[1] * d.y + L.xf[2] * d.z, L.xf[4] * d.x + L.xf[5] * d.y + L.xf[6] * d.z,
+                            L.xf[8] * d.x + L.xf[9] * d.y + L.xf[10] * d.z));
+        dist = kFltMax;
+        const float solidAngle = k2Pi * (1.f - L.cosSubtendedAngle);
+        sampleSpectrum<H>(P, L.spectrumId, wavelength, sg, importance, Li, wl);
+        pdf = 1.f / solidAngle;
+        return true;
+    }
+    // area lights: a point on the shape in object space, then finalizeAreaLightSample
+    f3 lp, n;
+    if (type == PLT_LIGHT_RECT) {
+        lp = mk3(ux * 2.f - 1.f, uy * 2.f - 1.f, 0.f);
+    } else if (type == PLT_LIGHT_DISC) {
+        const float r = sqrtf(ux);
+        float sp, cp;
+        sincosf(k2Pi * uy, &sp, &cp);
+        lp = mk3(r * cp, r * sp, 0.f);
+    } else {
+        float sp, cp;
+        sincosf(k2Pi * uy, &sp, &cp);
+        const float ct = 1.0f - 2.0f * ux;
+        const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        lp = mk3(st * cp, st * sp, ct);
+    }
+    const f3 posW = mk3(L.xf[0] * lp.x + L.xf[1] * lp.y + L.xf[2] * lp.z + L.xf[3], L.xf[4] * lp.x + L.xf[5] * lp.y + L.xf[6] * lp.z + L.xf[7],
+                        L.xf[8] * lp.x + L.xf[9] * lp.y + L.xf[10] * lp.z + L.xf[11]);
+    if (type == PLT_LIGHT_SPHERE)
+        n = normalize(mk3(L.xfIT[0] * lp.x + L.xfIT[1] * lp.y + L.xfIT[2] * lp.z, L.xfIT[3] * lp.x + L.xfIT[4] * lp.y + L.xfIT[5] * lp.z,
+                          L.xfIT[6] * lp.x + L.xfIT[7] * lp.y + L.xfIT[8] * lp.z));
+    else
+        n = mk3(L.nrm[0], L.nrm[1], L.nrm[2]);
+    const f3 toLight = posW - p;
+    const float distSqr = fmaxf(dot(toLight, toLight), 1e-9f);
+    dist = sqrtf(distSqr);
+    dir = toLight / dist;
+    const float cosTheta = dot(n, -dir);
+    if (cosTheta <= 0.f) return false;
+    sampleSpectrum<H>(P, L.spectrumId, wavelength, sg, importance, Li, wl);
+#pragma unroll
+    for (int j = 0; j < H; ++j) Li[j] *= L.surfaceArea * cosTheta / distSqr;
+    pdf = distSqr / (cosTheta * L.surfaceArea);
+    return true;
+}
+
 // evalTrianglePdf x triangle-selection pdf (EmissiveLightSamplerHelpers.slang:120-151,
 // EmissivePowerSampler.slang:81-122)
 PLT_DI float emissivePdf(const PtParams& P, const PtScene& S, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
@@ -1307,6 +1396,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     const bool importance = (P.opt & plt::kPtImportanceEmit) != 0;
     const bool doMnee = MNEE && (P.opt & plt::kPtDoMnee) != 0;
     const bool useEnv = (P.opt & plt::kPtUseEnv) != 0;
+    const bool useAnalytic = (P.opt & plt::kPtUseAnalytic) != 0;
     TraceCounters tc{0u, 0u, 0u, 0u};
     uint32_t evals = 0;
     MSData ms;
@@ -1324,11 +1414,12 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
         f3 pathOrigin = camPos(S);
         // light-type selection probabilities (getLightTypeSelectionProbabilities,
-        // LightSampling.slangh:40-55): the environment map and this scene's emissive geometry
+        // LightSampling.slangh:40-55): the environment map, this scene's emissive geometry and the
+        // analytic lights
         const bool hasEm = useEmissive && S.nLights > 0;
-        const float pSum = (useEnv ? 1.f : 0.f) + (hasEm ? 1.f : 0.f);
+        const float pSum = (useEnv ? 1.f : 0.f) + (hasEm ? 1.f : 0.f) + (useAnalytic ? 1.f : 0.f);
         const float invPSum = pSum > 0.f ? 1.f / pSum : 0.f;
-        const float pEnv = useEnv ? invPSum : 0.f, pEm = hasEm ? invPSum : 0.f;
+        const float pEnv = useEnv ? invPSum : 0.f, pEm = hasEm ? invPSum : 0.f, pAn = useAnalytic ? invPSum : 0.f;
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
         for (int p = 0; p <= (int)P.maxBounces; ++p) {
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
@@ -1381,22 +1472,30 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     SampleGen& selSg = (P.opt & plt::kPtPerTileSg) ? tilesg : sg;
                     float uType = selSg.next1D();
                     float selPdf;
-                    bool distant;
+                    int kind;   // 0 environment map, 1 emissive geometry, 2 analytic light
                     if (uType < pEnv) {
                         selPdf = pEnv;
-                        distant = true;
+                        kind = 0;
                     } else {
                         uType -= pEnv;
-                        if (!(uType < pEm)) continue;
-                        selPdf = pEm;
-                        distant = false;
+                        if (uType < pEm) {
+                            selPdf = pEm;
+                            kind = 1;
+                        } else {
+                            uType -= pEm;
+                            if (!(uType < pAn)) continue;
+                            selPdf = pAn;
+                            kind = 2;
+                        }
                     }
+                    bool distant = kind == 0;
+                    const bool misHere = doMis && kind != 2;   // no MIS for analytic lights (pltpt_solve.rt.slang:276)
                     const float invSel = 1.f / selPdf;
                     float Le[H], swl[H];
                     float tpdf;
                     bool anyPos = false;
                     f3 tposW, lorg, ldir;
-                    float ldist;
+                    float ldist, srcSize;
                     if (distant) {
                         // generateEnvMapSample (LightSampling.slangh:86-104, EnvMapSampler.slang:52-113)
                         const float e0 = sg.next1D();
@@ -1416,7 +1515,35 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                         lorg = newRayOriginToward(sd, ldir);
                         ldist = kFltMax;
                         tposW = lorg;
-                        sourceBeamDistant<H>(pb, -ldir, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
+                        srcSize = P.maxBeamOmega;
+                        sourceBeamDistant<H>(pb, -ldir, srcSize, Le, swl, P.maxBeamOmega);
+                    } else if (kind == 2) {
+                        // generateAnalyticLightSample (LightSampling.slangh:128-164): a light
+                        // chosen uniformly, sampleLight, a distant or an area beam
+                        const uint32_t nA = P.nALights;
+                        const uint32_t li = min((uint32_t)(sg.next1D() * (float)nA), nA - 1);
+                        const plt::AnalyticLightDev& AL = P.alights[li];
+                        float apdf;
+                        if (!sampleAnalytic<H>(P, AL, sd.posW, wavelength, sg, importance, ldir, ldist, Le, swl, apdf)) continue;
+#pragma unroll
+                        for (int j = 0; j < H; ++j) {
+                            Le[j] *= (float)nA;
+                            anyPos = anyPos || Le[j] > 0.f;
+                            Le[j] *= invSel;
+                        }
+                        tpdf = (apdf / (float)nA) * selPdf;
+                        lorg = newRayOriginToward(sd, ldir);
+                        distant = AL.type == PLT_LIGHT_DIRECTIONAL || AL.type == PLT_LIGHT_DISTANT;
+                        if (distant) {
+                            // Omega = 4 pi (1 - cos^2) as the reference computes it
+                            srcSize = 4.f * kPi * (1.f - AL.cosSubtendedAngle * AL.cosSubtendedAngle);
+                            tposW = mk3(0.f, 0.f, 0.f);
+                            sourceBeamDistant<H>(pb, -ldir, srcSize, Le, swl, P.maxBeamOmega);
+                        } else {
+                            srcSize = AL.surfaceArea;
+                            tposW = mk3(AL.pos[0], AL.pos[1], AL.pos[2]);
+                            sourceBeamArea<H>(pb, tposW, -ldir, srcSize, ldist, Le, swl, P.maxBeamOmega);
+                        }
                     } else {
                         const float uLight = sg.next1D();
                         uint32_t ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
@@ -1453,7 +1580,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                         const f3 toLight = lightPos - lorg;
                         ldist = sqrtf(dot(toLight, toLight));
                         ldir = rnormalize(toLight);
-                        sourceBeamArea<H>(pb, tposW, -ldir, P.sourcingArea, ldist, Le, swl, P.maxBeamOmega);
+                        srcSize = P.sourcingArea;
+                        sourceBeamArea<H>(pb, tposW, -ldir, srcSize, ldist, Le, swl, P.maxBeamOmega);
                     }
                     const bool isRefl = dot(sd.faceN, ldir) * dot(sd.faceN, sd.V) > 0.f;
                     if (!(anyPos && tpdf > 1e-6f && !(!sampleRefl && isRefl) && !(!sampleTrans && !isRefl))) continue;
@@ -1465,7 +1593,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                         const TraceResult vis =
                             traverse<true>(nodes, P.tris, lorg.x, lorg.y, lorg.z, ldir.x, ldir.y, ldir.z, 0.f, ldist, tc.nv, tc.tt, tc.overflow, root);
                         if (vis.prim != kNoHit) continue;
-                        if (doMis) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
+                        if (misHere) scaleBeam(pb, misWeight(tpdf, ptPdf(m, type, sd, ldir, pb.b.wl[0])));
                     } else {
                         // manifold sampling on NEE, pltpt_solve.rt.slang:293-353
                         const f3 lightDir = ldir;
@@ -1496,11 +1624,12 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 t->msOrigin = msOrigin;
                                 t->ldist = ldist;
                                 t->tpdf = tpdf;
+                                t->srcSize = srcSize;
 #pragma unroll
                                 for (int j = 0; j < H; ++j) { t->Le[j] = Le[j]; t->swl[j] = swl[j]; }
                                 t->pid = pid;
                                 t->p = (uint32_t)p;
-                                t->curMS = (curMS ? 1u : 0u) | (distant ? 2u : 0u);
+                                t->curMS = (curMS ? 1u : 0u) | (distant ? 2u : 0u) | (misHere ? 0u : 4u);
                                 continue;
                             }
                             if (!manifoldWalk(P, root, msOrigin, tposW, ldir, distant, ms, tc)) continue;
@@ -1520,7 +1649,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 misBsdfPdf = bounce.lndp;
                             }
                         }
-                        if (doMis) {
+                        if (misHere) {
                             if (ms.hitCount == 0 || !curMS) misBsdfPdf = ptPdf(m, type, sd, lsDir, pb.b.wl[0]);
                             scaleBeam(pb, misWeight(tpdf, misBsdfPdf * ms.pdf));
                         }
@@ -1590,6 +1719,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
         const int p = (int)t.p;
         const bool curMS = (t.curMS & 1u) != 0;
         const bool distant = (t.curMS & 2u) != 0;
+        const bool misHere = doMis && (t.curMS & 4u) == 0;
         const f3 msOrigin = t.msOrigin;
         const uint32_t gp = P.pidBase + pid;
         const PtScene& S = P.scenes[sceneOf(P, gp)];
@@ -1604,8 +1734,8 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
 #pragma unroll
         for (int j = 0; j < H; ++j) { Le[j] = t.Le[j]; swl[j] = t.swl[j]; }
         PBeam<H> pb;
-        if (distant) sourceBeamDistant<H>(pb, -t.ldir, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
-        else sourceBeamArea<H>(pb, t.tposW, -t.ldir, P.sourcingArea, t.ldist, Le, swl, P.maxBeamOmega);
+        if (distant) sourceBeamDistant<H>(pb, -t.ldir, t.srcSize, Le, swl, P.maxBeamOmega);
+        else sourceBeamArea<H>(pb, t.tposW, -t.ldir, t.srcSize, t.ldist, Le, swl, P.maxBeamOmega);
         if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
         bool evalCurrent = true;
         float misBsdfPdf = 0.f;
@@ -1619,7 +1749,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
             evalCurrent = false;
             misBsdfPdf = bounce.lndp;
         }
-        if (doMis) {
+        if (misHere) {
             if (!curMS) misBsdfPdf = ptPdf(m, type, sd, lsDir, pb.b.wl[0]);
             scaleBeam(pb, misWeight(t.tpdf, misBsdfPdf * ms.pdf));
         }

@@ -250,8 +250,11 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
             (nee && o.do_mis ? plt::kPtDoMis : 0u) | (o.do_russian_roulette ? plt::kPtDoRR : 0u) |
             (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u) |
             (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u) |
-            (o.use_env_light && ctx->hasEnv ? plt::kPtUseEnv : 0u);
+            (o.use_env_light && ctx->hasEnv ? plt::kPtUseEnv : 0u) |
+            (o.use_analytic_lights && ctx->nALights ? plt::kPtUseAnalytic : 0u);
     P.env = ctx->env;
+    P.alights = ctx->dALights;
+    P.nALights = ctx->nALights;
     P.propNet = ctx->dPropBf16;
     P.matFeat = ctx->dMatFeat;
     P.propProb = o.learned_proposal_prob;

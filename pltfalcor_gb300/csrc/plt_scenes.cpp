@@ -261,6 +261,9 @@ void envRotation(const float deg[3], float toWorld[9], float toLocal[9]) {
 }  // namespace
 
 void pltReleaseEnv(plt_context* ctx) {
+    cudaFree(ctx->dALights);
+    ctx->dALights = nullptr;
+    ctx->nALights = 0;
     cudaFree(ctx->dEnvTex);
     cudaFree(ctx->dEnvImp);
     ctx->dEnvTex = nullptr;
@@ -491,7 +494,58 @@ plt_status plt_set_env_map(plt_context* ctx, const float* pixels, uint32_t width
 
 plt_status plt_clear_env_map(plt_context* ctx) {
     if (!ctx) return PLT_INVALID_ARG;
-    pltReleaseEnv(ctx);
+    cudaFree(ctx->dEnvTex);
+    cudaFree(ctx->dEnvImp);
+    ctx->dEnvTex = nullptr;
+    ctx->dEnvImp = nullptr;
+    ctx->envTexCap = 0;
+    ctx->env = plt::EnvDev{};
+    ctx->hasEnv = false;
+    return PLT_OK;
+}
+
+// The scene's analytic lights (LightData, Scene/Lights/Light.cpp): validated and uploaded with the
+// inverse-transpose of each transform (AnalyticAreaLight::update, Light.cpp:341-346) and the area
+// lights' world normal (LightHelpers.slang:112, 164).
+plt_status plt_set_analytic_lights(plt_context* ctx, const plt_analytic_light* lights, uint32_t count) {
+    if (!ctx || (count > 0 && !lights)) return PLT_INVALID_ARG;
+    std::vector<plt::AnalyticLightDev> h(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const plt_analytic_light& l = lights[i];
+        if (l.type > PLT_LIGHT_SPHERE) return PLT_INVALID_ARG;
+        if (l.intensity_spectral_id != PLT_NO_SPECTRAL_PROFILE && l.intensity_spectral_id >= ctx->nProfiles) return PLT_INVALID_ARG;
+        plt::AnalyticLightDev& d = h[i];
+        std::memset(&d, 0, sizeof(d));
+        for (int k = 0; k < 3; ++k) { d.pos[k] = l.pos[k]; d.dir[k] = l.dir[k]; }
+        d.type = l.type;
+        d.spectrumId = l.intensity_spectral_id;
+        d.openingAngle = l.opening_angle;
+        d.cosOpeningAngle = l.cos_opening_angle;
+        d.penumbraAngle = l.penumbra_angle;
+        d.cosSubtendedAngle = l.cos_subtended_angle;
+        d.surfaceArea = l.surface_area;
+        for (int k = 0; k < 12; ++k) d.xf[k] = l.transform[k];
+        // inverse-transpose of the 3x3 part (cofactor matrix / determinant)
+        const double a[9] = {l.transform[0], l.transform[1], l.transform[2], l.transform[4], l.transform[5], l.transform[6],
+                             l.transform[8], l.transform[9], l.transform[10]};
+        const double cof[9] = {a[4] * a[8] - a[5] * a[7], a[5] * a[6] - a[3] * a[8], a[3] * a[7] - a[4] * a[6],
+                               a[2] * a[7] - a[1] * a[8], a[0] * a[8] - a[2] * a[6], a[1] * a[6] - a[0] * a[7],
+                               a[1] * a[5] - a[2] * a[4], a[2] * a[3] - a[0] * a[5], a[0] * a[4] - a[1] * a[3]};
+        const double det = a[0] * cof[0] + a[1] * cof[1] + a[2] * cof[2];
+        if (l.type >= PLT_LIGHT_DISTANT && !(std::fabs(det) > 0.0)) return PLT_INVALID_ARG;
+        for (int k = 0; k < 9; ++k) d.xfIT[k] = std::fabs(det) > 0.0 ? (float)(cof[k] / det) : 0.f;
+        const float n[3] = {d.xfIT[2], d.xfIT[5], d.xfIT[8]};
+        const float len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int k = 0; k < 3; ++k) d.nrm[k] = len > 0.f ? n[k] / len : 0.f;
+    }
+    cudaFree(ctx->dALights);
+    ctx->dALights = nullptr;
+    ctx->nALights = 0;
+    if (count) {
+        PLT_CUDA(ctx, cudaMalloc(&ctx->dALights, sizeof(plt::AnalyticLightDev) * count));
+        PLT_CUDA(ctx, cudaMemcpy(ctx->dALights, h.data(), sizeof(plt::AnalyticLightDev) * count, cudaMemcpyHostToDevice));
+    }
+    ctx->nALights = count;
     return PLT_OK;
 }
 

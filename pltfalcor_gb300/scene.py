@@ -185,6 +185,98 @@ def sky_env(width=256, height=128, seed=1, sun=(0.35, 0.22), sun_radiance=200.0)
     return img.astype(np.float32)
 
 
+def floor_spheres_scene(emitter=True):
+    """A diffuse floor (albedo 0.7) with closed spheres standing on it (every hit front-facing) and,
+    optionally, a small emissive quad facing the floor."""
+    verts, faces, mats, norms = [], [], [], []
+
+    def add(v, f, m, n):
+        faces.append(np.asarray(f) + sum(len(x) for x in verts))
+        verts.append(np.asarray(v, np.float64))
+        mats.append(np.full(len(f), m, np.uint32))
+        norms.append(np.broadcast_to(np.asarray(n, np.float64), np.shape(v)))
+
+    v, f = grid_quad(np.array([-60.0, -60.0, 0.0]), np.array([120.0, 0, 0]), np.array([0, 120.0, 0]), 4)
+    add(v, f, 0, (0.0, 0.0, 1.0))
+    sv, sf = icosphere(3)
+    for c, r in (((-2.0, 1.0, 1.0), 1.0), ((1.5, 2.5, 1.5), 1.5), ((2.0, -1.5, 0.6), 0.6)):
+        add(sv * r + np.array(c), sf, 0, sv)
+    emissive = []
+    if emitter:
+        e1, e2 = np.array([0.0, 1.0, 0.0]), np.array([1.0, 0.0, 0.0])
+        v, f = grid_quad(np.array([-0.5, -0.5, 6.0]), e1, e2, 1)
+        emissive = list(range(sum(len(x) for x in faces), sum(len(x) for x in faces) + len(f)))
+        add(v, f, 1, (0.0, 0.0, -1.0))
+    recs = np.concatenate([M.diffuse(1, albedo=(0.7, 0.7, 0.7)), M.diffuse(1, albedo=(0.5, 0.5, 0.5), emission_id=8)])
+    n = np.concatenate(norms)
+    n = n / np.linalg.norm(n, axis=1, keepdims=True)
+    return Scene(np.concatenate(verts), np.concatenate(faces), np.concatenate(mats), recs, emissive, 1, 0, (-60, 60),
+                   normals=n, tri_instance=np.arange(len(faces)).repeat([len(x) for x in faces]).astype(np.uint32))
+
+
+def _light(kind, spectrum, pos=(0.0, 0.0, 0.0), direction=(0.0, -1.0, 0.0), transform=None):
+    from . import capi
+    L = capi.AnalyticLight()
+    L.type, L.intensity_spectral_id = kind, spectrum
+    d = _unit(direction)
+    for i in range(3):
+        L.pos[i], L.dir[i] = float(pos[i]), float(d[i])
+    # LightData defaults (Scene/Lights/LightData.slang:48-67)
+    L.opening_angle, L.cos_opening_angle, L.penumbra_angle = float(np.pi), -1.0, 0.0
+    L.cos_subtended_angle = 0.9999893
+    T = np.eye(4)[:3] if transform is None else np.asarray(transform, np.float64).reshape(3, 4)
+    for i in range(12):
+        L.transform[i] = float(T.ravel()[i])
+    return L, T
+
+
+def point_light(pos, spectrum, direction=(0.0, -1.0, 0.0), opening_angle=np.pi, penumbra_angle=0.0):
+    """PointLight (a spot light when opening_angle < pi): Light.cpp setOpeningAngle / setPenumbraAngle."""
+    L, _ = _light(0, spectrum, pos, direction)
+    L.opening_angle = float(opening_angle)
+    L.cos_opening_angle = float(np.cos(np.float32(opening_angle)))
+    L.penumbra_angle = float(penumbra_angle)
+    return L
+
+
+def directional_light(direction, spectrum):
+    return _light(1, spectrum, direction=direction)[0]
+
+
+def distant_light(direction, spectrum, half_angle=0.5 * np.pi / 180.0):
+    """DistantLight: cosSubtendedAngle = cos(half angle), the frame rotating +z onto -dir
+    (DistantLight::update, Light.cpp:295-312)."""
+    d = _unit(direction)
+    up = np.array([0.0, 0.0, 1.0])
+    v = np.cross(up, -d)
+    s = np.linalg.norm(v)
+    R = np.eye(3)
+    if s > 0:
+        k = v / s
+        c = np.dot(up, -d)
+        K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+        R = np.eye(3) + s * K + (1 - c) * (K @ K)
+    T = np.concatenate([R, np.zeros((3, 1))], 1)
+    L, _ = _light(2, spectrum, direction=direction, transform=T)
+    L.cos_subtended_angle = float(np.cos(half_angle))
+    return L
+
+
+def area_light(kind, transform, spectrum):
+    """RectLight / DiscLight / SphereLight with a 3x4 model-to-world transform; surface area as the
+    classes' update() computes it (Light.cpp:360-402)."""
+    from . import capi
+    L, T = _light({"rect": capi.LIGHT_RECT, "disc": capi.LIGHT_DISC, "sphere": capi.LIGHT_SPHERE}[kind], spectrum, transform=transform)
+    rx, ry, rz = (float(np.linalg.norm(T[:, i])) for i in range(3))
+    if kind == "rect":
+        L.surface_area = 4.0 * rx * ry
+    elif kind == "disc":
+        L.surface_area = float(np.pi) * rx * ry
+    else:
+        L.surface_area = 4.0 * float(np.pi) * ((rx * ry) ** 1.6 + (ry * rz) ** 1.6 + (rx * rz) ** 1.6 / 3.0) ** (1.0 / 1.6)
+    return L
+
+
 def _unit(v):
     v = np.asarray(v, np.float64)
     return v / np.linalg.norm(v)

@@ -160,36 +160,6 @@ def test_env_off_and_cleared(torch_cuda, product_lib, profiles, env):
     assert on[..., :3].mean() > base[..., :3].mean()
 
 
-def _direct_scene(emitter):
-    """A diffuse floor (albedo 0.7) with closed spheres standing on it (every hit front-facing) and,
-    optionally, a small emissive quad facing the floor."""
-    from pltfalcor_gb300 import materials as M
-    verts, faces, mats, norms = [], [], [], []
-
-    def add(v, f, m, n):
-        faces.append(np.asarray(f) + sum(len(x) for x in verts))
-        verts.append(np.asarray(v, np.float64))
-        mats.append(np.full(len(f), m, np.uint32))
-        norms.append(np.broadcast_to(np.asarray(n, np.float64), np.shape(v)))
-
-    v, f = S.grid_quad(np.array([-60.0, -60.0, 0.0]), np.array([120.0, 0, 0]), np.array([0, 120.0, 0]), 4)
-    add(v, f, 0, (0.0, 0.0, 1.0))
-    sv, sf = S.icosphere(3)
-    for c, r in (((-2.0, 1.0, 1.0), 1.0), ((1.5, 2.5, 1.5), 1.5), ((2.0, -1.5, 0.6), 0.6)):
-        add(sv * r + np.array(c), sf, 0, sv)
-    emissive = []
-    if emitter:
-        e1, e2 = np.array([0.0, 1.0, 0.0]), np.array([1.0, 0.0, 0.0])
-        v, f = S.grid_quad(np.array([-0.5, -0.5, 6.0]), e1, e2, 1)
-        emissive = list(range(sum(len(x) for x in faces), sum(len(x) for x in faces) + len(f)))
-        add(v, f, 1, (0.0, 0.0, -1.0))
-    recs = np.concatenate([M.diffuse(1, albedo=(0.7, 0.7, 0.7)), M.diffuse(1, albedo=(0.5, 0.5, 0.5), emission_id=8)])
-    n = np.concatenate(norms)
-    n = n / np.linalg.norm(n, axis=1, keepdims=True)
-    return S.Scene(np.concatenate(verts), np.concatenate(faces), np.concatenate(mats), recs, emissive, 1, 0, (-60, 60),
-                   normals=n, tri_instance=np.arange(len(faces)).repeat([len(x) for x in faces]).astype(np.uint32))
-
-
 @pytest.mark.parametrize("emitter", [False, True])
 def test_env_direct_light_estimators_agree(torch_cuda, product_lib, profiles, env, emitter):
     """Direct light at the primary hit estimated by NEE (light-type selection between the map and
@@ -204,7 +174,7 @@ def test_env_direct_light_estimators_agree(torch_cuda, product_lib, profiles, en
     from the same generator stream as the primary hit's direction in the sample pass (both passes
     seed UniformSampleGenerator(pixel, frame)), which correlates the two on BSDF-sampled emitter hits."""
     prof = profiles[0]
-    scene = _direct_scene(emitter)
+    scene = S.floor_spheres_scene(emitter)
     w, h = 64, 48
     cam = S.look_at_camera((0.0, -9.0, 5.0), (0.0, 0.0, 0.5), (0.0, 0.0, 1.0), 70.0, w / h)
     envd = dict(env, rgb=S.sky_env(sun_radiance=5.0))
