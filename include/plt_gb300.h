@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define PLT_ABI_VERSION 2u
+#define PLT_ABI_VERSION 3u
 #define PLT_MAX_HWSS 8u                 /* hero wavelengths per beam (reference: <= 4, Utils/HWSS.slang:4-9) */
 #define PLT_SPECTRAL_MAX_BINS 128u      /* SpectralProfile::kMaxBins */
 #define PLT_NO_SPECTRAL_PROFILE 0xFFFFFFFFu
@@ -216,6 +216,7 @@ typedef struct plt_options {
      * Requires plt_proposal_init or plt_proposal_set_params first. */
     uint32_t learned_proposal;          /* default 0 */
     float learned_proposal_prob;        /* in (0, 1), default 0.5 */
+    uint32_t emissive_sampler;          /* emissiveSampler: 0 Uniform, 2 Power (EmissiveLightSamplerType), default 2 */
 } plt_options;
 
 #define PLT_OPTION_FP64_MULTILAYER 0x1u /* multilayer recursion in FP64 instead of the reference FP32 */

@@ -91,6 +91,7 @@ struct Options {
     float learnedProb = 0.5f;
     bool useEnv = false;
     bool useAnalytic = false;
+    bool uniformEmissive = false;   // emissiveSampler = Uniform (else Power)
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -1044,11 +1045,23 @@ struct Renderer {
         if (std::isfinite(L.x) && std::isfinite(L.y) && std::isfinite(L.z)) sv.Lrgb = sv.Lrgb + L;
     }
 
+    // LightCollection's active triangles: flux > 0 (LightCollection.cpp:512-524)
+    uint32_t activeCount() const {
+        uint32_t n = 0;
+        for (float f : s.lightFlux) n += f > 0.f ? 1u : 0u;
+        return n;
+    }
+    uint32_t activeLight(uint32_t idx) const {
+        for (uint32_t l = 0; l < (uint32_t)s.lightFlux.size(); ++l)
+            if (s.lightFlux[l] > 0.f && idx-- == 0) return l;
+        return kNone;
+    }
+
     // getLightTypeSelectionProbabilities (LightSampling.slangh:40-55): env map, emissive geometry
     // (the scene's emissive lights when it has any), no analytic lights
     void typeProbabilities(float& pEnv, float& pEm, float& pAn) const {
         const bool useEnv = o.useEnv && s.env.present;
-        const bool useEm = o.useEmissive && !s.lightTri.empty();
+        const bool useEm = o.useEmissive && activeCount() > 0;
         const bool useAn = o.useAnalytic && !s.alights.empty();
         const float sum = (useEnv ? 1.f : 0.f) + (useEm ? 1.f : 0.f) + (useAn ? 1.f : 0.f);
         const float inv = sum > 0.f ? 1.f / sum : 0.f;
@@ -1136,7 +1149,8 @@ struct Renderer {
     // (EmissivePowerSampler.slang:90-122)
     float emissivePdf(F3 posW, uint32_t light, F3 hitPos, F3 hitNormal) const {
         if (light == kNone) return 0.f;
-        const float sel = s.lightFlux[light] * s.invWeightsSum;
+        const uint32_t na = o.uniformEmissive ? activeCount() : 0u;
+        const float sel = o.uniformEmissive ? (na > 0 ? 1.f / (float)na : 0.f) : s.lightFlux[light] * s.invWeightsSum;
         const F3 toLight = hitPos - posW;
         const float distSqr = dot(toLight, toLight);
         if (distSqr <= FLT_MIN) return 0.f * sel;
@@ -1239,15 +1253,25 @@ struct Renderer {
         bool valid = false;
         const uint32_t nl = (uint32_t)s.lightTri.size();
         if (nl > 0) {
-            // EmissivePowerSampler.sampleLight
-            const float uLight = sv.sg.next1D();
-            uint32_t ti = std::min((uint32_t)(uLight * nl), nl - 1);
-            const uint32_t px = s.alias[2 * (size_t)ti], py = s.alias[2 * (size_t)ti + 1];
-            const float threshold = half_to_float((uint16_t)(px >> 16));
-            const uint32_t selectAbove = ((px & 0xFFFFu) << 8u) | ((py >> 24u) & 0xFFu);
-            const uint32_t selectBelow = py & 0xFFFFFFu;
-            ti = (sv.sg.next1D() >= threshold) ? selectAbove : selectBelow;
-            const float triSelPdf = s.lightFlux[ti] * s.invWeightsSum;
+            uint32_t ti;
+            float triSelPdf;
+            if (o.uniformEmissive) {
+                // EmissiveUniformSampler.sampleLight (EmissiveUniformSampler.slang)
+                const uint32_t na = activeCount();
+                const float uLight = sv.sg.next1D();
+                ti = activeLight(std::min((uint32_t)(uLight * (float)na), na - 1));
+                triSelPdf = 1.f / (float)na;
+            } else {
+                // EmissivePowerSampler.sampleLight
+                const float uLight = sv.sg.next1D();
+                ti = std::min((uint32_t)(uLight * nl), nl - 1);
+                const uint32_t px = s.alias[2 * (size_t)ti], py = s.alias[2 * (size_t)ti + 1];
+                const float threshold = half_to_float((uint16_t)(px >> 16));
+                const uint32_t selectAbove = ((px & 0xFFFFu) << 8u) | ((py >> 24u) & 0xFFu);
+                const uint32_t selectBelow = py & 0xFFFFFFu;
+                ti = (sv.sg.next1D() >= threshold) ? selectAbove : selectBelow;
+                triSelPdf = s.lightFlux[ti] * s.invWeightsSum;
+            }
             // sampleTriangle
             const float u0 = sv.sg.next1D(), u1 = sv.sg.next1D();
             const float su = std::sqrt(u0);
@@ -1701,6 +1725,7 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.learnedProb = opt->learned_proposal_prob;
     o.useEnv = opt->use_env_light != 0;
     o.useAnalytic = opt->use_analytic_lights != 0;
+    o.uniformEmissive = opt->emissive_sampler == 0;
     for (uint32_t i = 0; i < sc->n_lights; ++i) {
         const plt_analytic_light& l = sc->lights[i];
         s.alights.push_back(l);

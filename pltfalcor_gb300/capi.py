@@ -68,7 +68,7 @@ class Options(C.Structure):
                 ("do_importance_sample_emitters", C.c_uint32), ("do_mnee", C.c_uint32),
                 ("mnee_max_occluders", C.c_uint32), ("mnee_max_iterations", C.c_uint32),
                 ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32),
-                ("learned_proposal", C.c_uint32), ("learned_proposal_prob", C.c_float)]
+                ("learned_proposal", C.c_uint32), ("learned_proposal_prob", C.c_float), ("emissive_sampler", C.c_uint32)]
 
 
 class Camera(C.Structure):

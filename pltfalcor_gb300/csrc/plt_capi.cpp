@@ -73,6 +73,7 @@ plt_status plt_options_default(plt_options* o) {
     o->flags = 0;
     o->learned_proposal = 0;
     o->learned_proposal_prob = .5f;
+    o->emissive_sampler = 2u;
     return PLT_OK;
 }
 
@@ -84,6 +85,12 @@ plt_status plt_create(const plt_options* options, plt_context** out) {
     if (options) ctx->opt = *options;
     else plt_options_default(&ctx->opt);
     if (ctx->opt.hwss < 1 || ctx->opt.hwss > PLT_MAX_HWSS) { delete ctx; return PLT_INVALID_ARG; }
+    // PLTPT offers the Uniform and Power emissive samplers (PLTPT.cpp:80-83, 401-409)
+    if (ctx->opt.emissive_sampler != 0u && ctx->opt.emissive_sampler != 2u) {
+        const bool bvh = ctx->opt.emissive_sampler == 1u;
+        delete ctx;
+        return bvh ? PLT_NOT_SUPPORTED : PLT_INVALID_ARG;
+    }
     cudaError_t e = cudaGetDevice(&ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount, ctx->device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->dStatus, sizeof(uint32_t));

@@ -26,6 +26,7 @@ struct plt_scene_host {
 struct plt_scene_slot {
     uint32_t root = 0, triBase = 0, lightBase = 0, nLights = 0;
     float invWeightsSum = 0.f;
+    uint32_t activeBase = 0, nActive = 0;   // the scene's active (flux > 0) lights in dLightActive
 };
 
 struct plt_context {
@@ -75,6 +76,7 @@ struct plt_context {
     uint2* dAlias = nullptr;
     uint32_t* dPrimToLight = nullptr;
     uint32_t* dLightEmission = nullptr;
+    uint32_t* dLightActive = nullptr;   // active light triangles (flux > 0) of every scene, global light indices
     uint32_t nLights = 0;
     float invWeightsSum = 0.f;
     // render-pass buffers (one allocation, sized for ptNpix paths and ptMaxB bounces)

@@ -64,7 +64,8 @@ constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 // option bits of PtParams.opt
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
-                   kPtLearned = 0x200u, kPtUseEnv = 0x400u, kPtUseAnalytic = 0x800u;
+                   kPtLearned = 0x200u, kPtUseEnv = 0x400u, kPtUseAnalytic = 0x800u,
+                   kPtUniformEmissive = 0x1000u;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
 
@@ -76,6 +77,7 @@ struct PtScene {
     uint32_t width, height, pixelBase, root;
     uint32_t lightBase, nLights;
     float invWeightsSum;
+    uint32_t activeBase, nActive; // the scene's active lights (flux > 0) in PtParams.lightActive
     uint32_t pad;
     float* out;                   // [height][width][4]
 };
@@ -147,6 +149,7 @@ struct PtParams {
     const uint2* alias;           // [nl]
     const uint32_t* primToLight;  // [nt]
     const uint32_t* lightEmission;// [nl] emission profile id
+    const uint32_t* lightActive;  // active lights (flux > 0) of every scene, global light indices
     // scenes of this render (one for plt_render, several for plt_render_scenes)
     const PtScene* scenes;
     uint32_t nScenes;

@@ -1369,7 +1369,9 @@ PLT_DI bool sampleAnalytic(const PtParams& P, const plt::AnalyticLightDev& L, f3
 // EmissivePowerSampler.slang:81-122)
 PLT_DI float emissivePdf(const PtParams& P, const PtScene& S, f3 posW, uint32_t light, f3 hitPos, f3 hitNormal) {
     if (light == kNoHit) return 0.f;
-    const float sel = __ldg(P.lightFlux + light) * S.invWeightsSum;
+    // EmissiveUniformSampler.evalTriangleSelectionPdf (EmissiveUniformSampler.slang) or the power sampler's
+    const float sel = (P.opt & plt::kPtUniformEmissive) ? (S.nActive > 0 ? 1.f / (float)S.nActive : 0.f)
+                                                         : __ldg(P.lightFlux + light) * S.invWeightsSum;
     const f3 toLight = hitPos - posW;
     const float distSqr = dot(toLight, toLight);
     if (distSqr <= kFltMin) return 0.f;
@@ -1416,7 +1418,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         // light-type selection probabilities (getLightTypeSelectionProbabilities,
         // LightSampling.slangh:40-55): the environment map, this scene's emissive geometry and the
         // analytic lights
-        const bool hasEm = useEmissive && S.nLights > 0;
+        const bool hasEm = useEmissive && S.nActive > 0;   // Scene::useEmissiveLights: active lights present
         const float pSum = (useEnv ? 1.f : 0.f) + (hasEm ? 1.f : 0.f) + (useAnalytic ? 1.f : 0.f);
         const float invPSum = pSum > 0.f ? 1.f / pSum : 0.f;
         const float pEnv = useEnv ? invPSum : 0.f, pEm = hasEm ? invPSum : 0.f, pAn = useAnalytic ? invPSum : 0.f;
@@ -1545,14 +1547,24 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                             sourceBeamArea<H>(pb, tposW, -ldir, srcSize, ldist, Le, swl, P.maxBeamOmega);
                         }
                     } else {
-                        const float uLight = sg.next1D();
-                        uint32_t ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
-                        const uint2 a = __ldg(P.alias + S.lightBase + ti);
-                        const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
-                        const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
-                        const uint32_t selectBelow = a.y & 0xFFFFFFu;
-                        ti = S.lightBase + ((sg.next1D() >= threshold) ? selectAbove : selectBelow);
-                        const float triSelPdf = __ldg(P.lightFlux + ti) * S.invWeightsSum;
+                        uint32_t ti;
+                        float triSelPdf;
+                        if (P.opt & plt::kPtUniformEmissive) {
+                            // EmissiveUniformSampler.sampleLight: one draw over the active triangles
+                            const float uLight = sg.next1D();
+                            const uint32_t idx = min((uint32_t)(uLight * (float)S.nActive), S.nActive - 1);
+                            ti = __ldg(P.lightActive + S.activeBase + idx);
+                            triSelPdf = 1.f / (float)S.nActive;
+                        } else {
+                            const float uLight = sg.next1D();
+                            ti = min((uint32_t)(uLight * (float)S.nLights), S.nLights - 1);
+                            const uint2 a = __ldg(P.alias + S.lightBase + ti);
+                            const float threshold = __half2float(__ushort_as_half((unsigned short)(a.x >> 16)));
+                            const uint32_t selectAbove = ((a.x & 0xFFFFu) << 8u) | ((a.y >> 24u) & 0xFFu);
+                            const uint32_t selectBelow = a.y & 0xFFFFFFu;
+                            ti = S.lightBase + ((sg.next1D() >= threshold) ? selectAbove : selectBelow);
+                            triSelPdf = __ldg(P.lightFlux + ti) * S.invWeightsSum;
+                        }
                         const float u0 = sg.next1D(), u1 = sg.next1D();
                         const float su = sqrtf(u0);
                         const float bx = 1.f - su, by = u1 * su;

@@ -137,7 +137,7 @@ void pltReleaseRenderState(plt_context* ctx) {
     if (ctx->capStream) cudaStreamDestroy((cudaStream_t)ctx->capStream);
     cudaFree(ctx->dFrame);
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes, ctx->dAccum};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dLightActive, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes, ctx->dAccum};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -174,6 +174,8 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
         S.lightBase = sl.lightBase;
         S.nLights = sl.nLights;
         S.invWeightsSum = sl.invWeightsSum;
+        S.activeBase = sl.activeBase;
+        S.nActive = sl.nActive;
         S.out = rv.out_rgba;
         npix64 += (uint64_t)rv.width * rv.height;
         if (npix64 > (1u << 26)) return PLT_NOT_SUPPORTED;
@@ -239,6 +241,7 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.alias = ctx->dAlias;
     P.primToLight = ctx->dPrimToLight;
     P.lightEmission = ctx->dLightEmission;
+    P.lightActive = ctx->dLightActive;
     P.maxBounces = o.max_bounces;
     P.tileSize = o.tile_size ? o.tile_size : 512;
     P.hwss = o.hwss;
@@ -251,7 +254,8 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
             (nee && o.nee_use_per_tile_sg ? plt::kPtPerTileSg : 0u) | (o.do_importance_sample_emitters ? plt::kPtImportanceEmit : 0u) |
             (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u) |
             (o.use_env_light && ctx->hasEnv ? plt::kPtUseEnv : 0u) |
-            (o.use_analytic_lights && ctx->nALights ? plt::kPtUseAnalytic : 0u);
+            (o.use_analytic_lights && ctx->nALights ? plt::kPtUseAnalytic : 0u) |
+            (o.emissive_sampler == 0u ? plt::kPtUniformEmissive : 0u);
     P.env = ctx->env;
     P.alights = ctx->dALights;
     P.nALights = ctx->nALights;

@@ -349,7 +349,7 @@ plt_status pltUploadScenes(plt_context* ctx) {
         }
         if (all) {
             std::vector<float> nrm, tan, lpos, lnrm, larea, lflux;
-            std::vector<uint32_t> inst, p2l(ctx->nTris, 0xFFFFFFFFu), lem;
+            std::vector<uint32_t> inst, p2l(ctx->nTris, 0xFFFFFFFFu), lem, lactive;
             std::vector<uint2> alias;
             uint32_t instBase = 0;
             for (size_t i = 0; i < ns; ++i) {
@@ -375,6 +375,11 @@ plt_status pltUploadScenes(plt_context* ctx) {
                 lflux.insert(lflux.end(), L.flux.begin(), L.flux.end());
                 lem.insert(lem.end(), L.emission.begin(), L.emission.end());
                 alias.insert(alias.end(), L.table.begin(), L.table.end());
+                // LightCollection's active triangle list (flux > 0, LightCollection.cpp:512-524)
+                ctx->slots[i].activeBase = (uint32_t)lactive.size();
+                for (uint32_t l = 0; l < nl; ++l)
+                    if (L.flux[l] > 0.f) lactive.push_back(lightBase + l);
+                ctx->slots[i].nActive = (uint32_t)lactive.size() - ctx->slots[i].activeBase;
                 ctx->slots[i].lightBase = lightBase;
                 ctx->slots[i].nLights = nl;
                 ctx->slots[i].invWeightsSum = L.invWeightsSum;
@@ -389,6 +394,7 @@ plt_status pltUploadScenes(plt_context* ctx) {
             if ((st = upload(ctx, ctx->dAlias, alias.data(), alias.size())) != PLT_OK) return st;
             if ((st = upload(ctx, ctx->dLightEmission, lem.data(), lem.size())) != PLT_OK) return st;
             if ((st = upload(ctx, ctx->dPrimToLight, p2l.data(), p2l.size())) != PLT_OK) return st;
+            if ((st = upload(ctx, ctx->dLightActive, lactive.data(), lactive.size())) != PLT_OK) return st;
             ctx->nLights = (uint32_t)larea.size();
             ctx->invWeightsSum = ctx->slots[0].invWeightsSum;
             ctx->shadingReady = true;

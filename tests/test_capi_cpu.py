@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(product_lib):
 
 
 def test_abi_version_and_status_strings(product_lib):
-    assert product_lib.plt_abi_version() == 2
+    assert product_lib.plt_abi_version() == 3
     assert product_lib.plt_status_string(0) == b"ok"
     assert product_lib.plt_status_string(7) == b"bad material"
 
@@ -35,6 +35,7 @@ def test_options_default_matches_pltpt(product_lib):
     assert product_lib.plt_options_default(C.byref(o)) == 0
     # PLTPT.h:74-108 defaults
     assert (o.max_bounces, o.tile_size, o.hwss, o.mnee_max_occluders, o.mnee_max_iterations) == (32, 512, 4, 2, 60)
+    assert o.emissive_sampler == 2   # EmissiveLightSamplerType::Power (PLTPT.h:99)
     assert abs(o.mnee_solver_threshold - 5e-5) < 1e-9 and abs(o.sourcing_max_beam_omega - 0.025) < 1e-9
 
 

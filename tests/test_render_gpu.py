@@ -113,7 +113,7 @@ def test_render_options_and_frames(torch_cuda, oracle_lib, product_lib, profiles
     cam = S.room_camera(w, h)
     for kw in ({"do_mis": 0}, {"do_nee": 0}, {"do_russian_roulette": 0, "do_importance_sample_emitters": 0},
                {"hwss_do_mis": 0, "hwss": 2}, {"mnee_max_occluders": 1, "mnee_max_iterations": 8},
-               {"do_mnee": 0, "max_bounces": 3}):
+               {"do_mnee": 0, "max_bounces": 3}, {"emissive_sampler": 0}, {"emissive_sampler": 0, "do_mnee": 0}):
         opt = _options(**kw)
         gpu, grecs, _ = _render_gpu(torch_cuda, room, prof, opt, cam, w, h, frame=7)
         orc, orecs, _ = oracle.render(room, prof, cam, opt, w, h, frame=7, records=True)
