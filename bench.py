@@ -10,7 +10,8 @@ over the whole batch.
 
 value: queries/s with inputs resident in HBM (CUDA events on the launching stream; inputs and
 outputs together exceed L2, so no flush is needed).  e2e: the same metric through the C ABI with
-host (pinned) buffers -- every step copies the inputs host->device and all outputs device->host.
+host (pinned) buffers (plt_bsdf_batch_host) -- every step copies the inputs host->device and all
+outputs device->host, in chunks whose copies overlap the kernels.
 The reference arm (--impl reference) times the CPU restatement of the reference's BSDF code (the
 reference's own path is Slang shader code with no CPU build) on all host threads.
 Under torchrun each rank processes its own batch (weak scaling); rank 0 prints one JSON line.
@@ -551,23 +552,19 @@ def run_ours(args):
     ms_max = float(t.item())
     value = args.n * world * args.steps / (ms_max * 1e-3)
 
-    # end to end through the C ABI with host buffers: H2D inputs, launch, D2H outputs per step
-    pin = lambda a: torch.from_numpy(a).pin_memory()
-    h_in = [pin(wl.material.view("int32")), pin(wl.v), pin(wl.w), pin(wl.lobe.view("int32")), pin(wl.wavelengths),
-            pin(wl.stokes), pin(wl.coherence)]
-    d_in = [b.material, b.v, b.w, b.lobe, b.wavelengths, b.stokes, b.coherence]
+    # end to end through the C ABI with host buffers: plt_bsdf_batch_host on pinned host queries and
+    # results (every step copies all inputs to the device and all requested outputs back, chunked
+    # so copies in both directions overlap the kernels)
+    hb = DeviceBatch(wl, device="cpu", pin=True)
+    hq, hr = hb.queries(), hb.results(ops)
+    h_in = [hb.material, hb.v, hb.w, hb.lobe, hb.wavelengths, hb.stokes, hb.coherence]
     d_out = [b.out_stokes, b.out_coherence, b.out_pdf, b.out_sample_wo, b.out_sample_pdf, b.out_sample_weight,
              b.out_sample_lobe, b.out_sample_valid]
-    h_out = [torch.empty(t_.shape, dtype=t_.dtype).pin_memory() for t_ in d_out]
     h2d = sum(x.numel() * x.element_size() for x in h_in)
     d2h = sum(x.numel() * x.element_size() for x in d_out)
 
     def e2e_step():
-        for h, d in zip(h_in, d_in):
-            d.copy_(h, non_blocking=True)
-        ctx.batch(q, r, ops, stream)
-        for h, d in zip(h_out, d_out):
-            h.copy_(d, non_blocking=True)
+        ctx.batch_host(hq, hr, ops, stream)
     for _ in range(max(1, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()

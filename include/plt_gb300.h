@@ -272,6 +272,15 @@ plt_status plt_spectral_profile_for_emitter_type(const char* tables_dir, const c
  * capture, scripts/PLTPathTracer.py:19-27). */
 plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, uint32_t height, int half);
 
+/* plt_bsdf_batch with HOST queries and results (same structures, host pointers; pinned memory
+ * gives full copy bandwidth).  The batch is pipelined in chunks of 2^19 queries: input copies,
+ * kernels and output copies of different chunks overlap (two library copy streams plus the
+ * caller's stream); the results equal one plt_bsdf_batch over the whole batch.  Asynchronous:
+ * the results are on the host once `stream` has completed.  Holds four staging slots of device
+ * memory (about 70 MB each at HWSS 1) until plt_destroy. */
+plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* queries,
+                               const plt_bsdf_results* results, uint32_t ops, void* stream);
+
 /* Batched IMaterialInstance calls (see plt_bsdf_queries).  ops = PLT_OP_* mask.  One fused
  * launch serves every requested op; queries may mix materials in any order. */
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* queries,

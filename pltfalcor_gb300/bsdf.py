@@ -18,13 +18,15 @@ def _ptr(t):
 
 
 class DeviceBatch:
-    """A query batch resident on the GPU, with result buffers for the requested ops."""
+    """A query batch resident on the GPU (or, with device="cpu", in host memory, pinned when pin is
+    set: the buffers of plt_bsdf_batch_host), with result buffers for the requested ops."""
 
     def __init__(self, workload, device="cuda", pin=False, results=True):
         import torch
         self.workload = workload
         self.n, self.hwss = workload.n, workload.hwss
         d = torch.device(device)
+        self._pin_host = pin and d.type == "cpu"
 
         def up(a, dt):
             if a is None:
@@ -32,6 +34,8 @@ class DeviceBatch:
             t = torch.from_numpy(a)
             if dt is not None:
                 t = t.view(dt)
+            if self._pin_host:
+                return t.pin_memory()
             return t.to(d, non_blocking=pin)
         self.material = up(workload.material.view(np.int32), None)
         self.v = up(workload.v, None)
@@ -47,7 +51,8 @@ class DeviceBatch:
     def alloc_results(self, d):
         import torch
         n, h = self.n, self.hwss
-        f = lambda k: torch.zeros(k * n, dtype=torch.float32, device=d)
+        pin = getattr(self, "_pin_host", False)
+        f = lambda k: torch.zeros(k * n, dtype=torch.float32, device=d, pin_memory=pin)
         self.out_stokes = f(4 * h)
         self.out_coherence = f(4)
         self.out_beam_t = None
@@ -56,8 +61,8 @@ class DeviceBatch:
         self.out_sample_wo = f(3)
         self.out_sample_pdf = f(1)
         self.out_sample_weight = f(1)
-        self.out_sample_lobe = torch.zeros(n, dtype=torch.int32, device=d)
-        self.out_sample_valid = torch.zeros(n, dtype=torch.int32, device=d)
+        self.out_sample_lobe = torch.zeros(n, dtype=torch.int32, device=d, pin_memory=pin)
+        self.out_sample_valid = torch.zeros(n, dtype=torch.int32, device=d, pin_memory=pin)
 
     def queries(self, rng_offset=0, frame=None):
         """plt_bsdf_queries over the resident planes (plane stride = n)."""
@@ -133,6 +138,11 @@ class PLTContext:
     def batch(self, queries, results, ops, stream=None):
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
         capi.check(self.lib.plt_bsdf_batch(self.handle, C.byref(queries), C.byref(results), ops, s), "plt_bsdf_batch")
+
+    def batch_host(self, queries, results, ops, stream=None):
+        """plt_bsdf_batch_host: queries and results in host memory (a DeviceBatch on "cpu")."""
+        s = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        capi.check(self.lib.plt_bsdf_batch_host(self.handle, C.byref(queries), C.byref(results), ops, s), "plt_bsdf_batch_host")
 
     def eval(self, q, r, stream=None):
         self.batch(q, r, capi.OP_EVAL, stream)

@@ -19,7 +19,7 @@ CU_SOURCES = ["plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4
               "plt_pt.cu", "plt_pt_h1.cu", "plt_pt_h2.cu", "plt_pt_h3.cu", "plt_pt_h4.cu", "plt_pt_h8.cu", "plt_mlp.cu",
               "plt_envmap.cu"]
 CPP_SOURCES = ["plt_capi.cpp", "plt_materials.cpp", "plt_bsdf_dispatch.cpp", "plt_bvh.cpp", "plt_render.cpp", "plt_proposal.cpp",
-               "plt_scenes.cpp", "plt_io.cpp"]
+               "plt_scenes.cpp", "plt_io.cpp", "plt_host_batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Single-precision division and square root use the SFU approximations (<= 2 ulp, the accuracy
 # class D3D allows the reference shaders); denormals are kept.  The ray/triangle test uses

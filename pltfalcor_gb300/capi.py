@@ -120,6 +120,7 @@ EXPORTED_SYMBOLS = [
     "plt_spectral_profile_from_spd", "plt_write_exr", "plt_render_counters",
     "plt_set_env_map", "plt_clear_env_map", "plt_env_map_query",
     "plt_spectral_profiles_from_material", "plt_spectral_profile_for_emitter_type", "plt_set_analytic_lights",
+    "plt_bsdf_batch_host",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
@@ -150,6 +151,7 @@ def load_library(path=LIB_PATH):
         "plt_spectral_profile_from_samples": (i32, [C.POINTER(C.c_float), C.POINTER(C.c_float), u32, C.c_float, i32,
                                                     C.POINTER(SpectralProfile)]),
         "plt_bsdf_batch": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
+        "plt_bsdf_batch_host": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), u32, vp]),
         "plt_check_status": (i32, [vp, vp]),
         "plt_bsdf_eval": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),
         "plt_bsdf_pdf": (i32, [vp, C.POINTER(BsdfQueries), C.POINTER(BsdfResults), vp]),

@@ -118,6 +118,7 @@ plt_status plt_destroy(plt_context* ctx) {
     pltReleaseRenderState(ctx);
     pltReleaseProposal(ctx);
     pltReleaseEnv(ctx);
+    pltReleaseHostPipeline(ctx);
     delete ctx;
     return PLT_OK;
 }

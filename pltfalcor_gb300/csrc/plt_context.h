@@ -10,6 +10,8 @@
 #include "plt_host.h"
 #include "plt_internal.h"
 
+struct plt_host_pipeline;   // plt_bsdf_batch_host's staging slots, copy streams and events (plt_host_batch.cpp)
+
 // One scene of the context's scene set, kept on the host: its BVH (scene-local node and triangle
 // indices), triangles in leaf order, and its shading attributes.  The device holds all scenes
 // concatenated (pltUploadScenes).
@@ -121,6 +123,7 @@ struct plt_context {
     // analytic lights
     plt::AnalyticLightDev* dALights = nullptr;
     uint32_t nALights = 0;
+    plt_host_pipeline* hostPipe = nullptr;
 };
 
 // Frees the render-pass state of a context (plt_render.cpp).
@@ -132,6 +135,8 @@ float4 pltProposalFeatures(const plt_material_record& r, const pltdev::DevMateri
 // Frees the learned-proposal state (plt_proposal.cpp).
 void pltReleaseProposal(plt_context* ctx);
 
+// Frees plt_bsdf_batch_host's pipeline (plt_host_batch.cpp).
+void pltReleaseHostPipeline(plt_context* ctx);
 // Frees the environment light (plt_scenes.cpp).
 void pltReleaseEnv(plt_context* ctx);
 // Uploads the scene set if it changed (geometry, shading, light collections); plt_scenes.cpp.
