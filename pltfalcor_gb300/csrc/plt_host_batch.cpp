@@ -120,32 +120,13 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         PLT_CUDA(ctx, cudaMalloc(&hp->stage, slotBytes * kSlots));
         hp->slotBytes = slotBytes;
     }
-    // chunks of 2^19 queries (1.99 G queries/s end to end on the 2^22 mixed batch, against 1.77
-    // with 2^18: per-chunk kernel tails; 1.15 without the pipeline), with a ramp of 2^17 and 2^18
-    // at both ends of large batches so the pipeline fills and drains on small chunks
-    std::vector<uint32_t> sizes;
-    const uint32_t ramp = (1u << 17) + (1u << 18);
-    if (n >= 2 * ramp + kHostChunk) {
-        sizes = {1u << 17, 1u << 18};
-        for (uint32_t mid = n - 2 * ramp; mid > 0;) {
-            const uint32_t c = mid < kHostChunk ? mid : kHostChunk;
-            sizes.push_back(c);
-            mid -= c;
-        }
-        sizes.push_back(1u << 18);
-        sizes.push_back(1u << 17);
-    } else {
-        for (uint32_t rest = n; rest > 0;) {
-            const uint32_t c = rest < kHostChunk ? rest : kHostChunk;
-            sizes.push_back(c);
-            rest -= c;
-        }
-    }
-    const uint32_t nChunks = (uint32_t)sizes.size();
-    uint32_t b = 0;
-    for (uint32_t j = 0; j < nChunks; b += sizes[j], ++j) {
+    // chunks of 2^19 queries: 1.99 G queries/s end to end on the 2^22 mixed batch, against 1.77
+    // with 2^18 (per-chunk kernel tails) and 1.15 without the pipeline
+    const uint32_t chunk = kHostChunk;
+    const uint32_t nChunks = (n + chunk - 1) / chunk;
+    for (uint32_t j = 0; j < nChunks; ++j) {
         const int k = (int)(j % kSlots);
-        const uint32_t m = sizes[j];
+        const uint32_t b = j * chunk, m = n - b < chunk ? n - b : chunk;
         char* slot = static_cast<char*>(hp->stage) + (size_t)k * hp->slotBytes;
         // the slot's previous chunk has left it
         if (hp->used[k]) PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sIn, hp->evOut[k], 0));
