@@ -274,8 +274,9 @@ plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, ui
 
 /* plt_bsdf_batch with HOST queries and results (same structures, host pointers; pinned memory
  * gives full copy bandwidth).  The batch is pipelined in chunks of 2^19 queries: input copies,
- * kernels and output copies of different chunks overlap (two library copy streams plus the
- * caller's stream); the results equal one plt_bsdf_batch over the whole batch.  Asynchronous:
+ * kernels and output copies of different chunks (and of consecutive calls) overlap on the
+ * library's two copy streams and compute stream; the results equal one plt_bsdf_batch over the
+ * whole batch.  Asynchronous: host inputs are read, and results written, as the pipeline runs;
  * the results are on the host once `stream` has completed.  Holds four staging slots of device
  * memory (about 70 MB each at HWSS 1) until plt_destroy. */
 plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* queries,

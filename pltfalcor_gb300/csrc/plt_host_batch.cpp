@@ -1,9 +1,10 @@
 // plt_bsdf_batch_host: the BSDF batch with host-resident queries and results.  The batch is cut
 // into chunks of kHostChunk queries that flow through a three-stage pipeline: the chunk's input
-// planes are copied to a device staging slot on an input copy stream, plt_bsdf_batch runs on the
-// caller's stream, and the output planes are copied back on an output copy stream, so the two copy
+// planes are copied to a device staging slot on an input copy stream, plt_bsdf_batch runs on a
+// compute stream, and the output planes are copied back on an output copy stream, so the two copy
 // directions and the kernels of different chunks overlap (GB300's host link carries both
-// directions at once).  Every chunk samples with rng_offset = the batch's rng_offset + its first
+// directions at once), also across consecutive calls; the caller's stream waits for the last
+// output copy.  Every chunk samples with rng_offset = the batch's rng_offset + its first
 // query index, so the results equal one plt_bsdf_batch over the whole batch.  (Letting the kernels
 // read pinned host memory directly measured 11x slower on GB300: the shade kernel's per-tile
 // permuted accesses are latency-bound over the host link.)
@@ -39,7 +40,7 @@ struct Field {
 struct plt_host_pipeline {
     void* stage = nullptr;         // kSlots staging slots
     size_t slotBytes = 0;
-    cudaStream_t sIn = nullptr, sOut = nullptr;
+    cudaStream_t sIn = nullptr, sOut = nullptr, sComp = nullptr;
     cudaEvent_t evIn[kSlots] = {}, evDone[kSlots] = {}, evOut[kSlots] = {};
     bool used[kSlots] = {};
 };
@@ -49,6 +50,7 @@ void pltReleaseHostPipeline(plt_context* ctx) {
     if (!hp) return;
     if (hp->sIn) cudaStreamSynchronize(hp->sIn);
     if (hp->sOut) cudaStreamSynchronize(hp->sOut);
+    if (hp->sComp) cudaStreamSynchronize(hp->sComp);
     for (int k = 0; k < kSlots; ++k) {
         if (hp->evIn[k]) cudaEventDestroy(hp->evIn[k]);
         if (hp->evDone[k]) cudaEventDestroy(hp->evDone[k]);
@@ -56,6 +58,7 @@ void pltReleaseHostPipeline(plt_context* ctx) {
     }
     if (hp->sIn) cudaStreamDestroy(hp->sIn);
     if (hp->sOut) cudaStreamDestroy(hp->sOut);
+    if (hp->sComp) cudaStreamDestroy(hp->sComp);
     cudaFree(hp->stage);
     delete hp;
     ctx->hostPipe = nullptr;
@@ -103,6 +106,7 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         ctx->hostPipe = hp;
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sIn, cudaStreamNonBlocking));
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sOut, cudaStreamNonBlocking));
+        PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sComp, cudaStreamNonBlocking));
         for (int k = 0; k < kSlots; ++k) {
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evIn[k], cudaEventDisableTiming));
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evDone[k], cudaEventDisableTiming));
@@ -113,6 +117,7 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         // earlier calls may still be copying out of the slots
         PLT_CUDA(ctx, cudaStreamSynchronize(hp->sOut));
         PLT_CUDA(ctx, cudaStreamSynchronize(hp->sIn));
+        PLT_CUDA(ctx, cudaStreamSynchronize(hp->sComp));
         cudaFree(hp->stage);
         hp->stage = nullptr;
         hp->slotBytes = 0;
@@ -120,7 +125,7 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         PLT_CUDA(ctx, cudaMalloc(&hp->stage, slotBytes * kSlots));
         hp->slotBytes = slotBytes;
     }
-    // chunks of 2^19 queries: 1.99 G queries/s end to end on the 2^22 mixed batch, against 1.77
+    // chunks of 2^19 queries: 2.08 G queries/s end to end on the 2^22 mixed batch, against 1.77
     // with 2^18 (per-chunk kernel tails) and 1.15 without the pipeline
     const uint32_t chunk = kHostChunk;
     const uint32_t nChunks = (n + chunk - 1) / chunk;
@@ -137,7 +142,7 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
                                             (size_t)m * 4, f.planes, cudaMemcpyHostToDevice, hp->sIn));
         }
         PLT_CUDA(ctx, cudaEventRecord(hp->evIn[k], hp->sIn));
-        PLT_CUDA(ctx, cudaStreamWaitEvent(cs, hp->evIn[k], 0));
+        PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sComp, hp->evIn[k], 0));
         auto dIn = [&](int i) -> const void* { return in[i].host ? slot + in[i].off : nullptr; };
         auto dOut = [&](int i) -> void* { return out[i].host ? slot + out[i].off : nullptr; };
         plt_bsdf_queries q{m, H, hq->rng_offset + b, hq->frame,
@@ -148,9 +153,9 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
                            static_cast<float*>(dOut(3)), static_cast<float*>(dOut(4)), static_cast<float*>(dOut(5)),
                            static_cast<float*>(dOut(6)), static_cast<float*>(dOut(7)), static_cast<uint32_t*>(dOut(8)),
                            static_cast<uint32_t*>(dOut(9))};
-        const plt_status st = plt_bsdf_batch(ctx, &q, &r, ops, cs);
+        const plt_status st = plt_bsdf_batch(ctx, &q, &r, ops, hp->sComp);
         if (st != PLT_OK) return st;
-        PLT_CUDA(ctx, cudaEventRecord(hp->evDone[k], cs));
+        PLT_CUDA(ctx, cudaEventRecord(hp->evDone[k], hp->sComp));
         PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sOut, hp->evDone[k], 0));
         for (const Field& f : out) {
             if (!f.host) continue;
