@@ -16,7 +16,7 @@
 namespace {
 
 constexpr uint32_t kHostChunk = 1u << 19;   // largest chunk (staging slots are sized for it)
-constexpr int kSlots = 4;
+constexpr int kSlots = 4;   // 8 slots measured the same (2.07 G queries/s)
 
 plt_status cudaFail(plt_context* ctx, cudaError_t e) {
     if (ctx) ctx->lastCudaError = (int)e;
