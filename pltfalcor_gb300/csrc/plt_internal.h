@@ -66,6 +66,8 @@ constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
                    kPtLearned = 0x200u, kPtUseEnv = 0x400u, kPtUseAnalytic = 0x800u,
                    kPtUniformEmissive = 0x1000u;
+// solve-order sort keys per path length: 16 first-hit material types x 4 second-hit material groups
+constexpr uint32_t kSolveKeysPerLength = 64;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
 

@@ -27,7 +27,7 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
     if (p.nWave == 0) return cudaSuccess;
     // queue lengths, the manifold-walk count, the solve-order key histogram and its cursors
-    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * ((p.maxBounces + 1) * (1 + 2 * 16) + 2), stream);
+    cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * ((p.maxBounces + 1) * (1 + 2 * kSolveKeysPerLength) + 2), stream);
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
@@ -95,15 +95,24 @@ __global__ void ptResolveKernel(const PtParams P, double inv) {
 // vertex (evaluated by every replay of the path) runs the same material code.  Pass 1 counts the
 // keys; pass 2 gives every block a contiguous range of paths, reserves its share of each key's
 // slots and scatters.
-constexpr uint32_t kSortTypes = 16;
+constexpr uint32_t kSortTypes = plt::kSolveKeysPerLength;
 constexpr uint32_t kMaxKeys = 65 * kSortTypes;   // max_bounces <= 64
+// second-hit material groups: diffuse-like, dielectric, conductor and coated, grated and layered
+__device__ __forceinline__ uint32_t secondGroup(uint32_t t) {
+    return (t == kMatDiffuse || t == kMatOpaqueDielectric) ? 0u : (t == kMatDielectric || t == kMatThin) ? 1u
+         : (t == kMatConductor || t == kMatCoatedConductor || t == kMatCoatedOpaque) ? 2u : 3u;
+}
 __device__ __forceinline__ uint32_t solveKey(const PtParams& P, uint32_t i) {
     const uint32_t len = min(P.plen[i], P.maxBounces);
     const uint32_t prim = P.bPrim[i];   // record 0
-    uint32_t type = 0;
-    if (prim < P.nTris) type = min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), kSortTypes - 1);
-    // keys in solve order: longer paths first, then by type
-    return (P.maxBounces - len) * kSortTypes + type;
+    uint32_t type = 0, g1 = 0;
+    if (prim < P.nTris) type = min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), 15u);
+    if (len >= 1) {
+        const uint32_t prim1 = P.bPrim[P.npix + i];   // record 1
+        if (prim1 < P.nTris) g1 = secondGroup(__ldg(&P.mats[__ldg(P.triMat + prim1)].type));
+    }
+    // keys in solve order: longer paths first, then by first-hit type, then second-hit group
+    return ((P.maxBounces - len) * 16u + type) * 4u + g1;
 }
 __global__ void __launch_bounds__(256) ptLenCountKernel(const PtParams P) {
     __shared__ uint32_t h[kMaxKeys];
