@@ -199,6 +199,8 @@ struct PtParams {
     void* mneeTasks;              // [mneeCap] tasks of kMneeTaskBytes
     uint32_t mneeCap;
     uint32_t* mneeCount;
+    uint32_t* mneeSort;           // [32] walk-order key counts and cursors
+    uint32_t* mneeOrder;          // [mneeCap] walk order of the tasks (sorted by occluder count and material), or null
     // environment light (kPtUseEnv) and analytic lights (kPtUseAnalytic)
     EnvDev env;
     const AnalyticLightDev* alights;

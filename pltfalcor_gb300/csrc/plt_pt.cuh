@@ -1725,7 +1725,7 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
     uint32_t evals = 0;
     const MneeTask<H>* tasks = reinterpret_cast<const MneeTask<H>*>(P.mneeTasks);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const MneeTask<H>& t = tasks[i];
+        const MneeTask<H>& t = tasks[P.mneeOrder ? P.mneeOrder[i] : i];
         MSData ms = t.ms;
         const uint32_t pid = t.pid;
         const int p = (int)t.p;
@@ -1786,6 +1786,53 @@ __global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
     addTraversalBytes(P, tc.nv, tc.tt);
 }
 
+// The walk wavefront's order: tasks counting-sorted by (occluder count, material group of the first
+// occluder), so a warp's lanes run Newton walks of the same chain length over the same material
+// code.  Count pass, then a scatter pass in which every block reserves its share of each key's
+// slots after the exclusive prefix of the counts.
+template <int H> PLT_DI uint32_t mneeKey(const PtParams& P, const MneeTask<H>& t) {
+    const uint32_t hc = (uint32_t)min(max(t.ms.hitCount, 1), 4) - 1u;
+    const uint32_t prim = t.ms.hits[0].prim;
+    const uint32_t ty = prim < P.nTris ? __ldg(&P.mats[__ldg(P.triMat + prim)].type) : 0u;
+    const uint32_t g = (ty == kMatDielectric || ty == kMatThin) ? 0u : (ty == kMatMultilayer) ? 1u
+                     : (ty == kMatGratedConductor || ty == kMatGratedOpaque) ? 2u : 3u;
+    return hc * 4u + g;
+}
+template <int H>
+__global__ void __launch_bounds__(256) ptMneeCountKernel(const PtParams P) {
+    __shared__ uint32_t h[16];
+    if (threadIdx.x < 16) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t count = min(*((volatile uint32_t*)P.mneeCount), P.mneeCap);
+    const MneeTask<H>* tasks = reinterpret_cast<const MneeTask<H>*>(P.mneeTasks);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[mneeKey<H>(P, tasks[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 16 && h[threadIdx.x]) atomicAdd(P.mneeSort + threadIdx.x, h[threadIdx.x]);
+}
+template <int H>
+__global__ void __launch_bounds__(256) ptMneeScatterKernel(const PtParams P) {
+    __shared__ uint32_t h[16], base[16];
+    const uint32_t count = min(*((volatile uint32_t*)P.mneeCount), P.mneeCap);
+    const uint32_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint32_t begin = min(blockIdx.x * per, count), end = min(begin + per, count);
+    const MneeTask<H>* tasks = reinterpret_cast<const MneeTask<H>*>(P.mneeTasks);
+    if (threadIdx.x < 16) h[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[mneeKey<H>(P, tasks[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 16) {
+        uint32_t prefix = 0;
+        for (uint32_t k = 0; k < threadIdx.x; ++k) prefix += P.mneeSort[k];
+        base[threadIdx.x] = h[threadIdx.x] ? prefix + atomicAdd(P.mneeSort + 16 + threadIdx.x, h[threadIdx.x]) : 0u;
+        h[threadIdx.x] = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t k = mneeKey<H>(P, tasks[i]);
+        P.mneeOrder[base[k] + atomicAdd(&h[k], 1u)] = i;
+    }
+}
 template <int H>
 cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, cudaStream_t stream) {
     static int bps[2] = {-1, -1};
@@ -1809,6 +1856,10 @@ cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, c
             bpsW = b > 0 ? b : 1;
         }
         const uint32_t gw = (uint32_t)numSMs * (L.walkBlocksPerSM ? min((uint32_t)bpsW, L.walkBlocksPerSM) : (uint32_t)bpsW);
+        if (p.mneeOrder && p.mneeSort) {
+            ptMneeCountKernel<H><<<numSMs, 256, 0, stream>>>(p);
+            ptMneeScatterKernel<H><<<numSMs, 256, 0, stream>>>(p);
+        }
         ptMneeKernel<H><<<gw, 128, 0, stream>>>(p);
     }
     return cudaGetLastError();

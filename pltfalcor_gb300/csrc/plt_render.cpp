@@ -39,7 +39,7 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     const size_t n = npix, nb = (size_t)maxB + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     // the counters: per-segment queue lengths, the manifold-walk count, 16 solve-order keys per length (counts, cursors)
-    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb;
+    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32;
     const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
@@ -65,6 +65,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.mneeCount = P.qcount + nb + 1;
     P.lenCount = P.qcount + nb + 2;
     P.lenCursor = P.lenCount + plt::kSolveKeysPerLength * nb;
+    P.mneeSort = P.lenCursor + plt::kSolveKeysPerLength * nb;
+    P.mneeOrder = P.queue1;   // free during the solve pass
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
     P.bPrim = (uint32_t*)take(nb * n * 4);
