@@ -462,31 +462,36 @@ def capi_options(overrides):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's BSDF code (the oracle; the reference
+    path itself is Slang shader code with no CPU build and no graphics stack here) on all host
+    threads, over the same batch as the GPU arm: each step is one pass over all args.n queries.
+    Nothing here loads the product library: the spectral profiles come from the oracle's own
+    profile builder."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    from pltfalcor_gb300 import spectra
     from pltfalcor_gb300 import workloads as W
     threads = os.cpu_count()
-    prof, _ = spectra.standard_profiles()
-    n_step = 1 << 16
-    wl = W.mixed_material_batch(n=n_step, profiles=prof)
+    prof, _ = oracle.standard_profiles()
+    wl = W.mixed_material_batch(n=args.n, profiles=prof)
+    res = oracle.alloc_results(wl.n, wl.hwss)
     for _ in range(args.warmup):
-        oracle.run(wl, threads=threads)
+        oracle.run(wl, threads=threads, res=res)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.run(wl, threads=threads)
+        oracle.run(wl, threads=threads, res=res)
     dt = time.perf_counter() - t0
-    v = n_step * args.steps / dt
+    v = wl.n * args.steps / dt
     line = {"metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "step": "%d-query slice per step (bounded CPU sample)" % n_step},
+            "config": {"workload": WORKLOAD, "queries_per_gpu": wl.n, "hwss": 1, "materials": int(len(wl.records)),
+                       "step": "one pass over the whole batch"},
             "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-                             "sample": "%d x %d queries of the mixed-material batch, FP32 oracle restating the reference Slang BSDFs "
-                                       "(the reference path is shader code with no CPU build)" % (args.steps, n_step)},
+                             "sample": "%d passes over the %d-query mixed-material batch, FP32 oracle restating the reference Slang "
+                                       "BSDFs (the reference path is shader code with no CPU build), OpenMP" % (args.steps, wl.n)},
             "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -276,14 +276,19 @@ plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, ui
  * gives full copy bandwidth).  The batch is pipelined in chunks of 2^19 queries: input copies,
  * kernels and output copies of different chunks (and of consecutive calls) overlap on the
  * library's two copy streams and compute stream; the results equal one plt_bsdf_batch over the
- * whole batch.  Asynchronous: host inputs are read, and results written, as the pipeline runs;
- * the results are on the host once `stream` has completed.  Holds four staging slots of device
- * memory (about 70 MB each at HWSS 1) until plt_destroy. */
+ * whole batch.  Asynchronous and ordered on `stream`: no input is read before the work queued on
+ * `stream` ahead of the call has completed (so inputs that earlier work on `stream` writes are
+ * read complete), and the results are on the host once `stream` has completed.  The pipeline
+ * sorts through its own scratch, so it shares no scratch with plt_bsdf_batch.  Holds four staging
+ * slots of device memory (about 70 MB each at HWSS 1) until plt_destroy. */
 plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* queries,
                                const plt_bsdf_results* results, uint32_t ops, void* stream);
 
 /* Batched IMaterialInstance calls (see plt_bsdf_queries).  ops = PLT_OP_* mask.  One fused
- * launch serves every requested op; queries may mix materials in any order. */
+ * launch serves every requested op; queries may mix materials in any order.  Every launching entry
+ * point (batches, traversal, renders) must be called with the context's device current, else it
+ * returns PLT_INVALID_ARG.  Calls on one context share its sort scratch: queue them on one stream
+ * (or order them with events). */
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* queries,
                           const plt_bsdf_results* results, uint32_t ops, void* stream);
 
@@ -517,8 +522,9 @@ plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* 
  * until exit) instead of context memory, so the call itself allocates nothing.
  * Limits: queries->n <= PLT_NOALLOC_MAX_QUERIES, else PLT_TOO_LARGE (nothing launched).  The
  * first call on each device resolves the array's device address (set-up); make that first call
- * before starting any stream capture.  Calls share the array: calls that overlap on the GPU race,
- * so serialise them on one stream. */
+ * before starting any stream capture.  Like plt_bsdf_batch it runs only with the context's device
+ * current (PLT_INVALID_ARG otherwise).  Calls share the array: calls that overlap on the GPU race,
+ * so serialise them on one stream.  Not usable after a cudaDeviceReset in the same process. */
 plt_status plt_bsdf_batch_noalloc(plt_context* ctx, const plt_bsdf_queries* queries,
                                   const plt_bsdf_results* results, uint32_t ops, void* stream);
 

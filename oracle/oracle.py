@@ -80,6 +80,30 @@ def _p(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
+def standard_profiles():
+    """The workloads' spectral profiles (Au, Ag, Cu, Al eta and k, then D65; the order of
+    pltfalcor_gb300.spectra.standard_profiles) built by the oracle's own restatement of
+    genSpectralProfile (Scene/SceneBuilder.cpp:911-960), so a CPU-only run of the oracle never loads
+    the product library."""
+    import sys
+    root = os.path.dirname(HERE)
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from pltfalcor_gb300 import capi, spectra
+    lib = load()
+    t = spectra.load_tables()
+    names = [m + s for m in spectra.METALS for s in (".eta", ".k")] + ["D65"]
+    arr = (capi.SpectralProfile * len(names))()
+    for i, nm in enumerate(names):
+        wl = np.ascontiguousarray(t[nm]["wavelength_nm"], dtype=np.float32)
+        v = np.ascontiguousarray(t[nm]["value"], dtype=np.float32)
+        st = lib.plto_spectral_profile_from_samples(wl.ctypes.data_as(C.POINTER(C.c_float)), v.ctypes.data_as(C.POINTER(C.c_float)),
+                                                    len(wl), 1.0, int(nm == "D65"), C.byref(arr[i]))
+        if st != 0:
+            raise RuntimeError("oracle spectral profile %s failed with status %d" % (nm, st))
+    return arr, {nm: i for i, nm in enumerate(names)}
+
+
 def make_queries(wl, rng_offset=0):
     q = _Q()
     q.n, q.hwss, q.rng_offset, q.frame = wl.n, wl.hwss, rng_offset, wl.frame

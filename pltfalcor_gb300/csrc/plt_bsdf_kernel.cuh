@@ -167,18 +167,20 @@ cudaError_t launchBsdfBatchH(const BatchParams& p, int numSMs, cudaStream_t stre
     pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p.q.material, p.q.lobe, p.matType, p.nMats, p.q.n,
                                                                     p.perm, p.unitCounter);
     if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
+    // at most 64 profiles x 528 B = 33 KB: below the 48 KB default limit, so no attribute is set
     const size_t smem = (size_t)p.nProfiles * sizeof(pltdev::DevProfile);
-    static size_t cachedSmem = (size_t)-1;
-    static int blocksPerSM = 1;
-    if (smem != cachedSmem) {
-        if (smem > 48 * 1024) {
-            const cudaError_t e = cudaFuncSetAttribute(pltdev::bsdfShadeKernel<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
+    static_assert(64 * sizeof(pltdev::DevProfile) <= 48 * 1024, "profile staging exceeds the default shared-memory limit");
+    int blocksPerSM = 1;
+    if (p.launch && p.launch->smem[H] == smem) {
+        blocksPerSM = p.launch->blocks[H];
+    } else {
         int b = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::bsdfShadeKernel<H>, kShadeThreads, smem) != cudaSuccess || b < 1) b = 1;
         blocksPerSM = b;
-        cachedSmem = smem;
+        if (p.launch) {
+            p.launch->smem[H] = smem;
+            p.launch->blocks[H] = b;
+        }
     }
     uint32_t grid = (uint32_t)(numSMs * blocksPerSM);
     const uint32_t warpsNeeded = nTiles * (kBatchTile / 32);

@@ -107,6 +107,8 @@ plt_status plt_create(const plt_options* options, plt_context** out) {
 
 plt_status plt_destroy(plt_context* ctx) {
     if (!ctx) return PLT_INVALID_ARG;
+    // the host pipeline's streams may still run kernels that read the buffers below: drain them first
+    pltReleaseHostPipeline(ctx);
     cudaFree(ctx->dMats);
     cudaFree(ctx->dMatType);
     cudaFree(ctx->dProfiles);
@@ -118,7 +120,6 @@ plt_status plt_destroy(plt_context* ctx) {
     pltReleaseRenderState(ctx);
     pltReleaseProposal(ctx);
     pltReleaseEnv(ctx);
-    pltReleaseHostPipeline(ctx);
     delete ctx;
     return PLT_OK;
 }
@@ -228,44 +229,20 @@ plt_status plt_spectral_profile_from_samples(const float* wl, const float* value
 }
 
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops, void* stream) {
-    if (!ctx || !q || !r) return PLT_INVALID_ARG;
-    if (q->hwss < 1 || q->hwss > PLT_MAX_HWSS || (q->hwss > 4 && q->hwss != 8)) return q->hwss >= 1 && q->hwss <= PLT_MAX_HWSS ? PLT_NOT_SUPPORTED : PLT_INVALID_ARG;
-    if (ops == 0 || (ops & ~0xFu)) return PLT_INVALID_ARG;
-    if (q->n == 0) return PLT_OK;
-    if (!q->material || !q->v || !q->w || !q->wavelengths || !q->stokes || !q->coherence) return PLT_INVALID_ARG;
-    if (ctx->nMats == 0) return PLT_INVALID_ARG;
-    const void* ins[] = {q->material, q->v, q->w, q->lobe, q->wavelengths, q->stokes, q->coherence, q->beam_t};
-    for (const void* p : ins)
-        if (p && !aligned16(p)) return PLT_INVALID_ARG;
-    const void* outs[] = {r->stokes, r->coherence, r->beam_t, r->pdf, r->lambda_pdf, r->sample_wo, r->sample_pdf, r->sample_weight, r->sample_lobe, r->sample_valid};
-    for (const void* p : outs)
-        if (p && !aligned16(p)) return PLT_INVALID_ARG;
+    plt::BatchParams p{};
+    int numSMs = 0;
+    const plt_status s = plt::fillBatchParams(ctx, q, r, ops, &p, &numSMs);
+    if (s != PLT_OK || q->n == 0) return s;
     const size_t need = plt::bsdfScratchBytes(q->n);
     if (need > ctx->scratchCap) {
-        // grows once to the largest batch seen; the stream is synchronised by cudaFree/cudaMalloc
+        // grows once to the largest batch seen; cudaFree waits for every batch still using the old one
         cudaFree(ctx->dScratch);
         ctx->dScratch = nullptr;
         ctx->scratchCap = 0;
         PLT_CUDA(ctx, cudaMalloc(&ctx->dScratch, need));
         ctx->scratchCap = need;
     }
-    plt::BatchParams p{};
-    p.perm = static_cast<uint16_t*>(ctx->dScratch);
-    p.unitCounter = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx->dScratch) + (need - 256));
-    p.q = *q;
-    p.r = *r;
-    p.ops = ops;
-    p.mats = ctx->dMats;
-    p.matType = ctx->dMatType;
-    p.nMats = ctx->nMats;
-    p.profiles = ctx->dProfiles;
-    p.nProfiles = ctx->nProfiles;
-    p.flags = ctx->opt.flags;
-    p.status = ctx->dStatus;
-    for (int i = 0; i < 3; ++i) p.timing[i] = ctx->timing[i];
-    const cudaError_t e = plt::launchBsdfBatch(p, (int)q->hwss, ctx->numSMs, (cudaStream_t)stream);
-    if (e != cudaSuccess) return cudaFail(ctx, e);
-    return PLT_OK;
+    return pltLaunchBsdfBatch(ctx, p, ctx->dScratch, (cudaStream_t)stream);
 }
 
 plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* before_shade, void* after_shade) {
@@ -278,12 +255,21 @@ plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* 
 
 }  // extern "C"
 
+plt_status pltLaunchBsdfBatch(plt_context* ctx, plt::BatchParams& p, void* scratch, cudaStream_t stream) {
+    p.perm = static_cast<uint16_t*>(scratch);
+    p.unitCounter = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + (plt::bsdfScratchBytes(p.q.n) - 256));
+    const cudaError_t e = plt::launchBsdfBatch(p, (int)p.q.hwss, ctx->numSMs, stream);
+    return e == cudaSuccess ? PLT_OK : cudaFail(ctx, e);
+}
+
 plt_status plt::fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops,
                                 plt::BatchParams* out, int* numSMs) {
     if (!ctx || !q || !r || !out || !numSMs) return PLT_INVALID_ARG;
     if (q->hwss < 1 || q->hwss > PLT_MAX_HWSS) return PLT_INVALID_ARG;
     if (q->hwss > 4 && q->hwss != 8) return PLT_NOT_SUPPORTED;
     if (ops == 0 || (ops & ~0xFu)) return PLT_INVALID_ARG;
+    const plt_status ds = pltCheckDevice(ctx);
+    if (ds != PLT_OK) return ds;
     if (q->n > 0) {
         if (!q->material || !q->v || !q->w || !q->wavelengths || !q->stokes || !q->coherence) return PLT_INVALID_ARG;
         if (ctx->nMats == 0) return PLT_INVALID_ARG;
@@ -306,6 +292,8 @@ plt_status plt::fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, con
     p.nProfiles = ctx->nProfiles;
     p.flags = ctx->opt.flags;
     p.status = ctx->dStatus;
+    for (int i = 0; i < 3; ++i) p.timing[i] = ctx->timing[i];
+    p.launch = &ctx->shadeLaunch;
     *out = p;
     *numSMs = ctx->numSMs;
     return PLT_OK;
@@ -320,6 +308,8 @@ plt_status plt_bsdf_lambda_pdf(plt_context* c, const plt_bsdf_queries* q, const 
 
 static plt_status traceCommon(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, uint32_t* occluded, bool any, void* stream) {
     if (!ctx || !rays) return PLT_INVALID_ARG;
+    const plt_status ds = pltCheckDevice(ctx);
+    if (ds != PLT_OK) return ds;
     if (ctx->geometryDirty) {
         const plt_status s = pltUploadScenes(ctx);
         if (s != PLT_OK) return s;

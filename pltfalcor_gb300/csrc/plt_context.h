@@ -51,6 +51,9 @@ struct plt_context {
     plt::BvhBuildStats bvhStats{};
     int lastCudaError = 0;
     void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
+    plt::ShadeLaunchCache shadeLaunch = {{(size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1,
+                                          (size_t)-1, (size_t)-1},
+                                         {}};
 
     // host copies for the render pass (light collection, material properties)
     std::vector<plt_spectral_profile> hProfiles;
@@ -125,6 +128,24 @@ struct plt_context {
     uint32_t nALights = 0;
     plt_host_pipeline* hostPipe = nullptr;
 };
+
+// PLT_OK when the calling thread's current CUDA device is the one the context was created on; a
+// context's buffers, kernels' occupancy and scratch belong to that device, so every launching entry
+// point refuses (PLT_INVALID_ARG) to run on another one.
+inline plt_status pltCheckDevice(plt_context* ctx) {
+    int dev = -1;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        ctx->lastCudaError = (int)e;
+        return PLT_CUDA_ERROR;
+    }
+    return dev == ctx->device ? PLT_OK : PLT_INVALID_ARG;
+}
+
+// Points the batch's sort permutation and work counter into `scratch` (at least
+// bsdfScratchBytes(p.q.n) bytes) and launches the classify + shade kernels on `stream`
+// (plt_capi.cpp).
+plt_status pltLaunchBsdfBatch(plt_context* ctx, plt::BatchParams& p, void* scratch, cudaStream_t stream);
 
 // Frees the render-pass state of a context (plt_render.cpp).
 void pltReleaseRenderState(plt_context* ctx);

@@ -3,8 +3,11 @@
 // planes are copied to a device staging slot on an input copy stream, plt_bsdf_batch runs on a
 // compute stream, and the output planes are copied back on an output copy stream, so the two copy
 // directions and the kernels of different chunks overlap (GB300's host link carries both
-// directions at once), also across consecutive calls; the caller's stream waits for the last
-// output copy.  Every chunk samples with rng_offset = the batch's rng_offset + its first
+// directions at once), also across consecutive calls.  Ordering with the caller's stream: the
+// pipeline's streams first wait for everything queued on it before the call (so host inputs
+// written by earlier work on that stream are read complete), and the caller's stream waits for the
+// last output copy.  The chunk kernels sort through the pipeline's own scratch, never the
+// context's, so they cannot race with plt_bsdf_batch calls on other streams.  Every chunk samples with rng_offset = the batch's rng_offset + its first
 // query index, so the results equal one plt_bsdf_batch over the whole batch.  (Letting the kernels
 // read pinned host memory directly measured 11x slower on GB300: the shade kernel's per-tile
 // permuted accesses are latency-bound over the host link.)
@@ -40,7 +43,9 @@ struct Field {
 struct plt_host_pipeline {
     void* stage = nullptr;         // kSlots staging slots
     size_t slotBytes = 0;
+    void* scratch = nullptr;       // sort scratch of the chunk kernels (one chunk; sComp runs them in order)
     cudaStream_t sIn = nullptr, sOut = nullptr, sComp = nullptr;
+    cudaEvent_t evEntry = nullptr;  // the caller's stream at entry
     cudaEvent_t evIn[kSlots] = {}, evDone[kSlots] = {}, evOut[kSlots] = {};
     bool used[kSlots] = {};
 };
@@ -56,10 +61,12 @@ void pltReleaseHostPipeline(plt_context* ctx) {
         if (hp->evDone[k]) cudaEventDestroy(hp->evDone[k]);
         if (hp->evOut[k]) cudaEventDestroy(hp->evOut[k]);
     }
+    if (hp->evEntry) cudaEventDestroy(hp->evEntry);
     if (hp->sIn) cudaStreamDestroy(hp->sIn);
     if (hp->sOut) cudaStreamDestroy(hp->sOut);
     if (hp->sComp) cudaStreamDestroy(hp->sComp);
     cudaFree(hp->stage);
+    cudaFree(hp->scratch);
     delete hp;
     ctx->hostPipe = nullptr;
 }
@@ -74,8 +81,8 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
     const uint32_t n = hq->n, H = hq->hwss;
     if (n == 0) return PLT_OK;
     if (!hq->material || !hq->v || !hq->w || !hq->wavelengths || !hq->stokes || !hq->coherence) return PLT_INVALID_ARG;
+    if (const plt_status ds = pltCheckDevice(ctx); ds != PLT_OK) return ds;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-
 
     // staging layout of one slot: the input fields, then the requested output fields
     std::vector<Field> in = {{hq->material, 1, 0}, {hq->v, 3, 0}, {hq->w, 3, 0}, {hq->lobe, 1, 0},
@@ -107,6 +114,8 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sIn, cudaStreamNonBlocking));
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sOut, cudaStreamNonBlocking));
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sComp, cudaStreamNonBlocking));
+        PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evEntry, cudaEventDisableTiming));
+        PLT_CUDA(ctx, cudaMalloc(&hp->scratch, plt::bsdfScratchBytes(kHostChunk)));
         for (int k = 0; k < kSlots; ++k) {
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evIn[k], cudaEventDisableTiming));
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evDone[k], cudaEventDisableTiming));
@@ -129,6 +138,10 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
     // with 2^18 (per-chunk kernel tails) and 1.15 without the pipeline
     const uint32_t chunk = kHostChunk;
     const uint32_t nChunks = (n + chunk - 1) / chunk;
+    // nothing of this call starts before the work already queued on the caller's stream
+    PLT_CUDA(ctx, cudaEventRecord(hp->evEntry, cs));
+    PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sIn, hp->evEntry, 0));
+    PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sComp, hp->evEntry, 0));
     for (uint32_t j = 0; j < nChunks; ++j) {
         const int k = (int)(j % kSlots);
         const uint32_t b = j * chunk, m = n - b < chunk ? n - b : chunk;
@@ -153,7 +166,11 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
                            static_cast<float*>(dOut(3)), static_cast<float*>(dOut(4)), static_cast<float*>(dOut(5)),
                            static_cast<float*>(dOut(6)), static_cast<float*>(dOut(7)), static_cast<uint32_t*>(dOut(8)),
                            static_cast<uint32_t*>(dOut(9))};
-        const plt_status st = plt_bsdf_batch(ctx, &q, &r, ops, hp->sComp);
+        plt::BatchParams p{};
+        int numSMs = 0;
+        plt_status st = plt::fillBatchParams(ctx, &q, &r, ops, &p, &numSMs);
+        for (void*& t : p.timing) t = nullptr;   // plt_set_timing_events times plt_bsdf_batch, not the chunks
+        if (st == PLT_OK) st = pltLaunchBsdfBatch(ctx, p, hp->scratch, hp->sComp);
         if (st != PLT_OK) return st;
         PLT_CUDA(ctx, cudaEventRecord(hp->evDone[k], hp->sComp));
         PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sOut, hp->evDone[k], 0));

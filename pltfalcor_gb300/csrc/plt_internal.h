@@ -38,6 +38,14 @@ struct TraceParams {
 };
 cudaError_t launchTrace(const TraceParams& p, bool any, int numSMs, cudaStream_t stream);
 
+// Resident shade-kernel CTAs per SM at a dynamic shared-memory size, per hero-wavelength count
+// (index H).  Each context keeps its own, so contexts used from different host threads share no
+// mutable launch state.
+struct ShadeLaunchCache {
+    size_t smem[9];
+    int blocks[9];
+};
+
 struct BatchParams {
     plt_bsdf_queries q;
     plt_bsdf_results r;
@@ -54,6 +62,7 @@ struct BatchParams {
     // optional cudaEvent_t handles recorded on the launch stream before the classify kernel,
     // between the two kernels and after the shade kernel (per-kernel timing); null = not recorded
     void* timing[3];
+    ShadeLaunchCache* launch;  // host-side occupancy cache of the calling context (not read on the device)
 };
 
 // PLTPT render pass (sample + solve).  Per-material property word (matProps.x):
@@ -236,7 +245,8 @@ constexpr size_t bsdfScratchBytes(uint32_t n) {
 }
 
 // Validates a plt_bsdf_batch call and fills every BatchParams field except the scratch pointers
-// (perm, unitCounter); also returns the SM count for the launch.  No allocation.
+// (perm, unitCounter); also returns the SM count for the launch.  No allocation.  Returns
+// PLT_INVALID_ARG when the calling thread's current device is not the context's device.
 plt_status fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops,
                            BatchParams* out, int* numSMs);
 

@@ -11,7 +11,11 @@
 // All calls on a device share the array, so two calls whose work overlaps on the GPU race on it:
 // serialise them (one stream, or events).  Nothing in it needs clearing between calls: the
 // classify kernel rewrites the whole permutation range it uses and zeroes the work counter before
-// the shade kernel reads either.
+// the shade kernel reads either.  The call runs on the context's device only (PLT_INVALID_ARG when
+// another device is current), so the address it uses is always that device's copy of the array.
+// A cudaDeviceReset unloads the library's device code and invalidates every context of that
+// device together with the cached address: do not call this entry point after one in the same
+// process.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -150,7 +150,9 @@ namespace {
 plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t nViews, uint32_t frame_begin, uint32_t frame_count,
                        void* stream) {
     if (!ctx || !views || nViews == 0 || frame_count == 0) return PLT_INVALID_ARG;
-    plt_status s = pltUploadScenes(ctx);
+    plt_status s = pltCheckDevice(ctx);
+    if (s != PLT_OK) return s;
+    s = pltUploadScenes(ctx);
     if (s != PLT_OK) return s;
     if (!ctx->shadingReady || ctx->nTris == 0 || ctx->nMats == 0) return PLT_INVALID_ARG;
     const plt_options& o = ctx->opt;
@@ -391,6 +393,7 @@ plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape)
 plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame, uint32_t frames,
                            plt_launch_shape* best, float* best_ms, void* stream) {
     if (!ctx || !views || n_views == 0 || frames == 0) return PLT_INVALID_ARG;
+    if (const plt_status ds = pltCheckDevice(ctx); ds != PLT_OK) return ds;
     uint64_t total = 0;
     for (uint32_t v = 0; v < n_views; ++v) total += (uint64_t)views[v].width * views[v].height;
     if (total == 0) return PLT_INVALID_ARG;

@@ -45,7 +45,9 @@ def parse_spd(path):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_spectral_tables.py <reference source root (the directory holding Source/Tables)>")
+    root = sys.argv[1]
     out = {}
     for name, rel in TABLES.items():
         wl, val, header = parse_spd(os.path.join(root, rel))

@@ -52,3 +52,45 @@ def test_host_batch_equals_device_batch(torch_cuda, product_lib, n, hwss, ops, p
     for k in keys:
         assert np.array_equal(got[k].view(np.uint32), ref[k].view(np.uint32)), k
     ctx.close()
+
+
+def test_host_batch_ordered_on_callers_stream(torch_cuda, product_lib):
+    """The ordering contract of plt_bsdf_batch_host on one explicit stream, with no device-wide
+    synchronisation: a device batch and then the async device-to-host copies that produce the host
+    inputs are queued on `s` just before the call (behind a spin of a few milliseconds), so a
+    pipeline that started reading before the work queued on `s` finished would read zeros.  Only `s`
+    is synchronised, once, after a device batch queued behind the call; the host results must equal
+    the first device batch bit for bit, and the last device batch must equal it too (no shared
+    scratch between the pipeline and plt_bsdf_batch)."""
+    torch = torch_cuda
+    from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
+    prof, _ = spectra.standard_profiles()
+    n = (1 << 20) + 4100
+    wl = W.mixed_material_batch(n=(n + 7) // 8 * 8, profiles=prof)
+    wl = wl.subset(np.arange(n))
+    ops = capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF
+    ctx = PLTContext()
+    ctx.set_spectral_profiles(prof)
+    ctx.set_materials(wl.records)
+    d = DeviceBatch(wl)
+    d2 = DeviceBatch(wl)
+    h = DeviceBatch(wl, device="cpu", pin=True)
+    pairs = [(d.material, h.material), (d.v, h.v), (d.w, h.w), (d.lobe, h.lobe), (d.wavelengths, h.wavelengths),
+             (d.stokes, h.stokes), (d.coherence, h.coherence)]
+    for _, ht in pairs:
+        ht.zero_()
+    torch.cuda.synchronize()   # set-up uploads only; nothing below synchronises the device
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ctx.batch(d.queries(rng_offset=5), d.results(ops), ops, s)
+        torch.cuda._sleep(20_000_000)
+        for dt, ht in pairs:
+            ht.copy_(dt, non_blocking=True)
+        ctx.batch_host(h.queries(rng_offset=5), h.results(ops), ops, s)
+        ctx.batch(d2.queries(rng_offset=5), d2.results(ops), ops, s)
+    assert ctx.check_status(s) == capi.PLT_OK   # synchronises `s` only
+    ref, got, again = d.fetch(), h.fetch(), d2.fetch()
+    for k in ["stokes", "coherence", "pdf", "sample_wo", "sample_pdf", "sample_weight", "sample_lobe", "sample_valid"]:
+        assert np.array_equal(got[k].view(np.uint32), ref[k].view(np.uint32)), k
+        assert np.array_equal(again[k].view(np.uint32), ref[k].view(np.uint32)), k
+    ctx.close()
