@@ -253,14 +253,25 @@ def render_bench(dev, stream, frames, warmup, cpu_seconds=0.0, size=1024):
     return res
 
 
-def learned_bench(dev, stream, batches=16, spp=16, prob=0.25, width=256):
+def relmse(x, ref, eps=1e-2):
+    """Relative MSE of an image against a reference: mean over pixels and channels of
+    (x - ref)^2 / (ref^2 + eps)."""
+    import numpy as np
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + eps)))
+
+
+def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0, batch_spp=32):
     """Learned proposal against the analytic tracer on the 1.04 M-triangle procedural room (the render
-    leg's scene and options at width^2): the proposal is trained on 2^24 samples drawn from the exact
-    samplers of the scene's materials (256 Adam steps x 65536, lr 1e-3), then both tracers render
-    `batches` independent batches of `spp` frames.  Per-batch relMSE (eps 1e-2) is taken against the
-    mean of both tracers' batches (both are unbiased for the same image); relMSE falls as 1/spp, so the
-    time to relMSE <= 1e-3 is relMSE(spp) * spp / 1e-3 frames at the measured time per frame (CUDA
-    events), plus the training time for the learned tracer."""
+    leg's scene and options at width^2), measured against an independent reference: the analytic
+    tracer at ref_spp samples per pixel (frames disjoint from the compared renders).  The proposal
+    is trained on 2^24 samples drawn from the exact samplers of the scene's materials (256 Adam steps
+    x 65536, lr 1e-3).  Each tracer then renders batches of batch_spp frames for budget_s seconds
+    (CUDA events), the running mean compared with the reference (relMSE, eps 1e-2) after every batch.
+
+    Reported: both convergence curves; the directly measured time each tracer needs to reach the
+    lowest relMSE both reach (training time included for the learned one) and their ratio; and the
+    time to relMSE 1e-3 of the tracer's own error, from the curve fitted as V / spp + R, where R is the
+    reference's own contribution (it is itself an analytic render, at ref_spp spp)."""
     import numpy as np
     import torch
     from pltfalcor_gb300 import scene as S, spectra
@@ -273,22 +284,29 @@ def learned_bench(dev, stream, batches=16, spp=16, prob=0.25, width=256):
     cam = S.room_camera(W, H)
     out = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
 
-    def run(ctx):
-        imgs, ms = [], []
-        ctx.render(cam, W, H, out, 1 << 24, 1, stream)
-        for b in range(batches):
+    def curve(ctx, ref, frame0):
+        acc = np.zeros((H, W, 3))
+        spp, t_ms, pts = 0, 0.0, []
+        ctx.render(cam, W, H, out, 1 << 26, 1, stream)     # warm-up (graph recording)
+        torch.cuda.synchronize()
+        while t_ms < budget_s * 1e3:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            ctx.render(cam, W, H, out, b * spp, spp, stream)
+            ctx.render(cam, W, H, out, frame0 + spp, batch_spp, stream)
             e1.record(stream)
             torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1) / spp)
-            imgs.append(out[..., :3].double().cpu().numpy())
-        return np.stack(imgs), float(np.median(ms))
+            t_ms += e0.elapsed_time(e1)
+            acc += out[..., :3].double().cpu().numpy() * batch_spp
+            spp += batch_spp
+            pts.append((spp, t_ms * 1e-3, relmse(acc / spp, ref)))
+        return pts, acc / spp
 
     ctx = PLTContext(base)
     ctx.load_scene(sc, prof)
-    a, ms_a = run(ctx)
+    ctx.render(cam, W, H, out, 1 << 28, ref_spp, stream)
+    torch.cuda.synchronize()
+    ref = out[..., :3].double().cpu().numpy()
+    plain, img_p = curve(ctx, ref, 0)
     ctx.close()
     ctx = PLTContext(dict(base, learned_proposal=1, learned_proposal_prob=prob))
     ctx.load_scene(sc, prof)
@@ -298,25 +316,40 @@ def learned_bench(dev, stream, batches=16, spp=16, prob=0.25, width=256):
     hist = ctx.proposal_train(256, batch=65536, lr=1e-3, seed=1)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    b, ms_b = run(ctx)
+    learned, img_l = curve(ctx, ref, 0)
     st = ctx.check_status(stream)
     ctx.close()
-    ref = 0.5 * (a.mean(0) + b.mean(0))
-    rel = lambda x: np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2), axis=(1, 2, 3))
-    ra, rb = rel(a), rel(b)
-    ma, mb = a.mean(axis=(1, 2, 3)), b.mean(axis=(1, 2, 3))
-    se = float(np.sqrt(ma.var(ddof=1) / batches + mb.var(ddof=1) / batches))
-    t_a = float(ra.mean()) * spp / 1e-3 * ms_a * 1e-3
-    t_b = float(rb.mean()) * spp / 1e-3 * ms_b * 1e-3 + train_s
+
+    # fit relMSE(spp) = V / spp + R by least squares over the second half of each curve, with R shared
+    # (the reference's error, equal for both comparisons in expectation)
+    def design(pts):
+        p = pts[len(pts) // 2:]
+        return np.array([1.0 / s for s, _, _ in p]), np.array([m for _, _, m in p])
+    xp, yp = design(plain)
+    xl, yl = design(learned)
+    A = np.zeros((len(xp) + len(xl), 3))
+    A[:len(xp), 0], A[len(xp):, 1], A[:, 2] = xp, xl, 1.0
+    (Vp, Vl, R), *_ = np.linalg.lstsq(A, np.concatenate([yp, yl]), rcond=None)
+    ms_p = plain[-1][1] / plain[-1][0] * 1e3
+    ms_l = learned[-1][1] / learned[-1][0] * 1e3
+    t_p = Vp / 1e-3 * ms_p * 1e-3
+    t_l = Vl / 1e-3 * ms_l * 1e-3 + train_s
+    # directly measured: first time each curve reaches the lowest relMSE both curves reach
+    level = max(min(m for _, _, m in plain), min(m for _, _, m in learned))
+    first = lambda pts, extra: next(t for _, t, m in pts if m <= level) + extra
+    tm_p, tm_l = first(plain, 0.0), first(learned, train_s)
     return {"workload": "procedural room 1.04 M triangles, %dx%d, max depth 8, HWSS 4 + spectral MIS, NEE + MIS + manifold NEE, "
                         "RR; learned proposal probability %.2f, trained on 2^24 exact-sampler samples" % (W, H, prob),
-            "status": int(st), "spp_per_batch": spp, "batches": batches,
-            "relmse_plain": float(ra.mean()), "relmse_learned": float(rb.mean()),
-            "relmse_plain_median": float(np.median(ra)), "relmse_learned_median": float(np.median(rb)),
-            "image_mean_plain": float(ma.mean()), "image_mean_learned": float(mb.mean()), "image_mean_se": se,
-            "ms_per_spp_plain": ms_a, "ms_per_spp_learned": ms_b, "train_s": train_s,
+            "reference": "analytic tracer, %d spp, frames disjoint from the compared renders" % ref_spp,
+            "status": int(st), "budget_s_per_tracer": budget_s, "batch_spp": batch_spp,
+            "curve_plain": [[s, round(t, 4), m] for s, t, m in plain[::max(1, len(plain) // 12)]] + [list(plain[-1])],
+            "curve_learned": [[s, round(t, 4), m] for s, t, m in learned[::max(1, len(learned) // 12)]] + [list(learned[-1])],
+            "image_mean_plain": float(img_p.mean()), "image_mean_learned": float(img_l.mean()), "image_mean_reference": float(ref.mean()),
+            "ms_per_spp_plain": ms_p, "ms_per_spp_learned": ms_l, "train_s": train_s,
             "train_loss_first_last": [float(hist[:8].mean()), float(hist[-8:].mean())],
-            "time_to_relmse_1e-3_plain_s": t_a, "time_to_relmse_1e-3_learned_s": t_b, "speedup": t_a / t_b}
+            "measured_equal_relmse": {"relmse": level, "time_plain_s": tm_p, "time_learned_s": tm_l, "speedup": tm_p / tm_l},
+            "fit": {"V_plain": float(Vp), "V_learned": float(Vl), "R_reference": float(R)},
+            "time_to_relmse_1e-3_plain_s": float(t_p), "time_to_relmse_1e-3_learned_s": float(t_l), "speedup": float(t_p / t_l)}
 
 
 def scene_set_bench(dev, stream, count=64, frames=2):

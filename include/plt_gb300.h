@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define PLT_ABI_VERSION 3u
+#define PLT_ABI_VERSION 4u
 #define PLT_MAX_HWSS 8u                 /* hero wavelengths per beam (reference: <= 4, Utils/HWSS.slang:4-9) */
 #define PLT_SPECTRAL_MAX_BINS 128u      /* SpectralProfile::kMaxBins */
 #define PLT_NO_SPECTRAL_PROFILE 0xFFFFFFFFu
@@ -217,10 +217,49 @@ typedef struct plt_options {
     uint32_t learned_proposal;          /* default 0 */
     float learned_proposal_prob;        /* in (0, 1), default 0.5 */
     uint32_t emissive_sampler;          /* emissiveSampler: 0 Uniform, 2 Power (EmissiveLightSamplerType), default 2 */
+    uint32_t debug_view;                /* debugView: a PLT_DEBUG_VIEW_* value (DebugViewType.slangh), default 0 (none) */
+    float debug_view_intensity;         /* debugViewIntensity: lerp(colour, debug colour, intensity), default 1 */
+    uint32_t alpha_masking;             /* alphaMasking: hits on alpha-0 materials pass through, default 1 */
+    uint32_t sample_generator;          /* sampleGenerator: PLT_SAMPLE_GENERATOR_*, default 1 (uniform) */
 } plt_options;
 
+/* debugView values (RenderPasses/PLTPT/DebugViewType.slangh).  The debug colour of a pixel is the
+ * mean of the values each view writes along its path (pltpt_debug.slangh); colour-coded scalars
+ * use the magma (path length, spectral samples, coherence area) or inferno (coherence anisotropy,
+ * MNEE iterations) colour maps (ColourCoding.slang). */
+#define PLT_DEBUG_VIEW_NONE 0u
+#define PLT_DEBUG_VIEW_NANS 1u
+#define PLT_DEBUG_VIEW_INFS 2u
+#define PLT_DEBUG_VIEW_PATH_LENGTH 3u
+#define PLT_DEBUG_VIEW_HWSS_COMPS 4u
+#define PLT_DEBUG_VIEW_NORMALS 5u
+#define PLT_DEBUG_VIEW_ALBEDO 6u
+#define PLT_DEBUG_VIEW_ROUGHNESS 7u
+#define PLT_DEBUG_VIEW_UVS 8u
+#define PLT_DEBUG_VIEW_COHERENCE_AREA 9u
+#define PLT_DEBUG_VIEW_COHERENCE_ANISOTROPY 10u
+#define PLT_DEBUG_VIEW_POLARIZATION 11u
+#define PLT_DEBUG_VIEW_MNEE_ITERATIONS 12u
+#define PLT_DEBUG_VIEW_MNEE_BOUNCES 13u
+
+/* sampleGenerator values (Utils/Sampling/SampleGeneratorType.slangh): TinyUniformSampleGenerator
+ * (a TEA-seeded 32-bit LCG) and UniformSampleGenerator (SplitMix64-seeded xoshiro128**). */
+#define PLT_SAMPLE_GENERATOR_TINY_UNIFORM 0u
+#define PLT_SAMPLE_GENERATOR_UNIFORM 1u
+
 #define PLT_OPTION_FP64_MULTILAYER 0x1u /* multilayer recursion in FP64 instead of the reference FP32 */
+/* complex-IOR conductor Fresnel (Fresnel.slang:60-73) in FP64 where cos(theta_i) < 0.1 (grazing
+ * incidence), for every conductor surface: conductor, coated conductor and grated conductor */
+#define PLT_OPTION_FP64_CONDUCTOR_GRAZING 0x10u
 #define PLT_OPTION_NO_GRAPH 0x2u        /* plt_render*: launch each frame directly instead of replaying its recorded CUDA graph */
+/* Failure injection for tests of the device-side error paths (no counterpart in the reference).
+ * Neither faults, traps or hangs the GPU: each makes a bounded condition trip and the kernels
+ * report it in the status word that plt_check_status returns (PLT_QUEUE_TIMEOUT), leaving the
+ * context usable.  FAULT_COPY_WAIT: the BSDF shade kernel's wait for its spectral-table copy gives
+ * up at once (the CTAs then let the copy land and return without shading).  FAULT_SHORT_STACK:
+ * plt_trace_* traverse with a 2-entry stack, so deep rays overflow it. */
+#define PLT_OPTION_FAULT_COPY_WAIT 0x4u
+#define PLT_OPTION_FAULT_SHORT_STACK 0x8u
 
 typedef struct plt_context plt_context;
 

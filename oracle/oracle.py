@@ -46,6 +46,8 @@ def load():
         lib.plto_count_ops.argtypes = [vp, u32, vp, u32, vp, u32, C.POINTER(C.c_double)]
         lib.plto_rng_stream.restype = None
         lib.plto_rng_stream.argtypes = [u32, u32, u32, u32, C.POINTER(C.c_uint32)]
+        lib.plto_rng_stream_tiny.restype = None
+        lib.plto_rng_stream_tiny.argtypes = [u32, u32, u32, u32, C.POINTER(C.c_uint32)]
         lib.plto_half_to_float.restype = C.c_float
         lib.plto_half_to_float.argtypes = [C.c_uint16]
         lib.plto_rgb_to_spectrum.restype = C.c_float
@@ -125,9 +127,12 @@ def results_struct(res):
     return r
 
 
-def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, end=None, res=None, sr_seed=None):
+def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, end=None, res=None, sr_seed=None,
+        fp64_conductor_grazing=False):
     """Runs the oracle over queries [begin, end) of workload `wl`; returns the results dict.
-    precision: 32 (FP32), 64 (FP64) or 16 (FP32 with random rounding, seed `sr_seed`)."""
+    precision: 32 (FP32), 64 (FP64) or 16 (FP32 with random rounding, seed `sr_seed`);
+    fp64_multilayer / fp64_conductor_grazing: the FP32 oracle's twins of the library's
+    PLT_OPTION_FP64_MULTILAYER / PLT_OPTION_FP64_CONDUCTOR_GRAZING."""
     lib = load()
     if precision == 16:
         lib.plto_set_sr_seed(1 if sr_seed is None else sr_seed)
@@ -138,7 +143,8 @@ def run(wl, ops=None, precision=32, threads=0, fp64_multilayer=False, begin=0, e
     r = results_struct(res)
     recs = np.ascontiguousarray(wl.records)
     prof = wl.profiles
-    st = lib.plto_bsdf_batch_range(precision, int(fp64_multilayer), C.c_void_p(recs.ctypes.data), len(recs),
+    flags = (0x1 if fp64_multilayer else 0) | (0x10 if fp64_conductor_grazing else 0)
+    st = lib.plto_bsdf_batch_range(precision, flags, C.c_void_p(recs.ctypes.data), len(recs),
                                    C.cast(prof, C.c_void_p) if prof is not None else None, len(prof) if prof is not None else 0,
                                    C.byref(q), C.byref(r), ops, threads, begin, end)
     if st != 0:
@@ -188,9 +194,11 @@ def trace_brute(tri_verts, origin, direction, tmin=None, tmax=None, any_hit=Fals
     return prim, t, bary
 
 
-def rng_stream(px, py, frame, count):
+def rng_stream(px, py, frame, count, tiny=False):
+    """The generator's first `count` 32-bit outputs for (pixel, frame): UniformSampleGenerator, or
+    TinyUniformSampleGenerator with tiny=True."""
     out = (C.c_uint32 * count)()
-    load().plto_rng_stream(px, py, frame, count, out)
+    (load().plto_rng_stream_tiny if tiny else load().plto_rng_stream)(px, py, frame, count, out)
     return np.frombuffer(out, dtype=np.uint32).copy()
 
 

@@ -8,6 +8,8 @@
 // known-answer tests in tests/ pin the pieces that have closed forms.
 #pragma once
 
+#include <type_traits>
+
 #include "plt_math.hpp"
 #include "../include/plt_gb300.h"
 
@@ -63,15 +65,40 @@ inline uint64_t splitmix64_next(uint64_t& state) {
     return z ^ (z >> 31);
 }
 inline uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+// blockCipherTEA (Utils/Math/HashUtils.slang:59-71), 16 rounds; its first output word
+inline uint32_t teaFirstWord(uint32_t v0, uint32_t v1) {
+    const uint32_t k[4] = {0xa341316cu, 0xc8013ea4u, 0xad90777du, 0x7e95761eu};
+    uint32_t sum = 0;
+    for (int i = 0; i < 16; ++i) {
+        sum += 0x9e3779b9u;
+        v0 += ((v1 << 4) + k[0]) ^ (v1 + sum) ^ ((v1 >> 5) + k[1]);
+        v1 += ((v0 << 4) + k[2]) ^ (v0 + sum) ^ ((v0 >> 5) + k[3]);
+    }
+    return v0;
+}
+// UniformSampleGenerator, or with tiny TinyUniformSampleGenerator
+// (Utils/Sampling/TinyUniformSampleGenerator.slang:50-70: LCG, Pseudorandom/LCG.slang, seeded with
+// blockCipherTEA(interleave_32bit(pixel), sampleNumber).x; its state in s[0]).
 struct SampleGen {
     uint32_t s[4];
-    SampleGen(uint32_t px, uint32_t py, uint32_t sampleNumber) {
+    bool tiny = false;
+    SampleGen(uint32_t px, uint32_t py, uint32_t sampleNumber, bool tinyGen = false) {
+        if (tinyGen) {
+            tiny = true;
+            s[0] = teaFirstWord(interleave_32bit(px, py), sampleNumber);
+            s[1] = s[2] = s[3] = 0u;
+            return;
+        }
         uint64_t st = ((uint64_t)sampleNumber << 32) | (uint64_t)interleave_32bit(px, py);
         const uint64_t s0 = splitmix64_next(st);
         const uint64_t s1 = splitmix64_next(st);
         s[0] = (uint32_t)s0; s[1] = (uint32_t)(s0 >> 32); s[2] = (uint32_t)s1; s[3] = (uint32_t)(s1 >> 32);
     }
     uint32_t next() {
+        if (tiny) {
+            s[0] = 1664525u * s[0] + 1013904223u;
+            return s[0];
+        }
         const uint32_t result = rotl32(s[0] * 5u, 7) * 9u;
         const uint32_t t = s[1] << 9;
         s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
@@ -335,7 +362,20 @@ template <class R> inline R evalFresnelDielectric(R eta, R cosThetaI, R& cosThet
 }
 template <class R> inline R evalFresnelDielectric(R eta, R cosThetaI) { R c; return evalFresnelDielectric(eta, cosThetaI, c); }
 
+// The FP32 oracle's twin of PLT_OPTION_FP64_CONDUCTOR_GRAZING: set per thread around a query.
+inline thread_local bool g_fp64ConductorGrazing = false;
+constexpr float kFp64GrazingCos = 0.1f;
+template <class R> inline void fresnel_conductor(R cosThetaI, V2<R> eta, V2<R>& rs, V2<R>& rp);
 template <class R> inline void fresnel_conductor(R cosThetaI, V2<R> eta, V2<R>& rs, V2<R>& rp) {
+    if constexpr (std::is_same_v<R, float>) {
+        if (g_fp64ConductorGrazing && cosThetaI < kFp64GrazingCos) {
+            V2<double> a, b;
+            fresnel_conductor<double>((double)cosThetaI, V2<double>{(double)eta.x, (double)eta.y}, a, b);
+            rs = V2<float>{(float)a.x, (float)a.y};
+            rp = V2<float>{(float)b.x, (float)b.y};
+            return;
+        }
+    }
     if ((eta.x == R(0) && eta.y == R(0)) || cosThetaI < R(0)) {
         rs = rp = c_t(R(0), R(0));
         return;

@@ -54,7 +54,10 @@ int runBatch(const plt_material_record* mats, uint32_t nm, const plt_spectral_pr
         const uint32_t j = i + q->rng_offset;
         SampleGen sg(j & 0xFFFFu, j >> 16, q->frame);
         QueryResult<R> o;
-        if (!queryMaterial(m, sc, ops, V, W, lobe, b, &sg, o, fp64ml != 0)) { bad |= 2; continue; }
+        g_fp64ConductorGrazing = (fp64ml & PLT_OPTION_FP64_CONDUCTOR_GRAZING) != 0;
+        const bool ok = queryMaterial(m, sc, ops, V, W, lobe, b, &sg, o, (fp64ml & PLT_OPTION_FP64_MULTILAYER) != 0);
+        g_fp64ConductorGrazing = false;
+        if (!ok) { bad |= 2; continue; }
         if (ops & PLT_OP_EVAL) {
             if (r->stokes)
                 for (uint32_t c = 0; c < 4; ++c)
@@ -91,11 +94,15 @@ extern "C" {
 void plto_set_sr_seed(uint64_t seed) { g_sr_seed = seed; }
 
 // precision: 32 (FP32 reference), 64 (FP64 reference), 16 (FP32 with random rounding, seeded by
-// plto_set_sr_seed).  Processes queries [begin, end).
+// plto_set_sr_seed).  fp64_multilayer: PLT_OPTION_FP64_MULTILAYER / PLT_OPTION_FP64_CONDUCTOR_GRAZING
+// bits (a non-zero value without either bit, as older callers pass, means the multilayer option).
+// Processes queries [begin, end).
 int plto_bsdf_batch_range(int precision, int fp64_multilayer, const plt_material_record* mats, uint32_t nm,
                           const plt_spectral_profile* profs, uint32_t np, const plt_bsdf_queries* q,
                           const plt_bsdf_results* r, uint32_t ops, int threads, uint64_t begin, uint64_t end) {
     if (!mats || !q || !r || end > q->n || begin > end) return PLT_INVALID_ARG;
+    if (fp64_multilayer && !(fp64_multilayer & (PLT_OPTION_FP64_MULTILAYER | PLT_OPTION_FP64_CONDUCTOR_GRAZING)))
+        fp64_multilayer = PLT_OPTION_FP64_MULTILAYER;
     if (precision == 64) return runBatch<double>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
     if (precision == 16) return runBatch<SR>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
     return runBatch<float>(mats, nm, profs, np, q, r, ops, threads, fp64_multilayer, begin, end);
@@ -158,6 +165,12 @@ int plto_count_ops(const plt_material_record* mats, uint32_t nm, const plt_spect
 // First `count` raw 32-bit outputs of UniformSampleGenerator(pixel, sampleNumber).
 void plto_rng_stream(uint32_t px, uint32_t py, uint32_t sample_number, uint32_t count, uint32_t* out) {
     SampleGen sg(px, py, sample_number);
+    for (uint32_t i = 0; i < count; ++i) out[i] = sg.next();
+}
+
+// the TinyUniformSampleGenerator stream of (pixel, sample number), for tests
+void plto_rng_stream_tiny(uint32_t px, uint32_t py, uint32_t sample_number, uint32_t count, uint32_t* out) {
+    SampleGen sg(px, py, sample_number, true);
     for (uint32_t i = 0; i < count; ++i) out[i] = sg.next();
 }
 

@@ -92,7 +92,23 @@ struct Options {
     bool useEnv = false;
     bool useAnalytic = false;
     bool uniformEmissive = false;   // emissiveSampler = Uniform (else Power)
+    bool alphaMask = true;          // alphaMasking
+    bool tinySg = false;            // sampleGenerator = TinyUniform (else Uniform)
+    uint32_t debugView = 0;         // DebugViewType
+    float debugIntensity = 1.f;
 };
+
+// ---- debug views: writeDebugOutput and the colour maps of pltpt_debug.slangh / ColourCoding.slang
+#include "../pltfalcor_gb300/csrc/plt_colour_maps.h"
+
+F3 colourCode(const float (*t)[3], float val) {
+    val *= 256.f;
+    if (!std::isfinite(val)) return {NAN, 0.f, 0.f};
+    const int l = std::clamp((int)val, 0, 255), h = std::clamp((int)(val + 1.f), 0, 255);
+    const float fr = val - std::floor(val);
+    const F3 a = {t[l][0], t[l][1], t[l][2]}, b = {t[h][0], t[h][1], t[h][2]};
+    return a + (b - a) * fr;
+}
 
 // ---------------------------------------------------------------------------------------------
 // Light collection and the power sampler's alias table
@@ -850,7 +866,7 @@ struct Renderer {
 
     // ---- sample pass, pltpt_sample.rt.slang:36-185 ----
     void samplePass(uint32_t px, uint32_t py, Bounce* bounces) const {
-        SampleGen sg(px, py, frame);
+        SampleGen sg(px, py, frame, o.tinySg);
         const float wavelength = sampleOneWavelength(sg.next1D());
         F3 origin = f3(cam.pos), dir = cameraDir(px, py);
         float weight = 1.f, pdf = 1.f, thp = 1.f, lastNonDeltaPdf = 0.f;
@@ -883,7 +899,7 @@ struct Renderer {
             const uint32_t mid = s.triMat[prim];
             const ShadingData sd = prepareShadingData(s, v, mid, wi);
             const Props props = bsdfProps(s, mid);
-            if (sd.opacity == 0.f) {   // alpha mask
+            if (o.alphaMask && sd.opacity == 0.f) {   // alpha mask (kAlphaMasking)
                 origin = sd.newRayOrigin(false);
                 continue;
             }
@@ -978,6 +994,7 @@ struct Renderer {
     struct Solve {
         SampleGen sg, tilesg;
         F3 Lrgb = {0.f, 0.f, 0.f};
+        float dbg[4] = {0.f, 0.f, 0.f, 0.f};   // debugOutput (Path.slang:205)
         F3 pathOrigin, pathNormal;
         float wavelength = 0.f;
         uint64_t shadowRays = 0, unwindEvals = 0;
@@ -1011,8 +1028,31 @@ struct Renderer {
     }
 
     // measure, pltpt_solve.rt.slang:96-147
+    // writeDebugOutput, pltpt_debug.slangh:19-23
+    void debugWrite(Solve& sv, uint32_t view, F3 v) const {
+        if (o.debugView == view && std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z)) {
+            sv.dbg[0] += v.x;
+            sv.dbg[1] += v.y;
+            sv.dbg[2] += v.z;
+            sv.dbg[3] += 1.f;
+        }
+    }
+
     void measure(Solve& sv, int bounceIdx, float pathContribution, Beam<float>& beam) const {
         if (!o.useDirect && bounceIdx <= 1) return;
+        if (o.debugView) {
+            // coherence views before the propagation to the camera (pltpt_solve.rt.slang:102-106);
+            // coherenceAnisotropy through svd_symmetric (PLT.slang:193-197, MathHelpers.slang:583-605)
+            const float k = float(K_2PI) / (1e-3f * beam.wl[0]);
+            debugWrite(sv, PLT_DEBUG_VIEW_COHERENCE_AREA, colourCode(kMagma, std::sqrt(beam.coherenceArea(k)) / 150.f));
+            const M2<float> A = beam.invTheta(k);
+            const float a = A.m[0][0], b = A.m[1][0], c = A.m[0][1], d = A.m[1][1];
+            const float a2 = a * a, b2 = b * b, c2 = c * c, d2 = d * d;
+            const float y = 2.f * a * c + 2.f * b * d, x = a2 + b2 - c2 - d2;
+            const float s1 = a2 + b2 + c2 + d2, s2 = std::sqrt(x * x + y * y);
+            const float aniso = 1.f - std::sqrt((s1 + s2) / 2.f) / std::sqrt((s1 - s2) / 2.f);
+            debugWrite(sv, PLT_DEBUG_VIEW_COHERENCE_ANISOTROPY, colourCode(kInferno, aniso));
+        }
         propagate(beam, f3(cam.pos));
         if (cam.polarizer > 0.f) {
             const F3 W = normalize(f3(cam.w)), U = normalize(f3(cam.u));
@@ -1043,6 +1083,19 @@ struct Renderer {
         const F3 rgb = spectrumToRgb(Li, beam.wl, (uint32_t)beam.H) * pathContribution;
         const F3 L = {std::max(0.f, rgb.x), std::max(0.f, rgb.y), std::max(0.f, rgb.z)};
         if (std::isfinite(L.x) && std::isfinite(L.y) && std::isfinite(L.z)) sv.Lrgb = sv.Lrgb + L;
+        if (o.debugView) {
+            // markDebug, pltpt_debug.slangh:31-50
+            const F3& Ls = sv.Lrgb;
+            if (std::isnan(Ls.x) || std::isnan(Ls.y) || std::isnan(Ls.z)) debugWrite(sv, PLT_DEBUG_VIEW_NANS, {5.f, 0.f, 3.f});
+            if (std::isinf(Ls.x) || std::isinf(Ls.y) || std::isinf(Ls.z)) debugWrite(sv, PLT_DEBUG_VIEW_INFS, {2.f, 0.f, 5.f});
+            debugWrite(sv, PLT_DEBUG_VIEW_PATH_LENGTH, colourCode(kMagma, (float)bounceIdx / float(o.maxBounces - 1)));
+            debugWrite(sv, PLT_DEBUG_VIEW_HWSS_COMPS, colourCode(kMagma, (float)beam.H / float(o.hwss)));
+            const float S0 = beam.L[0][0], S1 = beam.L[1][0], S2 = beam.L[2][0], S3 = beam.L[3][0];
+            const float cp = std::sqrt(S3 * S3) / S0, lp = std::sqrt(S1 * S1 + S2 * S2) / S0;
+            const float lpd = .5f * std::atan2(S2, S1);
+            const float cl = std::cos(lpd), sl = std::sin(lpd);
+            debugWrite(sv, PLT_DEBUG_VIEW_POLARIZATION, F3{lp * (cl * cl), cp, lp * (sl * sl)});
+        }
     }
 
     // LightCollection's active triangles: flux > 0 (LightCollection.cpp:512-524)
@@ -1484,6 +1537,12 @@ struct Renderer {
             const F3 origin = !currentVertexMS ? V.posW : sv.pathOrigin;
             const bool mneeOk = manifoldNEESample(ls.origin, ls.dir, 0.f, ls.distance, origin, ls.beam.posW, lightDir, ls.beam.distant,
                                                   maxMSBounces, sv.sg, ms, sv);
+            if (o.debugView) {
+                // MNEE views, pltpt_solve.rt.slang:319-325
+                debugWrite(sv, PLT_DEBUG_VIEW_MNEE_ITERATIONS, colourCode(kInferno, ms.iterations / float(o.mneeMaxIterations)));
+                if (ms.hitCount > 0 && mneeOk)
+                    debugWrite(sv, PLT_DEBUG_VIEW_MNEE_BOUNCES, ms.hitCount == 1 ? F3{0.f, .3f, 1.f} : F3{1.f, 0.f, 0.f});
+            }
             if (!mneeOk || ms.pdf < 1e-6f) return;
             if (ms.hitCount > 0) {
                 if (!o.hwssMis && ms.dispersive) ls.beam.H = 1;
@@ -1577,7 +1636,7 @@ struct Renderer {
 
     void solvePass(uint32_t px, uint32_t py, const Bounce* bounces, float* rgb, uint64_t* stats) const {
         const uint32_t tile = o.tileSize;
-        Solve sv{SampleGen(px, py, frame), SampleGen(px / tile, py / tile, frame << 2)};
+        Solve sv{SampleGen(px, py, frame, o.tinySg), SampleGen(px / tile, py / tile, frame << 2, o.tinySg)};
         sv.wavelength = sampleOneWavelength(sv.sg.next1D());
         sv.pathOrigin = f3(cam.pos);
         sv.pathNormal = normalize(f3(cam.w));
@@ -1592,9 +1651,20 @@ struct Renderer {
             const ShadingData sd = prepareShadingData(s, v, mid, b.wi());
             if (o.doNee) NEE(sv, p, bounces, sd, v, mid);
             evalEmissive(sv, p, bounces, sd, mid);
+            if (o.debugView && p == 0) {
+                // geometry views (pltpt_solve.rt.slang:449-456); no texture coordinates, so uv = 0
+                debugWrite(sv, PLT_DEBUG_VIEW_NORMALS, sd.N);
+                debugWrite(sv, PLT_DEBUG_VIEW_UVS, F3{0.f, 0.f, 0.f});
+            }
             if ((b.flags & FLAG_TERMINATED) || p == (int)o.maxBounces) break;
             sv.pathOrigin = v.posW;
             sv.pathNormal = sd.N;
+        }
+        if (o.debugView) {
+            // lerp(colour, mean debug colour, intensity), pltpt_solve.rt.slang:470-475
+            const float t = o.debugIntensity;
+            const F3 dm = sv.dbg[3] > 0.f ? F3{sv.dbg[0], sv.dbg[1], sv.dbg[2]} / sv.dbg[3] : F3{0.f, 0.f, 0.f};
+            sv.Lrgb = sv.Lrgb + (dm - sv.Lrgb) * t;
         }
         rgb[0] = sv.Lrgb.x;
         rgb[1] = sv.Lrgb.y;
@@ -1726,6 +1796,10 @@ int plto_render(const plto_scene* sc, const plt_camera* cam, const plt_options* 
     o.useEnv = opt->use_env_light != 0;
     o.useAnalytic = opt->use_analytic_lights != 0;
     o.uniformEmissive = opt->emissive_sampler == 0;
+    o.alphaMask = opt->alpha_masking != 0;
+    o.tinySg = opt->sample_generator == PLT_SAMPLE_GENERATOR_TINY_UNIFORM;
+    o.debugView = opt->debug_view;
+    o.debugIntensity = opt->debug_view_intensity;
     for (uint32_t i = 0; i < sc->n_lights; ++i) {
         const plt_analytic_light& l = sc->lights[i];
         s.alights.push_back(l);

@@ -18,6 +18,9 @@ OP_ALL = 0xF
 MAX_HWSS = 8
 NO_SPECTRAL_PROFILE = 0xFFFFFFFF
 OPTION_FP64_MULTILAYER = 0x1
+OPTION_FP64_CONDUCTOR_GRAZING = 0x10
+OPTION_FAULT_COPY_WAIT = 0x4
+OPTION_FAULT_SHORT_STACK = 0x8
 
 
 class SpectralProfile(C.Structure):
@@ -68,7 +71,14 @@ class Options(C.Structure):
                 ("do_importance_sample_emitters", C.c_uint32), ("do_mnee", C.c_uint32),
                 ("mnee_max_occluders", C.c_uint32), ("mnee_max_iterations", C.c_uint32),
                 ("mnee_solver_threshold", C.c_float), ("flags", C.c_uint32),
-                ("learned_proposal", C.c_uint32), ("learned_proposal_prob", C.c_float), ("emissive_sampler", C.c_uint32)]
+                ("learned_proposal", C.c_uint32), ("learned_proposal_prob", C.c_float), ("emissive_sampler", C.c_uint32),
+                ("debug_view", C.c_uint32), ("debug_view_intensity", C.c_float), ("alpha_masking", C.c_uint32),
+                ("sample_generator", C.c_uint32)]
+
+DEBUG_VIEW_NONE, DEBUG_VIEW_NANS, DEBUG_VIEW_INFS, DEBUG_VIEW_PATH_LENGTH, DEBUG_VIEW_HWSS_COMPS, DEBUG_VIEW_NORMALS, \
+    DEBUG_VIEW_ALBEDO, DEBUG_VIEW_ROUGHNESS, DEBUG_VIEW_UVS, DEBUG_VIEW_COHERENCE_AREA, DEBUG_VIEW_COHERENCE_ANISOTROPY, \
+    DEBUG_VIEW_POLARIZATION, DEBUG_VIEW_MNEE_ITERATIONS, DEBUG_VIEW_MNEE_BOUNCES = range(14)
+SAMPLE_GENERATOR_TINY_UNIFORM, SAMPLE_GENERATOR_UNIFORM = 0, 1
 
 
 class Camera(C.Structure):

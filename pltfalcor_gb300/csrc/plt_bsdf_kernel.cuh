@@ -4,49 +4,112 @@
 //
 // Work layout on sm_103a, two launches:
 //  1. classify: one CTA per tile of 2048 queries counting-sorts the tile by (material type, lobe
-//     class) in shared memory and writes the tile's permutation (16-bit local indices) to the
-//     scratch buffer; block 0 resets the shade kernel's work counter.
-//  2. shade: a persistent, barrier-free grid.  Each warp takes 32-query units from one global
-//     atomic counter.  Units are issued group by group (128 tiles = 262144 queries per group) and,
-//     inside a group, slot-major: unit slot s of every tile before slot s + 1.  Slot s covers
-//     sorted positions [32 s, 32 s + 32) of its tile, which hold the same (material, lobe) class
-//     in every tile, so at any moment the GPU runs one or two materials' code paths (instruction
-//     cache and SIMT coherence) while the group's inputs and outputs (~35 MB) stay L2-resident
-//     between the eight material passes (DRAM traffic stays one read of the inputs and one write
-//     of the outputs).  The spectral tables are staged into shared memory once per CTA by a bulk
+//     class) in shared memory, writes the tile's permutation (16-bit local indices) and the start of
+//     each material type's range in it, and adds the tile's per-type counts to the batch totals.
+//     The last CTA to finish builds the schedule from those totals: per material type, a queue of
+//     work units (each a slice of one tile's range of that type, tiles in order) and, per SM, the
+//     type it starts on, with SM shares proportional to each type's queries x relative cost.
+//  2. shade: a persistent, barrier-free grid.  Every warp of an SM takes units from the queue of
+//     its SM's type, so each SM runs one material's code at a time (the instruction caches hold
+//     one material's eval + sample + pdf), and because every queue walks the tiles in order at a
+//     rate matched to its SM share, all types work on the same few tiles at a time and each tile's
+//     inputs and outputs stay L2-resident between the material passes over it (DRAM traffic stays
+//     about one read of the inputs and one write of the outputs).  A warp whose queue runs dry
+//     moves to the queue with the most work left.  Each unit's code is specialised for its type at
+//     compile time.  The spectral tables are staged into shared memory once per CTA by a bulk
 //     asynchronous copy on an mbarrier.
 #include "plt_bsdf_query.cuh"
 #include "plt_ptx.cuh"
 
 namespace pltdev {
 
-constexpr uint32_t kLobeClasses = 10;                  // lowest set lobe bit (0..7), 8: none, 9: unused
-constexpr uint32_t kBuckets = 16 * kLobeClasses;        // material type x lobe class
-// Tiles per group: ~1,800 warps are in flight, so a group of G tiles keeps about 1800 / G slots
-// (sorted positions x 32) busy at once; 128 tiles (262 K queries, 35 MB of inputs and outputs in
-// L2) keeps them within one or two material classes.  Measured on the mixed-material batch: 64
-// tiles 4.13, 128 tiles 4.84, 256 tiles 4.66, 512 tiles 3.38 G queries/s (beyond L2).
-#ifndef PLT_GROUP_TILES
-#define PLT_GROUP_TILES 128
-#endif
-constexpr uint32_t kGroupTiles = PLT_GROUP_TILES;
-constexpr uint32_t kUnitsPerTile = plt::kBatchTile / 32;
+using plt::kTypeSlots;
+constexpr uint32_t kLobeClasses = 10;                     // lowest set lobe bit (0..7), 8: none, 9: padding
+constexpr uint32_t kBuckets = kTypeSlots * kLobeClasses;  // material type x lobe class
+constexpr uint32_t kPadBucket = kBuckets - 1;             // positions past the end of the batch
+
+// Control words of a batch's schedule (BatchParams::ctrl).  C_COUNT, C_MAX and C_DONE are zero
+// when a batch starts: the schedule builder zeroes them after reading them.
+enum : uint32_t {
+    C_COUNT = 0,    // [16] queries per type (classify atomics)
+    C_MAX = 16,     // [16] largest per-tile count per type (classify atomics)
+    C_NEXT = 32,    // [16] next unit of each type's queue (the shade kernel's work counters)
+    C_DONE = 48,    // classify CTAs finished
+    C_UNITS = 64,   // [16] units per tile of each type's queue
+    C_USZ = 80,     // [16] queries per unit of each type (a multiple of 32)
+    C_TOTAL = 96,   // [16] queries per type
+    C_WORDS = 112
+};
+static_assert(C_WORDS * 4 <= plt::kBsdfCtrlBytes, "control words exceed their scratch block");
 
 PLT_DI uint32_t lobeClass(uint32_t lobe) {
     const uint32_t l = lobe & 0xFFu;
     return l ? (uint32_t)(__ffs((int)l) - 1) : 8u;
 }
 
+PLT_DI uint32_t smId() {
+    uint32_t s;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(s));
+    return s;
+}
+PLT_DI uint32_t smIdCount() {
+    uint32_t s;
+    asm volatile("mov.u32 %0, %%nsmid;" : "=r"(s));
+    return s;
+}
+PLT_DI uint32_t ldVolatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
+
+// Schedule of a batch, built by the last classify CTA (all 256 threads) once every tile's counts
+// are in: unit size and units per tile of each type, and the SM -> starting type table.
+PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
+    using namespace plt;
+    const uint32_t tid = threadIdx.x;
+    uint32_t* count = sh;          // [16]
+    float* cum = reinterpret_cast<float*>(sh + 16);   // [17] cumulative work
+    if (tid < kTypeSlots) {
+        const uint32_t total = atomicExch(P.ctrl + C_COUNT + tid, 0u);
+        const uint32_t mx = atomicExch(P.ctrl + C_MAX + tid, 0u);
+        // units: slices of about unitQueries of one tile's range, at most ceil(max / unitQueries) per tile
+        const uint32_t units = mx ? (mx + P.unitQueries - 1) / P.unitQueries : 0u;
+        const uint32_t usz = units ? ((mx + units - 1) / units + 31u) & ~31u : 0u;
+        P.ctrl[C_UNITS + tid] = units;
+        P.ctrl[C_USZ + tid] = usz;
+        P.ctrl[C_TOTAL + tid] = total;
+        P.ctrl[C_NEXT + tid] = 0u;
+        count[tid] = total;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float s = 0.f;
+        cum[0] = 0.f;
+        for (uint32_t t = 0; t < kTypeSlots; ++t) {
+            s += (float)count[t] * P.typeCost[t];
+            cum[t + 1] = s;
+        }
+        P.ctrl[C_DONE] = 0u;
+    }
+    __syncthreads();
+    // SM s starts on the type whose share of the cumulative work holds (s + 1/2) / nsmid
+    const uint32_t nsm = min(smIdCount(), kMaxSmIds);
+    const float total = cum[kTypeSlots];
+    for (uint32_t s = tid; s < kMaxSmIds; s += blockDim.x) {
+        const float x = ((float)(s % nsm) + 0.5f) / (float)nsm * total;
+        uint32_t t = 0;
+        while (t + 1 < kTypeSlots && !(x < cum[t + 1])) ++t;
+        while (t + 1 < kTypeSlots && count[t] == 0) ++t;   // never start on an empty queue
+        P.smType[s] = (uint8_t)t;
+    }
+}
+
 // internal linkage: each per-wavelength-count translation unit carries its own copy
-static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(const uint32_t* __restrict__ material,
-                                                                         const uint32_t* __restrict__ lobes,
-                                                                         const uint8_t* __restrict__ matType, uint32_t nMats,
-                                                                         uint32_t n, uint16_t* __restrict__ perm,
-                                                                         uint32_t* __restrict__ unitCounter) {
+static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(const BatchParams P) {
     using namespace plt;
     __shared__ uint32_t counts[kBuckets];
     __shared__ uint32_t offs[kBuckets];
+    __shared__ uint32_t sched[40];
+    __shared__ bool isLast;
     const uint32_t tid = threadIdx.x;
+    const uint32_t n = P.q.n;
     const uint32_t base = blockIdx.x * kBatchTile;
     for (uint32_t b = tid; b < kBuckets; b += kBatchThreads) counts[b] = 0;
     __syncthreads();
@@ -54,11 +117,11 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
 #pragma unroll
     for (int k = 0; k < kBatchItems; ++k) {
         const uint32_t idx = base + k * kBatchThreads + tid;
-        uint32_t b = kBuckets - 1;
+        uint32_t b = kPadBucket;
         if (idx < n) {
-            const uint32_t mid = __ldg(material + idx);
-            const uint32_t t = mid < nMats ? __ldg(matType + mid) : 14u;
-            b = (t & 15u) * kLobeClasses + lobeClass(lobes ? __ldg(lobes + idx) : 0xFFFFu);
+            const uint32_t mid = __ldg(P.q.material + idx);
+            const uint32_t t = mid < P.nMats ? __ldg(P.matType + mid) : 14u;
+            b = (t & 15u) * kLobeClasses + lobeClass(P.q.lobe ? __ldg(P.q.lobe + idx) : 0xFFFFu);
         }
         key[k] = (uint16_t)b;
         rank[k] = (uint16_t)atomicAdd(&counts[b], 1u);
@@ -85,9 +148,94 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kBatchItems; ++k) perm[base + offs[key[k]] + rank[k]] = (uint16_t)(k * kBatchThreads + tid);
-    if (blockIdx.x == 0 && tid == 0) *unitCounter = 0u;
+    for (int k = 0; k < kBatchItems; ++k) P.perm[base + offs[key[k]] + rank[k]] = (uint16_t)(k * kBatchThreads + tid);
+    // type t's range of this tile: [offs[t * kLobeClasses], start of type t + 1); the padding bucket
+    // comes last, so its start is the tile's query count
+    if (tid <= kTypeSlots) {
+        const uint32_t start = tid < kTypeSlots ? offs[tid * kLobeClasses] : offs[kPadBucket];
+        P.tileTypeOff[blockIdx.x * (kTypeSlots + 1) + tid] = (uint16_t)start;
+        if (tid < kTypeSlots) {
+            const uint32_t end = tid + 1 < kTypeSlots ? offs[(tid + 1) * kLobeClasses] : offs[kPadBucket];
+            if (end > start) {
+                atomicAdd(P.ctrl + C_COUNT + tid, end - start);
+                atomicMax(P.ctrl + C_MAX + tid, end - start);
+            }
+        }
+    }
+    // the last CTA to finish builds the schedule (the counters above are complete once every CTA
+    // has passed the fence)
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) isLast = atomicAdd(P.ctrl + C_DONE, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (isLast) {
+        __threadfence();
+        buildSchedule(P, sched);
+    }
 }
+
+// One unit: positions [lo, hi) of the tile's sorted permutation, all of material type T (T = 0:
+// a slot of invalid types or material ids, which only report their status and zero the outputs).
+template <int H, uint32_t T>
+__device__ __forceinline__ void shadeUnit(const BatchParams& P, const Ctx& c, uint32_t tileBase, uint32_t lo, uint32_t hi, uint32_t lane) {
+    for (uint32_t pos = lo; pos < hi; pos += 32) {
+        const uint32_t k = pos + lane;
+        if (k < hi) {
+            const uint32_t idx = tileBase + __ldg(P.perm + tileBase + k);
+            if (idx < P.q.n) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, __ldg(P.q.material + idx), T);
+        }
+    }
+}
+
+// The queue with the most estimated work left (remaining units x unit size x cost), or kTypeSlots
+// when every queue is empty.  Whole warp.
+PLT_DI uint32_t busiestQueue(const BatchParams& P, uint32_t nTiles, uint32_t lane) {
+    float work = -1.f;
+    if (lane < kTypeSlots) {
+        const uint32_t units = min(ldVolatile(P.ctrl + C_UNITS + lane), (uint32_t)plt::kBatchTile / 32u) * nTiles;
+        const uint32_t next = ldVolatile(P.ctrl + C_NEXT + lane);
+        if (next < units) work = (float)(units - next) * (float)ldVolatile(P.ctrl + C_USZ + lane) * P.typeCost[lane];
+    }
+    uint32_t best = lane;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const float w2 = __shfl_xor_sync(0xFFFFFFFFu, work, d);
+        const uint32_t b2 = __shfl_xor_sync(0xFFFFFFFFu, best, d);
+        if (w2 > work || (w2 == work && b2 < best)) {
+            work = w2;
+            best = b2;
+        }
+    }
+    return work > 0.f ? best : kTypeSlots;
+}
+
+// The queue that is furthest behind in tiles (its next unit's tile), and its distance behind queue t.
+// Queues without units (empty types) and finished queues do not count.  Whole warp.
+PLT_DI uint32_t laggingQueue(const BatchParams& P, uint32_t nTiles, uint32_t t, uint32_t lane, uint32_t& lead) {
+    constexpr uint32_t kMaxUnits = plt::kBatchTile / 32;
+    uint32_t tile = 0xFFFFFFFFu;   // this lane's queue position in tiles
+    if (lane < kTypeSlots) {
+        const uint32_t units = min(ldVolatile(P.ctrl + C_UNITS + lane), kMaxUnits);
+        const uint32_t next = ldVolatile(P.ctrl + C_NEXT + lane);
+        if (units && next < units * nTiles) tile = next / units;
+    }
+    const uint32_t own = __shfl_sync(0xFFFFFFFFu, tile, t);
+    uint32_t lo = tile, who = lane;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const uint32_t l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, d), w2 = __shfl_xor_sync(0xFFFFFFFFu, who, d);
+        if (l2 < lo || (l2 == lo && w2 < who)) {
+            lo = l2;
+            who = w2;
+        }
+    }
+    lead = (own != 0xFFFFFFFFu && lo != 0xFFFFFFFFu) ? own - lo : 0u;
+    return who;
+}
+
+// Largest lead in tiles a queue may have over the slowest queue before its warps help the slowest:
+// about 64 x 270 KB of a tile's inputs and outputs stay in L2 beside the ~100 tiles in flight.
+constexpr uint32_t kMaxQueueLead = 64;
 
 template <int H>
 __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdfShadeKernel(const BatchParams P) {
@@ -109,7 +257,7 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
             mbar_arrive_expect_tx(&bar, profBytes);
             bulk_g2s(sprof, P.profiles, profBytes, &bar);
         }
-        const bool landed = mbar_wait_bounded(&bar, 0, 1u << 22);
+        const bool landed = mbar_wait_bounded(&bar, 0, P.copyPolls);
         // every thread agrees before anyone leaves, so no barrier below waits on an exited thread
         if (!__syncthreads_and(landed)) {
             if (tid == 0) {
@@ -121,35 +269,50 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     }
     const Ctx c{sprof, P.nProfiles, P.flags};
 
-    const uint32_t n = P.q.n;
-    const uint32_t nTiles = (n + kBatchTile - 1) / kBatchTile;
-    // With PLT_SHADE_SPLIT_OPS each requested operation is its own slot-major pass over a group
-    // (eval, then pdf, lambdaPdf, sample): a warp runs one operation of one material at a time,
-    // a smaller code footprint per unit for the instruction caches, at the price of re-reading the
-    // group's L2-resident inputs once per operation.
-#if PLT_SHADE_SPLIT_OPS
-    uint32_t opList[4], nOps = 0;
-    for (uint32_t o : {PLT_OP_EVAL, PLT_OP_PDF, PLT_OP_LAMBDA_PDF, PLT_OP_SAMPLE})
-        if (P.ops & o) opList[nOps++] = o;
-#else
-    const uint32_t opList[1] = {0xFFFFFFFFu}, nOps = 1;
-#endif
-    const uint32_t totalUnits = nTiles * kUnitsPerTile * nOps;
+    const uint32_t nTiles = (P.q.n + kBatchTile - 1) / kBatchTile;
+    // the schedule never has more than kBatchTile / 32 units of at least 32 queries per tile; the
+    // clamps keep every loop bounded whatever the control words hold
+    constexpr uint32_t kMaxUnits = kBatchTile / 32;
+    uint32_t t = P.smType[smId() % kMaxSmIds] % kTypeSlots;
+    uint32_t units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
     for (;;) {
+        // keep every queue within kMaxQueueLead tiles of the slowest one, so that each tile is shaded
+        // by all its material types while its inputs and outputs are in L2
+        uint32_t lead;
+        const uint32_t slow = laggingQueue(P, nTiles, t, lane, lead);
+        if (lead > kMaxQueueLead && slow < kTypeSlots) {
+            t = slow;
+            units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
+        }
         uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(P.unitCounter, 1u);
+        if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
         u = __shfl_sync(0xFFFFFFFFu, u, 0);
-        if (u >= totalUnits) break;
-        const uint32_t group = u / (kUnitsPerTile * kGroupTiles * nOps);
-        uint32_t within = u - group * (kUnitsPerTile * kGroupTiles * nOps);
-        const uint32_t gTiles = min(kGroupTiles, nTiles - group * kGroupTiles);
-        const uint32_t op = within / (gTiles * kUnitsPerTile);
-        within -= op * (gTiles * kUnitsPerTile);
-        const uint32_t slot = within / gTiles;
-        const uint32_t tile = group * kGroupTiles + (within - slot * gTiles);
-        const uint32_t base = tile * kBatchTile;
-        const uint32_t idx = base + __ldg(P.perm + base + slot * 32u + lane);
-        if (idx < n) processQuery<H>(P, c, idx, opList[op]);
+        if (u >= units * nTiles) {
+            t = busiestQueue(P, nTiles, lane);
+            if (t >= kTypeSlots) break;
+            units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
+            continue;
+        }
+        const uint32_t tile = u / units, sub = u - tile * units;
+        const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
+        const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
+        const uint32_t lo = __ldg(off + t) + sub * usz, end = min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile);
+        const uint32_t hi = min(end, lo + usz);
+        if (lo >= hi) continue;
+        const uint32_t tileBase = tile * kBatchTile;
+        switch (t) {
+        case kMatDielectric: shadeUnit<H, kMatDielectric>(P, c, tileBase, lo, hi, lane); break;
+        case kMatConductor: shadeUnit<H, kMatConductor>(P, c, tileBase, lo, hi, lane); break;
+        case kMatOpaqueDielectric: shadeUnit<H, kMatOpaqueDielectric>(P, c, tileBase, lo, hi, lane); break;
+        case kMatCoatedConductor: shadeUnit<H, kMatCoatedConductor>(P, c, tileBase, lo, hi, lane); break;
+        case kMatCoatedOpaque: shadeUnit<H, kMatCoatedOpaque>(P, c, tileBase, lo, hi, lane); break;
+        case kMatGratedConductor: shadeUnit<H, kMatGratedConductor>(P, c, tileBase, lo, hi, lane); break;
+        case kMatGratedOpaque: shadeUnit<H, kMatGratedOpaque>(P, c, tileBase, lo, hi, lane); break;
+        case kMatThin: shadeUnit<H, kMatThin>(P, c, tileBase, lo, hi, lane); break;
+        case kMatMultilayer: shadeUnit<H, kMatMultilayer>(P, c, tileBase, lo, hi, lane); break;
+        case kMatDiffuse: shadeUnit<H, kMatDiffuse>(P, c, tileBase, lo, hi, lane); break;
+        default: shadeUnit<H, 0u>(P, c, tileBase, lo, hi, lane); break;
+        }
     }
 }
 
@@ -157,35 +320,61 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
 
 namespace plt {
 
+// Default relative cost per query of each material type (the schedule's SM shares): shade time
+// per query in ns of each material's 2^19 queries of the mixed-material batch run alone on GB300
+// (eval + sample + pdf, HWSS 1).  Opaque dielectric and diffuse are estimates.
+inline float defaultTypeCost(uint32_t t) {
+    using namespace pltdev;
+    switch (t) {
+    case kMatDielectric: return .105f;
+    case kMatConductor: return .090f;
+    case kMatCoatedOpaque: return .105f;
+    case kMatCoatedConductor: return .117f;
+    case kMatGratedOpaque: return .150f;
+    case kMatGratedConductor: return .160f;
+    case kMatThin: return .078f;
+    case kMatMultilayer: return .156f;
+    case kMatOpaqueDielectric: return .080f;
+    case kMatDiffuse: return .050f;
+    default: return .050f;
+    }
+}
+
 // classify: one CTA per tile; shade: persistent grid of SM count x resident CTAs per SM
 // (occupancy at this launch's shared memory).
 template <int H>
-cudaError_t launchBsdfBatchH(const BatchParams& p, int numSMs, cudaStream_t stream) {
-    const uint32_t nTiles = (p.q.n + kBatchTile - 1) / kBatchTile;
+cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t stream) {
+    const uint32_t nTiles = (p0.q.n + kBatchTile - 1) / kBatchTile;
     if (nTiles == 0) return cudaSuccess;
-    if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
-    pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p.q.material, p.q.lobe, p.matType, p.nMats, p.q.n,
-                                                                    p.perm, p.unitCounter);
-    if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
     // at most 64 profiles x 528 B = 33 KB: below the 48 KB default limit, so no attribute is set
-    const size_t smem = (size_t)p.nProfiles * sizeof(pltdev::DevProfile);
+    const size_t smem = (size_t)p0.nProfiles * sizeof(pltdev::DevProfile);
     static_assert(64 * sizeof(pltdev::DevProfile) <= 48 * 1024, "profile staging exceeds the default shared-memory limit");
     int blocksPerSM = 1;
-    if (p.launch && p.launch->smem[H] == smem) {
-        blocksPerSM = p.launch->blocks[H];
+    if (p0.launch && p0.launch->smem[H] == smem) {
+        blocksPerSM = p0.launch->blocks[H];
     } else {
         int b = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::bsdfShadeKernel<H>, kShadeThreads, smem) != cudaSuccess || b < 1) b = 1;
         blocksPerSM = b;
-        if (p.launch) {
-            p.launch->smem[H] = smem;
-            p.launch->blocks[H] = b;
+        if (p0.launch) {
+            p0.launch->smem[H] = smem;
+            p0.launch->blocks[H] = b;
         }
     }
     uint32_t grid = (uint32_t)(numSMs * blocksPerSM);
-    const uint32_t warpsNeeded = nTiles * (kBatchTile / 32);
+    const uint32_t warpsNeeded = (p0.q.n + 31u) / 32u;
     const uint32_t gridCap = (warpsNeeded + (kShadeThreads / 32) - 1) / (kShadeThreads / 32);
     if (grid > gridCap) grid = gridCap;
+    BatchParams p = p0;
+    // units of up to 256 queries, smaller when the batch gives fewer than ~4 units per warp
+    const uint32_t warps = grid * (kShadeThreads / 32);
+    uint32_t uq = (p.q.n / (4u * warps) + 31u) & ~31u;
+    p.unitQueries = uq < 32u ? 32u : (uq > 256u ? 256u : uq);
+    for (uint32_t t = 0; t < kTypeSlots; ++t)
+        if (!(p.typeCost[t] > 0.f)) p.typeCost[t] = defaultTypeCost(t);
+    if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
+    pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p);
+    if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
     pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
     if (p.timing[2]) cudaEventRecord((cudaEvent_t)p.timing[2], stream);
     return cudaGetLastError();

@@ -74,6 +74,10 @@ plt_status plt_options_default(plt_options* o) {
     o->learned_proposal = 0;
     o->learned_proposal_prob = .5f;
     o->emissive_sampler = 2u;
+    o->debug_view = PLT_DEBUG_VIEW_NONE;
+    o->debug_view_intensity = 1.f;
+    o->alpha_masking = 1;
+    o->sample_generator = PLT_SAMPLE_GENERATOR_UNIFORM;
     return PLT_OK;
 }
 
@@ -85,6 +89,16 @@ plt_status plt_create(const plt_options* options, plt_context** out) {
     if (options) ctx->opt = *options;
     else plt_options_default(&ctx->opt);
     if (ctx->opt.hwss < 1 || ctx->opt.hwss > PLT_MAX_HWSS) { delete ctx; return PLT_INVALID_ARG; }
+    // debugView (DebugViewType), sampleGenerator (SampleGeneratorType) value ranges
+    if (ctx->opt.debug_view > PLT_DEBUG_VIEW_MNEE_BOUNCES || ctx->opt.sample_generator > PLT_SAMPLE_GENERATOR_UNIFORM) {
+        delete ctx;
+        return PLT_INVALID_ARG;
+    }
+    // the albedo and roughness views need BSDFProperties.albedo / .roughness, which are not built
+    if (ctx->opt.debug_view == PLT_DEBUG_VIEW_ALBEDO || ctx->opt.debug_view == PLT_DEBUG_VIEW_ROUGHNESS) {
+        delete ctx;
+        return PLT_NOT_SUPPORTED;
+    }
     // PLTPT offers the Uniform and Power emissive samplers (PLTPT.cpp:80-83, 401-409)
     if (ctx->opt.emissive_sampler != 0u && ctx->opt.emissive_sampler != 2u) {
         const bool bvh = ctx->opt.emissive_sampler == 1u;
@@ -240,6 +254,7 @@ plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt
         ctx->dScratch = nullptr;
         ctx->scratchCap = 0;
         PLT_CUDA(ctx, cudaMalloc(&ctx->dScratch, need));
+        PLT_CUDA(ctx, cudaMemset(ctx->dScratch, 0, need));   // the schedule's control words start at zero
         ctx->scratchCap = need;
     }
     return pltLaunchBsdfBatch(ctx, p, ctx->dScratch, (cudaStream_t)stream);
@@ -256,8 +271,7 @@ plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* 
 }  // extern "C"
 
 plt_status pltLaunchBsdfBatch(plt_context* ctx, plt::BatchParams& p, void* scratch, cudaStream_t stream) {
-    p.perm = static_cast<uint16_t*>(scratch);
-    p.unitCounter = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + (plt::bsdfScratchBytes(p.q.n) - 256));
+    plt::pltBatchScratch(p, scratch);
     const cudaError_t e = plt::launchBsdfBatch(p, (int)p.q.hwss, ctx->numSMs, stream);
     return e == cudaSuccess ? PLT_OK : cudaFail(ctx, e);
 }
@@ -294,6 +308,7 @@ plt_status plt::fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, con
     p.status = ctx->dStatus;
     for (int i = 0; i < 3; ++i) p.timing[i] = ctx->timing[i];
     p.launch = &ctx->shadeLaunch;
+    p.copyPolls = (ctx->opt.flags & PLT_OPTION_FAULT_COPY_WAIT) ? 0u : (1u << 22);
     *out = p;
     *numSMs = ctx->numSMs;
     return PLT_OK;
@@ -334,6 +349,7 @@ static plt_status traceCommon(plt_context* ctx, const plt_rays* rays, const plt_
     p.occluded = occluded;
     p.stats = reinterpret_cast<unsigned long long*>(rays->stats);
     p.status = ctx->dStatus;
+    p.stackCap = (ctx->opt.flags & PLT_OPTION_FAULT_SHORT_STACK) ? 2 : 1 << 30;
     const cudaError_t e = plt::launchTrace(p, any, ctx->numSMs, (cudaStream_t)stream);
     return e == cudaSuccess ? PLT_OK : cudaFail(ctx, e);
 }

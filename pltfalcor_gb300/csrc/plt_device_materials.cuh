@@ -176,10 +176,10 @@ PLT_DI void condEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
         float s;
         MM M;
         if (isScatter) {
-            M = muellerRConductor(LdotH, ior, rs, rp);
+            M = muellerRConductor(LdotH, ior, rs, rp, c.flags);
             s = a.om * fabsf(toLight.z) * fracPGF(p, k * h.x, k * h.y);
         } else {
-            M = muellerRConductor(toLight.z, ior, rs, rp);
+            M = muellerRConductor(toLight.z, ior, rs, rp, c.flags);
             s = a.a;
         }
         const f4 v = s * mapply(M, b.getSP(j));
@@ -328,7 +328,7 @@ PLT_DI void coatEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
             const Alpha a = fracAlpha(p, wiIn, woIn, k);
             const float coh = b.mutualCoherenceK(k, quad);
             f2 rs, rp;
-            const MM M2R = muellerRConductor(LdotH, conductorIor(m, c, b.wl[j], coatior), rs, rp);
+            const MM M2R = muellerRConductor(LdotH, conductorIor(m, c, b.wl[j], coatior), rs, rp, c.flags);
             const MM M = mmul(mmul(MiT, M2R), MoT);
             const f4 SP = b.getSP(j);
             f4 newSP = m00Of(m->m00a, b.wl[j]) * mapply(M, SP);
@@ -493,7 +493,7 @@ PLT_DI void gratEval(const DevMaterial* __restrict__ m, const Ctx& c, f3 toLight
             const float s = m00Of(m->m00a, b.wl[j]) * om[j] * coh * inten;
             if (CONDUCTOR) {
                 f2 rs, rp;
-                const MM M0 = muellerRConductor(toLight.z, conductorIor(m, c, b.wl[j], __ldg(p + PF_EXTETA)), rs, rp);
+                const MM M0 = muellerRConductor(toLight.z, conductorIor(m, c, b.wl[j], __ldg(p + PF_EXTETA)), rs, rp, c.flags);
                 b.setSP(j, s * mapply(M0, b.getSP(j)));
             } else {
                 b.setSP(j, s * b.getSP(j));

@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/plt_gb300.h"
+
 namespace pltdev {
 
 #define PLT_DI __device__ __forceinline__
@@ -185,9 +187,37 @@ PLT_DI bool invOneMinus(MM m, MM& out) {
 PLT_DI MM muellerRDielectric(float cosI, float eta) { const FresnelD f = fresnel_dielectric(cosI, eta); return muellerFresnelReal(f.rs, f.rp); }
 PLT_DI MM muellerTDielectric(float cosI, float eta) { const FresnelD f = fresnel_dielectric(cosI, eta); return muellerFresnelReal(f.ts, f.tp); }
 
-// ---- complex-IOR conductor Fresnel: (a) FP32 as the reference; (b) FP64 for grazing angles ----
-PLT_DI MM muellerRConductor(float cosI, f2 eta, f2& rs, f2& rp) {
-    fresnel_conductor(cosI, eta, rs, rp);
+// fresnel_conductor evaluated in FP64 (the same expressions in double), rounded to FP32 at the end
+PLT_NI void fresnel_conductor_f64(float cosIf, f2 etaf, f2& rs, f2& rp) {
+    if ((etaf.x == 0.f && etaf.y == 0.f) || cosIf < 0.f) {
+        rs = rp = f2{0.f, 0.f};
+        return;
+    }
+    const double cosI = cosIf, ex = etaf.x, ey = etaf.y;
+    const double den = ex * ex + ey * ey;
+    const double ix = ex / den, iy = -ey / den;                    // 1 / eta
+    const double i2x = ix * ix - iy * iy, i2y = 2.0 * ix * iy;      // (1 / eta)^2
+    const double s2 = 1.0 - cosI * cosI;
+    const double t2x = 1.0 - i2x * s2, t2y = -(i2y * s2);
+    // csqrt as MathHelpers.slang writes it: (sqrt((r + x) / 2), sign(y) sqrt((r - x) / 2))
+    const double m = sqrt(t2x * t2x + t2y * t2y);
+    const double tx = sqrt(fmax(0.0, m + t2x) / 2.0);
+    const double ty = (t2y > 0.0 ? 1.0 : (t2y < 0.0 ? -1.0 : 0.0)) * sqrt(fmax(0.0, m - t2x) / 2.0);
+    const double etx = ex * tx - ey * ty, ety = ex * ty + ey * tx;  // eta t
+    auto cdivd = [](double ax, double ay, double bx, double by, f2& out) {
+        const double d = bx * bx + by * by;
+        out = f2{(float)((ax * bx + ay * by) / d), (float)((ay * bx - ax * by) / d)};
+    };
+    cdivd(cosI - etx, -ety, cosI + etx, ety, rs);
+    cdivd(ex * cosI - tx, ey * cosI - ty, ex * cosI + tx, ey * cosI + ty, rp);
+}
+
+// ---- complex-IOR conductor Fresnel: FP32 as the reference, or with PLT_OPTION_FP64_CONDUCTOR_GRAZING
+// in FP64 below cos(theta_i) = kFp64GrazingCos (about 84.3 degrees) ----
+constexpr float kFp64GrazingCos = 0.1f;
+PLT_DI MM muellerRConductor(float cosI, f2 eta, f2& rs, f2& rp, uint32_t flags = 0u) {
+    if ((flags & PLT_OPTION_FP64_CONDUCTOR_GRAZING) && cosI < kFp64GrazingCos) fresnel_conductor_f64(cosI, eta, rs, rp);
+    else fresnel_conductor(cosI, eta, rs, rp);
     return muellerFresnel(rs, rp);
 }
 
@@ -228,15 +258,47 @@ PLT_DI uint64_t splitmix64_next(uint64_t& s) {
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
 }
+// 16 rounds of the TEA block cipher on (v0, v1) with the fixed 128-bit key of
+// Utils/Math/HashUtils.slang:59-71 (Wheeler & Needham's TEA); the first output word.
+PLT_DI uint32_t teaSeed(uint32_t v0, uint32_t v1) {
+    uint32_t sum = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        sum += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + sum) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + sum) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+
+// The render pass's two sample generators (sampleGenerator): UniformSampleGenerator (init) and,
+// with tiny set, TinyUniformSampleGenerator (initTiny: Utils/Sampling/TinyUniformSampleGenerator
+// .slang:50-70, a 32-bit LCG with the Numerical Recipes constants of Pseudorandom/LCG.slang, its
+// state in s0).
 struct SampleGen {
     uint32_t s0, s1, s2, s3;
+    bool tiny = false;
     PLT_DI void init(uint32_t px, uint32_t py, uint32_t sampleNumber) {
         uint64_t st = ((uint64_t)sampleNumber << 32) | (uint64_t)interleave_32bit(px, py);
         const uint64_t a = splitmix64_next(st);
         const uint64_t b = splitmix64_next(st);
         s0 = (uint32_t)a; s1 = (uint32_t)(a >> 32); s2 = (uint32_t)b; s3 = (uint32_t)(b >> 32);
+        tiny = false;
+    }
+    PLT_DI void initTiny(uint32_t px, uint32_t py, uint32_t sampleNumber) {
+        s0 = teaSeed(interleave_32bit(px, py), sampleNumber);
+        s1 = s2 = s3 = 0u;
+        tiny = true;
+    }
+    PLT_DI void init(uint32_t px, uint32_t py, uint32_t sampleNumber, bool tinyGen) {
+        if (tinyGen) initTiny(px, py, sampleNumber);
+        else init(px, py, sampleNumber);
     }
     PLT_DI uint32_t next() {
+        if (tiny) {
+            s0 = 1664525u * s0 + 1013904223u;
+            return s0;
+        }
         const uint32_t result = __funnelshift_l(s0 * 5u, s0 * 5u, 7) * 9u;
         const uint32_t t = s1 << 9;
         s2 ^= s0; s3 ^= s1; s1 ^= s2; s0 ^= s3;

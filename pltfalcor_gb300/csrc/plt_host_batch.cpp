@@ -116,6 +116,7 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         PLT_CUDA(ctx, cudaStreamCreateWithFlags(&hp->sComp, cudaStreamNonBlocking));
         PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evEntry, cudaEventDisableTiming));
         PLT_CUDA(ctx, cudaMalloc(&hp->scratch, plt::bsdfScratchBytes(kHostChunk)));
+        PLT_CUDA(ctx, cudaMemset(hp->scratch, 0, plt::bsdfScratchBytes(kHostChunk)));   // control words start at zero
         for (int k = 0; k < kSlots; ++k) {
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evIn[k], cudaEventDisableTiming));
             PLT_CUDA(ctx, cudaEventCreateWithFlags(&hp->evDone[k], cudaEventDisableTiming));

@@ -35,6 +35,7 @@ struct TraceParams {
     uint32_t* occluded;           // any hit: [n]
     unsigned long long* stats;    // [2] node visits, triangle tests, or null
     uint32_t* status;
+    int32_t stackCap;             // traversal stack entries (the full depth; 2 under PLT_OPTION_FAULT_SHORT_STACK)
 };
 cudaError_t launchTrace(const TraceParams& p, bool any, int numSMs, cudaStream_t stream);
 
@@ -57,8 +58,16 @@ struct BatchParams {
     uint32_t nProfiles;
     uint32_t flags;
     uint32_t* status;
-    uint16_t* perm;            // scratch: per-tile sort permutation, kBatchTile entries per tile
-    uint32_t* unitCounter;     // scratch: shade kernel work counter
+    // scratch (bsdfScratchBytes): the per-tile sort permutation (kBatchTile 16-bit local indices
+    // per tile, sorted by material type then lobe class), each tile's material-type ranges in it
+    // (kTypeSlots + 1 offsets per tile), the schedule's control words and the SM -> type table
+    uint16_t* perm;
+    uint16_t* tileTypeOff;
+    uint32_t* ctrl;            // BatchCtrl words (see plt_bsdf_kernel.cuh)
+    uint8_t* smType;           // [kMaxSmIds] material type each SM starts on
+    uint32_t unitQueries;      // target queries per work unit (a multiple of 32)
+    uint32_t copyPolls;        // poll budget of the spectral-table copy wait (0 under PLT_OPTION_FAULT_COPY_WAIT)
+    float typeCost[16];        // relative cost per query of each material type (the schedule's SM shares)
     // optional cudaEvent_t handles recorded on the launch stream before the classify kernel,
     // between the two kernels and after the shade kernel (per-kernel timing); null = not recorded
     void* timing[3];
@@ -74,7 +83,7 @@ constexpr uint32_t kPropDoubleSided = 1u << 16, kPropAlphaZero = 1u << 17;
 constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u, kPtDoNee = 0x8u, kPtDoMis = 0x10u,
                    kPtDoRR = 0x20u, kPtPerTileSg = 0x40u, kPtImportanceEmit = 0x80u, kPtDoMnee = 0x100u,
                    kPtLearned = 0x200u, kPtUseEnv = 0x400u, kPtUseAnalytic = 0x800u,
-                   kPtUniformEmissive = 0x1000u;
+                   kPtUniformEmissive = 0x1000u, kPtTinySg = 0x2000u, kPtAlphaMask = 0x4000u;
 // solve-order sort keys per path length: 16 first-hit material types x 4 second-hit material groups
 constexpr uint32_t kSolveKeysPerLength = 64;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
@@ -169,6 +178,8 @@ struct PtParams {
     float sourcingArea, maxBeamOmega;
     uint32_t mneeMaxOccluders, mneeMaxIterations;
     float mneeThreshold;
+    uint32_t debugView;           // PLT_DEBUG_VIEW_* (0: none; manifold walks then run inline in the solve kernel)
+    float debugIntensity;
     // paths: the frame's paths of all views are processed in waves of at most `npix` paths (the
     // plane stride of the path state and bounce records); this wave holds paths
     // [pidBase, pidBase + nWave) of the frame's nTotal
@@ -235,17 +246,38 @@ constexpr int kShadeThreads = 128;     // shade CTA
 #define PLT_SHADE_MIN_BLOCKS 3   // 12 warps per SM, up to 170 registers: 4.15 G queries/s vs 4.05 at 4 blocks
 #endif
 constexpr int kShadeMinBlocks = PLT_SHADE_MIN_BLOCKS;
-#ifndef PLT_SHADE_SPLIT_OPS
-#define PLT_SHADE_SPLIT_OPS 0
-#endif
 
-// scratch bytes plt_bsdf_batch needs for n queries: the permutation, then the work counter
-constexpr size_t bsdfScratchBytes(uint32_t n) {
-    return (((size_t)n + kBatchTile - 1) / kBatchTile) * kBatchTile * sizeof(uint16_t) + 256;
+// Material types of the schedule (plt_material_type ids 0..15; invalid ids land in their own slot).
+constexpr uint32_t kTypeSlots = 16;
+// Upper bound of the %smid values of the SM -> type table.
+constexpr uint32_t kMaxSmIds = 256;
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+// Scratch layout of a batch of n queries: control words | SM table | permutation | tile type offsets.
+// The control words come first so that their place does not depend on n: a scratch buffer reused
+// for batches of any size keeps them.
+constexpr size_t bsdfPermBytes(uint32_t n) { return align256(((size_t)n + kBatchTile - 1) / kBatchTile * kBatchTile * sizeof(uint16_t)); }
+constexpr size_t bsdfTileOffBytes(uint32_t n) {
+    return align256(((size_t)n + kBatchTile - 1) / kBatchTile * (kTypeSlots + 1) * sizeof(uint16_t));
+}
+constexpr size_t kBsdfCtrlBytes = 1024;
+// scratch bytes plt_bsdf_batch needs for n queries; the control words must be zero before the first
+// batch (they are left zero by every batch)
+constexpr size_t bsdfScratchBytes(uint32_t n) { return bsdfPermBytes(n) + bsdfTileOffBytes(n) + kBsdfCtrlBytes + kMaxSmIds; }
+
+// Points a batch's scratch fields into `scratch` (bsdfScratchBytes(p.q.n) bytes, 256-byte aligned).
+inline void pltBatchScratch(BatchParams& p, void* scratch) {
+    char* b = static_cast<char*>(scratch);
+    p.ctrl = reinterpret_cast<uint32_t*>(b);
+    b += kBsdfCtrlBytes;
+    p.smType = reinterpret_cast<uint8_t*>(b);
+    b += kMaxSmIds;
+    p.perm = reinterpret_cast<uint16_t*>(b);
+    b += bsdfPermBytes(p.q.n);
+    p.tileTypeOff = reinterpret_cast<uint16_t*>(b);
 }
 
 // Validates a plt_bsdf_batch call and fills every BatchParams field except the scratch pointers
-// (perm, unitCounter); also returns the SM count for the launch.  No allocation.  Returns
+// (perm, tileTypeOff, ctrl, smType); also returns the SM count for the launch.  No allocation.  Returns
 // PLT_INVALID_ARG when the calling thread's current device is not the context's device.
 plt_status fillBatchParams(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops,
                            BatchParams* out, int* numSMs);

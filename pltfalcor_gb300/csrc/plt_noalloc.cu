@@ -10,8 +10,9 @@
 // is current and caches it; that first call should happen before any stream capture begins.
 // All calls on a device share the array, so two calls whose work overlaps on the GPU race on it:
 // serialise them (one stream, or events).  Nothing in it needs clearing between calls: the
-// classify kernel rewrites the whole permutation range it uses and zeroes the work counter before
-// the shade kernel reads either.  The call runs on the context's device only (PLT_INVALID_ARG when
+// classify kernel rewrites the whole permutation and tile ranges it uses, and the schedule's
+// counters, which must be zero when a batch starts, are zero in the freshly loaded array and are
+// zeroed again by every batch once it has read them.  The call runs on the context's device only (PLT_INVALID_ARG when
 // another device is current), so the address it uses is always that device's copy of the array.
 // A cudaDeviceReset unloads the library's device code and invalidates every context of that
 // device together with the cached address: do not call this entry point after one in the same
@@ -62,8 +63,7 @@ extern "C" plt_status plt_bsdf_batch_noalloc(plt_context* ctx, const plt_bsdf_qu
     if (s != PLT_OK || q->n == 0) return s;
     void* base = nullptr;
     if (scratchAddress(&base) != cudaSuccess) return PLT_CUDA_ERROR;
-    p.perm = static_cast<uint16_t*>(base);
-    p.unitCounter = reinterpret_cast<uint32_t*>(static_cast<char*>(base) + (plt::bsdfScratchBytes(q->n) - 256));
+    plt::pltBatchScratch(p, base);
     const cudaError_t e = plt::launchBsdfBatch(p, (int)q->hwss, numSMs, (cudaStream_t)stream);
     return e == cudaSuccess ? PLT_OK : PLT_CUDA_ERROR;
 }

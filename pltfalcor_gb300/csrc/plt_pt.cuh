@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
         const uint32_t local = gp - S.pixelBase;
         const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg;
-        sg.init(px, py, *P.frameDev);
+        sg.init(px, py, *P.frameDev, (P.opt & plt::kPtTinySg) != 0);
         const float wl = 380.0f + sg.next1D() * (720.0f - 380.0f);   // SpectrumSampler.sampleOne
         const f3 d = cameraDir(S, px, py);
         const uint32_t n = P.npix;
@@ -557,6 +557,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
         if (act) {
             pid = it == 0 ? slot : qin[slot];
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
+            sg.tiny = (P.opt & plt::kPtTinySg) != 0;
             org = ldPlane3(P.org, pid, n);
             dir = ldPlane3(P.dir, pid, n);
             weight = P.weight[pid]; pdf = P.pdf[pid]; thp = P.thp[pid]; lndp = P.lndp[pid];
@@ -576,7 +577,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
                 mid = __ldg(P.triMat + h.prim);
                 props = __ldg(P.matProps + mid);
                 sd = prepareSD(v, props.x, wi);
-                if (props.x & plt::kPropAlphaZero) {   // alpha mask: continue the same ray
+                if ((props.x & plt::kPropAlphaZero) && (P.opt & plt::kPtAlphaMask)) {   // alpha mask: continue the same ray
                     org = sd.newRayOrigin(false);
                     continue;
                 }
@@ -724,6 +725,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
             pid = it == 0 ? slot : qin[slot];
             SampleGen sg;
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
+            sg.tiny = (P.opt & plt::kPtTinySg) != 0;
             f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
             float weight = P.weight[pid], pdf = P.pdf[pid], thp = P.thp[pid], lndp = P.lndp[pid];
             uint32_t flags = P.pflags[pid], len = P.plen[pid];
@@ -755,7 +757,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
                 const uint32_t mid = __ldg(P.triMat + h.prim);
                 const uint2 props = __ldg(P.matProps + mid);
                 const SD sd = prepareSD(v, props.x, wi);
-                if (props.x & plt::kPropAlphaZero) {   // alpha mask: continue the same ray
+                if ((props.x & plt::kPropAlphaZero) && (P.opt & plt::kPtAlphaMask)) {   // alpha mask: continue the same ray
                     org = sd.newRayOrigin(false);
                     continue;
                 }
@@ -1188,6 +1190,46 @@ template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p
     return b;
 }
 
+// ---- debug views (pltpt_debug.slangh, DebugViewType.slangh) ------------------------------------
+#define PLT_COLOUR_MAP_STORAGE static __constant__ const
+#include "plt_colour_maps.h"
+
+// A path's debug colour: the sum of the values written by the selected view, and their count.
+struct DebugAcc {
+    float r, g, b, n;
+};
+// writeDebugOutput: added when the view is the selected one and the value is finite
+PLT_DI void dbgWrite(DebugAcc* d, uint32_t selected, uint32_t view, f3 v) {
+    if (d && selected == view && isfinite(v.x) && isfinite(v.y) && isfinite(v.z)) {
+        d->r += v.x;
+        d->g += v.y;
+        d->b += v.z;
+        d->n += 1.f;
+    }
+}
+// ccMagma / ccInferno (RenderPasses/PLTPT/ColourCoding.slang): lerp between the bins around
+// val * 256, both clamped to [0, 255] (a non-finite val gives a non-finite colour, never written)
+PLT_DI f3 colourCode(const float (*t)[3], float val) {
+    val *= 256.f;
+    if (!isfinite(val)) return mk3(val - val, 0.f, 0.f);
+    const int l = (int)fminf(fmaxf(val, 0.f), 255.f), h = (int)fminf(fmaxf(val + 1.f, 0.f), 255.f);
+    const float fr = val - floorf(val);
+    const f3 a = mk3(t[l][0], t[l][1], t[l][2]), b = mk3(t[h][0], t[h][1], t[h][2]);
+    return a + (b - a) * fr;
+}
+// PLTBeam.coherenceArea(k) = pi sqrt(1 / det(invTheta(k))) and coherenceAnisotropy(k) =
+// 1 - S00 / S11 of svd_symmetric(invTheta(k)) (PLT.slang:57-64,186-197; MathHelpers.slang:583-605)
+template <int H> PLT_DI void coherenceDebug(const DBeam<H>& b, float k, float& area, float& aniso) {
+    const float rmm = b.r_m * 1e+3f;
+    const float s = (k / k2Pi / rmm) * (k / k2Pi / rmm);
+    const float a = s * b.D0, c = s * b.D1, d = s * b.D2;
+    area = kPi * sqrtf(1.f / (a * d - c * c));
+    const float a2 = a * a, b2 = c * c, c2 = c * c, d2 = d * d;
+    const float y = 2.f * a * c + 2.f * c * d, x = a2 + b2 - c2 - d2;
+    const float s1 = a2 + b2 + c2 + d2, s2 = sqrtf(x * x + y * y);
+    aniso = 1.f - sqrtf((s1 + s2) / 2.f) / sqrtf((s1 - s2) / 2.f);
+}
+
 // Forward replay of one beam source of vertex p and its measurement (pltpt_solve.rt.slang:48-147):
 // the manifold vertices (last to first, manifoldForwardUnwind :80-93), the current vertex (NEE,
 // non-delta lobes), then vertices p-1 .. 0, the camera polariser and spectrumToRgb.  Adds the
@@ -1195,7 +1237,7 @@ template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p
 template <int H>
 PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int p, const Bnc<H>& bounce, PBeam<H>& pb, const MSData& ms,
                           int nMs, f3 msOrigin, bool evalCurrent, const Ctx& c, bool hwssMis, float& Lr, float& Lg, float& Lb,
-                          uint32_t& evals) {
+                          uint32_t& evals, DebugAcc* dbg = nullptr) {
     // forward replay: the manifold vertices (last to first, manifoldForwardUnwind,
     // pltpt_solve.rt.slang:80-93), the current vertex (NEE, non-delta lobes), then p-1 .. 0
     const int total = nMs + (evalCurrent ? 1 : 0) + p;
@@ -1238,6 +1280,13 @@ PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int
     }
     // measure (no camera polarizer unless set)
     if (!(P.opt & plt::kPtUseDirect) && p <= 1) return;
+    if (dbg) {
+        // coherence views, before the propagation to the camera (pltpt_solve.rt.slang:102-106)
+        float area, aniso;
+        coherenceDebug<H>(pb.b, k2Pi / (1e-3f * pb.b.wl[0]), area, aniso);
+        dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_COHERENCE_AREA, colourCode(kMagma, sqrtf(area) / 150.f));
+        dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_COHERENCE_ANISOTROPY, colourCode(kInferno, aniso));
+    }
     propagate(pb, camPos(S));
     if (S.cam.polarizer > 0.f) {
         const f3 Wc = rnormalize(mk3(S.cam.w[0], S.cam.w[1], S.cam.w[2]));
@@ -1275,6 +1324,19 @@ PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int
     const f3 rgb = spectrumToRgb<H>(Li, pb.b.wl, pb.comps);
     const float r = fmaxf(0.f, rgb.x * contrib), g = fmaxf(0.f, rgb.y * contrib), bb = fmaxf(0.f, rgb.z * contrib);
     if (isfinite(r) && isfinite(g) && isfinite(bb)) { Lr += r; Lg += g; Lb += bb; }
+    if (dbg) {
+        // markDebug (pltpt_debug.slangh:31-50): NaNs and infinities of the path's sum, path length,
+        // spectral samples carried, and the polarisation of the hero wavelength at the sensor
+        if (isnan(Lr) || isnan(Lg) || isnan(Lb)) dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_NANS, mk3(5.f, 0.f, 3.f));
+        if (isinf(Lr) || isinf(Lg) || isinf(Lb)) dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_INFS, mk3(2.f, 0.f, 5.f));
+        dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_PATH_LENGTH, colourCode(kMagma, (float)p / (float)(P.maxBounces - 1)));
+        dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_HWSS_COMPS, colourCode(kMagma, (float)pb.comps / (float)H));
+        const float S0 = pb.b.L[0][0], S1 = pb.b.L[1][0], S2 = pb.b.L[2][0], S3 = pb.b.L[3][0];
+        const float cp = sqrtf(S3 * S3) / S0, lp = sqrtf(S1 * S1 + S2 * S2) / S0;
+        const float lpd = .5f * atan2f(S2, S1);
+        const float cl = cosf(lpd), sl = sinf(lpd);
+        dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_POLARIZATION, mk3(lp * (cl * cl), cp, lp * (sl * sl)));
+    }
 }
 
 // sampleLight for analytic lights (Rendering/Lights/LightHelpers.slang:71-289): the direction and
@@ -1411,8 +1473,9 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         const uint32_t px = local % S.width, py = local / S.width;
         SampleGen sg, tilesg;
         const uint32_t frame = *P.frameDev;
-        sg.init(px, py, frame);
-        tilesg.init(px / P.tileSize, py / P.tileSize, frame << 2);
+        const bool tinySg = (P.opt & plt::kPtTinySg) != 0;
+        sg.init(px, py, frame, tinySg);
+        tilesg.init(px / P.tileSize, py / P.tileSize, frame << 2, tinySg);
         const float wavelength = 380.0f + sg.next1D() * (720.0f - 380.0f);
         f3 pathOrigin = camPos(S);
         // light-type selection probabilities (getLightTypeSelectionProbabilities,
@@ -1423,6 +1486,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
         const float invPSum = pSum > 0.f ? 1.f / pSum : 0.f;
         const float pEnv = useEnv ? invPSum : 0.f, pEm = hasEm ? invPSum : 0.f, pAn = useAnalytic ? invPSum : 0.f;
         float Lr = 0.f, Lg = 0.f, Lb = 0.f;
+        DebugAcc dacc{0.f, 0.f, 0.f, 0.f};
+        DebugAcc* dbg = P.debugView ? &dacc : nullptr;
         for (int p = 0; p <= (int)P.maxBounces; ++p) {
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
             // wasNEEAvailable, pltpt_solve.rt.slang:204-210
@@ -1444,7 +1509,7 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     PBeam<H> pb;
                     sourceBeamDistant<H>(pb, wo, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
-                    replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, pathOrigin, false, c, hwssMis, Lr, Lg, Lb, evals);
+                    replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, pathOrigin, false, c, hwssMis, Lr, Lg, Lb, evals, dbg);
                 }
                 break;
             }
@@ -1456,6 +1521,12 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
             const DevMaterial* __restrict__ m = P.mats + mid;
             const uint32_t type = __ldg(&m->type);
             const uint32_t lobes = (props.x >> 8) & 0xFFu;
+            if (dbg && p == 0) {
+                // geometry views at the primary hit (pltpt_solve.rt.slang:449-456); the scene has no
+                // texture coordinates, so sd.uv = 0
+                dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_NORMALS, sd.N);
+                dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_UVS, mk3(0.f, 0.f, 0.f));
+            }
             // two beam sources per vertex: NEE (pltpt_solve.rt.slang:245-366) and emission
             // (evalEmissive, :152-200); each is replayed through vertices p (NEE: non-delta lobes)
             // and p-1 .. 0 (forwardUnwind, :48-79), then measured (:96-147).
@@ -1623,7 +1694,9 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                         }
                         msOrigin = !curMS ? V.posW : pathOrigin;
                         const int occ = manifoldOccluders(P, root, lorg, ldir, ldist, maxMS, sg, ms, tc);
-                        if (occ == kMsFail || ms.pdf < 1e-6f) continue;
+                        bool mneeOk = occ != kMsFail;
+                        // without a debug view a sample with a negligible pdf is dropped before its walk
+                        if (mneeOk && ms.pdf < 1e-6f && !dbg) continue;
                         if (occ == kMsWalk) {
                             // the walk and the rest of this sample draw no random numbers: hand them
                             // to the walk wavefront (inline when its queue is full)
@@ -1644,8 +1717,17 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                                 t->curMS = (curMS ? 1u : 0u) | (distant ? 2u : 0u) | (misHere ? 0u : 4u);
                                 continue;
                             }
-                            if (!manifoldWalk(P, root, msOrigin, tposW, ldir, distant, ms, tc)) continue;
+                            mneeOk = manifoldWalk(P, root, msOrigin, tposW, ldir, distant, ms, tc);
                         }
+                        if (dbg) {
+                            // MNEE views (pltpt_solve.rt.slang:319-325)
+                            dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_MNEE_ITERATIONS,
+                                     colourCode(kInferno, (float)ms.iterations / (float)P.mneeMaxIterations));
+                            if (ms.hitCount > 0 && mneeOk)
+                                dbgWrite(dbg, P.debugView, PLT_DEBUG_VIEW_MNEE_BOUNCES,
+                                         ms.hitCount == 1 ? mk3(0.f, .3f, 1.f) : mk3(1.f, 0.f, 0.f));
+                        }
+                        if (!mneeOk || ms.pdf < 1e-6f) continue;
                         float misBsdfPdf = 0.f;
                         f3 lsDir = ldir;
                         if (ms.hitCount > 0) {
@@ -1686,10 +1768,19 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
                 }
-                replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals);
+                replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals, dbg);
             }
             if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
             pathOrigin = V.posW;
+        }
+        if (dbg) {
+            // the output colour moves towards the mean debug colour by the view intensity
+            // (pltpt_solve.rt.slang:470-475)
+            const float t = P.debugIntensity;
+            const f3 dm = dacc.n > 0.f ? mk3(dacc.r, dacc.g, dacc.b) / dacc.n : mk3(0.f, 0.f, 0.f);
+            Lr = Lr + t * (dm.x - Lr);
+            Lg = Lg + t * (dm.y - Lg);
+            Lb = Lb + t * (dm.z - Lb);
         }
         P.accum[3 * (size_t)gp] += (double)Lr;
         P.accum[3 * (size_t)gp + 1] += (double)Lg;

@@ -159,6 +159,9 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     if (o.hwss < 1 || (o.hwss > 4 && o.hwss != 8)) return PLT_NOT_SUPPORTED;   // 8: beyond the reference's 1-4
     if (o.mnee_max_occluders > 4) return PLT_NOT_SUPPORTED;
     if (o.max_bounces > 64) return PLT_NOT_SUPPORTED;
+    if (o.debug_view > PLT_DEBUG_VIEW_MNEE_BOUNCES) return PLT_INVALID_ARG;
+    if (o.debug_view == PLT_DEBUG_VIEW_ALBEDO || o.debug_view == PLT_DEBUG_VIEW_ROUGHNESS) return PLT_NOT_SUPPORTED;
+    if (o.sample_generator > PLT_SAMPLE_GENERATOR_UNIFORM) return PLT_INVALID_ARG;
     const bool learned = o.learned_proposal != 0;
     if (learned && (!ctx->propReady || !ctx->dMatFeat || !(o.learned_proposal_prob > 0.f && o.learned_proposal_prob < 1.f)))
         return PLT_INVALID_ARG;
@@ -259,7 +262,9 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
             (nee && o.do_mnee ? plt::kPtDoMnee : 0u) | (learned ? plt::kPtLearned : 0u) |
             (o.use_env_light && ctx->hasEnv ? plt::kPtUseEnv : 0u) |
             (o.use_analytic_lights && ctx->nALights ? plt::kPtUseAnalytic : 0u) |
-            (o.emissive_sampler == 0u ? plt::kPtUniformEmissive : 0u);
+            (o.emissive_sampler == 0u ? plt::kPtUniformEmissive : 0u) |
+            (o.sample_generator == PLT_SAMPLE_GENERATOR_TINY_UNIFORM ? plt::kPtTinySg : 0u) |
+            (o.alpha_masking ? plt::kPtAlphaMask : 0u);
     P.env = ctx->env;
     P.alights = ctx->dALights;
     P.nALights = ctx->nALights;
@@ -267,8 +272,9 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.matFeat = ctx->dMatFeat;
     P.propProb = o.learned_proposal_prob;
     P.wpss = learned ? static_cast<float*>(ctx->dPtMix) : nullptr;
-    // deferred manifold walks: one task slot per path and frame (a fuller queue walks inline)
-    if (nee && o.do_mnee) {
+    // deferred manifold walks: one task slot per path and frame (a fuller queue walks inline); a
+    // debug view keeps them inline, where the path's debug colour is accumulated
+    if (nee && o.do_mnee && o.debug_view == PLT_DEBUG_VIEW_NONE) {
         const size_t taskBytes = (size_t)npix * plt::kMneeTaskBytes;
         if (ctx->mneeBytes < taskBytes) {
             cudaFree(ctx->dMneeTasks);
@@ -286,6 +292,8 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     P.mneeMaxOccluders = o.mnee_max_occluders;
     P.mneeMaxIterations = o.mnee_max_iterations;
     P.mneeThreshold = o.mnee_solver_threshold;
+    P.debugView = o.debug_view;
+    P.debugIntensity = o.debug_view_intensity;
     P.sourcingArea = o.sourcing_area_from_emissive_geometry;
     P.maxBeamOmega = o.sourcing_max_beam_omega;
     P.npix = npix;

@@ -21,7 +21,7 @@ __device__ __forceinline__ void traceOne(const TraceParams& P, uint32_t i, uint3
     const float tmax = P.tmax ? __ldg(P.tmax + i) : 3.402823466e+38f;
     uint32_t overflow = 0;
     const TraceResult h = traverse<ANY>(reinterpret_cast<const float4*>(P.nodes), P.tris, ox, oy, oz, dx, dy, dz, tmin, tmax,
-                                        nodeVisits, triTests, overflow);
+                                        nodeVisits, triTests, overflow, 0, P.stackCap);
     if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     if (ANY) {
         P.occluded[i] = h.prim != 0xFFFFFFFFu ? 1u : 0u;

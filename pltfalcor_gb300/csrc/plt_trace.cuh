@@ -98,11 +98,13 @@ struct TraceResult {
 // Stack traversal of the two-wide BVH for one ray: closest hit with tmin <= t <= tmax (ties to
 // the lowest triangle id), or, with ANY, the first hit found (TraceRay with
 // ACCEPT_FIRST_HIT_AND_END_SEARCH).  Counts node visits and triangle tests; sets `overflow` when
-// the fixed-depth stack overflowed (the result is then possibly not the closest).
+// the fixed-depth stack (or the caller's smaller cap, stackCap) overflowed: the result is then
+// possibly not the closest.
 template <bool ANY>
 __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, float ox, float oy,
                                                 float oz, float dx, float dy, float dz, float tmin, float tmax,
-                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow, int32_t root = 0) {
+                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow, int32_t root = 0,
+                                                int stackCap = kStackDepth) {
     TraceResult res;
     res.prim = 0xFFFFFFFFu;
     res.t = tmax;
@@ -157,7 +159,7 @@ __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes
         if (hr && r.y < 0) { leaf(r.y); hr = false; if (ANY && done) break; }
         if (hl && hr) {
             const bool leftNear = tl <= tr;
-            if (sp < kStackDepth) stack[sp++] = make_int2(leftNear ? r.y : r.x, __float_as_int(leftNear ? tr : tl));
+            if (sp < stackCap && sp < kStackDepth) stack[sp++] = make_int2(leftNear ? r.y : r.x, __float_as_int(leftNear ? tr : tl));
             else overflow = 1;
             node = leftNear ? r.x : r.y;
             continue;

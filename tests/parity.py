@@ -104,8 +104,8 @@ def summarize(errs, tol=TOL, sel=None):
         else:
             b = bad_mask(errs, k, tol)
             b = b if sel is None else b[sel]
-            s[k] = {"max": float(vv.max()), "p99": float(np.quantile(vv, 0.99)), "frac_above_tol": float((vv > tol).mean()),
-                    "frac_bad": float(b.mean())}
+            s[k] = {"max": float(vv.max()), "p99": float(np.quantile(vv, 0.99)), "p50": float(np.quantile(vv, 0.5)),
+                    "frac_above_tol": float((vv > tol).mean()), "frac_bad": float(b.mean())}
     return s
 
 

@@ -112,28 +112,95 @@ def test_golden_fixtures(ctx, profiles):
         assert not fails, (name, fails)
 
 
+def grazing_conductor_batch(profiles, n=3 * 8192, seed=7):
+    """Conductor, coated-conductor and grated-conductor queries of the mixed-material batch with
+    both directions at grazing incidence (cos theta uniform in [0.001, 0.1], random azimuths)."""
+    wl = W.mixed_material_batch(n=8 * n, profiles=profiles)
+    types = np.asarray(wl.records["type"])[wl.material]
+    idx = np.nonzero(np.isin(types, [M.CONDUCTOR, M.COATED_CONDUCTOR, M.GRATED_CONDUCTOR]))[0][:n]
+    g = wl.subset(idx)
+    rng = np.random.default_rng(seed)
+    for key, sgn in (("v", 1.0), ("w", 1.0)):
+        c = rng.uniform(0.001, 0.1, g.n)
+        phi = rng.uniform(0.0, 2 * np.pi, g.n)
+        s = np.sqrt(1 - c * c)
+        setattr(g, key, np.ascontiguousarray(np.stack([s * np.cos(phi), s * np.sin(phi), sgn * c]).astype(np.float32).reshape(-1)))
+    return g
+
+
 def test_fp64_error_report(ctx, profiles, tmp_path):
-    """Error of the GPU (FP32) and of the FP32 oracle against the FP64 oracle, per material."""
+    """Error of the GPU (FP32) and of the FP32 oracle against the FP64 oracle, per material, and the
+    share of queries whose GPU result differs from the FP32 oracle's by more than a raw 1e-4;
+    then, at grazing incidence on the conductor materials, the same errors with and without
+    PLT_OPTION_FP64_CONDUCTOR_GRAZING.  PLT_FP64_REPORT=path writes the report as JSON."""
+    from pltfalcor_gb300.bsdf import PLTContext
     wl = W.mixed_material_batch(n=8 * 8192, profiles=profiles[0])
     g = run_gpu(ctx, wl, ops=0xF)
     o32 = oracle.run(wl, ops=0xF, precision=32)
     o64 = oracle.run(wl, ops=0xF, precision=64)
     types = np.asarray(wl.records["type"])[wl.material]
-    report = {}
+    report = {"workload": "mixed_material_batch 65536 queries (seed 1), eval + pdf + sample + lambdaPdf, HWSS 1",
+              "tolerance": "raw relative error 1e-4 (errors as tests/parity.py defines them)", "materials": {}}
     eg = parity.errors(g, o64, wl.n, 1, 0xF)
     eo = parity.errors(o32, o64, wl.n, 1, 0xF)
+    e32 = parity.errors(g, o32, wl.n, 1, 0xF)
     for t in np.unique(types):
         sel = types == t
-        report[M.TYPE_NAMES[int(t)]] = {"gpu_fp32_vs_fp64": parity.summarize(eg, sel=sel),
-                                        "oracle_fp32_vs_fp64": parity.summarize(eo, sel=sel)}
+        name = M.TYPE_NAMES[int(t)]
+        gs, os_ = parity.summarize(eg, sel=sel), parity.summarize(eo, sel=sel)
+        raw = {k: float((v[sel] > parity.TOL).mean()) for k, v in e32.items() if v.dtype != bool}
+        report["materials"][name] = {
+            "queries": int(sel.sum()),
+            "gpu_fp32_vs_fp64": {k: {q: v[q] for q in ("p50", "p99", "max")} for k, v in gs.items() if "p99" in v},
+            "oracle_fp32_vs_fp64": {k: {q: v[q] for q in ("p50", "p99", "max")} for k, v in os_.items() if "p99" in v},
+            "gpu_vs_oracle_fp32_frac_above_1e-4": raw}
         for k in ("stokes", "pdf"):
             # the GPU is no further from FP64 than the FP32 reference arithmetic, within 10x at p99
-            gp, op = report[M.TYPE_NAMES[int(t)]]["gpu_fp32_vs_fp64"][k]["p99"], report[M.TYPE_NAMES[int(t)]]["oracle_fp32_vs_fp64"][k]["p99"]
-            assert gp <= max(10 * op, 1e-5), (M.TYPE_NAMES[int(t)], k, gp, op)
+            gp, op = gs[k]["p99"], os_[k]["p99"]
+            assert gp <= max(10 * op, 1e-5), (name, k, gp, op)
+    # grazing incidence on conductors: the FP64 Fresnel option against the FP32 default
+    gw = grazing_conductor_batch(profiles[0])
+    gtypes = np.asarray(gw.records["type"])[gw.material]
+    g64 = oracle.run(gw, ops=1, precision=64)
+    plain = run_gpu(ctx, gw, ops=1)
+    c2 = PLTContext({"flags": capi.OPTION_FP64_CONDUCTOR_GRAZING})
+    c2.set_spectral_profiles(profiles[0])
+    opt = run_gpu(c2, gw, ops=1)
+    c2.close()
+    ep, eopt = parity.errors(plain, g64, gw.n, 1, 1), parity.errors(opt, g64, gw.n, 1, 1)
+    graz = {}
+    for t in np.unique(gtypes):
+        sel = gtypes == t
+        graz[M.TYPE_NAMES[int(t)]] = {
+            "queries": int(sel.sum()),
+            "gpu_fp32_vs_fp64_stokes": {q: float(np.quantile(ep["stokes"][sel], x)) for q, x in (("p50", .5), ("p99", .99))} |
+                                       {"max": float(ep["stokes"][sel].max())},
+            "gpu_fp64_grazing_option_vs_fp64_stokes": {q: float(np.quantile(eopt["stokes"][sel], x)) for q, x in (("p50", .5), ("p99", .99))} |
+                                                      {"max": float(eopt["stokes"][sel].max())}}
+    report["grazing_conductors"] = {"workload": "conductor, coated conductor and grated conductor queries, both directions with "
+                                                "cos theta in [0.001, 0.1], eval, HWSS 1; option PLT_OPTION_FP64_CONDUCTOR_GRAZING "
+                                                "(FP64 complex Fresnel below cos theta 0.1)", "materials": graz}
     out = os.environ.get("PLT_FP64_REPORT")
     if out:
         with open(out, "w") as f:
             json.dump(report, f, indent=1)
+
+
+def test_fp64_conductor_grazing_option(torch_cuda, product_lib, profiles):
+    """PLT_OPTION_FP64_CONDUCTOR_GRAZING against the FP32 oracle with the same option, at grazing
+    incidence on every conductor material and on the whole mixed batch (where it is inactive for
+    most queries)."""
+    from pltfalcor_gb300.bsdf import PLTContext
+    c = PLTContext({"flags": capi.OPTION_FP64_CONDUCTOR_GRAZING})
+    c.set_spectral_profiles(profiles[0])
+    for wl in (grazing_conductor_batch(profiles[0], n=3 * 2048), W.mixed_material_batch(n=8 * 2048, profiles=profiles[0])):
+        g = run_gpu(c, wl, ops=0xF)
+        o = oracle.run(wl, ops=0xF, precision=32, fp64_conductor_grazing=True)
+        o64 = oracle.run(wl, ops=0xF, precision=64)
+        orr = [oracle.run(wl, ops=0xF, precision=16, sr_seed=s, fp64_conductor_grazing=True) for s in (1, 2)]
+        errs = parity.compare(g, o, wl.n, 1, 0xF, o64, orr)
+        assert not parity.check(errs), parity.summarize(errs)
+    c.close()
 
 
 def test_fp64_multilayer_option(torch_cuda, product_lib, profiles):

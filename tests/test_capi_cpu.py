@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(product_lib):
 
 
 def test_abi_version_and_status_strings(product_lib):
-    assert product_lib.plt_abi_version() == 3
+    assert product_lib.plt_abi_version() == 4
     assert product_lib.plt_status_string(0) == b"ok"
     assert product_lib.plt_status_string(7) == b"bad material"
 
@@ -37,6 +37,21 @@ def test_options_default_matches_pltpt(product_lib):
     assert (o.max_bounces, o.tile_size, o.hwss, o.mnee_max_occluders, o.mnee_max_iterations) == (32, 512, 4, 2, 60)
     assert o.emissive_sampler == 2   # EmissiveLightSamplerType::Power (PLTPT.h:99)
     assert abs(o.mnee_solver_threshold - 5e-5) < 1e-9 and abs(o.sourcing_max_beam_omega - 0.025) < 1e-9
+    # every key of PLTPT::parseDictionary (PLTPT.cpp:147-175) has a field with the PLTPT.h default
+    keys = {"maxBounces": o.max_bounces, "tileSize": o.tile_size, "debugView": o.debug_view,
+            "debugViewIntensity": o.debug_view_intensity, "sourcingAreaFromEmissiveGeometry": o.sourcing_area_from_emissive_geometry,
+            "sourcingMaxBeamOmega": o.sourcing_max_beam_omega, "sampleGenerator": o.sample_generator, "HWSS": o.hwss,
+            "HWSSDoMIS": o.hwss_do_mis, "useDirectLights": o.use_direct_light, "useEnvLights": o.use_env_light,
+            "useEmissiveLights": o.use_emissive_lights, "useAnalyticLights": o.use_analytic_lights, "alphaMasking": o.alpha_masking,
+            "doNEE": o.do_nee, "NEEUsePerTileSG": o.nee_use_per_tile_sg, "doMIS": o.do_mis, "emissiveSampler": o.emissive_sampler,
+            "doRussianRoulette": o.do_russian_roulette, "doImportanceSampleEmitters": o.do_importance_sample_emitters,
+            "doMNEE": o.do_mnee, "MNEEMaxOccluders": o.mnee_max_occluders, "MNEEMaxIterations": o.mnee_max_iterations}
+    assert keys["debugView"] == capi.DEBUG_VIEW_NONE and keys["debugViewIntensity"] == 1.0
+    assert keys["sampleGenerator"] == capi.SAMPLE_GENERATOR_UNIFORM   # SAMPLE_GENERATOR_DEFAULT
+    assert keys["alphaMasking"] == 1 and keys["sourcingAreaFromEmissiveGeometry"] == 1.0
+    assert all(keys[k] == 1 for k in ("HWSSDoMIS", "useDirectLights", "useEnvLights", "useEmissiveLights", "useAnalyticLights",
+                                      "doNEE", "doMIS", "doRussianRoulette", "doImportanceSampleEmitters", "doMNEE"))
+    assert keys["NEEUsePerTileSG"] == 0
 
 
 def test_spectral_profile_builder_matches_oracle(product_lib, oracle_lib):

@@ -124,6 +124,46 @@ def test_rng_streams_match(oracle_lib, px, py, frame):
     assert [int(r.next_u32()[0]) for _ in range(16)] == ref
 
 
+def _tea_py(v0, v1, key, rounds):
+    """Independent restatement of the published TEA encryption (Wheeler & Needham 1994)."""
+    M = 0xFFFFFFFF
+    s = 0
+    for _ in range(rounds):
+        s = (s + 0x9E3779B9) & M
+        v0 = (v0 + ((((v1 << 4) & M) + key[0]) ^ (v1 + s) ^ ((v1 >> 5) + key[1]))) & M
+        v1 = (v1 + ((((v0 << 4) & M) + key[2]) ^ (v0 + s) ^ ((v0 >> 5) + key[3]))) & M
+    return v0, v1
+
+
+def test_tea_published_vector():
+    # the standard TEA test vector: key 0, plaintext 0, 32 cycles
+    assert _tea_py(0, 0, [0, 0, 0, 0], 32) == (0x41EA3A0A, 0x94BAA940)
+
+
+def test_lcg_published_sequence():
+    # Numerical Recipes "quick and dirty" generator (a = 1664525, c = 1013904223) from state 0
+    s, out = 0, []
+    for _ in range(6):
+        s = (1664525 * s + 1013904223) & 0xFFFFFFFF
+        out.append(s)
+    assert out == [0x3C6EF35F, 0x47502932, 0xD1CCF6E9, 0xAAF95334, 0x6252E503, 0x9F2EC686]
+
+
+@pytest.mark.parametrize("px,py,frame", [(0, 0, 0), (3, 5, 9), (65535, 1, 7), (1000, 64, 123456)])
+def test_tiny_rng_stream_matches(oracle_lib, px, py, frame):
+    """TinyUniformSampleGenerator: LCG seeded with blockCipherTEA(interleave(pixel), frame).x, 16
+    rounds with the key of Utils/Math/HashUtils.slang:59-71."""
+    def il(v):
+        v &= 0xFFFF
+        return sum(((v >> b) & 1) << (2 * b) for b in range(16))
+    seed, _ = _tea_py(il(px) | (il(py) << 1), frame, [0xA341316C, 0xC8013EA4, 0xAD90777D, 0x7E95761E], 16)
+    ref, s = [], seed
+    for _ in range(16):
+        s = (1664525 * s + 1013904223) & 0xFFFFFFFF
+        ref.append(s)
+    assert list(oracle.rng_stream(px, py, frame, 16, tiny=True)) == ref
+
+
 def test_half_decode(oracle_lib):
     vals = {0x3C00: 1.0, 0x3E00: 1.5, 0x0001: 2.0 ** -24, 0x7BFF: 65504.0, 0xC000: -2.0, 0x0000: 0.0}
     for h, f in vals.items():
