@@ -260,6 +260,9 @@ typedef struct plt_options {
  * plt_trace_* traverse with a 2-entry stack, so deep rays overflow it. */
 #define PLT_OPTION_FAULT_COPY_WAIT 0x4u
 #define PLT_OPTION_FAULT_SHORT_STACK 0x8u
+/* plt_render*: replay every beam through its path inside the solve kernel instead of deferring the
+ * replays to the material-sorted replay wavefront (same results up to float summation order) */
+#define PLT_OPTION_INLINE_REPLAY 0x20u
 
 typedef struct plt_context plt_context;
 

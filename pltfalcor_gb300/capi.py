@@ -21,6 +21,7 @@ OPTION_FP64_MULTILAYER = 0x1
 OPTION_FP64_CONDUCTOR_GRAZING = 0x10
 OPTION_FAULT_COPY_WAIT = 0x4
 OPTION_FAULT_SHORT_STACK = 0x8
+OPTION_INLINE_REPLAY = 0x20
 
 
 class SpectralProfile(C.Structure):

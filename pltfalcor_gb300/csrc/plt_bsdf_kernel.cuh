@@ -111,6 +111,9 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     const uint32_t tid = threadIdx.x;
     const uint32_t n = P.q.n;
     const uint32_t base = blockIdx.x * kBatchTile;
+    // the shade kernel may be scheduled once every classify CTA has started: it stages its tables
+    // and then waits for this grid to complete (programmatic dependent launch)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     for (uint32_t b = tid; b < kBuckets; b += kBatchThreads) counts[b] = 0;
     __syncthreads();
     uint16_t key[kBatchItems], rank[kBatchItems];
@@ -209,34 +212,6 @@ PLT_DI uint32_t busiestQueue(const BatchParams& P, uint32_t nTiles, uint32_t lan
     return work > 0.f ? best : kTypeSlots;
 }
 
-// The queue that is furthest behind in tiles (its next unit's tile), and its distance behind queue t.
-// Queues without units (empty types) and finished queues do not count.  Whole warp.
-PLT_DI uint32_t laggingQueue(const BatchParams& P, uint32_t nTiles, uint32_t t, uint32_t lane, uint32_t& lead) {
-    constexpr uint32_t kMaxUnits = plt::kBatchTile / 32;
-    uint32_t tile = 0xFFFFFFFFu;   // this lane's queue position in tiles
-    if (lane < kTypeSlots) {
-        const uint32_t units = min(ldVolatile(P.ctrl + C_UNITS + lane), kMaxUnits);
-        const uint32_t next = ldVolatile(P.ctrl + C_NEXT + lane);
-        if (units && next < units * nTiles) tile = next / units;
-    }
-    const uint32_t own = __shfl_sync(0xFFFFFFFFu, tile, t);
-    uint32_t lo = tile, who = lane;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-        const uint32_t l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, d), w2 = __shfl_xor_sync(0xFFFFFFFFu, who, d);
-        if (l2 < lo || (l2 == lo && w2 < who)) {
-            lo = l2;
-            who = w2;
-        }
-    }
-    lead = (own != 0xFFFFFFFFu && lo != 0xFFFFFFFFu) ? own - lo : 0u;
-    return who;
-}
-
-// Largest lead in tiles a queue may have over the slowest queue before its warps help the slowest:
-// about 64 x 270 KB of a tile's inputs and outputs stay in L2 beside the ~100 tiles in flight.
-constexpr uint32_t kMaxQueueLead = 64;
-
 template <int H>
 __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdfShadeKernel(const BatchParams P) {
     using namespace plt;
@@ -268,6 +243,9 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
         }
     }
     const Ctx c{sprof, P.nProfiles, P.flags};
+    // the classify grid's permutation and schedule are complete and visible past this point
+    // (a no-op when the kernel was not launched as a programmatic dependent)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     const uint32_t nTiles = (P.q.n + kBatchTile - 1) / kBatchTile;
     // the schedule never has more than kBatchTile / 32 units of at least 32 queries per tile; the
@@ -276,14 +254,6 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     uint32_t t = P.smType[smId() % kMaxSmIds] % kTypeSlots;
     uint32_t units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
     for (;;) {
-        // keep every queue within kMaxQueueLead tiles of the slowest one, so that each tile is shaded
-        // by all its material types while its inputs and outputs are in L2
-        uint32_t lead;
-        const uint32_t slow = laggingQueue(P, nTiles, t, lane, lead);
-        if (lead > kMaxQueueLead && slow < kTypeSlots) {
-            t = slow;
-            units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
-        }
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
         u = __shfl_sync(0xFFFFFFFFu, u, 0);
@@ -366,16 +336,40 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     const uint32_t gridCap = (warpsNeeded + (kShadeThreads / 32) - 1) / (kShadeThreads / 32);
     if (grid > gridCap) grid = gridCap;
     BatchParams p = p0;
-    // units of up to 256 queries, smaller when the batch gives fewer than ~4 units per warp
-    const uint32_t warps = grid * (kShadeThreads / 32);
-    uint32_t uq = (p.q.n / (4u * warps) + 31u) & ~31u;
-    p.unitQueries = uq < 32u ? 32u : (uq > 256u ? 256u : uq);
+    // units of one warp iteration (32 queries): a unit stays in flight for one iteration only, so the
+    // tiles the GPU works on at a time stay few (L2 locality of the scattered loads and stores).
+    // Measured on the 2^22 mixed batch: 32-query units 0.79 ms, 256-query units 0.86 ms per launch;
+    // bounding each queue's lead over the slowest one (16 or 32 tiles) made it slower (1.2-2.0 ms),
+    // since every unit then re-reads the contended queue counters and SMs leave their type
+#ifndef PLT_UNIT_QUERIES
+#define PLT_UNIT_QUERIES 32
+#endif
+    p.unitQueries = PLT_UNIT_QUERIES;
     for (uint32_t t = 0; t < kTypeSlots; ++t)
         if (!(p.typeCost[t] > 0.f)) p.typeCost[t] = defaultTypeCost(t);
     if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
     pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p);
-    if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
-    pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
+    cudaError_t e = cudaSuccess;
+    if (p.timing[1]) {
+        // per-kernel timing: an event between the kernels, so an ordinary launch
+        cudaEventRecord((cudaEvent_t)p.timing[1], stream);
+        pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
+    } else {
+        // programmatic dependent launch: the shade CTAs are scheduled while classify finishes and
+        // stage their spectral tables before waiting on it (hides the launch gap of small batches)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(kShadeThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, pltdev::bsdfShadeKernel<H>, p);
+    }
+    if (e != cudaSuccess) return e;
     if (p.timing[2]) cudaEventRecord((cudaEvent_t)p.timing[2], stream);
     return cudaGetLastError();
 }

@@ -91,6 +91,8 @@ struct plt_context {
     size_t ptMixBytes = 0;
     void* dMneeTasks = nullptr;   // deferred manifold walks of the solve pass
     size_t mneeBytes = 0;
+    void* dReplayTasks = nullptr; // deferred forward replays of the solve pass, then their order
+    size_t replayBytes = 0;
     uint32_t ptNpix = 0, ptMaxB = 0;
     uint64_t lastPaths = 0;       // paths of all views in the last render
     double* dAccum = nullptr;     // [paths of all views][3] frame accumulation

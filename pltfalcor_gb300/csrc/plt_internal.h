@@ -88,6 +88,10 @@ constexpr uint32_t kPtHwssMis = 0x1u, kPtUseDirect = 0x2u, kPtUseEmissive = 0x4u
 constexpr uint32_t kSolveKeysPerLength = 64;
 // bytes reserved per deferred manifold walk (the device task structure is checked against it)
 constexpr size_t kMneeTaskBytes = 320;
+// bytes reserved per deferred forward replay (a sourced beam at up to 8 wavelengths and its vertex)
+constexpr size_t kReplayTaskBytes = 288;
+// replay-order sort keys: vertices to evaluate (0..15) x material type of the first one (16)
+constexpr uint32_t kReplayKeys = 256;
 
 // One scene of a render: its BVH root in the combined node array, its light range in the combined
 // light arrays (the power sampler's table holds scene-local indices), its camera, image size, the
@@ -221,6 +225,12 @@ struct PtParams {
     uint32_t* mneeCount;
     uint32_t* mneeSort;           // [32] walk-order key counts and cursors
     uint32_t* mneeOrder;          // [mneeCap] walk order of the tasks (sorted by occluder count and material), or null
+    // deferred forward replays of the solve pass (null: replays run inline)
+    void* replayTasks;            // [replayCap] tasks of kReplayTaskBytes
+    uint32_t replayCap;
+    uint32_t* replayCount;
+    uint32_t* replaySort;         // [2 kReplayKeys] replay-order key counts and cursors
+    uint32_t* replayOrder;        // [replayCap] replay order (sorted by vertex count and first material)
     // environment light (kPtUseEnv) and analytic lights (kPtUseAnalytic)
     EnvDev env;
     const AnalyticLightDev* alights;

@@ -1339,6 +1339,16 @@ PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int
     }
 }
 
+// replayMeasure called out of line from the solve kernel: with deferred replays it runs only for
+// manifold samples walked inline, a full replay queue and debug views, so its code stays out of the
+// solve kernel's hot instruction stream.
+template <int H>
+__device__ __noinline__ void replayInline(const PtParams& P, const PtScene& S, uint32_t pid, int p, const Bnc<H>& bounce, PBeam<H>& pb,
+                                          const MSData& ms, int nMs, f3 msOrigin, bool evalCurrent, const Ctx& c, bool hwssMis,
+                                          float& Lr, float& Lg, float& Lb, uint32_t& evals, DebugAcc* dbg) {
+    replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals, dbg);
+}
+
 // sampleLight for analytic lights (Rendering/Lights/LightHelpers.slang:71-289): the direction and
 // distance to the light, the incident radiance already divided by the pdf (Li, at the sampled
 // wavelengths wl) and the solid-angle pdf (0 for point and directional lights).  False when the
@@ -1444,6 +1454,27 @@ PLT_DI float emissivePdf(const PtParams& P, const PtScene& S, f3 posW, uint32_t 
     return sel * (distSqr / denom);
 }
 
+// A deferred forward replay (no manifold vertices): the beam as sourced and weighted at vertex p of
+// path pid, to be replayed through vertex p (NEE on non-delta lobes: evalCurrent) and p-1 .. 0 and
+// measured.  The replay draws no random numbers, so it can run after the solve kernel in any order.
+template <int H> struct ReplayTask {
+    PBeam<H> pb;
+    uint32_t pid, p, evalCurrent;
+};
+
+// Hands a replay to the replay wavefront; false when the queue is full (the caller replays inline).
+template <int H>
+PLT_DI bool deferReplay(const PtParams& P, uint32_t pid, int p, bool evalCurrent, const PBeam<H>& pb) {
+    const uint32_t slot = warpAggregatedAdd(P.replayCount, true);
+    if (slot >= P.replayCap) return false;
+    ReplayTask<H>* t = reinterpret_cast<ReplayTask<H>*>(static_cast<char*>(P.replayTasks) + (size_t)slot * plt::kReplayTaskBytes);
+    t->pb = pb;
+    t->pid = pid;
+    t->p = (uint32_t)p;
+    t->evalCurrent = evalCurrent ? 1u : 0u;
+    return true;
+}
+
 // MNEE = false compiles the solve kernel without manifold sampling (the do_mnee = 0 pass): the
 // occluder search and the task hand-off would otherwise enlarge the kernel for every option set.
 #ifndef PLT_SOLVE_MIN_BLOCKS
@@ -1509,7 +1540,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     PBeam<H> pb;
                     sourceBeamDistant<H>(pb, wo, P.maxBeamOmega, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
-                    replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, pathOrigin, false, c, hwssMis, Lr, Lg, Lb, evals, dbg);
+                    if (!(P.replayTasks && !dbg && deferReplay<H>(P, pid, p, false, pb)))
+                        replayInline<H>(P, S, pid, p, bounce, pb, ms, 0, pathOrigin, false, c, hwssMis, Lr, Lg, Lb, evals, dbg);
                 }
                 break;
             }
@@ -1768,7 +1800,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
                     sourceBeamArea<H>(pb, sd.posW, bounce.wi, P.sourcingArea, dist, Le, swl, P.maxBeamOmega);
                     if (!hwssMis && (bounce.flags & kFlagDispersive)) pb.comps = 1;
                 }
-                replayMeasure<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals, dbg);
+                if (!(nMs == 0 && P.replayTasks && !dbg && deferReplay<H>(P, pid, p, evalCurrent, pb)))
+                    replayInline<H>(P, S, pid, p, bounce, pb, ms, nMs, msOrigin, evalCurrent, c, hwssMis, Lr, Lg, Lb, evals, dbg);
             }
             if ((bounce.flags & kFlagTerminated) || p == (int)P.maxBounces) break;
             pathOrigin = V.posW;
@@ -1924,6 +1957,98 @@ __global__ void __launch_bounds__(256) ptMneeScatterKernel(const PtParams P) {
         P.mneeOrder[base[k] + atomicAdd(&h[k], 1u)] = i;
     }
 }
+// The replay wavefront: the solve kernel's deferred replays counting-sorted by (vertices to
+// evaluate, material type of the first of them), so a warp's lanes evaluate the same material code
+// over paths of the same length (the material-sorted queue of the forward unwind,
+// pltpt_solve.rt.slang:48-79), then replayed one thread each and added to the pixel's accumulator.
+template <int H> PLT_DI uint32_t replayKey(const PtParams& P, const ReplayTask<H>& t) {
+    const uint32_t nEval = t.p + t.evalCurrent;
+    const int first = t.evalCurrent ? (int)t.p : (int)t.p - 1;
+    uint32_t ty = 0;
+    if (first >= 0) {
+        const uint32_t prim = P.bPrim[(size_t)first * P.npix + t.pid];
+        if (prim < P.nTris) ty = min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), 15u);
+    }
+    return min(nEval, 15u) * 16u + ty;
+}
+template <int H> PLT_DI const ReplayTask<H>& replayTask(const PtParams& P, uint32_t i) {
+    return *reinterpret_cast<const ReplayTask<H>*>(static_cast<const char*>(P.replayTasks) + (size_t)i * plt::kReplayTaskBytes);
+}
+template <int H>
+__global__ void __launch_bounds__(256) ptReplayCountKernel(const PtParams P) {
+    __shared__ uint32_t h[plt::kReplayKeys];
+    for (uint32_t b = threadIdx.x; b < plt::kReplayKeys; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const uint32_t count = min(*((volatile uint32_t*)P.replayCount), P.replayCap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[replayKey<H>(P, replayTask<H>(P, i))], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < plt::kReplayKeys; b += blockDim.x)
+        if (h[b]) atomicAdd(P.replaySort + b, h[b]);
+}
+template <int H>
+__global__ void __launch_bounds__(256) ptReplayScatterKernel(const PtParams P) {
+    __shared__ uint32_t h[plt::kReplayKeys], base[plt::kReplayKeys];
+    const uint32_t count = min(*((volatile uint32_t*)P.replayCount), P.replayCap);
+    const uint32_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint32_t begin = min(blockIdx.x * per, count), end = min(begin + per, count);
+    for (uint32_t b = threadIdx.x; b < plt::kReplayKeys; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[replayKey<H>(P, replayTask<H>(P, i))], 1u);
+    __syncthreads();
+    // each key's first slot: the exclusive prefix of the key counts (warp scan over 8 keys per lane)
+    if (threadIdx.x < 32) {
+        constexpr uint32_t per8 = plt::kReplayKeys / 32;
+        uint32_t s = 0;
+        for (uint32_t j = 0; j < per8; ++j) s += P.replaySort[threadIdx.x * per8 + j];
+        uint32_t incl = s;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if ((int)threadIdx.x >= d) incl += v;
+        }
+        uint32_t run = incl - s;
+        for (uint32_t j = 0; j < per8; ++j) {
+            const uint32_t b = threadIdx.x * per8 + j;
+            base[b] = h[b] ? run + atomicAdd(P.replaySort + plt::kReplayKeys + b, h[b]) : 0u;
+            run += P.replaySort[b];
+            h[b] = 0;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t k = replayKey<H>(P, replayTask<H>(P, i));
+        P.replayOrder[base[k] + atomicAdd(&h[k], 1u)] = i;
+    }
+}
+template <int H>
+__global__ void __launch_bounds__(128) ptReplayKernel(const PtParams P) {
+    static_assert(sizeof(ReplayTask<H>) <= plt::kReplayTaskBytes, "ReplayTask stride");
+    const uint32_t count = min(*((volatile uint32_t*)P.replayCount), P.replayCap);
+    const Ctx c{P.profiles, P.nProfiles, P.flags};
+    const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
+    uint32_t evals = 0;
+    MSData ms;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const ReplayTask<H>& t = replayTask<H>(P, P.replayOrder[i]);
+        PBeam<H> pb = t.pb;
+        const uint32_t pid = t.pid;
+        const int p = (int)t.p;
+        const uint32_t gp = P.pidBase + pid;
+        const PtScene& S = P.scenes[sceneOf(P, gp)];
+        const Bnc<H> bounce = readBounce<H>(P, pid, p);
+        float Lr = 0.f, Lg = 0.f, Lb = 0.f;
+        replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, mk3(0.f, 0.f, 0.f), t.evalCurrent != 0, c, hwssMis, Lr, Lg, Lb, evals);
+        if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
+            atomicAdd(P.accum + 3 * (size_t)gp, (double)Lr);
+            atomicAdd(P.accum + 3 * (size_t)gp + 1, (double)Lg);
+            atomicAdd(P.accum + 3 * (size_t)gp + 2, (double)Lb);
+        }
+    }
+    unsigned long long s2 = evals;
+    for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xFFFFFFFFu, s2, o);
+    if ((threadIdx.x & 31u) == 0 && s2) atomicAdd(P.stats + 2, s2);
+}
+
 template <int H>
 cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, cudaStream_t stream) {
     static int bps[2] = {-1, -1};
@@ -1952,6 +2077,17 @@ cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, c
             ptMneeScatterKernel<H><<<numSMs, 256, 0, stream>>>(p);
         }
         ptMneeKernel<H><<<gw, 128, 0, stream>>>(p);
+    }
+    if (p.replayTasks) {
+        static int bpsR = -1;
+        if (bpsR < 0) {
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptReplayKernel<H>, 128, 0);
+            bpsR = b > 0 ? b : 1;
+        }
+        ptReplayCountKernel<H><<<numSMs, 256, 0, stream>>>(p);
+        ptReplayScatterKernel<H><<<numSMs, 256, 0, stream>>>(p);
+        ptReplayKernel<H><<<(uint32_t)numSMs * (uint32_t)bpsR, 128, 0, stream>>>(p);
     }
     return cudaGetLastError();
 }

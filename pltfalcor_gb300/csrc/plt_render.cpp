@@ -38,8 +38,9 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     ctx->ptBytes = 0;
     const size_t n = npix, nb = (size_t)maxB + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    // the counters: per-segment queue lengths, the manifold-walk count, 16 solve-order keys per length (counts, cursors)
-    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32;
+    // the counters: per-segment queue lengths, the manifold-walk count, the solve-order keys per
+    // length (counts, cursors), the walk-order keys, the replay count and the replay-order keys
+    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys;
     const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
@@ -66,6 +67,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.lenCount = P.qcount + nb + 2;
     P.lenCursor = P.lenCount + plt::kSolveKeysPerLength * nb;
     P.mneeSort = P.lenCursor + plt::kSolveKeysPerLength * nb;
+    P.replayCount = P.mneeSort + 32;
+    P.replaySort = P.replayCount + 1;
     P.mneeOrder = P.queue1;   // free during the solve pass
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
@@ -139,7 +142,7 @@ void pltReleaseRenderState(plt_context* ctx) {
     if (ctx->capStream) cudaStreamDestroy((cudaStream_t)ctx->capStream);
     cudaFree(ctx->dFrame);
     void* ptrs[] = {ctx->dProfileIcdf, ctx->dMatProps, ctx->dPos, ctx->dIdx, ctx->dNrm, ctx->dTan, ctx->dTriInst, ctx->dLightPos, ctx->dLightNrm,
-                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dLightActive, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dScenes, ctx->dAccum};
+                    ctx->dLightArea, ctx->dLightFlux, ctx->dAlias, ctx->dPrimToLight, ctx->dLightEmission, ctx->dLightActive, ctx->dPt, ctx->dPtStats, ctx->dPtMix, ctx->dMneeTasks, ctx->dReplayTasks, ctx->dScenes, ctx->dAccum};
     for (void* p : ptrs) cudaFree(p);
 }
 
@@ -288,6 +291,26 @@ plt_status renderViews(plt_context* ctx, const plt_render_view* views, uint32_t 
     } else {
         P.mneeTasks = nullptr;
         P.mneeCap = 0;
+    }
+    // deferred forward replays: 3/2 task slots per path and frame (beyond that they replay inline);
+    // with a debug view they stay inline, where the path's debug colour is accumulated
+    if (o.debug_view == PLT_DEBUG_VIEW_NONE && !(o.flags & PLT_OPTION_INLINE_REPLAY)) {
+        const uint32_t cap = npix + npix / 2;
+        const size_t bytes = (size_t)cap * (plt::kReplayTaskBytes + sizeof(uint32_t));
+        if (ctx->replayBytes < bytes) {
+            cudaFree(ctx->dReplayTasks);
+            ctx->dReplayTasks = nullptr;
+            ctx->replayBytes = 0;
+            PLT_CUDA(ctx, cudaMalloc(&ctx->dReplayTasks, bytes));
+            ctx->replayBytes = bytes;
+        }
+        P.replayTasks = ctx->dReplayTasks;
+        P.replayCap = cap;
+        P.replayOrder = reinterpret_cast<uint32_t*>(static_cast<char*>(ctx->dReplayTasks) + (size_t)cap * plt::kReplayTaskBytes);
+    } else {
+        P.replayTasks = nullptr;
+        P.replayCap = 0;
+        P.replayOrder = nullptr;
     }
     P.mneeMaxOccluders = o.mnee_max_occluders;
     P.mneeMaxIterations = o.mnee_max_iterations;
