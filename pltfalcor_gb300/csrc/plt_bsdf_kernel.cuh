@@ -38,7 +38,9 @@ enum : uint32_t {
     C_UNITS = 64,   // [16] units per tile of each type's queue
     C_USZ = 80,     // [16] queries per unit of each type (a multiple of 32)
     C_TOTAL = 96,   // [16] queries per type
-    C_WORDS = 112
+    C_COST = 112,   // [16] measured cost per query of each type (float; exponential average over batches)
+    C_CYC = 128,    // [16] x u64: warp cycles spent on each type's units in the last batch
+    C_WORDS = 160
 };
 static_assert(C_WORDS * 4 <= plt::kBsdfCtrlBytes, "control words exceed their scratch block");
 
@@ -66,6 +68,24 @@ PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
     const uint32_t tid = threadIdx.x;
     uint32_t* count = sh;          // [16]
     float* cum = reinterpret_cast<float*>(sh + 16);   // [17] cumulative work
+    float* cost = reinterpret_cast<float*>(sh + 33);  // [16] cost per query
+    uint32_t* measured = sh + 49;  // 1 while every queried type has a measured cost
+    if (tid == 0) *measured = 1u;
+    __syncthreads();
+    if (tid < kTypeSlots) {
+        // the previous batch's cycles per query of this type, folded into its running average
+        unsigned long long* cyc = reinterpret_cast<unsigned long long*>(P.ctrl + C_CYC) + tid;
+        const unsigned long long c = atomicExch(cyc, 0ull);
+        const uint32_t prev = P.ctrl[C_TOTAL + tid];
+        float avg = __uint_as_float(P.ctrl[C_COST + tid]);
+        if (prev >= 1024u && c > 0ull) {
+            const float m = (float)c / (float)prev;
+            avg = avg > 0.f ? 0.5f * avg + 0.5f * m : m;
+            P.ctrl[C_COST + tid] = __float_as_uint(avg);
+        }
+        cost[tid] = avg;
+    }
+    __syncthreads();
     if (tid < kTypeSlots) {
         const uint32_t total = atomicExch(P.ctrl + C_COUNT + tid, 0u);
         const uint32_t mx = atomicExch(P.ctrl + C_MAX + tid, 0u);
@@ -79,11 +99,17 @@ PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
         count[tid] = total;
     }
     __syncthreads();
+#ifndef PLT_ADAPTIVE_COSTS
+#define PLT_ADAPTIVE_COSTS 1
+#endif
+    if (tid < kTypeSlots && count[tid] > 0u && (!PLT_ADAPTIVE_COSTS || !(cost[tid] > 0.f))) atomicAnd(measured, 0u);
+    __syncthreads();
     if (tid == 0) {
+        // SM shares: queries x measured cost once every queried type has one, else the priors
         float s = 0.f;
         cum[0] = 0.f;
         for (uint32_t t = 0; t < kTypeSlots; ++t) {
-            s += (float)count[t] * P.typeCost[t];
+            s += (float)count[t] * (*measured ? cost[t] : P.typeCost[t]);
             cum[t + 1] = s;
         }
         P.ctrl[C_DONE] = 0u;
@@ -106,7 +132,7 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     using namespace plt;
     __shared__ uint32_t counts[kBuckets];
     __shared__ uint32_t offs[kBuckets];
-    __shared__ uint32_t sched[40];
+    __shared__ uint32_t sched[56];
     __shared__ bool isLast;
     const uint32_t tid = threadIdx.x;
     const uint32_t n = P.q.n;
@@ -217,8 +243,10 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     using namespace plt;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned long long cycles[kTypeSlots];   // this CTA's warp cycles per type
     DevProfile* sprof = reinterpret_cast<DevProfile*>(smem);
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    if (tid < kTypeSlots) cycles[tid] = 0ull;
 
     // Stage the spectral profiles into shared memory with one bulk asynchronous copy.
     const uint32_t profBytes = P.nProfiles * (uint32_t)sizeof(DevProfile);
@@ -270,6 +298,7 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
         const uint32_t hi = min(end, lo + usz);
         if (lo >= hi) continue;
         const uint32_t tileBase = tile * kBatchTile;
+        const long long t0 = clock64();
         switch (t) {
         case kMatDielectric: shadeUnit<H, kMatDielectric>(P, c, tileBase, lo, hi, lane); break;
         case kMatConductor: shadeUnit<H, kMatConductor>(P, c, tileBase, lo, hi, lane); break;
@@ -283,7 +312,13 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
         case kMatDiffuse: shadeUnit<H, kMatDiffuse>(P, c, tileBase, lo, hi, lane); break;
         default: shadeUnit<H, 0u>(P, c, tileBase, lo, hi, lane); break;
         }
+        __syncwarp();
+        if (lane == 0) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
     }
+    // the measured cost per type feeds the next batch's SM shares
+    __syncthreads();
+    if (tid < kTypeSlots && cycles[tid])
+        atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + C_CYC) + tid, cycles[tid]);
 }
 
 }  // namespace pltdev
