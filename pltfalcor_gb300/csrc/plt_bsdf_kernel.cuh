@@ -376,10 +376,7 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     // Measured on the 2^22 mixed batch: 32-query units 0.79 ms, 256-query units 0.86 ms per launch;
     // bounding each queue's lead over the slowest one (16 or 32 tiles) made it slower (1.2-2.0 ms),
     // since every unit then re-reads the contended queue counters and SMs leave their type
-#ifndef PLT_UNIT_QUERIES
-#define PLT_UNIT_QUERIES 32
-#endif
-    p.unitQueries = PLT_UNIT_QUERIES;
+    p.unitQueries = 32;
     for (uint32_t t = 0; t < kTypeSlots; ++t)
         if (!(p.typeCost[t] > 0.f)) p.typeCost[t] = defaultTypeCost(t);
     if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);

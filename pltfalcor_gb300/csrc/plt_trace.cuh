@@ -18,10 +18,14 @@ struct TriHit {
     bool hit;
 };
 
-// intersectRayTriangle with a rounding-exact evaluation; A = v0 - o etc.
-__device__ __forceinline__ TriHit watertight(float ox, float oy, float oz, float dx, float dy, float dz, float4 v0, float4 v1, float4 v2) {
-    TriHit h;
-    h.hit = false;
+// The ray-only part of intersectRayTriangle: the dominant axis kz, the other two (swapped for a
+// negative direction along kz) and the shear constants.  The same for every triangle of a ray.
+struct WtRay {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+__device__ __forceinline__ WtRay wtRay(float dx, float dy, float dz) {
+    WtRay r;
     const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
     int kz = 0;
     if (ay > ax && ay > az) kz = 1;
@@ -32,9 +36,21 @@ __device__ __forceinline__ TriHit watertight(float ox, float oy, float oz, float
     if (dkz < 0.f) { const int s = kx; kx = ky; ky = s; }
     const float dkx = kx == 0 ? dx : (kx == 1 ? dy : dz);
     const float dky = ky == 0 ? dx : (ky == 1 ? dy : dz);
-    const float Sx = __fdiv_rn(dkx, dkz);
-    const float Sy = __fdiv_rn(dky, dkz);
-    const float Sz = __fdiv_rn(1.f, dkz);
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = __fdiv_rn(dkx, dkz);
+    r.Sy = __fdiv_rn(dky, dkz);
+    r.Sz = __fdiv_rn(1.f, dkz);
+    return r;
+}
+
+// intersectRayTriangle with a rounding-exact evaluation; A = v0 - o etc.
+__device__ __forceinline__ TriHit watertight(float ox, float oy, float oz, const WtRay& R, float4 v0, float4 v1, float4 v2) {
+    TriHit h;
+    h.hit = false;
+    const int kx = R.kx, ky = R.ky, kz = R.kz;
+    const float Sx = R.Sx, Sy = R.Sy, Sz = R.Sz;
     const float A[3] = {__fsub_rn(v0.x, ox), __fsub_rn(v0.y, oy), __fsub_rn(v0.z, oz)};
     const float B[3] = {__fsub_rn(v1.x, ox), __fsub_rn(v1.y, oy), __fsub_rn(v1.z, oz)};
     const float C[3] = {__fsub_rn(v2.x, ox), __fsub_rn(v2.y, oy), __fsub_rn(v2.z, oz)};
@@ -115,6 +131,7 @@ __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes
     const float dsum = fabsf(dx) + fabsf(dy) + fabsf(dz);
     if (!(dsum > 0.f) || !(dsum < INFINITY)) return res;
     const float ix = safeRcp(dx), iy = safeRcp(dy), iz = safeRcp(dz);
+    const WtRay wr = wtRay(dx, dy, dz);
     float bestT = tmax, bestB1 = 0.f, bestB2 = 0.f;
     uint32_t bestPrim = 0xFFFFFFFFu;
     bool done = false;
@@ -128,7 +145,7 @@ __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes
         for (uint32_t k = first; k < first + count; ++k) {
             const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
             ++triTests;
-            const TriHit h = watertight(ox, oy, oz, dx, dy, dz, v0, v1, v2);
+            const TriHit h = watertight(ox, oy, oz, wr, v0, v1, v2);
             if (!h.hit || !(h.t >= tmin) || !(h.t <= bestT)) continue;
             const uint32_t prim = __float_as_uint(v0.w);
             if (ANY) {
