@@ -24,8 +24,12 @@
 namespace pltdev {
 
 using plt::kTypeSlots;
-constexpr uint32_t kLobeClasses = 10;                     // lowest set lobe bit (0..7), 8: none, 9: padding
-constexpr uint32_t kBuckets = kTypeSlots * kLobeClasses;  // material type x lobe class
+// Sub-buckets of a material type: 0..7 the lowest set lobe bit, 8 no lobe bit; a material whose
+// type byte has bit 7 set is bucketed by its work class instead (bits 4..6: stack layers in fours
+// for multilayers), 8..15, so a warp's lanes run loops of similar trip counts.  The last bucket
+// (type 15, class 15) holds the padding.
+constexpr uint32_t kLobeClasses = 16;
+constexpr uint32_t kBuckets = kTypeSlots * kLobeClasses;  // material type x lobe / work class
 constexpr uint32_t kPadBucket = kBuckets - 1;             // positions past the end of the batch
 
 // Control words of a batch's schedule (BatchParams::ctrl).  C_COUNT, C_MAX and C_DONE are zero
@@ -150,14 +154,15 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
         if (idx < n) {
             const uint32_t mid = __ldg(P.q.material + idx);
             const uint32_t t = mid < P.nMats ? __ldg(P.matType + mid) : 14u;
-            b = (t & 15u) * kLobeClasses + lobeClass(P.q.lobe ? __ldg(P.q.lobe + idx) : 0xFFFFu);
+            const uint32_t cls = (t & 0x80u) ? 8u + ((t >> 4) & 7u) : lobeClass(P.q.lobe ? __ldg(P.q.lobe + idx) : 0xFFFFu);
+            b = (t & 15u) * kLobeClasses + cls;
         }
         key[k] = (uint16_t)b;
         rank[k] = (uint16_t)atomicAdd(&counts[b], 1u);
     }
     __syncthreads();
     if (tid < 32) {
-        // exclusive scan of kBuckets counters by one warp: 5 consecutive buckets per lane
+        // exclusive scan of kBuckets counters by one warp: 8 consecutive buckets per lane
         constexpr uint32_t per = kBuckets / 32;
         uint32_t s = 0;
 #pragma unroll

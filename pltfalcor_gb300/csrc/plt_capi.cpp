@@ -2,6 +2,7 @@
 // tables, batched BSDF launches, status.  No exception crosses the ABI.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -177,6 +178,17 @@ plt_status plt_set_spectral_profiles(plt_context* ctx, const plt_spectral_profil
     return PLT_OK;
 }
 
+namespace {
+// The high bits of a material's type byte for the batch sort: bit 7 set and the work class in bits
+// 4..6 when the trip count of its evaluation loop varies between materials of the type, so the
+// classify pass gives a warp materials of similar cost (stack layers in fours for multilayers, which
+// expose one lobe); 0 for the rest, which are sorted by the query's lobe.
+uint32_t batchWorkClass(uint32_t type, const pltdev::DevMaterial& d) {
+    if (type != PLT_MATERIAL_MULTILAYERED_STACK) return 0u;
+    return 0x80u | (std::min((d.aux > 0u ? d.aux - 1u : 0u) >> 2, 7u) << 4);
+}
+}  // namespace
+
 plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, uint32_t count) {
     if (!ctx || (count > 0 && !mats)) return PLT_INVALID_ARG;
     std::vector<pltdev::DevMaterial> h(count);
@@ -184,7 +196,7 @@ plt_status plt_set_materials(plt_context* ctx, const plt_material_record* mats, 
     for (uint32_t i = 0; i < count; ++i) {
         const plt_status s = plt::decodeMaterial(mats[i], ctx->nProfiles, h[i]);
         if (s != PLT_OK) return s;
-        types[i] = (uint8_t)mats[i].type;
+        types[i] = (uint8_t)(mats[i].type | batchWorkClass(mats[i].type, h[i]));
     }
     if (count > ctx->capMats) {
         cudaFree(ctx->dMats);

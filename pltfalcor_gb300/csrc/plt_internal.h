@@ -229,7 +229,7 @@ struct PtParams {
     void* replayTasks;            // [replayCap] tasks of kReplayTaskBytes
     uint32_t replayCap;
     uint32_t* replayCount;
-    uint32_t* replaySort;         // [2 kReplayKeys] replay-order key counts and cursors
+    uint32_t* replaySort;         // [2 kReplayKeys + 1] replay-order key counts and cursors, the replay work counter
     uint32_t* replayOrder;        // [replayCap] replay order (sorted by vertex count and first material)
     // environment light (kPtUseEnv) and analytic lights (kPtUseAnalytic)
     EnvDev env;

@@ -27,9 +27,9 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
     if (p.nWave == 0) return cudaSuccess;
     // queue lengths, the manifold-walk count, the solve-order key histogram and its cursors, the
-    // walk-order keys, the replay count and the replay-order keys
+    // walk-order keys, the replay count, the replay-order keys and the replay kernel's work counter
     cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * ((p.maxBounces + 1) * (1 + 2 * kSolveKeysPerLength) + 2 + 32 + 1 +
-                                                                      2 * kReplayKeys), stream);
+                                                                      2 * kReplayKeys + 1), stream);
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);

@@ -1957,10 +1957,12 @@ __global__ void __launch_bounds__(256) ptMneeScatterKernel(const PtParams P) {
         P.mneeOrder[base[k] + atomicAdd(&h[k], 1u)] = i;
     }
 }
-// The replay wavefront: the solve kernel's deferred replays counting-sorted by (vertices to
-// evaluate, material type of the first of them), so a warp's lanes evaluate the same material code
-// over paths of the same length (the material-sorted queue of the forward unwind,
+// The replay wavefront: the solve kernel's deferred replays counting-sorted by (material type of
+// the first vertex to evaluate, vertices to evaluate), so a warp's lanes evaluate the same material
+// code over paths of the same length (the material-sorted queue of the forward unwind,
 // pltpt_solve.rt.slang:48-79), then replayed one thread each and added to the pixel's accumulator.
+// The replay kernel's warps take 32 consecutive tasks of that order at a time from one counter, so
+// the warps resident on an SM at any moment work on neighbouring keys: one or two materials' code.
 template <int H> PLT_DI uint32_t replayKey(const PtParams& P, const ReplayTask<H>& t) {
     const uint32_t nEval = t.p + t.evalCurrent;
     const int first = t.evalCurrent ? (int)t.p : (int)t.p - 1;
@@ -1969,7 +1971,7 @@ template <int H> PLT_DI uint32_t replayKey(const PtParams& P, const ReplayTask<H
         const uint32_t prim = P.bPrim[(size_t)first * P.npix + t.pid];
         if (prim < P.nTris) ty = min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), 15u);
     }
-    return min(nEval, 15u) * 16u + ty;
+    return ty * 16u + min(nEval, 15u);
 }
 template <int H> PLT_DI const ReplayTask<H>& replayTask(const PtParams& P, uint32_t i) {
     return *reinterpret_cast<const ReplayTask<H>*>(static_cast<const char*>(P.replayTasks) + (size_t)i * plt::kReplayTaskBytes);
@@ -2028,20 +2030,29 @@ __global__ void __launch_bounds__(128) ptReplayKernel(const PtParams P) {
     const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
     uint32_t evals = 0;
     MSData ms;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const ReplayTask<H>& t = replayTask<H>(P, P.replayOrder[i]);
-        PBeam<H> pb = t.pb;
-        const uint32_t pid = t.pid;
-        const int p = (int)t.p;
-        const uint32_t gp = P.pidBase + pid;
-        const PtScene& S = P.scenes[sceneOf(P, gp)];
-        const Bnc<H> bounce = readBounce<H>(P, pid, p);
-        float Lr = 0.f, Lg = 0.f, Lb = 0.f;
-        replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, mk3(0.f, 0.f, 0.f), t.evalCurrent != 0, c, hwssMis, Lr, Lg, Lb, evals);
-        if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
-            atomicAdd(P.accum + 3 * (size_t)gp, (double)Lr);
-            atomicAdd(P.accum + 3 * (size_t)gp + 1, (double)Lg);
-            atomicAdd(P.accum + 3 * (size_t)gp + 2, (double)Lb);
+    uint32_t* next = P.replaySort + 2 * plt::kReplayKeys;   // the warps' work counter
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t c0 = 0;
+        if (lane == 0) c0 = atomicAdd(next, 32u);
+        c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+        if (c0 >= count) break;
+        const uint32_t i = c0 + lane;
+        if (i < count) {
+            const ReplayTask<H>& t = replayTask<H>(P, P.replayOrder[i]);
+            PBeam<H> pb = t.pb;
+            const uint32_t pid = t.pid;
+            const int p = (int)t.p;
+            const uint32_t gp = P.pidBase + pid;
+            const PtScene& S = P.scenes[sceneOf(P, gp)];
+            const Bnc<H> bounce = readBounce<H>(P, pid, p);
+            float Lr = 0.f, Lg = 0.f, Lb = 0.f;
+            replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, mk3(0.f, 0.f, 0.f), t.evalCurrent != 0, c, hwssMis, Lr, Lg, Lb, evals);
+            if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
+                atomicAdd(P.accum + 3 * (size_t)gp, (double)Lr);
+                atomicAdd(P.accum + 3 * (size_t)gp + 1, (double)Lg);
+                atomicAdd(P.accum + 3 * (size_t)gp + 2, (double)Lb);
+            }
         }
     }
     unsigned long long s2 = evals;

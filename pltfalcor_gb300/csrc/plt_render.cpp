@@ -39,8 +39,9 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     const size_t n = npix, nb = (size_t)maxB + 1;
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     // the counters: per-segment queue lengths, the manifold-walk count, the solve-order keys per
-    // length (counts, cursors), the walk-order keys, the replay count and the replay-order keys
-    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys;
+    // length (counts, cursors), the walk-order keys, the replay count, the replay-order keys and
+    // the replay kernel's work counter
+    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys + 1;
     const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
