@@ -202,6 +202,8 @@ struct PtParams {
     uint32_t* plen;
     uint32_t* queue0;             // [npix]
     uint32_t* queue1;             // [npix]
+    uint32_t* segPrim;            // [npix] closest hit of each queue slot of the segment (ptSegTraceKernel), or null:
+    float* segBary;               // [2][npix]   the segment kernels then trace inline
     uint32_t* qcount;             // [maxBounces + 2]
     uint32_t* lenCount;           // [16 (maxBounces + 1)] paths per solve-order key (length, first-hit type)
     uint32_t* lenCursor;          // [16 (maxBounces + 1)]

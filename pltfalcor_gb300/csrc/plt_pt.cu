@@ -33,9 +33,11 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
-    static int bpsInit = -1, bpsBounce = -1, bpsLearned = -1;
+    static int bpsInit = -1, bpsBounce = -1, bpsLearned = -1, bpsSegTrace = -1;
     if (bpsBounce < 0) {
         int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptSegTraceKernel, 128, 0);
+        bpsSegTrace = b > 0 ? b : 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kPlainBounce, 128, 0);
         bpsBounce = b > 0 ? b : 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptBounceKernel<true>, 128, kLearnedSmem);
@@ -46,12 +48,20 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
     auto blocks = [&](int occ, uint32_t want) { return (uint32_t)numSMs * (want ? std::min<uint32_t>(want, (uint32_t)occ) : (uint32_t)occ); };
     const uint32_t need = (p.nWave + 127) / 128;
     pltdev::ptInitKernel<<<std::min<uint32_t>(need, blocks(bpsInit, 0)), 128, 0, stream>>>(p);
+    // each segment: its closest hits traced with dynamic fetch, then the segment kernel shades them
+    const uint32_t gridT = std::min<uint32_t>(need, blocks(bpsSegTrace, 0));
     if (p.opt & kPtLearned) {
         const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsLearned, L.segBlocksPerSM));
-        for (uint32_t it = 0; it <= p.maxBounces; ++it) pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
+        for (uint32_t it = 0; it <= p.maxBounces; ++it) {
+            if (p.segPrim) pltdev::ptSegTraceKernel<<<gridT, 128, 0, stream>>>(p, it);
+            pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
+        }
     } else {
         const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsBounce, L.segBlocksPerSM));
-        for (uint32_t it = 0; it <= p.maxBounces; ++it) kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
+        for (uint32_t it = 0; it <= p.maxBounces; ++it) {
+            if (p.segPrim) pltdev::ptSegTraceKernel<<<gridT, 128, 0, stream>>>(p, it);
+            kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
+        }
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     PtParams q = p;

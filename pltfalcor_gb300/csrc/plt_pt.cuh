@@ -501,6 +501,48 @@ __global__ void __launch_bounds__(128) ptInitKernel(const PtParams P) {
 // the analytic tracer's expectation whatever the network outputs; the exact BSDF is evaluated as
 // before.  A primary sample of q outside the unit square ends a path that takes a non-delta lobe.
 // Residency of the analytic variant (blocks of 128 per SM; the register budget follows from it).
+// The segment's closest hits, traced ahead of the segment kernel by ptSegTraceKernel.
+PLT_DI TraceResult segmentHit(const PtParams& P, uint32_t slot) {
+    TraceResult h;
+    h.prim = P.segPrim[slot];
+    h.t = 0.f;
+    h.b1 = P.segBary[slot];
+    h.b2 = P.segBary[P.npix + slot];
+    return h;
+}
+
+// The closest hits of a segment's queue (the rays the paths continue along), traced with dynamic
+// fetch (dynamicTraversal) ahead of the segment kernel, which then shades them: traversal alone
+// keeps a warp's lanes full (a lane whose ray has finished takes the next one) where, inside the
+// segment kernel, every lane waited for the longest ray of its warp and then for the shading of
+// each other's materials.  Each CTA traces a contiguous share of the queue's slots.
+__global__ void __launch_bounds__(128) ptSegTraceKernel(const PtParams P, uint32_t it) {
+    __shared__ uint32_t next;
+    const uint32_t n = P.npix;
+    const uint32_t count = it == 0 ? P.nWave : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
+    const uint32_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint32_t begin = min(blockIdx.x * per, count), end = min(begin + per, count);
+    if (threadIdx.x == 0) next = begin;
+    __syncthreads();
+    uint32_t nv = 0, tt = 0, overflow = 0;
+    dynamicTraversal<false>(
+        reinterpret_cast<const float4*>(P.nodes), P.tris, kStackDepth, end, &next,
+        [&](uint32_t slot) {
+            const uint32_t pid = it == 0 ? slot : qin[slot];
+            const f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
+            return TravRay{org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, (int32_t)__ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root)};
+        },
+        [&](uint32_t slot, uint32_t prim, float, float b1, float b2) {
+            P.segPrim[slot] = prim;
+            P.segBary[slot] = b1;
+            P.segBary[n + slot] = b2;
+        },
+        nv, tt, overflow);
+    if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
+    addTraversalBytes(P, nv, tt);
+}
+
 #ifndef PLT_BOUNCE_MIN_BLOCKS
 #define PLT_BOUNCE_MIN_BLOCKS 7
 #endif
@@ -565,8 +607,10 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
             wavelength = P.wl[pid];
             if constexpr (LEARNED) wps = P.wpss[pid];
             for (int guard = 0; guard < 64; ++guard) {
-                h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
-                                    __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
+                if (guard == 0 && P.segPrim) h = segmentHit(P, slot);
+                else
+                    h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
+                                        __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;
@@ -745,8 +789,10 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
                 ++recorded;
             };
             for (int guard = 0; guard < 64; ++guard) {
-                const TraceResult h = traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt, overflow,
-                                                      __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
+                const TraceResult h = guard == 0 && P.segPrim
+                                          ? segmentHit(P, slot)
+                                          : traverse<false>(nodes, P.tris, org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, nv, tt,
+                                                            overflow, __ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root));
                 const f3 wi = -dir;
                 if (h.prim == kNoHit) {
                     flags |= kFlagMiss;

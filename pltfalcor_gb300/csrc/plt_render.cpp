@@ -42,7 +42,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     // length (counts, cursors), the walk-order keys, the replay count, the replay-order keys and
     // the replay kernel's work counter
     const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys + 1;
-    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4);
+    const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4) +
+                             al(n * 4) + al(2 * n * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
     PLT_CUDA(ctx, cudaMalloc(&ctx->dPt, total));
@@ -71,6 +72,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.replayCount = P.mneeSort + 32;
     P.replaySort = P.replayCount + 1;
     P.mneeOrder = P.queue1;   // free during the solve pass
+    P.segPrim = (uint32_t*)take(n * 4);
+    P.segBary = (float*)take(2 * n * 4);
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
     P.bPrim = (uint32_t*)take(nb * n * 4);

@@ -198,4 +198,159 @@ __device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes
     return res;
 }
 
+// ---- dynamic-fetch traversal (Aila & Laine, "Understanding the Efficiency of Ray Traversal on
+// GPUs", HPG 2009) ---------------------------------------------------------------------------------
+// One lane's ray in flight: its traversal state between node visits.  The visit order is that of
+// traverse(), so the hit found is the same.
+constexpr int32_t kTravDone = -2147483647 - 1;   // `node` of a ray that cannot hit anything
+
+struct TravLane {
+    float ox, oy, oz, ix, iy, iz, tmin, bestT, bestB1, bestB2;
+    uint32_t bestPrim;
+    WtRay wr;
+    int32_t node;
+    int sp;   // entries on the lane's stack (kept apart from this struct, so its scalars stay in registers)
+
+    __device__ __forceinline__ void start(float px, float py, float pz, float dx, float dy, float dz, float t0, float t1, int32_t root) {
+        ox = px;
+        oy = py;
+        oz = pz;
+        tmin = t0;
+        bestT = t1;
+        bestB1 = bestB2 = 0.f;
+        bestPrim = 0xFFFFFFFFu;
+        sp = 0;
+        node = root;
+        // a zero or non-finite direction cannot hit anything (see traverse)
+        const float dsum = fabsf(dx) + fabsf(dy) + fabsf(dz);
+        if (!(dsum > 0.f) || !(dsum < INFINITY)) node = kTravDone;
+        ix = safeRcp(dx);
+        iy = safeRcp(dy);
+        iz = safeRcp(dz);
+        wr = wtRay(dx, dy, dz);
+    }
+
+    // One node visit (and the triangles of the leaves it hits); true when the ray has finished.
+    template <bool ANY>
+    __device__ __forceinline__ bool step(const float4* __restrict__ nodes, const float4* __restrict__ tris, int2* stack, int stackCap,
+                                         uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow) {
+        if (node == kTravDone) return true;
+        ++nodeVisits;
+        const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
+        const int4 rr = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
+        const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
+        const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
+        float tl = 0.f, tr = 0.f;
+        bool hl = rr.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
+        bool hr = rr.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const bool h = side ? hr : hl;
+            const int32_t ref = side ? rr.y : rr.x;
+            if (!h || ref >= 0) continue;
+            if (side) hr = false;
+            else hl = false;
+            const uint32_t v = (uint32_t)~ref;
+            const uint32_t first = v >> 4, count = (v & 15u) + 1u;
+            for (uint32_t k = first; k < first + count; ++k) {
+                const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
+                ++triTests;
+                const TriHit th = watertight(ox, oy, oz, wr, v0, v1, v2);
+                if (!th.hit || !(th.t >= tmin) || !(th.t <= bestT)) continue;
+                const uint32_t prim = __float_as_uint(v0.w);
+                if (ANY) {
+                    bestT = th.t;
+                    bestPrim = prim;
+                    return true;
+                }
+                if (th.t < bestT || prim < bestPrim) {
+                    bestT = th.t;
+                    bestPrim = prim;
+                    bestB1 = th.b1;
+                    bestB2 = th.b2;
+                }
+            }
+        }
+        if (hl && hr) {
+            const bool leftNear = tl <= tr;
+            if (sp < stackCap && sp < kStackDepth) stack[sp++] = make_int2(leftNear ? rr.y : rr.x, __float_as_int(leftNear ? tr : tl));
+            else overflow = 1;
+            node = leftNear ? rr.x : rr.y;
+            return false;
+        }
+        if (hl) {
+            node = rr.x;
+            return false;
+        }
+        if (hr) {
+            node = rr.y;
+            return false;
+        }
+        // pop the nearest pending node that can still hold a closer hit
+        while (sp > 0) {
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= bestT * kTfarScale) {
+                node = e.x;
+                return false;
+            }
+        }
+        return true;
+    }
+};
+
+// Lanes of a warp whose ray has finished take new rays together once at least this many are idle
+// (or the whole warp is).  Measured on 2^20 random closest-hit rays of a 1.04 M-triangle scene
+// (rays/s): 1 lane 1.36 G, 4 1.46 G, 8 1.47 G, 16 1.43 G, 32 1.18 G; 1024^2 primary rays 1.68,
+// 2.07, 2.22, 2.20 and 2.33 G.
+#ifndef PLT_TRACE_REFILL
+#define PLT_TRACE_REFILL 8
+#endif
+
+// A ray handed to dynamicTraversal: origin, direction, [tmin, tmax] and the BVH root.
+struct TravRay {
+    float ox, oy, oz, dx, dy, dz, tmin, tmax;
+    int32_t root;
+};
+
+// Traces rays [begin, end) with one ray per lane and dynamic fetch: every loop iteration visits one
+// node per active lane; a lane whose ray r has finished calls finish(r, prim, t, b1, b2) and goes
+// idle, and idle lanes are refilled together (fetch(r) returns ray r's TravRay) from the shared
+// counter `next` (initialised to begin by the caller, then a __syncthreads), so a warp keeps its
+// lanes busy instead of waiting for the longest ray of a fixed set of 32.  Whole warps only.
+template <bool ANY, class Fetch, class Finish>
+__device__ __forceinline__ void dynamicTraversal(const float4* __restrict__ nodes, const float4* __restrict__ tris, int stackCap, uint32_t end,
+                                                 uint32_t* next, Fetch fetch, Finish finish, uint32_t& nodeVisits, uint32_t& triTests,
+                                                 uint32_t& overflow) {
+    constexpr uint32_t kNoRay = 0xFFFFFFFFu, kFull = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t ray = kNoRay;
+    bool drained = false;
+    TravLane L;
+    L.node = kTravDone;
+    int2 stack[kStackDepth];
+    for (;;) {
+        const unsigned idle = __ballot_sync(kFull, ray == kNoRay);
+        if (idle == kFull && drained) break;
+        if (!drained && (idle == kFull || __popc(idle) >= PLT_TRACE_REFILL)) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(next, (uint32_t)__popc(idle));
+            base = __shfl_sync(kFull, base, 0);
+            if (base >= end) drained = true;
+            if (ray == kNoRay) {
+                const uint32_t r = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (r < end) {
+                    ray = r;
+                    const TravRay q = fetch(r);
+                    L.start(q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, q.tmin, q.tmax, q.root);
+                }
+            }
+        }
+        if (ray == kNoRay) continue;
+        if (L.template step<ANY>(nodes, tris, stack, stackCap, nodeVisits, triTests, overflow)) {
+            finish(ray, L.bestPrim, L.bestT, L.bestB1, L.bestB2);
+            ray = kNoRay;
+        }
+    }
+}
+
 }  // namespace pltdev
