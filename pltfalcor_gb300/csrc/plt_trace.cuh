@@ -111,97 +111,11 @@ struct TraceResult {
     float t, b1, b2;
 };
 
-// Stack traversal of the two-wide BVH for one ray: closest hit with tmin <= t <= tmax (ties to
-// the lowest triangle id), or, with ANY, the first hit found (TraceRay with
-// ACCEPT_FIRST_HIT_AND_END_SEARCH).  Counts node visits and triangle tests; sets `overflow` when
-// the fixed-depth stack (or the caller's smaller cap, stackCap) overflowed: the result is then
-// possibly not the closest.
-template <bool ANY>
-__device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, float ox, float oy,
-                                                float oz, float dx, float dy, float dz, float tmin, float tmax,
-                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow, int32_t root = 0,
-                                                int stackCap = kStackDepth) {
-    TraceResult res;
-    res.prim = 0xFFFFFFFFu;
-    res.t = tmax;
-    res.b1 = res.b2 = 0.f;
-    // A zero or non-finite direction (e.g. the zero vector a grating returns for an evanescent
-    // diffraction order) makes every watertight test yield t = NaN, so nothing can be hit; the
-    // slab test would not cull anything for it (fminf/fmaxf drop NaNs), so return the miss here.
-    const float dsum = fabsf(dx) + fabsf(dy) + fabsf(dz);
-    if (!(dsum > 0.f) || !(dsum < INFINITY)) return res;
-    const float ix = safeRcp(dx), iy = safeRcp(dy), iz = safeRcp(dz);
-    const WtRay wr = wtRay(dx, dy, dz);
-    float bestT = tmax, bestB1 = 0.f, bestB2 = 0.f;
-    uint32_t bestPrim = 0xFFFFFFFFu;
-    bool done = false;
-    int2 stack[kStackDepth];
-    int sp = 0;
-    int32_t node = root;   // a scene's root in a combined node array (0 for a single scene)
-
-    auto leaf = [&](int32_t ref) {
-        const uint32_t v = (uint32_t)~ref;
-        const uint32_t first = v >> 4, count = (v & 15u) + 1u;
-        for (uint32_t k = first; k < first + count; ++k) {
-            const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
-            ++triTests;
-            const TriHit h = watertight(ox, oy, oz, wr, v0, v1, v2);
-            if (!h.hit || !(h.t >= tmin) || !(h.t <= bestT)) continue;
-            const uint32_t prim = __float_as_uint(v0.w);
-            if (ANY) {
-                bestT = h.t;
-                bestPrim = prim;
-                done = true;
-                return;
-            }
-            if (h.t < bestT || prim < bestPrim) {
-                bestT = h.t;
-                bestPrim = prim;
-                bestB1 = h.b1;
-                bestB2 = h.b2;
-            }
-        }
-    };
-
-    for (;;) {
-        ++nodeVisits;
-        const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
-        const int4 r = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
-        const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
-        const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
-        float tl = 0.f, tr = 0.f;
-        bool hl = r.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
-        bool hr = r.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
-        if (hl && r.x < 0) { leaf(r.x); hl = false; if (ANY && done) break; }
-        if (hr && r.y < 0) { leaf(r.y); hr = false; if (ANY && done) break; }
-        if (hl && hr) {
-            const bool leftNear = tl <= tr;
-            if (sp < stackCap && sp < kStackDepth) stack[sp++] = make_int2(leftNear ? r.y : r.x, __float_as_int(leftNear ? tr : tl));
-            else overflow = 1;
-            node = leftNear ? r.x : r.y;
-            continue;
-        }
-        if (hl) { node = r.x; continue; }
-        if (hr) { node = r.y; continue; }
-        // pop the nearest pending node that can still hold a closer hit
-        bool found = false;
-        while (sp > 0) {
-            const int2 e = stack[--sp];
-            if (__int_as_float(e.y) <= bestT * kTfarScale) { node = e.x; found = true; break; }
-        }
-        if (!found) break;
-    }
-    res.prim = bestPrim;
-    res.t = bestT;
-    res.b1 = bestB1;
-    res.b2 = bestB2;
-    return res;
-}
-
-// ---- dynamic-fetch traversal (Aila & Laine, "Understanding the Efficiency of Ray Traversal on
-// GPUs", HPG 2009) ---------------------------------------------------------------------------------
-// One lane's ray in flight: its traversal state between node visits.  The visit order is that of
-// traverse(), so the hit found is the same.
+// ---- traversal state and steps; dynamic fetch (Aila & Laine, "Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009) -------------------------------------------------------------------
+// One lane's ray in flight: its traversal state between steps.  Any visit order finds the same
+// closest hit: boxes are culled only beyond the current closest distance (with the kTfarScale
+// margin) and equal distances resolve to the lowest triangle id.
 constexpr int32_t kTravDone = -2147483647 - 1;   // `node` of a ray that cannot hit anything
 
 struct TravLane {
@@ -230,80 +144,120 @@ struct TravLane {
         wr = wtRay(dx, dy, dz);
     }
 
-    // One node visit (and the triangles of the leaves it hits); true when the ray has finished.
-    template <bool ANY>
-    __device__ __forceinline__ bool step(const float4* __restrict__ nodes, const float4* __restrict__ tris, int2* stack, int stackCap,
-                                         uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow) {
-        if (node == kTravDone) return true;
-        ++nodeVisits;
-        const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
-        const int4 rr = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
-        const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
-        const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
-        float tl = 0.f, tr = 0.f;
-        bool hl = rr.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
-        bool hr = rr.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const bool h = side ? hr : hl;
-            const int32_t ref = side ? rr.y : rr.x;
-            if (!h || ref >= 0) continue;
-            if (side) hr = false;
-            else hl = false;
-            const uint32_t v = (uint32_t)~ref;
-            const uint32_t first = v >> 4, count = (v & 15u) + 1u;
-            for (uint32_t k = first; k < first + count; ++k) {
-                const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
-                ++triTests;
-                const TriHit th = watertight(ox, oy, oz, wr, v0, v1, v2);
-                if (!th.hit || !(th.t >= tmin) || !(th.t <= bestT)) continue;
-                const uint32_t prim = __float_as_uint(v0.w);
-                if (ANY) {
-                    bestT = th.t;
-                    bestPrim = prim;
-                    return true;
-                }
-                if (th.t < bestT || prim < bestPrim) {
-                    bestT = th.t;
-                    bestPrim = prim;
-                    bestB1 = th.b1;
-                    bestB2 = th.b2;
-                }
-            }
-        }
-        if (hl && hr) {
-            const bool leftNear = tl <= tr;
-            if (sp < stackCap && sp < kStackDepth) stack[sp++] = make_int2(leftNear ? rr.y : rr.x, __float_as_int(leftNear ? tr : tl));
-            else overflow = 1;
-            node = leftNear ? rr.x : rr.y;
-            return false;
-        }
-        if (hl) {
-            node = rr.x;
-            return false;
-        }
-        if (hr) {
-            node = rr.y;
-            return false;
-        }
-        // pop the nearest pending node that can still hold a closer hit
+    // The nearest pending node (inner or leaf) that can still hold a closer hit, or kTravDone.
+    __device__ __forceinline__ int32_t pop(const int2* stack) {
         while (sp > 0) {
             const int2 e = stack[--sp];
-            if (__int_as_float(e.y) <= bestT * kTfarScale) {
-                node = e.x;
-                return false;
+            if (__int_as_float(e.y) <= bestT * kTfarScale) return e.x;
+        }
+        return kTravDone;
+    }
+
+    // Tests the triangles of leaf `ref`; true when an any-hit query has found its hit.
+    template <bool ANY>
+    __device__ __forceinline__ bool testLeaf(const float4* __restrict__ tris, int32_t ref, uint32_t& triTests) {
+        const uint32_t v = (uint32_t)~ref;
+        const uint32_t first = v >> 4, count = (v & 15u) + 1u;
+        for (uint32_t k = first; k < first + count; ++k) {
+            const float4 v0 = __ldg(tris + 3 * k), v1 = __ldg(tris + 3 * k + 1), v2 = __ldg(tris + 3 * k + 2);
+            ++triTests;
+            const TriHit th = watertight(ox, oy, oz, wr, v0, v1, v2);
+            if (!th.hit || !(th.t >= tmin) || !(th.t <= bestT)) continue;
+            const uint32_t prim = __float_as_uint(v0.w);
+            if (ANY) {
+                bestT = th.t;
+                bestPrim = prim;
+                return true;
+            }
+            if (th.t < bestT || prim < bestPrim) {
+                bestT = th.t;
+                bestPrim = prim;
+                bestB1 = th.b1;
+                bestB2 = th.b2;
             }
         }
-        return true;
+        return false;
+    }
+
+    // One step in while-while form with speculative leaf postponement (Aila & Laine 2009): inner
+    // nodes are visited until every lane of the warp holds a leaf to test (a lane that reaches a
+    // leaf first keeps it and goes on with the next inner node), then each lane tests its leaves.
+    // Leaves are nodes of the traversal order here (pushed and popped like inner nodes); the closest
+    // hit found is the same.  True when the ray has finished.
+    template <bool ANY>
+    __device__ __forceinline__ bool stepWW(const float4* __restrict__ nodes, const float4* __restrict__ tris, int2* stack, int stackCap,
+                                           uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow) {
+        int32_t leaf = 0;   // the postponed leaf (a negative reference), 0: none
+        while (node >= 0) {
+            ++nodeVisits;
+            const float4 a = __ldg(nodes + 4 * node), b = __ldg(nodes + 4 * node + 1), c = __ldg(nodes + 4 * node + 2);
+            const int4 rr = __ldg(reinterpret_cast<const int4*>(nodes) + 4 * node + 3);
+            const float lmn[3] = {a.x, a.y, a.z}, lmx[3] = {a.w, b.x, b.y};
+            const float rmn[3] = {b.z, b.w, c.x}, rmx[3] = {c.y, c.z, c.w};
+            float tl = 0.f, tr = 0.f;
+            const bool hl = rr.x != plt::kNoChild && slab(lmn, lmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tl);
+            const bool hr = rr.y != plt::kNoChild && slab(rmn, rmx, ox, oy, oz, ix, iy, iz, tmin, bestT, tr);
+            if (hl && hr) {
+                const bool leftNear = tl <= tr;
+                if (sp < stackCap && sp < kStackDepth) stack[sp++] = make_int2(leftNear ? rr.y : rr.x, __float_as_int(leftNear ? tr : tl));
+                else overflow = 1;
+                node = leftNear ? rr.x : rr.y;
+            } else if (hl) {
+                node = rr.x;
+            } else if (hr) {
+                node = rr.y;
+            } else {
+                node = pop(stack);
+            }
+            if (node < 0 && node != kTravDone && leaf == 0) {
+                leaf = node;
+                node = pop(stack);
+            }
+            if (!__any_sync(__activemask(), leaf == 0)) break;
+        }
+        while (leaf < 0) {
+            if (testLeaf<ANY>(tris, leaf, triTests)) return true;
+            leaf = 0;
+            if (node < 0 && node != kTravDone) {
+                leaf = node;
+                node = pop(stack);
+            }
+        }
+        return node == kTravDone;
     }
 };
 
+// Stack traversal of the two-wide BVH for one ray: closest hit with tmin <= t <= tmax (ties to
+// the lowest triangle id), or, with ANY, the first hit found (TraceRay with
+// ACCEPT_FIRST_HIT_AND_END_SEARCH).  The ray's lane runs while-while steps (TravLane::stepWW) until
+// it has finished, so the lanes of a warp tracing together test their leaves together.  Counts node
+// visits and triangle tests; sets `overflow` when the fixed-depth stack (or the caller's smaller
+// cap, stackCap) overflowed: the result is then possibly not the closest.
+template <bool ANY>
+__device__ __forceinline__ TraceResult traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris, float ox, float oy,
+                                                float oz, float dx, float dy, float dz, float tmin, float tmax,
+                                                uint32_t& nodeVisits, uint32_t& triTests, uint32_t& overflow, int32_t root = 0,
+                                                int stackCap = kStackDepth) {
+    TravLane L;
+    L.start(ox, oy, oz, dx, dy, dz, tmin, tmax, root);
+    int2 stack[kStackDepth];
+    while (!L.template stepWW<ANY>(nodes, tris, stack, stackCap, nodeVisits, triTests, overflow)) {
+    }
+    TraceResult res;
+    res.prim = L.bestPrim;
+    res.t = L.bestT;
+    res.b1 = L.bestB1;
+    res.b2 = L.bestB2;
+    return res;
+}
+
 // Lanes of a warp whose ray has finished take new rays together once at least this many are idle
 // (or the whole warp is).  Measured on 2^20 random closest-hit rays of a 1.04 M-triangle scene
-// (rays/s): 1 lane 1.36 G, 4 1.46 G, 8 1.47 G, 16 1.43 G, 32 1.18 G; 1024^2 primary rays 1.68,
-// 2.07, 2.22, 2.20 and 2.33 G.
+// (rays/s) with one node visit per step: 1 lane 1.36 G, 4 1.46 G, 8 1.47 G, 16 1.43 G, 32 1.18 G
+// (1024^2 primary rays 1.68, 2.07, 2.22, 2.20, 2.33 G); with while-while steps (stepWW): 4 lanes
+// 2.00 G, 8 2.00 G, 16 2.00 G (primary 2.79, 2.89, 3.06 G).
 #ifndef PLT_TRACE_REFILL
-#define PLT_TRACE_REFILL 8
+#define PLT_TRACE_REFILL 16
 #endif
 
 // A ray handed to dynamicTraversal: origin, direction, [tmin, tmax] and the BVH root.
@@ -312,8 +266,8 @@ struct TravRay {
     int32_t root;
 };
 
-// Traces rays [begin, end) with one ray per lane and dynamic fetch: every loop iteration visits one
-// node per active lane; a lane whose ray r has finished calls finish(r, prim, t, b1, b2) and goes
+// Traces rays [begin, end) with one ray per lane and dynamic fetch: every loop iteration is one
+// while-while step (TravLane::stepWW) per active lane; a lane whose ray r has finished calls finish(r, prim, t, b1, b2) and goes
 // idle, and idle lanes are refilled together (fetch(r) returns ray r's TravRay) from the shared
 // counter `next` (initialised to begin by the caller, then a __syncthreads), so a warp keeps its
 // lanes busy instead of waiting for the longest ray of a fixed set of 32.  Whole warps only.
@@ -346,7 +300,7 @@ __device__ __forceinline__ void dynamicTraversal(const float4* __restrict__ node
             }
         }
         if (ray == kNoRay) continue;
-        if (L.template step<ANY>(nodes, tris, stack, stackCap, nodeVisits, triTests, overflow)) {
+        if (L.template stepWW<ANY>(nodes, tris, stack, stackCap, nodeVisits, triTests, overflow)) {
             finish(ray, L.bestPrim, L.bestT, L.bestB1, L.bestB2);
             ray = kNoRay;
         }
