@@ -1276,6 +1276,33 @@ template <int H> PLT_DI void coherenceDebug(const DBeam<H>& b, float k, float& a
     aniso = 1.f - sqrtf((s1 + s2) / 2.f) / sqrtf((s1 - s2) / 2.f);
 }
 
+// One vertex of a forward replay: the beam propagated to the vertex (at msPos for a manifold
+// vertex) and replaced by the BSDF's response towards qwo, with the lambda pdfs of spectral MIS
+// (the body of forwardUnwind / manifoldForwardUnwind, pltpt_solve.rt.slang:48-93).
+template <int H>
+PLT_DI void replayVertex(const PtParams& P, uint32_t qprim, float qb1, float qb2, f3 qwo, uint32_t qlobe, bool msVertex, f3 msPos,
+                         PBeam<H>& pb, const Ctx& c, bool hwssMis, uint32_t& evals) {
+    VData qv = vertexData(P, qprim, qb1, qb2);
+    if (msVertex) qv.posW = msPos;
+    const uint32_t qmid = __ldg(P.triMat + qprim);
+    const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
+    propagate(pb, qsd.posW);
+    const DevMaterial* __restrict__ qm = P.mats + qmid;
+    const uint32_t qtype = __ldg(&qm->type);
+    ptEval<H>(qm, qtype, c, qsd, qwo, qlobe, pb.b);
+    ++evals;
+    if (hwssMis) {
+        float lp[H];
+        ptLambdaPdf<H>(qm, qtype, qsd, qwo, qlobe, pb.b, lp);
+#pragma unroll
+        for (int j = 0; j < H; ++j) pb.spdf[j] *= lp[j];
+    }
+}
+
+template <int H>
+PLT_DI void replayFinish(const PtParams& P, const PtScene& S, int p, const Bnc<H>& bounce, PBeam<H>& pb, bool hwssMis, float& Lr, float& Lg,
+                         float& Lb, DebugAcc* dbg);
+
 // Forward replay of one beam source of vertex p and its measurement (pltpt_solve.rt.slang:48-147):
 // the manifold vertices (last to first, manifoldForwardUnwind :80-93), the current vertex (NEE,
 // non-delta lobes), then vertices p-1 .. 0, the camera polariser and spectrumToRgb.  Adds the
@@ -1308,22 +1335,17 @@ PLT_DI void replayMeasure(const PtParams& P, const PtScene& S, uint32_t pid, int
             const Bnc<H> bq = readBounce<H>(P, pid, q);
             qprim = bq.prim; qlobe = bq.lobe; qb1 = bq.b1; qb2 = bq.b2; qwo = bq.wi;
         }
-        VData qv = vertexData(P, qprim, qb1, qb2);
-        if (msVertex) qv.posW = msPos;
-        const uint32_t qmid = __ldg(P.triMat + qprim);
-        const SD qsd = prepareSD(qv, __ldg(P.matProps + qmid).x, -pb.b.r);
-        propagate(pb, qsd.posW);
-        const DevMaterial* __restrict__ qm = P.mats + qmid;
-        const uint32_t qtype = __ldg(&qm->type);
-        ptEval<H>(qm, qtype, c, qsd, qwo, qlobe, pb.b);
-        ++evals;
-        if (hwssMis) {
-            float lp[H];
-            ptLambdaPdf<H>(qm, qtype, qsd, qwo, qlobe, pb.b, lp);
-#pragma unroll
-            for (int j = 0; j < H; ++j) pb.spdf[j] *= lp[j];
-        }
+        replayVertex<H>(P, qprim, qb1, qb2, qwo, qlobe, msVertex, msPos, pb, c, hwssMis, evals);
     }
+    replayFinish<H>(P, S, p, bounce, pb, hwssMis, Lr, Lg, Lb, dbg);
+}
+
+// The measurement that ends a forward replay (pltpt_solve.rt.slang:96-147): the beam propagated to
+// the camera, the camera polariser, spectral MIS or the component count, spectrumToRgb; adds the
+// contribution to (Lr, Lg, Lb).
+template <int H>
+PLT_DI void replayFinish(const PtParams& P, const PtScene& S, int p, const Bnc<H>& bounce, PBeam<H>& pb, bool hwssMis, float& Lr, float& Lg,
+                         float& Lb, DebugAcc* dbg) {
     // measure (no camera polarizer unless set)
     if (!(P.opt & plt::kPtUseDirect) && p <= 1) return;
     if (dbg) {
@@ -1523,8 +1545,14 @@ PLT_DI bool deferReplay(const PtParams& P, uint32_t pid, int p, bool evalCurrent
 
 // MNEE = false compiles the solve kernel without manifold sampling (the do_mnee = 0 pass): the
 // occluder search and the task hand-off would otherwise enlarge the kernel for every option set.
+// Resident CTAs of 128 threads per SM the solve kernel is compiled for: 16, the SM's 64 warps, at
+// 32 registers (the rest of its state spills to local memory, which stays in L1).  Measured per
+// 1024^2 frame with the walk kernel at 5 (three runs, each against its own baseline): 1 (228
+// registers, 2 CTAs) 16.34 ms, 5 14.93, 7 14.06, 8 13.83; 8 14.18, 10 13.77, 12 13.54; 10 13.61,
+// 12 13.72, 14 12.99, 16 12.98.  The kernel is latency-bound (traversal, scattered path records),
+// and the extra warps hide more than the spills cost.
 #ifndef PLT_SOLVE_MIN_BLOCKS
-#define PLT_SOLVE_MIN_BLOCKS 1
+#define PLT_SOLVE_MIN_BLOCKS 16
 #endif
 template <int H, bool MNEE>
 __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const PtParams P) {
@@ -1884,8 +1912,13 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
 // Finishes the sample exactly as the solve kernel would (pltpt_solve.rt.slang:293-366: the walk,
 // the beam's new direction, 1 / pdf, the MIS weight, the manifold replay and the measurement) and
 // adds it to the pixel's accumulator.
+// Resident CTAs per SM of the walk kernel (96 registers): 1 (128 registers) 16.05 ms per frame, 5
+// 14.77 ms, 6 14.92 ms.
+#ifndef PLT_MNEE_MIN_BLOCKS
+#define PLT_MNEE_MIN_BLOCKS 5
+#endif
 template <int H>
-__global__ void __launch_bounds__(128) ptMneeKernel(const PtParams P) {
+__global__ void __launch_bounds__(128, PLT_MNEE_MIN_BLOCKS) ptMneeKernel(const PtParams P) {
     static_assert(sizeof(MneeTask<H>) <= plt::kMneeTaskBytes, "MneeTask stride");
     const uint32_t count = min(*((volatile uint32_t*)P.mneeCount), P.mneeCap);
     const Ctx c{P.profiles, P.nProfiles, P.flags};
@@ -2068,38 +2101,94 @@ __global__ void __launch_bounds__(256) ptReplayScatterKernel(const PtParams P) {
         P.replayOrder[base[k] + atomicAdd(&h[k], 1u)] = i;
     }
 }
+// The replay kernel: each CTA takes 128 consecutive tasks of the sorted order (one counter), stages
+// them in shared memory and replays them vertex by vertex.  Before each vertex the CTA counting-sorts
+// its tasks by the material type of the vertex they evaluate next and thread t replays the task at
+// sorted position t, so a warp's lanes run one material's eval code at every vertex, not only at the
+// first (a task's later vertices are of any material).  Then each thread measures its own task.  A
+// task's arithmetic is that of replayMeasure, vertex for vertex.
+constexpr uint32_t kReplayCtaTasks = 128;
+#ifndef PLT_REPLAY_MIN_BLOCKS
+#define PLT_REPLAY_MIN_BLOCKS 1
+#endif
 template <int H>
-__global__ void __launch_bounds__(128) ptReplayKernel(const PtParams P) {
+__global__ void __launch_bounds__(kReplayCtaTasks, PLT_REPLAY_MIN_BLOCKS) ptReplayKernel(const PtParams P) {
     static_assert(sizeof(ReplayTask<H>) <= plt::kReplayTaskBytes, "ReplayTask stride");
+    __shared__ __align__(16) unsigned char stBytes[kReplayCtaTasks * sizeof(ReplayTask<H>)];
+    __shared__ uint32_t hist[17], taskAt[kReplayCtaTasks], chunk;
+    ReplayTask<H>* st = reinterpret_cast<ReplayTask<H>*>(stBytes);
     const uint32_t count = min(*((volatile uint32_t*)P.replayCount), P.replayCap);
     const Ctx c{P.profiles, P.nProfiles, P.flags};
     const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
+    const uint32_t n = P.npix;
+    const uint32_t t = threadIdx.x;
     uint32_t evals = 0;
-    MSData ms;
-    uint32_t* next = P.replaySort + 2 * plt::kReplayKeys;   // the warps' work counter
-    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* next = P.replaySort + 2 * plt::kReplayKeys;   // the CTAs' work counter
     for (;;) {
-        uint32_t c0 = 0;
-        if (lane == 0) c0 = atomicAdd(next, 32u);
-        c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+        if (t == 0) chunk = atomicAdd(next, kReplayCtaTasks);
+        __syncthreads();
+        const uint32_t c0 = chunk;
         if (c0 >= count) break;
-        const uint32_t i = c0 + lane;
-        if (i < count) {
-            const ReplayTask<H>& t = replayTask<H>(P, P.replayOrder[i]);
-            PBeam<H> pb = t.pb;
-            const uint32_t pid = t.pid;
-            const int p = (int)t.p;
+        const uint32_t nHere = min(kReplayCtaTasks, count - c0);
+        if (t < nHere) st[t] = replayTask<H>(P, P.replayOrder[c0 + t]);
+        __syncthreads();
+        const uint32_t pid = t < nHere ? st[t].pid : 0u;
+        const int p = t < nHere ? (int)st[t].p : 0;
+        const uint32_t ec = t < nHere ? st[t].evalCurrent : 0u;
+        const int total = t < nHere ? p + (int)ec : 0;
+        for (int r = 0;; ++r) {
+            // this thread's task: its vertex r (the current one first when it is evaluated, then
+            // p-1 .. 0) and the material type there; 16 once the task has no vertex r
+            uint32_t key = 16u;
+            if (r < total) {
+                const int q = (ec && r == 0) ? p : p - 1 - (r - (int)ec);
+                const uint32_t prim = P.bPrim[(size_t)q * n + pid];
+                key = prim < P.nTris ? min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), 15u) : 0u;
+            }
+            if (t < 17) hist[t] = 0u;
+            __syncthreads();
+            const uint32_t rank = key < 16u ? atomicAdd(&hist[key], 1u) : 0u;
+            __syncthreads();
+            if (t == 0) {
+                uint32_t run = 0;
+                for (int k = 0; k < 16; ++k) {
+                    const uint32_t h = hist[k];
+                    hist[k] = run;
+                    run += h;
+                }
+                hist[16] = run;
+            }
+            __syncthreads();
+            const uint32_t active = hist[16];
+            if (active == 0u) break;
+            if (key < 16u) taskAt[hist[key] + rank] = t;
+            __syncthreads();
+            if (t < active) {
+                ReplayTask<H>& T = st[taskAt[t]];
+                const int tp = (int)T.p;
+                const bool cur = T.evalCurrent && r == 0;
+                const int q = cur ? tp : tp - 1 - (r - (int)T.evalCurrent);
+                const Bnc<H> bq = readBounce<H>(P, T.pid, q);
+                PBeam<H> pb = T.pb;
+                replayVertex<H>(P, bq.prim, bq.b1, bq.b2, bq.wi, cur ? kLobeNonDelta : bq.lobe, false, mk3(0.f, 0.f, 0.f), pb, c, hwssMis, evals);
+                T.pb = pb;
+            }
+            __syncthreads();
+        }
+        if (t < nHere) {
             const uint32_t gp = P.pidBase + pid;
             const PtScene& S = P.scenes[sceneOf(P, gp)];
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
+            PBeam<H> pb = st[t].pb;
             float Lr = 0.f, Lg = 0.f, Lb = 0.f;
-            replayMeasure<H>(P, S, pid, p, bounce, pb, ms, 0, mk3(0.f, 0.f, 0.f), t.evalCurrent != 0, c, hwssMis, Lr, Lg, Lb, evals);
+            replayFinish<H>(P, S, p, bounce, pb, hwssMis, Lr, Lg, Lb, nullptr);
             if (Lr != 0.f || Lg != 0.f || Lb != 0.f) {
                 atomicAdd(P.accum + 3 * (size_t)gp, (double)Lr);
                 atomicAdd(P.accum + 3 * (size_t)gp + 1, (double)Lg);
                 atomicAdd(P.accum + 3 * (size_t)gp + 2, (double)Lb);
             }
         }
+        __syncthreads();   // the staged tasks and `chunk` are read before the next chunk replaces them
     }
     unsigned long long s2 = evals;
     for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xFFFFFFFFu, s2, o);
@@ -2139,12 +2228,12 @@ cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, c
         static int bpsR = -1;
         if (bpsR < 0) {
             int b = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptReplayKernel<H>, 128, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ptReplayKernel<H>, kReplayCtaTasks, 0);
             bpsR = b > 0 ? b : 1;
         }
         ptReplayCountKernel<H><<<numSMs, 256, 0, stream>>>(p);
         ptReplayScatterKernel<H><<<numSMs, 256, 0, stream>>>(p);
-        ptReplayKernel<H><<<(uint32_t)numSMs * (uint32_t)bpsR, 128, 0, stream>>>(p);
+        ptReplayKernel<H><<<(uint32_t)numSMs * (uint32_t)bpsR, kReplayCtaTasks, 0, stream>>>(p);
     }
     return cudaGetLastError();
 }
