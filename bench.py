@@ -280,11 +280,13 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
 
     Reported: both convergence curves (spp, seconds, relMSE, trimmed relMSE); on the trimmed relMSE,
     the directly measured time each tracer needs to reach the lowest error both reach (training time
-    included for the learned one) and their ratio, and the time to relMSE 1e-3 of the tracer's own
-    error from the curve fitted as V / spp + R, where R is the reference's own contribution (it is
-    itself an analytic render, at ref_spp spp).  The plain relMSE is dominated by rare caustic and
-    grazing-grating fireflies (single pixels 10^3 x the reference), so it does not fall as 1/spp
-    within the budget and no fit is made on it."""
+    included for the learned one) and their ratio; the time to relMSE 1e-3 from the curve fitted as
+    V / spp + R (R the reference's own contribution: it is itself an analytic render, at ref_spp spp,
+    and dominates these curves, so this fit is unstable); and the headline, from the variance per spp
+    (each batch against the pooled mean of every render, see below), which needs no converged
+    reference.  The plain relMSE is dominated by rare caustic and grazing-grating fireflies (single
+    pixels 10^3 x the reference), so it does not fall as 1/spp within the budget and no fit is made
+    on it."""
     import numpy as np
     import torch
     from pltfalcor_gb300 import scene as S, spectra
@@ -297,7 +299,7 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
     cam = S.room_camera(W, H)
     out = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
 
-    def curve(ctx, ref, frame0):
+    def curve(ctx, ref, frame0, batches):
         acc = np.zeros((H, W, 3))
         spp, t_ms, pts = 0, 0.0, []
         ctx.render(cam, W, H, out, 1 << 26, 1, stream)     # warm-up (graph recording)
@@ -309,7 +311,9 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
             e1.record(stream)
             torch.cuda.synchronize()
             t_ms += e0.elapsed_time(e1)
-            acc += out[..., :3].double().cpu().numpy() * batch_spp
+            img = out[..., :3].double().cpu().numpy()
+            batches.append(img)
+            acc += img * batch_spp
             spp += batch_spp
             pts.append((spp, t_ms * 1e-3, relmse(acc / spp, ref), relmse(acc / spp, ref, trim=1e-3)))
         return pts, acc / spp
@@ -319,7 +323,8 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
     ctx.render(cam, W, H, out, 1 << 28, ref_spp, stream)
     torch.cuda.synchronize()
     ref = out[..., :3].double().cpu().numpy()
-    plain, img_p = curve(ctx, ref, 0)
+    batches_p, batches_l = [], []
+    plain, img_p = curve(ctx, ref, 0, batches_p)
     ctx.close()
     ctx = PLTContext(dict(base, learned_proposal=1, learned_proposal_prob=prob))
     ctx.load_scene(sc, prof)
@@ -329,7 +334,7 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
     hist = ctx.proposal_train(256, batch=65536, lr=1e-3, seed=1)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
-    learned, img_l = curve(ctx, ref, 0)
+    learned, img_l = curve(ctx, ref, 0, batches_l)
     st = ctx.check_status(stream)
     ctx.close()
 
@@ -351,6 +356,17 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
     level = max(min(m for _, _, _, m in plain), min(m for _, _, _, m in learned))
     first = lambda pts, extra: next(t for _, t, _, m in pts if m <= level) + extra
     tm_p, tm_l = first(plain, 0.0), first(learned, train_s)
+    # variance per spp without a converged reference: every batch of batch_spp frames is an
+    # independent estimate of the same image from either tracer (both are unbiased), so each batch's
+    # trimmed relMSE is taken against the pooled mean of all batches of both tracers and of the
+    # reference render (~100x the spp of one batch, so its own error is negligible); the median over
+    # a tracer's batches is its error at batch_spp, which falls as 1/spp.
+    pooled = (sum(batches_p) + sum(batches_l)) * batch_spp + ref * ref_spp
+    pooled /= (len(batches_p) + len(batches_l)) * batch_spp + ref_spp
+    e_p = float(np.median([relmse(b, pooled, trim=1e-3) for b in batches_p]))
+    e_l = float(np.median([relmse(b, pooled, trim=1e-3) for b in batches_l]))
+    tv_p = e_p * batch_spp / 1e-3 * ms_p * 1e-3
+    tv_l = e_l * batch_spp / 1e-3 * ms_l * 1e-3 + train_s
     curve = lambda pts: [[s, round(t, 4), round(m, 6), round(mt, 6)] for s, t, m, mt in pts[::max(1, len(pts) // 12)]] + \
         [[pts[-1][0], round(pts[-1][1], 4), round(pts[-1][2], 6), round(pts[-1][3], 6)]]
     return {"workload": "procedural room 1.04 M triangles, %dx%d, max depth 8, HWSS 4 + spectral MIS, NEE + MIS + manifold NEE, "
@@ -365,8 +381,13 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
             "measured_equal_relmse": {"metric": "relmse_trimmed_0.1%", "relmse": level, "time_plain_s": tm_p, "time_learned_s": tm_l,
                                       "speedup": tm_p / tm_l},
             "fit": {"metric": "relmse_trimmed_0.1%", "V_plain": float(Vp), "V_learned": float(Vl), "R_reference": float(R)},
-            "time_to_relmse_1e-3_plain_s": t_p, "time_to_relmse_1e-3_learned_s": t_l,
-            "speedup": (t_p / t_l) if (t_p and t_l) else None}
+            "reference_fit": {"time_to_relmse_1e-3_plain_s": t_p, "time_to_relmse_1e-3_learned_s": t_l,
+                              "speedup": (t_p / t_l) if (t_p and t_l) else None},
+            "variance_per_spp": {"metric": "relmse_trimmed_0.1% of one %d-spp batch against the pooled mean of all renders, median "
+                                           "over batches" % batch_spp,
+                                 "relmse_plain": e_p, "relmse_learned": e_l, "batches_plain": len(batches_p), "batches_learned": len(batches_l),
+                                 "time_to_relmse_1e-3_plain_s": tv_p, "time_to_relmse_1e-3_learned_s": tv_l},
+            "time_to_relmse_1e-3_plain_s": tv_p, "time_to_relmse_1e-3_learned_s": tv_l, "speedup": tv_p / tv_l}
 
 
 def scene_set_bench(dev, stream, count=64, frames=2):

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define PLT_ABI_VERSION 4u
+#define PLT_ABI_VERSION 5u
 #define PLT_MAX_HWSS 8u                 /* hero wavelengths per beam (reference: <= 4, Utils/HWSS.slang:4-9) */
 #define PLT_SPECTRAL_MAX_BINS 128u      /* SpectralProfile::kMaxBins */
 #define PLT_NO_SPECTRAL_PROFILE 0xFFFFFFFFu
@@ -50,7 +50,8 @@ typedef enum plt_status {
     PLT_CUDA_ERROR = 5,
     PLT_NOT_SUPPORTED = 6,
     PLT_BAD_MATERIAL = 7,
-    PLT_TOO_LARGE = 8
+    PLT_TOO_LARGE = 8,
+    PLT_BOUNDS_VIOLATION = 9   /* a PLT_BOUNDS_CHECK build found an index outside its buffer */
 } plt_status;
 
 /* MaterialType ids, Source/Falcor/Scene/Material/MaterialTypes.slang:36-53 */
@@ -505,12 +506,20 @@ plt_status plt_render_counters(plt_context* ctx, uint64_t* out, uint32_t n);
 plt_status plt_render_bounces(plt_context* ctx, uint32_t* prim, uint32_t* lobe, uint32_t* flags);
 
 /* Synchronises `stream`, then reports and clears the context's device status word, which every
- * launch since the previous check ORs into: PLT_BAD_MATERIAL (a material index out of range or of
- * an unknown type; those queries return zeros), PLT_NAN_INPUT (a non-finite direction or
- * wavelength), PLT_QUEUE_TIMEOUT (a bounded device wait gave up or a traversal stack overflowed).
- * Mirrors the reference's
- * logError/throw reporting (PLTPT.cpp:173,409), which has no device-side status. */
+ * launch since the previous check ORs into: PLT_BOUNDS_VIOLATION (a library built with
+ * -DPLT_BOUNDS_CHECK=1 found an index outside its buffer; see plt_last_bounds_violation),
+ * PLT_BAD_MATERIAL (a material index out of range or of an unknown type; those queries return
+ * zeros), PLT_NAN_INPUT (a non-finite direction or wavelength), PLT_QUEUE_TIMEOUT (a bounded device
+ * wait gave up or a traversal stack overflowed).  Mirrors the reference's logError/throw reporting
+ * (PLTPT.cpp:173,409), which has no device-side status. */
 plt_status plt_check_status(plt_context* ctx, void* stream);
+
+/* The first bounds violation of the launches that the last plt_check_status returning
+ * PLT_BOUNDS_VIOLATION covered (host pointer, 3 values): the site (1 queue entry, 2 path id, 3
+ * bounce record, 4 triangle, 5 material, 6 deferred task, 7 image accumulator, 8 batch query, 9
+ * sort permutation), the index and the buffer's bound; zeros when there was none.  Only a library
+ * built with -DPLT_BOUNDS_CHECK=1 checks indices (the default build does not). */
+plt_status plt_last_bounds_violation(const plt_context* ctx, uint32_t* out3);
 
 /* Learned MIS proposal (no counterpart in the reference, whose PLTPT samples only the analytic
  * BSDF samplers).  A conditional MLP 16 -> 64 -> 64 -> 64 -> 32 with SiLU maps the features of a

@@ -191,6 +191,13 @@ class PLTContext:
         s = C.c_void_p(stream.cuda_stream) if stream is not None else None
         return self.lib.plt_check_status(self.handle, s)
 
+    def last_bounds_violation(self):
+        """(site, index, bound) of the first violation the last check_status reported as
+        PLT_BOUNDS_VIOLATION (a -DPLT_BOUNDS_CHECK=1 build), zeros when none."""
+        out = (C.c_uint32 * 3)()
+        capi.check(self.lib.plt_last_bounds_violation(self.handle, out), "plt_last_bounds_violation")
+        return tuple(int(x) for x in out)
+
     # ---- PLTPT render pass ----
     def set_scene_shading(self, normals, tangents=None, tri_instance=None):
         n = np.ascontiguousarray(normals, np.float32)

@@ -131,12 +131,14 @@ EXPORTED_SYMBOLS = [
     "plt_spectral_profile_from_spd", "plt_write_exr", "plt_render_counters",
     "plt_set_env_map", "plt_clear_env_map", "plt_env_map_query",
     "plt_spectral_profiles_from_material", "plt_spectral_profile_for_emitter_type", "plt_set_analytic_lights",
-    "plt_bsdf_batch_host",
+    "plt_bsdf_batch_host", "plt_last_bounds_violation",
 ]
 NOALLOC_MAX_QUERIES = 1 << 20
 PROPOSAL_PARAMS = 11488
 PLT_TOO_LARGE = 8
 STATUS_NAMES[PLT_TOO_LARGE] = "PLT_TOO_LARGE"
+PLT_BOUNDS_VIOLATION = 9
+STATUS_NAMES[PLT_BOUNDS_VIOLATION] = "PLT_BOUNDS_VIOLATION"
 
 _lib = None
 
@@ -152,6 +154,7 @@ def load_library(path=LIB_PATH):
     vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
     sig = {
         "plt_abi_version": (u32, []),
+        "plt_last_bounds_violation": (i32, [vp, C.POINTER(C.c_uint32)]),
         "plt_status_string": (C.c_char_p, [i32]),
         "plt_options_default": (i32, [C.POINTER(Options)]),
         "plt_create": (i32, [C.POINTER(Options), C.POINTER(vp)]),

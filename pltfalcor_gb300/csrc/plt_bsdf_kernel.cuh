@@ -18,6 +18,7 @@
 //     moves to the queue with the most work left.  Each unit's code is specialised for its type at
 //     compile time.  The spectral tables are staged into shared memory once per CTA by a bulk
 //     asynchronous copy on an mbarrier.
+#include "plt_bounds.cuh"
 #include "plt_bsdf_query.cuh"
 #include "plt_ptx.cuh"
 
@@ -47,6 +48,9 @@ enum : uint32_t {
     C_WORDS = 160
 };
 static_assert(C_WORDS * 4 <= plt::kBsdfCtrlBytes, "control words exceed their scratch block");
+
+// entries of the sort permutation: whole tiles
+PLT_DI size_t permSlots(uint32_t n) { return ((size_t)n + plt::kBatchTile - 1) / plt::kBatchTile * plt::kBatchTile; }
 
 PLT_DI uint32_t lobeClass(uint32_t lobe) {
     const uint32_t l = lobe & 0xFFu;
@@ -182,7 +186,8 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kBatchItems; ++k) P.perm[base + offs[key[k]] + rank[k]] = (uint16_t)(k * kBatchThreads + tid);
+    for (int k = 0; k < kBatchItems; ++k)
+        P.perm[pltIdx(P.status, base + offs[key[k]] + rank[k], permSlots(n), kSitePerm)] = (uint16_t)(k * kBatchThreads + tid);
     // type t's range of this tile: [offs[t * kLobeClasses], start of type t + 1); the padding bucket
     // comes last, so its start is the tile's query count
     if (tid <= kTypeSlots) {
@@ -215,7 +220,7 @@ __device__ __forceinline__ void shadeUnit(const BatchParams& P, const Ctx& c, ui
     for (uint32_t pos = lo; pos < hi; pos += 32) {
         const uint32_t k = pos + lane;
         if (k < hi) {
-            const uint32_t idx = tileBase + __ldg(P.perm + tileBase + k);
+            const uint32_t idx = tileBase + __ldg(P.perm + pltIdx(P.status, tileBase + k, permSlots(P.q.n), kSitePerm));
             if (idx < P.q.n) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, __ldg(P.q.material + idx), T);
         }
     }

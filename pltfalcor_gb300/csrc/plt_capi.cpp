@@ -13,6 +13,7 @@
 #include "plt_internal.h"
 
 #include "plt_context.h"
+#include "plt_nvtx.h"
 
 namespace {
 
@@ -45,6 +46,7 @@ const char* plt_status_string(plt_status s) {
     case PLT_NOT_SUPPORTED: return "not supported";
     case PLT_BAD_MATERIAL: return "bad material";
     case PLT_TOO_LARGE: return "batch larger than the allocation-free scratch capacity";
+    case PLT_BOUNDS_VIOLATION: return "index outside its buffer (bounds-check build)";
     }
     return "unknown status";
 }
@@ -108,8 +110,8 @@ plt_status plt_create(const plt_options* options, plt_context** out) {
     }
     cudaError_t e = cudaGetDevice(&ctx->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->numSMs, cudaDevAttrMultiProcessorCount, ctx->device);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->dStatus, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dStatus, sizeof(uint32_t) * plt::kStatusWords);
+    if (e == cudaSuccess) e = cudaMemset(ctx->dStatus, 0, sizeof(uint32_t) * plt::kStatusWords);
     if (e != cudaSuccess) {
         const plt_status s = e == cudaErrorMemoryAllocation ? PLT_OOM : PLT_CUDA_ERROR;
         if (ctx->dStatus) cudaFree(ctx->dStatus);
@@ -255,6 +257,7 @@ plt_status plt_spectral_profile_from_samples(const float* wl, const float* value
 }
 
 plt_status plt_bsdf_batch(plt_context* ctx, const plt_bsdf_queries* q, const plt_bsdf_results* r, uint32_t ops, void* stream) {
+    const plt::NvtxRange range("bsdf_batch");
     plt::BatchParams p{};
     int numSMs = 0;
     const plt_status s = plt::fillBatchParams(ctx, q, r, ops, &p, &numSMs);
@@ -277,6 +280,12 @@ plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* 
     ctx->timing[0] = before_classify;
     ctx->timing[1] = before_shade;
     ctx->timing[2] = after_shade;
+    return PLT_OK;
+}
+
+plt_status plt_last_bounds_violation(const plt_context* ctx, uint32_t* out3) {
+    if (!ctx || !out3) return PLT_INVALID_ARG;
+    for (int k = 0; k < 3; ++k) out3[k] = ctx->boundsReport[k];
     return PLT_OK;
 }
 
@@ -334,6 +343,7 @@ plt_status plt_bsdf_sample(plt_context* c, const plt_bsdf_queries* q, const plt_
 plt_status plt_bsdf_lambda_pdf(plt_context* c, const plt_bsdf_queries* q, const plt_bsdf_results* r, void* s) { return plt_bsdf_batch(c, q, r, PLT_OP_LAMBDA_PDF, s); }
 
 static plt_status traceCommon(plt_context* ctx, const plt_rays* rays, const plt_hits* hits, uint32_t* occluded, bool any, void* stream) {
+    const plt::NvtxRange range(any ? "trace_any" : "trace_closest");
     if (!ctx || !rays) return PLT_INVALID_ARG;
     const plt_status ds = pltCheckDevice(ctx);
     if (ds != PLT_OK) return ds;
@@ -385,10 +395,15 @@ plt_status plt_scene_stats(const plt_context* ctx, uint32_t* out4) {
 // every launch since the last check) into a status, then clears it.
 plt_status plt_check_status(plt_context* ctx, void* stream) {
     if (!ctx) return PLT_INVALID_ARG;
-    uint32_t st = 0;
+    uint32_t w[plt::kStatusWords] = {};
     PLT_CUDA(ctx, cudaStreamSynchronize((cudaStream_t)stream));
-    PLT_CUDA(ctx, cudaMemcpy(&st, ctx->dStatus, sizeof(st), cudaMemcpyDeviceToHost));
-    PLT_CUDA(ctx, cudaMemset(ctx->dStatus, 0, sizeof(st)));
+    PLT_CUDA(ctx, cudaMemcpy(w, ctx->dStatus, sizeof(w), cudaMemcpyDeviceToHost));
+    PLT_CUDA(ctx, cudaMemset(ctx->dStatus, 0, sizeof(w)));
+    const uint32_t st = w[0];
+    if (st & plt::kStatusBoundsViolation) {
+        for (int k = 0; k < 3; ++k) ctx->boundsReport[k] = w[1 + k];
+        return PLT_BOUNDS_VIOLATION;
+    }
     if (st & (plt::kStatusCopyTimeout | plt::kStatusStackOverflow)) return PLT_QUEUE_TIMEOUT;
     if (st & (plt::kStatusBadMaterialId | plt::kStatusUnknownType)) return PLT_BAD_MATERIAL;
     if (st & plt::kStatusNanInput) return PLT_NAN_INPUT;

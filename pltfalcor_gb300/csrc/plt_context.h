@@ -50,6 +50,7 @@ struct plt_context {
     uint32_t nTris = 0;
     plt::BvhBuildStats bvhStats{};
     int lastCudaError = 0;
+    uint32_t boundsReport[3] = {0u, 0u, 0u};   // the last reported bounds violation (site, index, bound)
     void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
     plt::ShadeLaunchCache shadeLaunch = {{(size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1,
                                           (size_t)-1, (size_t)-1},

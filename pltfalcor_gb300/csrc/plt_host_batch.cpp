@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "plt_context.h"
+#include "plt_nvtx.h"
 
 namespace {
 
@@ -74,6 +75,7 @@ void pltReleaseHostPipeline(plt_context* ctx) {
 extern "C" {
 
 plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, const plt_bsdf_results* hr, uint32_t ops, void* stream) {
+    const plt::NvtxRange range("bsdf_batch_host");
     if (!ctx || !hq || !hr) return PLT_INVALID_ARG;
     if (hq->hwss < 1 || hq->hwss > PLT_MAX_HWSS) return PLT_INVALID_ARG;
     if (hq->hwss > 4 && hq->hwss != 8) return PLT_NOT_SUPPORTED;

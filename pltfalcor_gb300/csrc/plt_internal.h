@@ -19,6 +19,10 @@ constexpr uint32_t kStatusNanInput = 0x2u;
 constexpr uint32_t kStatusUnknownType = 0x4u;
 constexpr uint32_t kStatusCopyTimeout = 0x8u;
 constexpr uint32_t kStatusStackOverflow = 0x10u;
+constexpr uint32_t kStatusBoundsViolation = 0x20u;   // PLT_BOUNDS_CHECK builds: an index outside its buffer
+// The context's device status block: [0] the status bits above; [1..3] the first bounds violation
+// of a PLT_BOUNDS_CHECK build (site, index, bound).
+constexpr uint32_t kStatusWords = 4;
 
 // One batch of ray queries against the context's BVH (device pointers).
 struct TraceParams {

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "plt_context.h"
+#include "plt_nvtx.h"
 
 namespace plt {
 cudaError_t launchProposalData(const pltdev::DevMaterial* mats, const float4* matFeat, const uint2* matProps, const uint32_t* enabled,
@@ -171,6 +172,7 @@ plt_status plt_proposal_adam_step(plt_context* ctx, const float* grad, float lr,
 }
 
 plt_status plt_proposal_train(plt_context* ctx, uint32_t steps, uint32_t batch, float lr, uint32_t seed, float* loss_history, void* stream) {
+    const plt::NvtxRange range("proposal_train");
     if (!ctx || batch == 0 || !(lr > 0.f)) return PLT_INVALID_ARG;
     if (!ctx->propReady) {
         const plt_status s = plt_proposal_init(ctx, seed);

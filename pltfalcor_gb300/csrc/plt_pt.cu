@@ -4,6 +4,7 @@
 #include <algorithm>
 
 #define PLT_PT_SAMPLE_PASS
+#include "plt_nvtx.h"
 #include "plt_pt.cuh"
 
 namespace pltdev {
@@ -47,7 +48,11 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
     }
     auto blocks = [&](int occ, uint32_t want) { return (uint32_t)numSMs * (want ? std::min<uint32_t>(want, (uint32_t)occ) : (uint32_t)occ); };
     const uint32_t need = (p.nWave + 127) / 128;
-    pltdev::ptInitKernel<<<std::min<uint32_t>(need, blocks(bpsInit, 0)), 128, 0, stream>>>(p);
+    {
+        const NvtxRange r("pt_init");
+        pltdev::ptInitKernel<<<std::min<uint32_t>(need, blocks(bpsInit, 0)), 128, 0, stream>>>(p);
+    }
+    const NvtxRange rSample("pt_segments");
     // each segment: its closest hits traced with dynamic fetch, then the segment kernel shades them
     const uint32_t gridT = std::min<uint32_t>(need, blocks(bpsSegTrace, 0));
     if (p.opt & kPtLearned) {
@@ -64,6 +69,7 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
         }
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const NvtxRange rSolve("pt_solve");
     PtParams q = p;
     q.order = nullptr;
     // path_order 0: sort waves of at least 2^18 paths (small waves are latency-bound and keep the

@@ -19,6 +19,8 @@
 #include "plt_bsdf_query.cuh"
 #include "plt_envmap.cuh"
 #include "plt_mlp.cuh"
+#include "plt_bounds.cuh"
+#include "plt_nvtx.h"
 #include "plt_trace.cuh"
 
 namespace pltdev {
@@ -94,6 +96,7 @@ struct VData {
 };
 // computeVertexData, Scene/Scene.slang:530-567 (identity world matrix)
 PLT_DI VData vertexData(const PtParams& P, uint32_t prim, float b1, float b2) {
+    prim = (uint32_t)pltIdx(P.status, prim, P.nTris, kSitePrim);
     const float w0 = 1.f - b1 - b2;
     const uint32_t i0 = __ldg(P.idx + 3 * prim), i1 = __ldg(P.idx + 3 * prim + 1), i2 = __ldg(P.idx + 3 * prim + 2);
     const f3 p0 = ld3s(P.pos, i0), p1 = ld3s(P.pos, i1), p2 = ld3s(P.pos, i2);
@@ -529,7 +532,7 @@ __global__ void __launch_bounds__(128) ptSegTraceKernel(const PtParams P, uint32
     dynamicTraversal<false>(
         reinterpret_cast<const float4*>(P.nodes), P.tris, kStackDepth, end, &next,
         [&](uint32_t slot) {
-            const uint32_t pid = it == 0 ? slot : qin[slot];
+            const uint32_t pid = (uint32_t)pltIdx(P.status, it == 0 ? slot : qin[pltIdx(P.status, slot, n, kSiteQueue)], n, kSitePath);
             const f3 org = ldPlane3(P.org, pid, n), dir = ldPlane3(P.dir, pid, n);
             return TravRay{org.x, org.y, org.z, dir.x, dir.y, dir.z, 0.f, kFltMax, (int32_t)__ldg(&P.scenes[sceneOf(P, P.pidBase + pid)].root)};
         },
@@ -583,6 +586,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
         uint2 props = make_uint2(0u, 0u);
         float rcpThp = 1.f;
         auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe, uint32_t extra) {
+            len = (uint32_t)pltIdx(P.status, len, (size_t)P.maxBounces + 1, kSiteBounce);
             const size_t o = (size_t)len * n + pid;
             P.bFlags[o] = flags | extra;
             P.bPrim[o] = prim;
@@ -597,7 +601,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
             ++recorded;
         };
         if (act) {
-            pid = it == 0 ? slot : qin[slot];
+            pid = (uint32_t)pltIdx(P.status, it == 0 ? slot : qin[pltIdx(P.status, slot, n, kSiteQueue)], n, kSitePath);
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
             sg.tiny = (P.opt & plt::kPtTinySg) != 0;
             org = ldPlane3(P.org, pid, n);
@@ -618,7 +622,7 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
                     break;
                 }
                 const VData v = vertexData(P, h.prim, h.b1, h.b2);
-                mid = __ldg(P.triMat + h.prim);
+                mid = (uint32_t)pltIdx(P.status, __ldg(P.triMat + h.prim), P.nMats, kSiteMaterial);
                 props = __ldg(P.matProps + mid);
                 sd = prepareSD(v, props.x, wi);
                 if ((props.x & plt::kPropAlphaZero) && (P.opt & plt::kPtAlphaMask)) {   // alpha mask: continue the same ray
@@ -766,7 +770,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
         bool live = false;
         uint32_t pid = 0;
         if (slot < count) {
-            pid = it == 0 ? slot : qin[slot];
+            pid = (uint32_t)pltIdx(P.status, it == 0 ? slot : qin[pltIdx(P.status, slot, n, kSiteQueue)], n, kSitePath);
             SampleGen sg;
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
             sg.tiny = (P.opt & plt::kPtTinySg) != 0;
@@ -775,6 +779,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
             uint32_t flags = P.pflags[pid], len = P.plen[pid];
             const float wavelength = P.wl[pid];
             auto append = [&](uint32_t prim, float b1, float b2, f3 wi, uint32_t lobe) {
+                len = (uint32_t)pltIdx(P.status, len, (size_t)P.maxBounces + 1, kSiteBounce);
                 const size_t o = (size_t)len * n + pid;
                 P.bFlags[o] = flags;
                 P.bPrim[o] = prim;
@@ -800,7 +805,7 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
                     break;
                 }
                 const VData v = vertexData(P, h.prim, h.b1, h.b2);
-                const uint32_t mid = __ldg(P.triMat + h.prim);
+                const uint32_t mid = (uint32_t)pltIdx(P.status, __ldg(P.triMat + h.prim), P.nMats, kSiteMaterial);
                 const uint2 props = __ldg(P.matProps + mid);
                 const SD sd = prepareSD(v, props.x, wi);
                 if ((props.x & plt::kPropAlphaZero) && (P.opt & plt::kPtAlphaMask)) {   // alpha mask: continue the same ray
@@ -1223,6 +1228,8 @@ template <int H> struct Bnc {
 };
 template <int H> PLT_DI Bnc<H> readBounce(const PtParams& P, uint32_t pid, int p) {
     const uint32_t n = P.npix;
+    pid = (uint32_t)pltIdx(P.status, pid, n, kSitePath);
+    p = (int)pltIdx(P.status, (size_t)p, (size_t)P.maxBounces + 1, kSiteBounce);
     const size_t o = (size_t)p * n + pid;
     Bnc<H> b;
     b.prim = P.bPrim[o];
@@ -1570,8 +1577,8 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
     uint32_t evals = 0;
     MSData ms;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.nWave; slot += gridDim.x * blockDim.x) {
-        const uint32_t pid = P.order ? P.order[slot] : slot;
-        const uint32_t gp = P.pidBase + pid;
+        const uint32_t pid = (uint32_t)pltIdx(P.status, P.order ? P.order[pltIdx(P.status, slot, P.npix, kSiteQueue)] : slot, P.npix, kSitePath);
+        const uint32_t gp = (uint32_t)pltIdx(P.status, P.pidBase + pid, P.nTotal, kSiteAccum);
         const PtScene& S = P.scenes[sceneOf(P, gp)];
         const int32_t root = (int32_t)S.root;
         const uint32_t local = gp - S.pixelBase;
@@ -1928,7 +1935,7 @@ __global__ void __launch_bounds__(128, PLT_MNEE_MIN_BLOCKS) ptMneeKernel(const P
     uint32_t evals = 0;
     const MneeTask<H>* tasks = reinterpret_cast<const MneeTask<H>*>(P.mneeTasks);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const MneeTask<H>& t = tasks[P.mneeOrder ? P.mneeOrder[i] : i];
+        const MneeTask<H>& t = tasks[pltIdx(P.status, P.mneeOrder ? P.mneeOrder[pltIdx(P.status, i, P.mneeCap, kSiteTask)] : i, P.mneeCap, kSiteTask)];
         MSData ms = t.ms;
         const uint32_t pid = t.pid;
         const int p = (int)t.p;
@@ -1936,7 +1943,7 @@ __global__ void __launch_bounds__(128, PLT_MNEE_MIN_BLOCKS) ptMneeKernel(const P
         const bool distant = (t.curMS & 2u) != 0;
         const bool misHere = doMis && (t.curMS & 4u) == 0;
         const f3 msOrigin = t.msOrigin;
-        const uint32_t gp = P.pidBase + pid;
+        const uint32_t gp = (uint32_t)pltIdx(P.status, P.pidBase + pid, P.nTotal, kSiteAccum);
         const PtScene& S = P.scenes[sceneOf(P, gp)];
         if (!manifoldWalk(P, (int32_t)S.root, msOrigin, t.tposW, t.ldir, distant, ms, tc)) continue;
         const Bnc<H> bounce = readBounce<H>(P, pid, p);
@@ -2130,7 +2137,7 @@ __global__ void __launch_bounds__(kReplayCtaTasks, PLT_REPLAY_MIN_BLOCKS) ptRepl
         const uint32_t c0 = chunk;
         if (c0 >= count) break;
         const uint32_t nHere = min(kReplayCtaTasks, count - c0);
-        if (t < nHere) st[t] = replayTask<H>(P, P.replayOrder[c0 + t]);
+        if (t < nHere) st[t] = replayTask<H>(P, (uint32_t)pltIdx(P.status, P.replayOrder[pltIdx(P.status, c0 + t, P.replayCap, kSiteTask)], P.replayCap, kSiteTask));
         __syncthreads();
         const uint32_t pid = t < nHere ? st[t].pid : 0u;
         const int p = t < nHere ? (int)st[t].p : 0;
@@ -2176,7 +2183,7 @@ __global__ void __launch_bounds__(kReplayCtaTasks, PLT_REPLAY_MIN_BLOCKS) ptRepl
             __syncthreads();
         }
         if (t < nHere) {
-            const uint32_t gp = P.pidBase + pid;
+            const uint32_t gp = (uint32_t)pltIdx(P.status, P.pidBase + pid, P.nTotal, kSiteAccum);
             const PtScene& S = P.scenes[sceneOf(P, gp)];
             const Bnc<H> bounce = readBounce<H>(P, pid, p);
             PBeam<H> pb = st[t].pb;
@@ -2211,6 +2218,7 @@ cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, c
     if (mnee) ptSolveKernel<H, true><<<grid, 128, 0, stream>>>(p);
     else ptSolveKernel<H, false><<<grid, 128, 0, stream>>>(p);
     if (mnee && p.mneeTasks) {
+        const plt::NvtxRange r("pt_walks");
         static int bpsW = -1;
         if (bpsW < 0) {
             int b = 0;
@@ -2225,6 +2233,7 @@ cudaError_t launchSolve(const PtParams& p, const plt::PtLaunch& L, int numSMs, c
         ptMneeKernel<H><<<gw, 128, 0, stream>>>(p);
     }
     if (p.replayTasks) {
+        const plt::NvtxRange r("pt_replays");
         static int bpsR = -1;
         if (bpsR < 0) {
             int b = 0;

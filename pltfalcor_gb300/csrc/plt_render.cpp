@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "plt_context.h"
+#include "plt_nvtx.h"
 
 namespace {
 
@@ -399,11 +400,13 @@ plt_status plt_render(plt_context* ctx, const plt_camera* camera, uint32_t width
     v.height = height;
     v.camera = *camera;
     v.out_rgba = out_rgba;
+    const plt::NvtxRange range("render");
     return renderViews(ctx, &v, 1, frame_begin, frame_count, stream);
 }
 
 plt_status plt_render_scenes(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame_begin, uint32_t frame_count,
                              void* stream) {
+    const plt::NvtxRange range("render_scenes");
     return renderViews(ctx, views, n_views, frame_begin, frame_count, stream);
 }
 
@@ -427,6 +430,7 @@ plt_status plt_get_launch_shape(const plt_context* ctx, plt_launch_shape* shape)
 // on the caller's stream) over `frames` frames after one untimed frame that records its graph.
 plt_status plt_render_tune(plt_context* ctx, const plt_render_view* views, uint32_t n_views, uint32_t frame, uint32_t frames,
                            plt_launch_shape* best, float* best_ms, void* stream) {
+    const plt::NvtxRange range("render_tune");
     if (!ctx || !views || n_views == 0 || frames == 0) return PLT_INVALID_ARG;
     if (const plt_status ds = pltCheckDevice(ctx); ds != PLT_OK) return ds;
     uint64_t total = 0;

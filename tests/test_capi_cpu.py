@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(product_lib):
 
 
 def test_abi_version_and_status_strings(product_lib):
-    assert product_lib.plt_abi_version() == 4
+    assert product_lib.plt_abi_version() == 5
     assert product_lib.plt_status_string(0) == b"ok"
     assert product_lib.plt_status_string(7) == b"bad material"
 
