@@ -383,7 +383,7 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
             "fit": {"metric": "relmse_trimmed_0.1%", "V_plain": float(Vp), "V_learned": float(Vl), "R_reference": float(R)},
             "reference_fit": {"time_to_relmse_1e-3_plain_s": t_p, "time_to_relmse_1e-3_learned_s": t_l,
                               "speedup": (t_p / t_l) if (t_p and t_l) else None},
-            "variance_per_spp": {"metric": "relmse_trimmed_0.1% of one %d-spp batch against the pooled mean of all renders, median "
+            "variance_per_spp": {"metric": "relmse_trimmed_0.1%% of one %d-spp batch against the pooled mean of all renders, median "
                                            "over batches" % batch_spp,
                                  "relmse_plain": e_p, "relmse_learned": e_l, "batches_plain": len(batches_p), "batches_learned": len(batches_l),
                                  "time_to_relmse_1e-3_plain_s": tv_p, "time_to_relmse_1e-3_learned_s": tv_l},
