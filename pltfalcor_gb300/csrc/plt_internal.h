@@ -95,6 +95,8 @@ constexpr size_t kMneeTaskBytes = 320;
 // bytes reserved per deferred forward replay (a sourced beam at up to 8 wavelengths and its vertex)
 constexpr size_t kReplayTaskBytes = 288;
 // replay-order sort keys: vertices to evaluate (0..15) x material type of the first one (16)
+constexpr uint32_t kSegKeys = 16;         // segment shading order: the hit's material type, 15 for a miss
+constexpr uint32_t kSegSortWords = 48;    // per segment: kSegKeys counts, kSegKeys cursors, the work counter
 constexpr uint32_t kReplayKeys = 256;
 
 // One scene of a render: its BVH root in the combined node array, its light range in the combined
@@ -208,6 +210,8 @@ struct PtParams {
     uint32_t* queue1;             // [npix]
     uint32_t* segPrim;            // [npix] closest hit of each queue slot of the segment (ptSegTraceKernel), or null:
     float* segBary;               // [2][npix]   the segment kernels then trace inline
+    uint32_t* segOrder;           // [npix] the segment's queue slots sorted by the hit's material type, or null
+    uint32_t* segSort;            // [maxBounces + 1][kSegSortWords]: key counts, cursors, the shade kernel's work counter
     uint32_t* qcount;             // [maxBounces + 2]
     uint32_t* lenCount;           // [16 (maxBounces + 1)] paths per solve-order key (length, first-hit type)
     uint32_t* lenCursor;          // [16 (maxBounces + 1)]

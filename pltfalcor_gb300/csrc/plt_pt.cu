@@ -28,13 +28,15 @@ static void (*const kPlainBounce)(const PtParams, uint32_t) = pltdev::ptBounceAn
 cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, cudaStream_t stream) {
     if (p.nWave == 0) return cudaSuccess;
     // queue lengths, the manifold-walk count, the solve-order key histogram and its cursors, the
-    // walk-order keys, the replay count, the replay-order keys and the replay kernel's work counter
+    // walk-order keys, the replay count, the replay-order keys and the replay kernel's work counter,
+    // the segments' shading-order keys and work counters
     cudaError_t e = cudaMemsetAsync(p.qcount, 0, sizeof(uint32_t) * ((p.maxBounces + 1) * (1 + 2 * kSolveKeysPerLength) + 2 + 32 + 1 +
-                                                                      2 * kReplayKeys + 1), stream);
+                                                                      2 * kReplayKeys + 1 + kSegSortWords * (p.maxBounces + 1)), stream);
     if (e != cudaSuccess) return e;
     // shared memory of the learned variant: the network and one 32-row activation tile per warp
     constexpr size_t kLearnedSmem = sizeof(pltdev::mlp::SmemNet) + 4 * 32 * pltdev::mlp::kSWH * sizeof(pltdev::mlp::bf16);
     static int bpsInit = -1, bpsBounce = -1, bpsLearned = -1, bpsSegTrace = -1;
+    const uint32_t gridS = std::min<uint32_t>((p.nWave + 255) / 256, (uint32_t)numSMs * 2);
     if (bpsBounce < 0) {
         int b = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, pltdev::ptSegTraceKernel, 128, 0);
@@ -53,18 +55,21 @@ cudaError_t launchRenderFrame(const PtParams& p, const PtLaunch& L, int numSMs, 
         pltdev::ptInitKernel<<<std::min<uint32_t>(need, blocks(bpsInit, 0)), 128, 0, stream>>>(p);
     }
     const NvtxRange rSample("pt_segments");
-    // each segment: its closest hits traced with dynamic fetch, then the segment kernel shades them
+    // each segment: its closest hits traced with dynamic fetch (and counted by material type), the
+    // queue slots sorted by that type, then the segment kernel shades them in that order
     const uint32_t gridT = std::min<uint32_t>(need, blocks(bpsSegTrace, 0));
     if (p.opt & kPtLearned) {
         const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsLearned, L.segBlocksPerSM));
         for (uint32_t it = 0; it <= p.maxBounces; ++it) {
             if (p.segPrim) pltdev::ptSegTraceKernel<<<gridT, 128, 0, stream>>>(p, it);
+            if (p.segPrim && p.segOrder) pltdev::ptSegScatterKernel<<<gridS, 256, 0, stream>>>(p, it);
             pltdev::ptBounceKernel<true><<<gridB, 128, kLearnedSmem, stream>>>(p, it);
         }
     } else {
         const uint32_t gridB = std::min<uint32_t>(need, blocks(bpsBounce, L.segBlocksPerSM));
         for (uint32_t it = 0; it <= p.maxBounces; ++it) {
             if (p.segPrim) pltdev::ptSegTraceKernel<<<gridT, 128, 0, stream>>>(p, it);
+            if (p.segPrim && p.segOrder) pltdev::ptSegScatterKernel<<<gridS, 256, 0, stream>>>(p, it);
             kPlainBounce<<<gridB, 128, 0, stream>>>(p, it);
         }
     }

@@ -519,9 +519,16 @@ PLT_DI TraceResult segmentHit(const PtParams& P, uint32_t slot) {
 // keeps a warp's lanes full (a lane whose ray has finished takes the next one) where, inside the
 // segment kernel, every lane waited for the longest ray of its warp and then for the shading of
 // each other's materials.  Each CTA traces a contiguous share of the queue's slots.
+// The material-type key of a segment hit for the shading order (kSegKeys - 1 for a miss).
+PLT_DI uint32_t segKey(const PtParams& P, uint32_t prim) {
+    if (prim >= P.nTris) return plt::kSegKeys - 1u;
+    return min(__ldg(&P.mats[__ldg(P.triMat + prim)].type), plt::kSegKeys - 2u);
+}
+
 __global__ void __launch_bounds__(128) ptSegTraceKernel(const PtParams P, uint32_t it) {
-    __shared__ uint32_t next;
+    __shared__ uint32_t next, hist[plt::kSegKeys];
     const uint32_t n = P.npix;
+    if (threadIdx.x < plt::kSegKeys) hist[threadIdx.x] = 0u;
     const uint32_t count = it == 0 ? P.nWave : *((volatile uint32_t*)(P.qcount + it));
     const uint32_t* qin = (it & 1u) ? P.queue0 : P.queue1;
     const uint32_t per = (count + gridDim.x - 1) / gridDim.x;
@@ -540,10 +547,42 @@ __global__ void __launch_bounds__(128) ptSegTraceKernel(const PtParams P, uint32
             P.segPrim[slot] = prim;
             P.segBary[slot] = b1;
             P.segBary[n + slot] = b2;
+            if (P.segOrder) atomicAdd(&hist[segKey(P, prim)], 1u);
         },
         nv, tt, overflow);
     if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     addTraversalBytes(P, nv, tt);
+    if (P.segOrder) {
+        __syncthreads();
+        if (threadIdx.x < plt::kSegKeys && hist[threadIdx.x]) atomicAdd(P.segSort + it * plt::kSegSortWords + threadIdx.x, hist[threadIdx.x]);
+    }
+}
+
+// The segment's shading order: its queue slots counting-sorted by the hit's material type (keys
+// counted by ptSegTraceKernel), so the segment kernel's warps, which take consecutive positions of
+// this order from one counter, shade one material at a time and an SM's resident warps one or two.
+// Each block reserves its share of each key's positions after the exclusive prefix of the counts.
+__global__ void __launch_bounds__(256) ptSegScatterKernel(const PtParams P, uint32_t it) {
+    __shared__ uint32_t h[plt::kSegKeys], base[plt::kSegKeys];
+    const uint32_t count = it == 0 ? P.nWave : *((volatile uint32_t*)(P.qcount + it));
+    const uint32_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint32_t begin = min(blockIdx.x * per, count), end = min(begin + per, count);
+    uint32_t* cnt = P.segSort + it * plt::kSegSortWords;
+    if (threadIdx.x < plt::kSegKeys) h[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&h[segKey(P, P.segPrim[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < plt::kSegKeys) {
+        uint32_t prefix = 0;
+        for (uint32_t k = 0; k < threadIdx.x; ++k) prefix += cnt[k];
+        base[threadIdx.x] = h[threadIdx.x] ? prefix + atomicAdd(cnt + plt::kSegKeys + threadIdx.x, h[threadIdx.x]) : 0u;
+        h[threadIdx.x] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const uint32_t k = segKey(P, P.segPrim[i]);
+        P.segOrder[pltIdx(P.status, base[k] + atomicAdd(&h[k], 1u), count, kSiteQueue)] = i;
+    }
 }
 
 #ifndef PLT_BOUNCE_MIN_BLOCKS
@@ -569,8 +608,9 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t rounds = (count + stride - 1) / stride;
     for (uint32_t rr = 0; rr < rounds; ++rr) {
-        const uint32_t slot = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool act = slot < count;
+        const uint32_t pos = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool act = pos < count;
+        const uint32_t slot = act && P.segOrder ? P.segOrder[pos] : pos;   // the shading order when sorted
         bool live = false;
         uint32_t pid = 0;
         SampleGen sg;
@@ -743,8 +783,8 @@ __global__ void __launch_bounds__(128, LEARNED ? 3 : PLT_BOUNCE_MIN_BLOCKS) ptBo
             P.plen[pid] = len;
             if constexpr (LEARNED) P.wpss[pid] = wps;
         }
-        const uint32_t pos = warpAggregatedAdd(P.qcount + it + 1, live);
-        if (live) qout[pos] = pid;
+        const uint32_t qpos = warpAggregatedAdd(P.qcount + it + 1, live);
+        if (live) qout[qpos] = pid;
     }
     if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     unsigned long long r = recorded;
@@ -763,13 +803,25 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
     uint32_t nv = 0, tt = 0, overflow = 0, recorded = 0;
     const Ctx c{P.profiles, P.nProfiles, P.flags};
+    // warps take 32 consecutive positions of the shading order at a time (the queue order when the
+    // segment is not sorted)
+    uint32_t* next = P.segOrder ? P.segSort + it * plt::kSegSortWords + 2 * plt::kSegKeys : nullptr;
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (count + stride - 1) / stride;
-    for (uint32_t rr = 0; rr < rounds; ++rr) {
-        const uint32_t slot = rr * stride + blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t rr = 0;; ++rr) {
+        uint32_t c0 = 0;
+        if (next) {
+            if (lane == 0) c0 = atomicAdd(next, 32u);
+            c0 = __shfl_sync(0xFFFFFFFFu, c0, 0);
+        } else {
+            c0 = rr * stride + blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+        }
+        if (c0 >= count) break;
+        const uint32_t pos = c0 + lane;
+        const uint32_t slot = next && pos < count ? P.segOrder[pos] : pos;
         bool live = false;
         uint32_t pid = 0;
-        if (slot < count) {
+        if (pos < count) {
             pid = (uint32_t)pltIdx(P.status, it == 0 ? slot : qin[pltIdx(P.status, slot, n, kSiteQueue)], n, kSitePath);
             SampleGen sg;
             sg.s0 = P.sg[pid]; sg.s1 = P.sg[n + pid]; sg.s2 = P.sg[2 * n + pid]; sg.s3 = P.sg[3 * n + pid];
@@ -872,8 +924,8 @@ __global__ void __launch_bounds__(128, PLT_BOUNCE_MIN_BLOCKS) ptBounceAnalyticKe
             P.pflags[pid] = flags;
             P.plen[pid] = len;
         }
-        const uint32_t pos = warpAggregatedAdd(P.qcount + it + 1, live);
-        if (live) qout[pos] = pid;
+        const uint32_t qpos = warpAggregatedAdd(P.qcount + it + 1, live);
+        if (live) qout[qpos] = pid;
     }
     if (overflow) atomicOr(P.status, plt::kStatusStackOverflow);
     unsigned long long r = recorded;

@@ -42,9 +42,10 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     // the counters: per-segment queue lengths, the manifold-walk count, the solve-order keys per
     // length (counts, cursors), the walk-order keys, the replay count, the replay-order keys and
     // the replay kernel's work counter
-    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys + 1;
+    const size_t nCounters = nb + 2 + 2 * (size_t)plt::kSolveKeysPerLength * nb + 32 + 1 + 2 * (size_t)plt::kReplayKeys + 1 +
+                             (size_t)plt::kSegSortWords * nb;
     const size_t pathBytes = al(4 * n * 4) + 2 * al(3 * n * 4) + 5 * al(n * 4) + 2 * al(n * 4) + 2 * al(n * 4) + al(nCounters * 4) +
-                             al(n * 4) + al(2 * n * 4);
+                             al(n * 4) + al(2 * n * 4) + al(n * 4);
     const size_t bounceBytes = 2 * al(nb * n * 4) * 2 + 5 * al(nb * n * 4);
     const size_t total = pathBytes + bounceBytes;
     PLT_CUDA(ctx, cudaMalloc(&ctx->dPt, total));
@@ -75,6 +76,8 @@ plt_status ensureRenderBuffers(plt_context* ctx, uint32_t npix, uint32_t maxB) {
     P.mneeOrder = P.queue1;   // free during the solve pass
     P.segPrim = (uint32_t*)take(n * 4);
     P.segBary = (float*)take(2 * n * 4);
+    P.segOrder = (uint32_t*)take(n * 4);
+    P.segSort = P.replaySort + 2 * plt::kReplayKeys + 1;
     P.bBary = (float*)take(2 * nb * n * 4);
     P.bEw = (float*)take(2 * nb * n * 4);
     P.bPrim = (uint32_t*)take(nb * n * 4);
