@@ -280,11 +280,11 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
 
     Reported: both convergence curves (spp, seconds, relMSE, trimmed relMSE); on the trimmed relMSE,
     the directly measured time each tracer needs to reach the lowest error both reach (training time
-    included for the learned one) and their ratio; the time to relMSE 1e-3 from the curve fitted as
-    V / spp + R (R the reference's own contribution: it is itself an analytic render, at ref_spp spp,
-    and dominates these curves, so this fit is unstable); and the headline, from the variance per spp
-    (each batch against the pooled mean of every render, see below), which needs no converged
-    reference.  The plain relMSE is dominated by rare caustic and grazing-grating fireflies (single
+    included for the learned one) and their ratio; the curves fitted as V / spp + R (R the
+    reference's own contribution: it is itself an analytic render, at ref_spp spp, and dominates
+    these curves, so V is unstable and no time is projected from it); and the headline time to relMSE
+    1e-3, from the variance per spp (each batch against the pooled mean of every render, see below),
+    which needs no converged reference.  The plain relMSE is dominated by rare caustic and grazing-grating fireflies (single
     pixels 10^3 x the reference), so it does not fall as 1/spp within the budget and no fit is made
     on it."""
     import numpy as np
@@ -350,8 +350,6 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
     (Vp, Vl, R), *_ = np.linalg.lstsq(A, np.concatenate([yp, yl]), rcond=None)
     ms_p = plain[-1][1] / plain[-1][0] * 1e3
     ms_l = learned[-1][1] / learned[-1][0] * 1e3
-    t_p = Vp / 1e-3 * ms_p * 1e-3 if Vp > 0 else None
-    t_l = Vl / 1e-3 * ms_l * 1e-3 + train_s if Vl > 0 else None
     # directly measured: first time each curve reaches the lowest trimmed relMSE both curves reach
     level = max(min(m for _, _, _, m in plain), min(m for _, _, _, m in learned))
     first = lambda pts, extra: next(t for _, t, _, m in pts if m <= level) + extra
@@ -380,9 +378,9 @@ def learned_bench(dev, stream, prob=0.25, width=256, ref_spp=4096, budget_s=12.0
             "train_loss_first_last": [float(hist[:8].mean()), float(hist[-8:].mean())],
             "measured_equal_relmse": {"metric": "relmse_trimmed_0.1%", "relmse": level, "time_plain_s": tm_p, "time_learned_s": tm_l,
                                       "speedup": tm_p / tm_l},
-            "fit": {"metric": "relmse_trimmed_0.1%", "V_plain": float(Vp), "V_learned": float(Vl), "R_reference": float(R)},
-            "reference_fit": {"time_to_relmse_1e-3_plain_s": t_p, "time_to_relmse_1e-3_learned_s": t_l,
-                              "speedup": (t_p / t_l) if (t_p and t_l) else None},
+            "fit": {"metric": "relmse_trimmed_0.1%", "V_plain": float(Vp), "V_learned": float(Vl), "R_reference": float(R),
+                    "note": "V / spp + R over the second half of each curve; R (the reference's own error) dominates, so V is "
+                            "unstable from run to run and no time is projected from it"},
             "variance_per_spp": {"metric": "relmse_trimmed_0.1%% of one %d-spp batch against the pooled mean of all renders, median "
                                            "over batches" % batch_spp,
                                  "relmse_plain": e_p, "relmse_learned": e_l, "batches_plain": len(batches_p), "batches_learned": len(batches_l),
@@ -732,6 +730,55 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def per_material_bench(n, steps, warmup):
+    """The BSDF shade kernel per material: the mixed-material batch of n queries, then each of its
+    material types' queries alone (contiguous, n / 8 each), eval + sample + pdf at HWSS 1; CUDA events
+    around the shade launch (plt_set_timing_events), median of `steps` after `warmup` untimed runs.
+    With --steps 1 --warmup 0 the process launches exactly 9 shade kernels in that order (the
+    profiling command of the per-material instruction mix).  Prints one JSON line."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from pltfalcor_gb300 import capi, spectra, workloads as W, materials as M
+    from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    prof, _ = spectra.standard_profiles()
+    full = W.mixed_material_batch(n=n, profiles=prof)
+    ops = capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF
+    ctx = PLTContext()
+    ctx.set_spectral_profiles(prof)
+    ctx.set_materials(full.records)
+    s = torch.cuda.current_stream()
+
+    def timed(wl):
+        b = DeviceBatch(wl)
+        q, r = b.queries(), b.results(ops)
+        for _ in range(warmup):
+            ctx.batch(q, r, ops, s)
+        ms = []
+        for _ in range(steps):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            for e in ev:
+                e.record(s)   # creates the events (torch creates them lazily); the library re-records them
+            ctx.lib.plt_set_timing_events(ctx.handle, *[C.c_void_p(e.cuda_event) for e in ev])
+            ctx.batch(q, r, ops, s)
+            torch.cuda.synchronize()
+            ms.append(ev[1].elapsed_time(ev[2]))
+        ctx.lib.plt_set_timing_events(ctx.handle, None, None, None)
+        assert ctx.check_status(s) == 0
+        m = float(np.median(ms))
+        return {"queries": wl.n, "shade_ms": m, "queries_per_s": wl.n / (m * 1e-3)}
+
+    out = {"metric": "BSDF shade kernel per material (eval+sample+pdf, HWSS 1)", "mixed": timed(full)}
+    types = full.meta["types"]
+    for t, ty in enumerate(M.BENCH_TYPES):
+        out[M.TYPE_NAMES[int(ty)]] = timed(full.subset(np.nonzero(types == t)[0]))
+    out["sum_of_materials_ms"] = sum(v["shade_ms"] for k, v in out.items() if isinstance(v, dict) and k != "mixed")
+    ctx.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -746,8 +793,11 @@ def main():
     ap.add_argument("--no-scene-set", action="store_true")
     ap.add_argument("--render-size", type=int, default=1024, help="render leg image width = height (profiling uses small sizes)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--per-material", action="store_true", help="only the shade kernel per material (diagnostic), one JSON line")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.per_material:
+        per_material_bench(args.n, args.steps, args.warmup)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -78,33 +78,39 @@ PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
     float* cum = reinterpret_cast<float*>(sh + 16);   // [17] cumulative work
     float* cost = reinterpret_cast<float*>(sh + 33);  // [16] cost per query
     uint32_t* measured = sh + 49;  // 1 while every queried type has a measured cost
+    uint32_t* mxs = sh + 50;       // [16] largest per-tile count per type
     if (tid == 0) *measured = 1u;
+    // one round trip: the first warp reads the cost counters, the second takes the batch's counts
+    unsigned long long cyc = 0ull;
+    uint32_t prev = 0u, avgBits = 0u;
+    if (tid < kTypeSlots) {
+        cyc = atomicExch(reinterpret_cast<unsigned long long*>(P.ctrl + C_CYC) + tid, 0ull);
+        prev = P.ctrl[C_TOTAL + tid];
+        avgBits = P.ctrl[C_COST + tid];
+    } else if (tid >= 32 && tid < 32 + kTypeSlots) {
+        const uint32_t k = tid - 32;
+        count[k] = atomicExch(P.ctrl + C_COUNT + k, 0u);
+        mxs[k] = atomicExch(P.ctrl + C_MAX + k, 0u);
+    }
     __syncthreads();
     if (tid < kTypeSlots) {
         // the previous batch's cycles per query of this type, folded into its running average
-        unsigned long long* cyc = reinterpret_cast<unsigned long long*>(P.ctrl + C_CYC) + tid;
-        const unsigned long long c = atomicExch(cyc, 0ull);
-        const uint32_t prev = P.ctrl[C_TOTAL + tid];
-        float avg = __uint_as_float(P.ctrl[C_COST + tid]);
-        if (prev >= 1024u && c > 0ull) {
-            const float m = (float)c / (float)prev;
+        float avg = __uint_as_float(avgBits);
+        if (prev >= 1024u && cyc > 0ull) {
+            const float m = (float)cyc / (float)prev;
             avg = avg > 0.f ? 0.5f * avg + 0.5f * m : m;
             P.ctrl[C_COST + tid] = __float_as_uint(avg);
         }
         cost[tid] = avg;
-    }
-    __syncthreads();
-    if (tid < kTypeSlots) {
-        const uint32_t total = atomicExch(P.ctrl + C_COUNT + tid, 0u);
-        const uint32_t mx = atomicExch(P.ctrl + C_MAX + tid, 0u);
+    } else if (tid >= 32 && tid < 32 + kTypeSlots) {
+        const uint32_t k = tid - 32, mx = mxs[k];
         // units: slices of about unitQueries of one tile's range, at most ceil(max / unitQueries) per tile
         const uint32_t units = mx ? (mx + P.unitQueries - 1) / P.unitQueries : 0u;
         const uint32_t usz = units ? ((mx + units - 1) / units + 31u) & ~31u : 0u;
-        P.ctrl[C_UNITS + tid] = units;
-        P.ctrl[C_USZ + tid] = usz;
-        P.ctrl[C_TOTAL + tid] = total;
-        P.ctrl[C_NEXT + tid] = 0u;
-        count[tid] = total;
+        P.ctrl[C_UNITS + k] = units;
+        P.ctrl[C_USZ + k] = usz;
+        P.ctrl[C_TOTAL + k] = count[k];
+        P.ctrl[C_NEXT + k] = 0u;
     }
     __syncthreads();
 #ifndef PLT_ADAPTIVE_COSTS
@@ -140,7 +146,7 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     using namespace plt;
     __shared__ uint32_t counts[kBuckets];
     __shared__ uint32_t offs[kBuckets];
-    __shared__ uint32_t sched[56];
+    __shared__ uint32_t sched[72];
     __shared__ bool isLast;
     const uint32_t tid = threadIdx.x;
     const uint32_t n = P.q.n;
@@ -289,8 +295,10 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     // the schedule never has more than kBatchTile / 32 units of at least 32 queries per tile; the
     // clamps keep every loop bounded whatever the control words hold
     constexpr uint32_t kMaxUnits = kBatchTile / 32;
+    // each type's units per tile, one per lane (read together with this SM's type: one round trip)
+    const uint32_t unitsOf = lane < kTypeSlots ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
     uint32_t t = P.smType[smId() % kMaxSmIds] % kTypeSlots;
-    uint32_t units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
+    uint32_t units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
     for (;;) {
         uint32_t u = 0;
         if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
@@ -298,7 +306,7 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
         if (u >= units * nTiles) {
             t = busiestQueue(P, nTiles, lane);
             if (t >= kTypeSlots) break;
-            units = min(__ldg(P.ctrl + C_UNITS + t), kMaxUnits);
+            units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
             continue;
         }
         const uint32_t tile = u / units, sub = u - tile * units;
