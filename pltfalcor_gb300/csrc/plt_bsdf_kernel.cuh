@@ -45,7 +45,8 @@ enum : uint32_t {
     C_TOTAL = 96,   // [16] queries per type
     C_COST = 112,   // [16] measured cost per query of each type (float; exponential average over batches)
     C_CYC = 128,    // [16] x u64: warp cycles spent on each type's units in the last batch
-    C_WORDS = 160
+    C_SMALL = 160,  // the work counter of a small batch (zeroed by its classify grid)
+    C_WORDS = 161
 };
 static_assert(C_WORDS * 4 <= plt::kBsdfCtrlBytes, "control words exceed their scratch block");
 
@@ -199,13 +200,18 @@ static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(
     if (tid <= kTypeSlots) {
         const uint32_t start = tid < kTypeSlots ? offs[tid * kLobeClasses] : offs[kPadBucket];
         P.tileTypeOff[blockIdx.x * (kTypeSlots + 1) + tid] = (uint16_t)start;
-        if (tid < kTypeSlots) {
+        if (tid < kTypeSlots && !P.smallBatch) {
             const uint32_t end = tid + 1 < kTypeSlots ? offs[(tid + 1) * kLobeClasses] : offs[kPadBucket];
             if (end > start) {
                 atomicAdd(P.ctrl + C_COUNT + tid, end - start);
                 atomicMax(P.ctrl + C_MAX + tid, end - start);
             }
         }
+    }
+    if (P.smallBatch) {
+        // a small batch is shaded in the tiles' sorted order from one counter: no schedule
+        if (blockIdx.x == 0 && tid == 0) P.ctrl[C_SMALL] = 0u;
+        return;
     }
     // the last CTA to finish builds the schedule (the counters above are complete once every CTA
     // has passed the fence)
@@ -295,26 +301,58 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     // the schedule never has more than kBatchTile / 32 units of at least 32 queries per tile; the
     // clamps keep every loop bounded whatever the control words hold
     constexpr uint32_t kMaxUnits = kBatchTile / 32;
+    // A small batch takes its units from one counter: 32 consecutive positions of a tile's sorted
+    // permutation, in tile order, split where the material type changes (a few-tile batch is
+    // latency-bound and gains nothing from the per-type queues).  Both kinds of unit are shaded at
+    // the one call site below, so a query's arithmetic is the same whichever schedule it gets.
+    const bool small = P.smallBatch != 0u;
+    const uint32_t totalSmall = nTiles * kMaxUnits;
+    uint32_t sTile = 0, sPos = 0, sEnd = 0;   // small batch: the current unit's remaining positions
     // each type's units per tile, one per lane (read together with this SM's type: one round trip)
-    const uint32_t unitsOf = lane < kTypeSlots ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
-    uint32_t t = P.smType[smId() % kMaxSmIds] % kTypeSlots;
+    const uint32_t unitsOf = !small && lane < kTypeSlots ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
+    uint32_t t = small ? 0u : P.smType[smId() % kMaxSmIds] % kTypeSlots;
     uint32_t units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
     for (;;) {
-        uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
-        u = __shfl_sync(0xFFFFFFFFu, u, 0);
-        if (u >= units * nTiles) {
-            t = busiestQueue(P, nTiles, lane);
-            if (t >= kTypeSlots) break;
-            units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
-            continue;
+        uint32_t tile, lo, hi;
+        if (small) {
+            if (sPos >= sEnd) {
+                uint32_t u = 0;
+                if (lane == 0) u = atomicAdd(P.ctrl + C_SMALL, 1u);
+                u = __shfl_sync(0xFFFFFFFFu, u, 0);
+                if (u >= totalSmall) break;
+                sTile = u / kMaxUnits;
+                sPos = (u - sTile * kMaxUnits) * 32u;
+                sEnd = min(sPos + 32u, min((uint32_t)kBatchTile, P.q.n - sTile * kBatchTile));
+                if (sPos >= sEnd) continue;
+            }
+            // the type whose range of the tile's permutation holds sPos, and where that range ends
+            const uint16_t* off = P.tileTypeOff + sTile * (kTypeSlots + 1);
+            t = 0;
+            while (t + 1 < kTypeSlots && (uint32_t)__ldg(off + t + 1) <= sPos) ++t;
+            tile = sTile;
+            lo = sPos;
+            hi = min(sEnd, (uint32_t)__ldg(off + t + 1));
+            if (hi <= lo) hi = sEnd;   // (padding: the positions past the tile's queries are never in a unit)
+            sPos = hi;
+        } else {
+            uint32_t u = 0;
+            if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
+            u = __shfl_sync(0xFFFFFFFFu, u, 0);
+            if (u >= units * nTiles) {
+                t = busiestQueue(P, nTiles, lane);
+                if (t >= kTypeSlots) break;
+                units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
+                continue;
+            }
+            tile = u / units;
+            const uint32_t sub = u - tile * units;
+            const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
+            const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
+            lo = __ldg(off + t) + sub * usz;
+            const uint32_t end = min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile);
+            hi = min(end, lo + usz);
+            if (lo >= hi) continue;
         }
-        const uint32_t tile = u / units, sub = u - tile * units;
-        const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
-        const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
-        const uint32_t lo = __ldg(off + t) + sub * usz, end = min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile);
-        const uint32_t hi = min(end, lo + usz);
-        if (lo >= hi) continue;
         const uint32_t tileBase = tile * kBatchTile;
         const long long t0 = clock64();
         switch (t) {
@@ -331,7 +369,7 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
         default: shadeUnit<H, 0u>(P, c, tileBase, lo, hi, lane); break;
         }
         __syncwarp();
-        if (lane == 0) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
+        if (lane == 0 && !small) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
     }
     // the measured cost per type feeds the next batch's SM shares
     __syncthreads();
@@ -362,6 +400,10 @@ inline float defaultTypeCost(uint32_t t) {
     default: return .050f;
     }
 }
+
+// Batches of at most this many tiles (65,536 queries) skip the per-type schedule: its last-CTA
+// build and the queue look-ups cost more latency than a few-tile batch loses to mixed-type warps.
+constexpr uint32_t kSmallBatchTiles = 32;
 
 // classify: one CTA per tile; shade: persistent grid of SM count x resident CTAs per SM
 // (occupancy at this launch's shared memory).
@@ -395,6 +437,7 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     // bounding each queue's lead over the slowest one (16 or 32 tiles) made it slower (1.2-2.0 ms),
     // since every unit then re-reads the contended queue counters and SMs leave their type
     p.unitQueries = 32;
+    p.smallBatch = nTiles <= kSmallBatchTiles ? 1u : 0u;
     for (uint32_t t = 0; t < kTypeSlots; ++t)
         if (!(p.typeCost[t] > 0.f)) p.typeCost[t] = defaultTypeCost(t);
     if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
