@@ -1,4 +1,4 @@
-// Host SAH BVH builder (binned, 16 bins per axis on triangle centroids).
+// Host SAH BVH builder (binned, 32 bins per axis on triangle centroids).
 #include "plt_bvh.h"
 
 #include <algorithm>
@@ -66,8 +66,10 @@ struct Builder {
         for (uint32_t i = b; i < e; ++i) cb.grow(&cent[3 * refs[i]]);
         const Box pb = rangeBox(b, e);
         const double pa = pb.area();
-        // binned SAH over the three axes
-        constexpr int B = 16;
+        // binned SAH over the three axes; 32 bins: on the 1.04 M-triangle room 34.6 node visits per
+        // camera ray and 3.53 G rays/s against 47.1 and 3.05 with 16 bins (random rays 2.00 against
+        // 1.97 G/s), for 0.3 s more build time
+        constexpr int B = 32;
         int bestAxis = -1, bestSplit = -1;
         double bestCost = (double)n;  // leaf cost
         for (int a = 0; a < 3; ++a) {
