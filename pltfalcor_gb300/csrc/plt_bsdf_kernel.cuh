@@ -308,6 +308,11 @@ PLT_DI void shadeRange(const BatchParams& P, const Ctx& c, uint32_t t, uint32_t 
     }
 }
 
+// The shade kernel.  A batch of more than kSmallBatchTiles tiles is shaded from the per-type unit
+// queues of the classify schedule; a small batch's warps take units of 32 consecutive positions of
+// a tile's sorted permutation from one counter, in tile order, split where the material type
+// changes (a few-tile batch is latency-bound and gains nothing from the queues).  Both schedules
+// end in the one call of the typed code, so a query gives the same bits in any batch.
 template <int H>
 __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdfShadeKernel(const BatchParams P) {
     using namespace plt;
@@ -323,78 +328,64 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdf
     // (a no-op when the kernel was not launched as a programmatic dependent)
     asm volatile("griddepcontrol.wait;" ::: "memory");
 
+    const bool small = P.smallBatch != 0u;
     const uint32_t nTiles = (P.q.n + kBatchTile - 1) / kBatchTile;
     // the schedule never has more than kBatchTile / 32 units of at least 32 queries per tile; the
     // clamps keep every loop bounded whatever the control words hold
     constexpr uint32_t kMaxUnits = kBatchTile / 32;
     // each type's units per tile, one per lane (read together with this SM's type: one round trip)
-    const uint32_t unitsOf = lane < kTypeSlots ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
-    uint32_t t = P.smType[smId() % kMaxSmIds] % kTypeSlots;
+    const uint32_t unitsOf = lane < kTypeSlots && !small ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
+    uint32_t t = small ? 0u : P.smType[smId() % kMaxSmIds] % kTypeSlots;
     uint32_t units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
+    uint32_t sTile = 0, sPos = 0, sEnd = 0;   // a small batch's current unit: remaining positions
     for (;;) {
-        uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
-        u = __shfl_sync(0xFFFFFFFFu, u, 0);
-        if (u >= units * nTiles) {
-            t = busiestQueue(P, nTiles, lane);
-            if (t >= kTypeSlots) break;
-            units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
-            continue;
+        uint32_t tile, lo, hi;
+        if (small) {
+            if (sPos >= sEnd) {
+                uint32_t u = 0;
+                if (lane == 0) u = atomicAdd(P.ctrl + C_SMALL, 1u);
+                u = __shfl_sync(0xFFFFFFFFu, u, 0);
+                if (u >= nTiles * kMaxUnits) break;
+                sTile = u / kMaxUnits;
+                sPos = (u - sTile * kMaxUnits) * 32u;
+                sEnd = min(sPos + 32u, min((uint32_t)kBatchTile, P.q.n - sTile * kBatchTile));
+                if (sPos >= sEnd) continue;
+            }
+            // the type whose range of the tile's permutation holds sPos, and where that range ends
+            const uint16_t* off = P.tileTypeOff + sTile * (kTypeSlots + 1);
+            t = 0;
+            while (t + 1 < kTypeSlots && (uint32_t)__ldg(off + t + 1) <= sPos) ++t;
+            tile = sTile;
+            lo = sPos;
+            hi = min(sEnd, max(lo + 1u, (uint32_t)__ldg(off + t + 1)));
+            sPos = hi;
+        } else {
+            uint32_t u = 0;
+            if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
+            u = __shfl_sync(0xFFFFFFFFu, u, 0);
+            if (u >= units * nTiles) {
+                t = busiestQueue(P, nTiles, lane);
+                if (t >= kTypeSlots) break;
+                units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
+                continue;
+            }
+            tile = u / units;
+            const uint32_t sub = u - tile * units;
+            const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
+            const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
+            lo = __ldg(off + t) + sub * usz;
+            hi = min(min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile), lo + usz);
+            if (lo >= hi) continue;
         }
-        const uint32_t tile = u / units, sub = u - tile * units;
-        const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
-        const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
-        const uint32_t lo = __ldg(off + t) + sub * usz, end = min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile);
-        const uint32_t hi = min(end, lo + usz);
-        if (lo >= hi) continue;
         const long long t0 = clock64();
         shadeRange<H>(P, c, t, tile * kBatchTile, lo, hi, lane);
         __syncwarp();
-        if (lane == 0) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
+        if (lane == 0 && !small) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
     }
     // the measured cost per type feeds the next batch's SM shares
     __syncthreads();
     if (tid < kTypeSlots && cycles[tid])
         atomicAdd(reinterpret_cast<unsigned long long*>(P.ctrl + C_CYC) + tid, cycles[tid]);
-}
-
-// The shade kernel of a small batch (at most kSmallBatchTiles tiles): warps take units of 32
-// consecutive positions of a tile's sorted permutation from one counter, in tile order, split where
-// the material type changes, and shade them with the same typed code as bsdfShadeKernel (a few-tile
-// batch is latency-bound and gains nothing from the per-type queues and their schedule).
-template <int H>
-__global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdfShadeSmallKernel(const BatchParams P) {
-    using namespace plt;
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar;
-    DevProfile* sprof = reinterpret_cast<DevProfile*>(smem);
-    const uint32_t lane = threadIdx.x & 31u;
-    if (!stageProfiles(P, sprof, &bar)) return;
-    const Ctx c{sprof, P.nProfiles, P.flags};
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    const uint32_t nTiles = (P.q.n + kBatchTile - 1) / kBatchTile;
-    constexpr uint32_t kMaxUnits = kBatchTile / 32;
-    const uint32_t totalUnits = nTiles * kMaxUnits;
-    uint32_t sTile = 0, sPos = 0, sEnd = 0;   // the current unit's remaining positions
-    for (;;) {
-        if (sPos >= sEnd) {
-            uint32_t u = 0;
-            if (lane == 0) u = atomicAdd(P.ctrl + C_SMALL, 1u);
-            u = __shfl_sync(0xFFFFFFFFu, u, 0);
-            if (u >= totalUnits) break;
-            sTile = u / kMaxUnits;
-            sPos = (u - sTile * kMaxUnits) * 32u;
-            sEnd = min(sPos + 32u, min((uint32_t)kBatchTile, P.q.n - sTile * kBatchTile));
-            if (sPos >= sEnd) continue;
-        }
-        // the type whose range of the tile's permutation holds sPos, and where that range ends
-        const uint16_t* off = P.tileTypeOff + sTile * (kTypeSlots + 1);
-        uint32_t t = 0;
-        while (t + 1 < kTypeSlots && (uint32_t)__ldg(off + t + 1) <= sPos) ++t;
-        const uint32_t lo = sPos, hi = max(lo + 1u, min(sEnd, (uint32_t)__ldg(off + t + 1)));
-        sPos = min(hi, sEnd);
-        shadeRange<H>(P, c, t, sTile * kBatchTile, lo, sPos, lane);
-    }
 }
 
 }  // namespace pltdev
@@ -466,8 +457,7 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     if (p.timing[1]) {
         // per-kernel timing: an event between the kernels, so an ordinary launch
         cudaEventRecord((cudaEvent_t)p.timing[1], stream);
-        if (p.smallBatch) pltdev::bsdfShadeSmallKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
-        else pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
+        pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
     } else {
         // programmatic dependent launch: the shade CTAs are scheduled while classify finishes and
         // stage their spectral tables before waiting on it (hides the launch gap of small batches)
@@ -481,7 +471,7 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        e = p.smallBatch ? cudaLaunchKernelEx(&cfg, pltdev::bsdfShadeSmallKernel<H>, p) : cudaLaunchKernelEx(&cfg, pltdev::bsdfShadeKernel<H>, p);
+        e = cudaLaunchKernelEx(&cfg, pltdev::bsdfShadeKernel<H>, p);
     }
     if (e != cudaSuccess) return e;
     if (p.timing[2]) cudaEventRecord((cudaEvent_t)p.timing[2], stream);

@@ -209,11 +209,16 @@ PLT_DI float fracPdf(const float* __restrict__ p, f3 wi, f3 wo, float k) { retur
 // ------------------------------------------------------------------------------------------
 // Interference (Interference.slang:36-57)
 // ------------------------------------------------------------------------------------------
+// sqrt(max(0, x y)) as sqrt|x| sqrt|y|: the product of two intensities of ~1e-20 is subnormal,
+// which the BSDF batch units flush to zero, while the split form keeps its cross term.
+PLT_DI float geoMean(float x, float y) {
+    return ((x > 0.f && y > 0.f) || (x < 0.f && y < 0.f)) ? sqrtf(fabsf(x)) * sqrtf(fabsf(y)) : 0.f;
+}
 PLT_DI f4 interfere(f4 a, f4 b, float ps, float pp, float coh) {
     const float S1 = (a.x + a.y) / 2.f, P1 = (a.x - a.y) / 2.f;
     const float S2 = (b.x + b.y) / 2.f, P2 = (b.x - b.y) / 2.f;
-    const float S = S1 + S2 + 2.f * sqrtf(fmaxf(0.f, S1 * S2)) * ps * coh;
-    const float P = P1 + P2 + 2.f * sqrtf(fmaxf(0.f, P1 * P2)) * pp * coh;
+    const float S = S1 + S2 + 2.f * geoMean(S1, S2) * ps * coh;
+    const float P = P1 + P2 + 2.f * geoMean(P1, P2) * pp * coh;
     const float n = a.x + b.x > 1e-6f ? (S + P) / (a.x + b.x) : 0.f;
     return f4{S + P, S - P, (a.z + b.z) * n, (a.w + b.w) * n};
 }
