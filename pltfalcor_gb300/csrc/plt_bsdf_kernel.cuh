@@ -142,82 +142,142 @@ PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
     }
 }
 
+// The material ids and lobes of one tile's items (kBatchItems per thread).
+PLT_DI void loadTileKeys(const BatchParams& P, uint32_t base, uint32_t* mid, uint32_t* lob) {
+    using namespace plt;
+    const uint32_t n = P.q.n;
+#pragma unroll
+    for (int k = 0; k < kBatchItems; ++k) {
+        const uint32_t idx = base + k * kBatchThreads + threadIdx.x;
+        mid[k] = idx < n ? __ldg(P.q.material + idx) : 0xFFFFFFFFu;
+        lob[k] = idx < n && P.q.lobe ? __ldg(P.q.lobe + idx) : 0xFFFFu;
+    }
+}
+
+// Persistent: each CTA sorts tiles blockIdx.x, blockIdx.x + gridDim.x, ... (a grid of the resident
+// CTAs), loading the next tile's material ids and lobes while it sorts the current one, and adds
+// its tiles' per-type counts to the batch totals once.  Measured on the 2^22 batch (2,048 tiles):
+// one CTA per tile lived ~13 us (6 us of it waiting on its loads) and ran in three waves, 38 us.
+#ifndef PLT_CLASSIFY_MIN_BLOCKS
+#define PLT_CLASSIFY_MIN_BLOCKS 4
+#endif
+#ifndef PLT_CLASSIFY_MATCH
+#define PLT_CLASSIFY_MATCH 0
+#endif
 // internal linkage: each per-wavelength-count translation unit carries its own copy
-static __global__ void __launch_bounds__(plt::kBatchThreads) bsdfClassifyKernel(const BatchParams P) {
+static __global__ void __launch_bounds__(plt::kBatchThreads, PLT_CLASSIFY_MIN_BLOCKS) bsdfClassifyKernel(const BatchParams P) {
     using namespace plt;
     __shared__ uint32_t counts[kBuckets];
     __shared__ uint32_t offs[kBuckets];
     __shared__ uint32_t sched[72];
+    __shared__ uint32_t ctaCount[kTypeSlots], ctaMax[kTypeSlots];
+    __shared__ __align__(16) uint16_t tilePerm[kBatchTile];   // the tile's permutation, stored coalesced
     __shared__ bool isLast;
     const uint32_t tid = threadIdx.x;
     const uint32_t n = P.q.n;
-    const uint32_t base = blockIdx.x * kBatchTile;
+    const uint32_t nTiles = (n + kBatchTile - 1) / kBatchTile;
     // the shade kernel may be scheduled once every classify CTA has started: it stages its tables
     // and then waits for this grid to complete (programmatic dependent launch)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    for (uint32_t b = tid; b < kBuckets; b += kBatchThreads) counts[b] = 0;
-    __syncthreads();
-    uint16_t key[kBatchItems], rank[kBatchItems];
-#pragma unroll
-    for (int k = 0; k < kBatchItems; ++k) {
-        const uint32_t idx = base + k * kBatchThreads + tid;
-        uint32_t b = kPadBucket;
-        if (idx < n) {
-            const uint32_t mid = __ldg(P.q.material + idx);
-            const uint32_t t = mid < P.nMats ? __ldg(P.matType + mid) : 14u;
-            const uint32_t cls = (t & 0x80u) ? 8u + ((t >> 4) & 7u) : lobeClass(P.q.lobe ? __ldg(P.q.lobe + idx) : 0xFFFFu);
-            b = (t & 15u) * kLobeClasses + cls;
-        }
-        key[k] = (uint16_t)b;
-        rank[k] = (uint16_t)atomicAdd(&counts[b], 1u);
+    if (tid < kTypeSlots) {
+        ctaCount[tid] = 0u;
+        ctaMax[tid] = 0u;
     }
-    __syncthreads();
-    if (tid < 32) {
-        // exclusive scan of kBuckets counters by one warp: 8 consecutive buckets per lane
-        constexpr uint32_t per = kBuckets / 32;
-        uint32_t s = 0;
+    uint32_t mid[kBatchItems], lob[kBatchItems];
+    loadTileKeys(P, blockIdx.x * kBatchTile, mid, lob);
+    for (uint32_t tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
+        const uint32_t base = tile * kBatchTile;
+        for (uint32_t b = tid; b < kBuckets; b += kBatchThreads) counts[b] = 0;
+        __syncthreads();
+        // the material types of this tile's items, then the next tile's ids and lobes in flight
+        // while this one is counted, scanned and scattered
+        uint32_t key32[kBatchItems];
 #pragma unroll
-        for (uint32_t j = 0; j < per; ++j) s += counts[tid * per + j];
-        uint32_t incl = s;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
-            if ((int)tid >= d) incl += v;
+        for (int k = 0; k < kBatchItems; ++k) {
+            const uint32_t t = mid[k] < P.nMats ? __ldg(P.matType + mid[k]) : 14u;
+            uint32_t b = kPadBucket;
+            if (base + k * kBatchThreads + tid < n) {
+                const uint32_t cls = (t & 0x80u) ? 8u + ((t >> 4) & 7u) : lobeClass(lob[k]);
+                b = (t & 15u) * kLobeClasses + cls;
+            }
+            key32[k] = b;
         }
-        uint32_t run = incl - s;
+        loadTileKeys(P, tile + gridDim.x < nTiles ? (tile + gridDim.x) * kBatchTile : n, mid, lob);
+        // bucket << 16 | rank within the bucket
+#if PLT_CLASSIFY_MATCH
+        // one shared-memory atomic per distinct bucket of a warp (same-address atomics serialise)
+        const uint32_t lane = tid & 31u, below = (1u << lane) - 1u;
 #pragma unroll
-        for (uint32_t j = 0; j < per; ++j) {
-            offs[tid * per + j] = run;
-            run += counts[tid * per + j];
+        for (int k = 0; k < kBatchItems; ++k) {
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key32[k]);
+            const uint32_t leader = (uint32_t)__ffs((int)peers) - 1u;
+            uint32_t first = 0;
+            if (lane == leader) first = atomicAdd(&counts[key32[k]], (uint32_t)__popc(peers));
+            first = __shfl_sync(0xFFFFFFFFu, first, (int)leader);
+            key32[k] = key32[k] << 16 | (first + (uint32_t)__popc(peers & below));
         }
-    }
-    __syncthreads();
+#else
 #pragma unroll
-    for (int k = 0; k < kBatchItems; ++k)
-        P.perm[pltIdx(P.status, base + offs[key[k]] + rank[k], permSlots(n), kSitePerm)] = (uint16_t)(k * kBatchThreads + tid);
-    // type t's range of this tile: [offs[t * kLobeClasses], start of type t + 1); the padding bucket
-    // comes last, so its start is the tile's query count
-    if (tid <= kTypeSlots) {
-        const uint32_t start = tid < kTypeSlots ? offs[tid * kLobeClasses] : offs[kPadBucket];
-        P.tileTypeOff[blockIdx.x * (kTypeSlots + 1) + tid] = (uint16_t)start;
-        if (tid < kTypeSlots && !P.smallBatch) {
-            const uint32_t end = tid + 1 < kTypeSlots ? offs[(tid + 1) * kLobeClasses] : offs[kPadBucket];
-            if (end > start) {
-                atomicAdd(P.ctrl + C_COUNT + tid, end - start);
-                atomicMax(P.ctrl + C_MAX + tid, end - start);
+        for (int k = 0; k < kBatchItems; ++k) key32[k] = key32[k] << 16 | atomicAdd(&counts[key32[k]], 1u);
+#endif
+        __syncthreads();
+        if (tid < 32) {
+            // exclusive scan of kBuckets counters by one warp: 8 consecutive buckets per lane
+            constexpr uint32_t per = kBuckets / 32;
+            uint32_t s = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < per; ++j) s += counts[tid * per + j];
+            uint32_t incl = s;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+                if ((int)tid >= d) incl += v;
+            }
+            uint32_t run = incl - s;
+#pragma unroll
+            for (uint32_t j = 0; j < per; ++j) {
+                offs[tid * per + j] = run;
+                run += counts[tid * per + j];
             }
         }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kBatchItems; ++k)
+            tilePerm[pltIdx(P.status, offs[key32[k] >> 16] + (key32[k] & 0xFFFFu), (uint32_t)kBatchTile, kSitePerm)] = (uint16_t)(k * kBatchThreads + tid);
+        // type t's range of this tile: [offs[t * kLobeClasses], start of type t + 1); the padding
+        // bucket comes last, so its start is the tile's query count
+        __syncthreads();
+        // 16 bytes per thread: the tile's 2,048 16-bit entries in one coalesced store
+        static_assert(kBatchTile * sizeof(uint16_t) == kBatchThreads * sizeof(uint4), "one 16-byte store per thread");
+        reinterpret_cast<uint4*>(P.perm + base)[tid] = reinterpret_cast<const uint4*>(tilePerm)[tid];
+        if (tid <= kTypeSlots) {
+            const uint32_t start = tid < kTypeSlots ? offs[tid * kLobeClasses] : offs[kPadBucket];
+            P.tileTypeOff[tile * (kTypeSlots + 1) + tid] = (uint16_t)start;
+            if (tid < kTypeSlots) {
+                const uint32_t end = tid + 1 < kTypeSlots ? offs[(tid + 1) * kLobeClasses] : offs[kPadBucket];
+                ctaCount[tid] += end - start;
+                ctaMax[tid] = max(ctaMax[tid], end - start);
+            }
+        }
+        __syncthreads();   // counts and offs are rewritten for the next tile
     }
     if (P.smallBatch) {
         // a small batch is shaded in the tiles' sorted order from one counter: no schedule
         if (blockIdx.x == 0 && tid == 0) P.ctrl[C_SMALL] = 0u;
         return;
     }
-    // the last CTA to finish builds the schedule (the counters above are complete once every CTA
-    // has passed the fence)
-    __threadfence();
+    if (tid < kTypeSlots && ctaCount[tid]) {
+        atomicAdd(P.ctrl + C_COUNT + tid, ctaCount[tid]);
+        atomicMax(P.ctrl + C_MAX + tid, ctaMax[tid]);
+    }
+    // the last CTA to finish builds the schedule: the barrier orders this CTA's count atomics
+    // before thread 0's fence, so they are complete once every CTA has counted itself done (the
+    // permutation's plain stores need no fence: the shade grid reads them after this grid ends)
     __syncthreads();
-    if (tid == 0) isLast = atomicAdd(P.ctrl + C_DONE, 1u) == gridDim.x - 1;
+    if (tid == 0) {
+        __threadfence();
+        isLast = atomicAdd(P.ctrl + C_DONE, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
     if (isLast) {
         __threadfence();
@@ -451,8 +511,15 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     p.smallBatch = nTiles <= kSmallBatchTiles ? 1u : 0u;
     for (uint32_t t = 0; t < kTypeSlots; ++t)
         if (!(p.typeCost[t] > 0.f)) p.typeCost[t] = defaultTypeCost(t);
+    // the classify grid: the resident CTAs (persistent over the tiles), at most one per tile
+    int cb = p0.launch ? p0.launch->classifyBlocks[H] : 0;
+    if (cb < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cb, pltdev::bsdfClassifyKernel, kBatchThreads, 0) != cudaSuccess || cb < 1) cb = 1;
+        if (p0.launch) p0.launch->classifyBlocks[H] = cb;
+    }
+    const uint32_t classifyGrid = min(nTiles, (uint32_t)(numSMs * cb));
     if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
-    pltdev::bsdfClassifyKernel<<<nTiles, kBatchThreads, 0, stream>>>(p);
+    pltdev::bsdfClassifyKernel<<<classifyGrid, kBatchThreads, 0, stream>>>(p);
     cudaError_t e = cudaSuccess;
     if (p.timing[1]) {
         // per-kernel timing: an event between the kernels, so an ordinary launch

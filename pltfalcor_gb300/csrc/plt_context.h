@@ -54,6 +54,7 @@ struct plt_context {
     void* timing[3] = {nullptr, nullptr, nullptr};   // cudaEvent_t handles recorded by plt_bsdf_batch
     plt::ShadeLaunchCache shadeLaunch = {{(size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1, (size_t)-1,
                                           (size_t)-1, (size_t)-1},
+                                         {},
                                          {}};
 
     // host copies for the render pass (light collection, material properties)

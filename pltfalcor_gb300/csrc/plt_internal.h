@@ -49,6 +49,7 @@ cudaError_t launchTrace(const TraceParams& p, bool any, int numSMs, cudaStream_t
 struct ShadeLaunchCache {
     size_t smem[9];
     int blocks[9];
+    int classifyBlocks[9];   // resident classify CTAs per SM (0: not yet queried)
 };
 
 struct BatchParams {
