@@ -22,17 +22,22 @@ CPP_SOURCES = ["plt_capi.cpp", "plt_materials.cpp", "plt_bsdf_dispatch.cpp", "pl
                "plt_scenes.cpp", "plt_io.cpp", "plt_host_batch.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Single-precision division and square root use the SFU approximations (<= 2 ulp, the accuracy
-# class D3D allows the reference shaders).  The BSDF batch units flush subnormals to zero, as
-# D3D and Vulkan shaders do by default (FP32 results below 1.2e-38 carry no radiance the parity
-# bound can see; the interference cross term, the one place a product of two small intensities
-# becomes subnormal, is computed in a form that does not underflow).  The render and traversal
-# units keep subnormals: the ray/triangle test is bit-exact against the oracle.
+# class D3D allows the reference shaders).  The BSDF batch units also flush subnormals to zero and
+# take the SFU approximations of sin, cos, exp, log and exp2 (--use_fast_math), as D3D and Vulkan
+# shaders do by default: FP32 results below 1.2e-38 carry no radiance the parity bound can see (the
+# interference cross term, the one place a product of two small intensities becomes subnormal, is
+# computed in a form that does not underflow), and the approximations' errors (absolute 2^-20.5 for
+# sin and cos up to 100 pi, relative ~2^-21 for exp2) are inside D3D's bounds for the shaders'
+# intrinsics.  Divisions and square roots that must be exact stay explicitly rounded intrinsics.
+# The render and traversal units keep subnormals and the accurate functions: the ray/triangle test
+# is bit-exact against the oracle.
 CU_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
-FTZ_SOURCES = {"plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4.cu", "plt_bsdf_h8.cu", "plt_noalloc.cu"}
+BSDF_UNITS = {"plt_bsdf_h1.cu", "plt_bsdf_h2.cu", "plt_bsdf_h3.cu", "plt_bsdf_h4.cu", "plt_bsdf_h8.cu", "plt_noalloc.cu"}
 
 
-def ftz_flag(source):
-    return "-ftz=true" if os.path.basename(source) in FTZ_SOURCES else "-ftz=false"
+def unit_flags(source):
+    """nvcc flags specific to one translation unit (see above)."""
+    return ["-ftz=true", "--use_fast_math"] if os.path.basename(source) in BSDF_UNITS else ["-ftz=false"]
 
 
 def _nvcc():
@@ -80,7 +85,7 @@ def build(verbose=False, force=False, ptxas_verbose=False, defines=(), build_dir
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                   "--expt-relaxed-constexpr", ftz_flag(s), *cuflags, *dflags, "-c", src, "-o", obj]
+                   "--expt-relaxed-constexpr", *unit_flags(s), *cuflags, *dflags, "-c", src, "-o", obj]
             if ptxas_verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

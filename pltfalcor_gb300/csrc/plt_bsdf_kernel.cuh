@@ -293,7 +293,7 @@ __device__ __forceinline__ void shadeUnit(const BatchParams& P, const Ctx& c, ui
         const uint32_t k = pos + lane;
         if (k < hi) {
             const uint32_t idx = tileBase + __ldg(P.perm + pltIdx(P.status, tileBase + k, permSlots(P.q.n), kSitePerm));
-            if (idx < P.q.n) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, __ldg(P.q.material + idx), T);
+            if (idx < P.q.n) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, ldPlane(P.q.material + idx), T);
         }
     }
 }
@@ -374,7 +374,7 @@ PLT_DI void shadeRange(const BatchParams& P, const Ctx& c, uint32_t t, uint32_t 
 // changes (a few-tile batch is latency-bound and gains nothing from the queues).  Both schedules
 // end in the one call of the typed code, so a query gives the same bits in any batch.
 template <int H>
-__global__ void __launch_bounds__(plt::kShadeThreads, plt::kShadeMinBlocks) bsdfShadeKernel(const BatchParams P) {
+__global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) bsdfShadeKernel(const BatchParams P) {
     using namespace plt;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;

@@ -10,7 +10,41 @@ namespace pltdev {
 
 using plt::BatchParams;
 
-PLT_DI f3 ld3(const float* __restrict__ p, uint32_t i, uint32_t n) { return mk3(__ldg(p + i), __ldg(p + n + i), __ldg(p + 2 * n + i)); }
+// Loads of the query planes.  A material type's queries are spread over their tile, so each
+// 32-byte sector of a plane is read by several types' warps at different times.  PLT_PLANE_LOAD 1
+// asks L2 to fetch the whole 128-byte line on a miss, so the neighbouring queries' reads hit L2:
+// on the 2^22 mixed batch the shade kernel moves 0.80 GB instead of 0.93 GB in the same time.  2
+// also skips L1 allocation: 1.58 GB and 9 % slower (warps re-read their sectors).
+#ifndef PLT_PLANE_LOAD
+#define PLT_PLANE_LOAD 1
+#endif
+PLT_DI float ldPlane(const float* p) {
+#if PLT_PLANE_LOAD == 1
+    float v;
+    asm("ld.global.nc.L2::128B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+#elif PLT_PLANE_LOAD == 2
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::128B.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+PLT_DI uint32_t ldPlane(const uint32_t* p) {
+#if PLT_PLANE_LOAD == 1
+    uint32_t v;
+    asm("ld.global.nc.L2::128B.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#elif PLT_PLANE_LOAD == 2
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::128B.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+#else
+    return __ldg(p);
+#endif
+}
+PLT_DI f3 ld3(const float* __restrict__ p, uint32_t i, uint32_t n) { return mk3(ldPlane(p + i), ldPlane(p + n + i), ldPlane(p + 2 * n + i)); }
 PLT_DI void st3(float* p, uint32_t i, uint32_t n, f3 v) { p[i] = v.x; p[n + i] = v.y; p[2 * n + i] = v.z; }
 
 // grating frame: T = (gx, gy, 0), B = cross(N, T) = (-gy, gx, 0), N = +z
@@ -130,19 +164,19 @@ __device__ __forceinline__ void processQueryTyped(const BatchParams& P, const Ct
     const DevMaterial* __restrict__ m = P.mats + (badId ? 0u : mid);
     const f3 V = ld3(P.q.v, i, n);
     const f3 W = ld3(P.q.w, i, n);
-    const uint32_t lobe = P.q.lobe ? __ldg(P.q.lobe + i) : kLobeAll;
+    const uint32_t lobe = P.q.lobe ? ldPlane(P.q.lobe + i) : kLobeAll;
 
     DBeam<H> b;
 #pragma unroll
     for (int c4 = 0; c4 < 4; ++c4)
 #pragma unroll
-        for (int j = 0; j < H; ++j) b.L[c4][j] = __ldg(P.q.stokes + (size_t)(c4 * H + j) * n + i);
+        for (int j = 0; j < H; ++j) b.L[c4][j] = ldPlane(P.q.stokes + (size_t)(c4 * H + j) * n + i);
 #pragma unroll
-    for (int j = 0; j < H; ++j) b.wl[j] = __ldg(P.q.wavelengths + (size_t)j * n + i);
-    b.D0 = __ldg(P.q.coherence + i);
-    b.D1 = __ldg(P.q.coherence + n + i);
-    b.D2 = __ldg(P.q.coherence + 2 * n + i);
-    b.r_m = __ldg(P.q.coherence + 3 * n + i);
+    for (int j = 0; j < H; ++j) b.wl[j] = ldPlane(P.q.wavelengths + (size_t)j * n + i);
+    b.D0 = ldPlane(P.q.coherence + i);
+    b.D1 = ldPlane(P.q.coherence + n + i);
+    b.D2 = ldPlane(P.q.coherence + 2 * n + i);
+    b.r_m = ldPlane(P.q.coherence + 3 * n + i);
     b.r = -V;
     b.t = P.q.beam_t ? ld3(P.q.beam_t, i, n) : canonical_tangent(b.r);
 

@@ -264,10 +264,18 @@ constexpr int kBatchThreads = 256;     // classify CTA
 constexpr int kBatchItems = 8;
 constexpr int kBatchTile = kBatchThreads * kBatchItems;
 constexpr int kShadeThreads = 128;     // shade CTA
+// Resident shade CTAs per SM the register allocation must allow.  One wavelength per beam: 4 (16
+// warps, at most 128 registers; the natural allocation of the BSDF units' code is 154, which gives
+// 3): 0.563 against 0.620 ms on the 2^22 mixed batch, and configuration 0's 2,048 warps fit in one
+// wave (14.4 against 16.3 us).  More wavelengths: 3 (up to 170 registers; 4 spills 60 to 1,400
+// bytes per thread).
 #ifndef PLT_SHADE_MIN_BLOCKS
-#define PLT_SHADE_MIN_BLOCKS 3   // 12 warps per SM, up to 170 registers: 4.15 G queries/s vs 4.05 at 4 blocks
+#define PLT_SHADE_MIN_BLOCKS 3
 #endif
-constexpr int kShadeMinBlocks = PLT_SHADE_MIN_BLOCKS;
+#ifndef PLT_SHADE_MIN_BLOCKS_H1
+#define PLT_SHADE_MIN_BLOCKS_H1 4
+#endif
+template <int H> constexpr int shadeMinBlocks() { return H == 1 ? PLT_SHADE_MIN_BLOCKS_H1 : PLT_SHADE_MIN_BLOCKS; }
 
 // Material types of the schedule (plt_material_type ids 0..15; invalid ids land in their own slot).
 constexpr uint32_t kTypeSlots = 16;
