@@ -70,6 +70,13 @@ PLT_DI uint32_t smIdCount() {
 }
 PLT_DI uint32_t ldVolatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
+// weight of the last batch's measured cost per query in each type's running average
+// (0.2 and a minimum over the last two batches measured no better: per-launch DRAM traffic
+// alternates between ~0.76 and ~1.15 GB with any of them)
+#ifndef PLT_COST_EMA
+#define PLT_COST_EMA 0.5f
+#endif
+
 // Schedule of a batch, built by the last classify CTA (all 256 threads) once every tile's counts
 // are in: unit size and units per tile of each type, and the SM -> starting type table.
 PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
@@ -99,7 +106,7 @@ PLT_DI void buildSchedule(const BatchParams& P, uint32_t* sh) {
         float avg = __uint_as_float(avgBits);
         if (prev >= 1024u && cyc > 0ull) {
             const float m = (float)cyc / (float)prev;
-            avg = avg > 0.f ? 0.5f * avg + 0.5f * m : m;
+            avg = avg > 0.f ? (1.f - PLT_COST_EMA) * avg + PLT_COST_EMA * m : m;
             P.ctrl[C_COST + tid] = __float_as_uint(avg);
         }
         cost[tid] = avg;
