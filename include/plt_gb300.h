@@ -316,14 +316,15 @@ plt_status plt_spectral_profile_for_emitter_type(const char* tables_dir, const c
 plt_status plt_write_exr(const char* path, const float* rgba, uint32_t width, uint32_t height, int half);
 
 /* plt_bsdf_batch with HOST queries and results (same structures, host pointers; pinned memory
- * gives full copy bandwidth).  The batch is pipelined in chunks of 2^19 queries: input copies,
+ * gives full copy bandwidth).  The batch is pipelined in chunks of 2^21 queries: input copies,
  * kernels and output copies of different chunks (and of consecutive calls) overlap on the
  * library's two copy streams and compute stream; the results equal one plt_bsdf_batch over the
  * whole batch.  Asynchronous and ordered on `stream`: no input is read before the work queued on
  * `stream` ahead of the call has completed (so inputs that earlier work on `stream` writes are
  * read complete), and the results are on the host once `stream` has completed.  The pipeline
  * sorts through its own scratch, so it shares no scratch with plt_bsdf_batch.  Holds four staging
- * slots of device memory (about 70 MB each at HWSS 1) until plt_destroy. */
+ * slots of device memory until plt_destroy, each sized for the largest chunk seen (132 bytes per
+ * query of a chunk at HWSS 1 with every op: about 277 MB for 2^21 queries). */
 plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* queries,
                                const plt_bsdf_results* results, uint32_t ops, void* stream);
 

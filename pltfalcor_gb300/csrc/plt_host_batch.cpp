@@ -19,8 +19,17 @@
 
 namespace {
 
-constexpr uint32_t kHostChunk = 1u << 19;   // largest chunk (staging slots are sized for it)
-constexpr int kSlots = 4;   // 8 slots measured the same (2.07 G queries/s)
+// Largest chunk.  The copies of a chunk are one 2-D copy per field (rows = the field's planes), and
+// the host link moves long rows faster: the 2^22 mixed batch's copies alone (GB300, both directions
+// at once, no kernels) take 2.00 ms per batch with 2^19-query chunks, 1.88 ms with 2^20 and 1.77 ms
+// with 2^21, against 1.68 ms for one 285 MB and one 268 MB copy.  End to end with the kernels
+// (slots rotating across calls): 2.05, 2.22, 2.33 and, with the whole batch as one chunk, 2.13 G
+// queries/s.
+#ifndef PLT_HOST_CHUNK_LOG2
+#define PLT_HOST_CHUNK_LOG2 21
+#endif
+constexpr uint32_t kHostChunk = 1u << PLT_HOST_CHUNK_LOG2;
+constexpr int kSlots = 4;   // 8 slots measured the same (2.07 G queries/s with 2^19-query chunks)
 
 plt_status cudaFail(plt_context* ctx, cudaError_t e) {
     if (ctx) ctx->lastCudaError = (int)e;
@@ -49,6 +58,7 @@ struct plt_host_pipeline {
     cudaEvent_t evEntry = nullptr;  // the caller's stream at entry
     cudaEvent_t evIn[kSlots] = {}, evDone[kSlots] = {}, evOut[kSlots] = {};
     bool used[kSlots] = {};
+    uint32_t nextSlot = 0;         // slots rotate across calls, so a call's first chunks do not wait on the previous call's last
 };
 
 void pltReleaseHostPipeline(plt_context* ctx) {
@@ -96,12 +106,14 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
                               {lp ? hr->lambda_pdf : nullptr, H, 0},     {sm ? hr->sample_wo : nullptr, 3, 0},
                               {sm ? hr->sample_pdf : nullptr, 1, 0},     {sm ? hr->sample_weight : nullptr, 1, 0},
                               {sm ? hr->sample_lobe : nullptr, 1, 0},    {sm ? hr->sample_valid : nullptr, 1, 0}};
+    // chunks of at most kHostChunk queries; a smaller batch is one chunk (slots sized for it)
+    const uint32_t chunk = n < kHostChunk ? n : kHostChunk;
     size_t off = 0;
     auto place = [&](std::vector<Field>& fs) {
         for (Field& f : fs) {
             if (!f.host) continue;
             f.off = off;
-            off += ((size_t)f.planes * kHostChunk * 4 + 255) & ~(size_t)255;
+            off += ((size_t)f.planes * chunk * 4 + 255) & ~(size_t)255;
         }
     };
     place(in);
@@ -137,16 +149,13 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         PLT_CUDA(ctx, cudaMalloc(&hp->stage, slotBytes * kSlots));
         hp->slotBytes = slotBytes;
     }
-    // chunks of 2^19 queries: 2.08 G queries/s end to end on the 2^22 mixed batch, against 1.77
-    // with 2^18 (per-chunk kernel tails) and 1.15 without the pipeline
-    const uint32_t chunk = kHostChunk;
     const uint32_t nChunks = (n + chunk - 1) / chunk;
     // nothing of this call starts before the work already queued on the caller's stream
     PLT_CUDA(ctx, cudaEventRecord(hp->evEntry, cs));
     PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sIn, hp->evEntry, 0));
     PLT_CUDA(ctx, cudaStreamWaitEvent(hp->sComp, hp->evEntry, 0));
     for (uint32_t j = 0; j < nChunks; ++j) {
-        const int k = (int)(j % kSlots);
+        const int k = (int)((hp->nextSlot + j) % kSlots);
         const uint32_t b = j * chunk, m = n - b < chunk ? n - b : chunk;
         char* slot = static_cast<char*>(hp->stage) + (size_t)k * hp->slotBytes;
         // the slot's previous chunk has left it
@@ -186,7 +195,8 @@ plt_status plt_bsdf_batch_host(plt_context* ctx, const plt_bsdf_queries* hq, con
         hp->used[k] = true;
     }
     // the caller's stream completes when the last results have reached the host
-    PLT_CUDA(ctx, cudaStreamWaitEvent(cs, hp->evOut[(nChunks - 1) % kSlots], 0));
+    PLT_CUDA(ctx, cudaStreamWaitEvent(cs, hp->evOut[(hp->nextSlot + nChunks - 1) % kSlots], 0));
+    hp->nextSlot = (hp->nextSlot + nChunks) % kSlots;
     return PLT_OK;
 }
 
