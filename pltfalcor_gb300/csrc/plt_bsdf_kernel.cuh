@@ -70,6 +70,18 @@ PLT_DI uint32_t smIdCount() {
 }
 PLT_DI uint32_t ldVolatile(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
 
+// A bound on how far a type's queue may lead the slowest one (tiles; 0 = none).  Measured on the
+// 2^22 mixed batch (4 launches each): none 0.543 ms and 0.66-1.17 GB of DRAM traffic per launch;
+// 32 tiles checked every 8 units 0.566 ms and 0.61-0.62 GB (1.11x the algorithmic bytes); 96 tiles
+// 0.566 ms, 0.78-0.82 GB; 192 tiles 0.578 ms, 1.03-1.05 GB; checks every 16 or 32 units 0.68-0.71 ms
+// (helping warps crowd the slowest queue).  Off: the batch's time is what counts.
+#ifndef PLT_LEAD_TILES
+#define PLT_LEAD_TILES 0
+#endif
+#ifndef PLT_LEAD_CHECK
+#define PLT_LEAD_CHECK 8
+#endif
+
 // weight of the last batch's measured cost per query in each type's running average
 // (0.2 and a minimum over the last two batches measured no better: per-launch DRAM traffic
 // alternates between ~0.76 and ~1.15 GB with any of them)
@@ -327,6 +339,20 @@ PLT_DI uint32_t busiestQueue(const BatchParams& P, uint32_t nTiles, uint32_t lan
     return work > 0.f ? best : kTypeSlots;
 }
 
+// The queue whose next unit lies in the lowest tile among the queues with work left, packed as
+// tile << 8 | type (0xFFFFFFFF when every queue is empty).  Whole warp; `unitsOf` is each lane's
+// type's units per tile.
+PLT_DI uint32_t slowestQueue(const BatchParams& P, uint32_t nTiles, uint32_t unitsOf, uint32_t lane) {
+    uint32_t key = 0xFFFFFFFFu;
+    if (lane < kTypeSlots && unitsOf) {
+        const uint32_t next = ldVolatile(P.ctrl + C_NEXT + lane);
+        if (next < unitsOf * nTiles) key = (next / unitsOf) << 8 | lane;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) key = min(key, __shfl_xor_sync(0xFFFFFFFFu, key, d));
+    return key;
+}
+
 // Stages the spectral profiles into shared memory with one bulk asynchronous copy; false (after
 // reporting the timeout and letting a late copy land) when the copy did not land within the poll
 // budget.  All threads of the CTA.
@@ -405,6 +431,12 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) 
     uint32_t t = small ? 0u : P.smType[smId() % kMaxSmIds] % kTypeSlots;
     uint32_t units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
     uint32_t sTile = 0, sPos = 0, sEnd = 0;   // a small batch's current unit: remaining positions
+    uint32_t t0q = 0;   // the queue the current unit came from
+#if PLT_LEAD_TILES
+    // a warp whose own queue leads the slowest queue by more than PLT_LEAD_TILES tiles takes its
+    // next PLT_LEAD_CHECK units from the slowest queue (checked every PLT_LEAD_CHECK units)
+    uint32_t ownTile = 0, sinceCheck = 0, helpLeft = 0, helpType = 0;
+#endif
     for (;;) {
         uint32_t tile, lo, hi;
         if (small) {
@@ -427,27 +459,54 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) 
             hi = min(sEnd, max(lo + 1u, (uint32_t)__ldg(off + t + 1)));
             sPos = hi;
         } else {
+            uint32_t qt = t, qunits = units;
+#if PLT_LEAD_TILES
+            if (helpLeft) {
+                qt = helpType;
+                --helpLeft;
+            } else if (++sinceCheck >= PLT_LEAD_CHECK) {
+                sinceCheck = 0;
+                const uint32_t slow = slowestQueue(P, nTiles, unitsOf, lane);
+                if (slow != 0xFFFFFFFFu && (slow & 0xFFu) != t && ownTile > (slow >> 8) + PLT_LEAD_TILES) {
+                    helpType = slow & 0xFFu;
+                    helpLeft = PLT_LEAD_CHECK - 1;
+                    qt = helpType;
+                }
+            }
+            if (qt != t) qunits = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)qt);
+#endif
             uint32_t u = 0;
-            if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + t, 1u);
+            if (lane == 0) u = atomicAdd(P.ctrl + C_NEXT + qt, 1u);
             u = __shfl_sync(0xFFFFFFFFu, u, 0);
-            if (u >= units * nTiles) {
+            if (u >= qunits * nTiles) {
+#if PLT_LEAD_TILES
+                if (qt != t) {
+                    helpLeft = 0;
+                    continue;
+                }
+#endif
                 t = busiestQueue(P, nTiles, lane);
                 if (t >= kTypeSlots) break;
                 units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
                 continue;
             }
-            tile = u / units;
-            const uint32_t sub = u - tile * units;
-            const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + t), (uint32_t)kBatchTile));
+            tile = u / qunits;
+#if PLT_LEAD_TILES
+            if (qt == t) ownTile = tile;
+#endif
+            const uint32_t sub = u - tile * qunits;
+            const uint32_t usz = max(32u, min(__ldg(P.ctrl + C_USZ + qt), (uint32_t)kBatchTile));
             const uint16_t* off = P.tileTypeOff + tile * (kTypeSlots + 1);
-            lo = __ldg(off + t) + sub * usz;
-            hi = min(min((uint32_t)__ldg(off + t + 1), (uint32_t)kBatchTile), lo + usz);
+            lo = __ldg(off + qt) + sub * usz;
+            hi = min(min((uint32_t)__ldg(off + qt + 1), (uint32_t)kBatchTile), lo + usz);
             if (lo >= hi) continue;
+            t0q = qt;
         }
+        const uint32_t st = small ? t : t0q;
         const long long t0 = clock64();
-        shadeRange<H>(P, c, t, tile * kBatchTile, lo, hi, lane);
+        shadeRange<H>(P, c, st, tile * kBatchTile, lo, hi, lane);
         __syncwarp();
-        if (lane == 0 && !small) atomicAdd(&cycles[t], (unsigned long long)(clock64() - t0));
+        if (lane == 0 && !small) atomicAdd(&cycles[st], (unsigned long long)(clock64() - t0));
     }
     // the measured cost per type feeds the next batch's SM shares
     __syncthreads();
