@@ -1971,10 +1971,11 @@ __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const
 // Finishes the sample exactly as the solve kernel would (pltpt_solve.rt.slang:293-366: the walk,
 // the beam's new direction, 1 / pdf, the MIS weight, the manifold replay and the measurement) and
 // adds it to the pixel's accumulator.
-// Resident CTAs per SM of the walk kernel (96 registers): 1 (128 registers) 16.05 ms per frame, 5
-// 14.77 ms, 6 14.92 ms.
+// Resident CTAs per SM of the walk kernel: an early version measured 1 (128 registers) 16.05 ms per
+// frame, 5 (96) 14.77 ms, 6 14.92 ms; the current one 4 (128 registers) 11.97 ms, 5 12.26 ms and 6
+// 12.20 ms.
 #ifndef PLT_MNEE_MIN_BLOCKS
-#define PLT_MNEE_MIN_BLOCKS 5
+#define PLT_MNEE_MIN_BLOCKS 4
 #endif
 template <int H>
 __global__ void __launch_bounds__(128, PLT_MNEE_MIN_BLOCKS) ptMneeKernel(const PtParams P) {
