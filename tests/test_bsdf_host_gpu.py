@@ -19,7 +19,10 @@ def torch_cuda():
     return torch
 
 
-@pytest.mark.parametrize("n,hwss,ops,pin", [((1 << 20) + (1 << 18) + 7, 1, capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF, True),
+# the first case spans two 2^21-query chunks (the second partial, not a multiple of 4, shaded by
+# the small-batch schedule when short); three calls walk the four staging slots round
+@pytest.mark.parametrize("n,hwss,ops,pin", [((1 << 21) + (1 << 18) + 7, 1, capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF, True),
+                                            ((1 << 21) + 4100, 1, capi.OP_EVAL | capi.OP_PDF, True),
                                             (300_001, 4, capi.OP_ALL, False), (4096, 2, capi.OP_SAMPLE, True)])
 def test_host_batch_equals_device_batch(torch_cuda, product_lib, n, hwss, ops, pin):
     from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
@@ -35,7 +38,7 @@ def test_host_batch_equals_device_batch(torch_cuda, product_lib, n, hwss, ops, p
     torch_cuda.cuda.synchronize()
     ref = d.fetch()
     h = DeviceBatch(wl, device="cpu", pin=pin)
-    for rep in range(2):
+    for rep in range(3):
         ctx.batch_host(h.queries(rng_offset=11), h.results(ops), ops)
         torch_cuda.cuda.synchronize()
     assert ctx.check_status() == capi.PLT_OK
@@ -65,7 +68,7 @@ def test_host_batch_ordered_on_callers_stream(torch_cuda, product_lib):
     torch = torch_cuda
     from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
     prof, _ = spectra.standard_profiles()
-    n = (1 << 20) + 4100
+    n = (1 << 21) + 4100   # two chunks, the second short
     wl = W.mixed_material_batch(n=(n + 7) // 8 * 8, profiles=prof)
     wl = wl.subset(np.arange(n))
     ops = capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF
@@ -93,4 +96,31 @@ def test_host_batch_ordered_on_callers_stream(torch_cuda, product_lib):
     for k in ["stokes", "coherence", "pdf", "sample_wo", "sample_pdf", "sample_weight", "sample_lobe", "sample_valid"]:
         assert np.array_equal(got[k].view(np.uint32), ref[k].view(np.uint32)), k
         assert np.array_equal(again[k].view(np.uint32), ref[k].view(np.uint32)), k
+    ctx.close()
+
+
+def test_host_batch_slots_grow_between_calls(torch_cuda, product_lib):
+    """One context, calls of growing then shrinking size: the staging slots are sized for the
+    first call's chunk and reallocated (after the pipeline drains) when a later call's chunk is
+    larger; every call's results equal plt_bsdf_batch's bit for bit."""
+    from pltfalcor_gb300.bsdf import DeviceBatch, PLTContext
+    prof, _ = spectra.standard_profiles()
+    ops = capi.OP_EVAL | capi.OP_SAMPLE | capi.OP_PDF
+    ctx = PLTContext()
+    ctx.set_spectral_profiles(prof)
+    full = W.mixed_material_batch(n=(1 << 21) + 104, profiles=prof)
+    ctx.set_materials(full.records)
+    for n, off in ((4096, 3), ((1 << 21) + 100, 5), (70_001, 7)):
+        wl = full.subset(np.arange(n))
+        d = DeviceBatch(wl)
+        ctx.batch(d.queries(rng_offset=off), d.results(ops), ops)
+        torch_cuda.cuda.synchronize()
+        ref = d.fetch()
+        h = DeviceBatch(wl, device="cpu", pin=True)
+        ctx.batch_host(h.queries(rng_offset=off), h.results(ops), ops)
+        torch_cuda.cuda.synchronize()
+        assert ctx.check_status() == capi.PLT_OK
+        got = h.fetch()
+        for k in ["stokes", "coherence", "pdf", "sample_wo", "sample_pdf", "sample_weight", "sample_lobe", "sample_valid"]:
+            assert np.array_equal(got[k].view(np.uint32), ref[k].view(np.uint32)), (n, k)
     ctx.close()
