@@ -45,8 +45,7 @@ enum : uint32_t {
     C_TOTAL = 96,   // [16] queries per type
     C_COST = 112,   // [16] measured cost per query of each type (float; exponential average over batches)
     C_CYC = 128,    // [16] x u64: warp cycles spent on each type's units in the last batch
-    C_SMALL = 160,  // the work counter of a small batch (zeroed by its classify grid)
-    C_WORDS = 161
+    C_WORDS = 160
 };
 static_assert(C_WORDS * 4 <= plt::kBsdfCtrlBytes, "control words exceed their scratch block");
 
@@ -280,11 +279,6 @@ static __global__ void __launch_bounds__(plt::kBatchThreads, PLT_CLASSIFY_MIN_BL
         }
         __syncthreads();   // counts and offs are rewritten for the next tile
     }
-    if (P.smallBatch) {
-        // a small batch is shaded in the tiles' sorted order from one counter: no schedule
-        if (blockIdx.x == 0 && tid == 0) P.ctrl[C_SMALL] = 0u;
-        return;
-    }
     if (tid < kTypeSlots && ctaCount[tid]) {
         atomicAdd(P.ctrl + C_COUNT + tid, ctaCount[tid]);
         atomicMax(P.ctrl + C_MAX + tid, ctaMax[tid]);
@@ -306,15 +300,11 @@ static __global__ void __launch_bounds__(plt::kBatchThreads, PLT_CLASSIFY_MIN_BL
 
 // One unit: positions [lo, hi) of the tile's sorted permutation, all of material type T (T = 0:
 // a slot of invalid types or material ids, which only report their status and zero the outputs).
+// One query of material type T (T = 0: an invalid type or material id, which only reports its
+// status and zeroes the outputs), when `valid`.
 template <int H, uint32_t T>
-__device__ __forceinline__ void shadeUnit(const BatchParams& P, const Ctx& c, uint32_t tileBase, uint32_t lo, uint32_t hi, uint32_t lane) {
-    for (uint32_t pos = lo; pos < hi; pos += 32) {
-        const uint32_t k = pos + lane;
-        if (k < hi) {
-            const uint32_t idx = tileBase + __ldg(P.perm + pltIdx(P.status, tileBase + k, permSlots(P.q.n), kSitePerm));
-            if (idx < P.q.n) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, ldPlane(P.q.material + idx), T);
-        }
-    }
+__device__ __forceinline__ void shadeUnit(const BatchParams& P, const Ctx& c, uint32_t idx, bool valid) {
+    if (valid) processQueryTyped<H>(P, c, idx, 0xFFFFFFFFu, ldPlane(P.q.material + idx), T);
 }
 
 // The queue with the most estimated work left (remaining units x unit size x cost), or kTypeSlots
@@ -382,30 +372,31 @@ PLT_DI bool stageProfiles(const BatchParams& P, DevProfile* sprof, uint64_t* bar
     return true;
 }
 
-// Positions [lo, hi) of a tile's sorted permutation, all of material type t, with the code
-// specialised for t at compile time.
+// This lane's query (when `valid`), of material type t, with the code specialised for t at compile
+// time.  The warp's lanes all pass the same t.
 template <int H>
-PLT_DI void shadeRange(const BatchParams& P, const Ctx& c, uint32_t t, uint32_t tileBase, uint32_t lo, uint32_t hi, uint32_t lane) {
+PLT_DI void shadeRange(const BatchParams& P, const Ctx& c, uint32_t t, uint32_t idx, bool v) {
     switch (t) {
-    case kMatDielectric: shadeUnit<H, kMatDielectric>(P, c, tileBase, lo, hi, lane); break;
-    case kMatConductor: shadeUnit<H, kMatConductor>(P, c, tileBase, lo, hi, lane); break;
-    case kMatOpaqueDielectric: shadeUnit<H, kMatOpaqueDielectric>(P, c, tileBase, lo, hi, lane); break;
-    case kMatCoatedConductor: shadeUnit<H, kMatCoatedConductor>(P, c, tileBase, lo, hi, lane); break;
-    case kMatCoatedOpaque: shadeUnit<H, kMatCoatedOpaque>(P, c, tileBase, lo, hi, lane); break;
-    case kMatGratedConductor: shadeUnit<H, kMatGratedConductor>(P, c, tileBase, lo, hi, lane); break;
-    case kMatGratedOpaque: shadeUnit<H, kMatGratedOpaque>(P, c, tileBase, lo, hi, lane); break;
-    case kMatThin: shadeUnit<H, kMatThin>(P, c, tileBase, lo, hi, lane); break;
-    case kMatMultilayer: shadeUnit<H, kMatMultilayer>(P, c, tileBase, lo, hi, lane); break;
-    case kMatDiffuse: shadeUnit<H, kMatDiffuse>(P, c, tileBase, lo, hi, lane); break;
-    default: shadeUnit<H, 0u>(P, c, tileBase, lo, hi, lane); break;
+    case kMatDielectric: shadeUnit<H, kMatDielectric>(P, c, idx, v); break;
+    case kMatConductor: shadeUnit<H, kMatConductor>(P, c, idx, v); break;
+    case kMatOpaqueDielectric: shadeUnit<H, kMatOpaqueDielectric>(P, c, idx, v); break;
+    case kMatCoatedConductor: shadeUnit<H, kMatCoatedConductor>(P, c, idx, v); break;
+    case kMatCoatedOpaque: shadeUnit<H, kMatCoatedOpaque>(P, c, idx, v); break;
+    case kMatGratedConductor: shadeUnit<H, kMatGratedConductor>(P, c, idx, v); break;
+    case kMatGratedOpaque: shadeUnit<H, kMatGratedOpaque>(P, c, idx, v); break;
+    case kMatThin: shadeUnit<H, kMatThin>(P, c, idx, v); break;
+    case kMatMultilayer: shadeUnit<H, kMatMultilayer>(P, c, idx, v); break;
+    case kMatDiffuse: shadeUnit<H, kMatDiffuse>(P, c, idx, v); break;
+    default: shadeUnit<H, 0u>(P, c, idx, v); break;
     }
 }
 
 // The shade kernel.  A batch of more than kSmallBatchTiles tiles is shaded from the per-type unit
-// queues of the classify schedule; a small batch's warps take units of 32 consecutive positions of
-// a tile's sorted permutation from one counter, in tile order, split where the material type
-// changes (a few-tile batch is latency-bound and gains nothing from the queues).  Both schedules
-// end in the one call of the typed code, so a query gives the same bits in any batch.
+// queues of the classify schedule.  A small batch is not classified (it is latency-bound and gains
+// nothing from the queues or the sort): warp w takes the 32 consecutive queries of units w,
+// w + warps, ..., and shades them once per material type among them, the lanes of that type
+// active.  Both schedules end in the one call of the typed code, so a query gives the same bits in
+// any batch.
 template <int H>
 __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) bsdfShadeKernel(const BatchParams P) {
     using namespace plt;
@@ -430,7 +421,11 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) 
     const uint32_t unitsOf = lane < kTypeSlots && !small ? min(__ldg(P.ctrl + C_UNITS + lane), kMaxUnits) : 0u;
     uint32_t t = small ? 0u : P.smType[smId() % kMaxSmIds] % kTypeSlots;
     uint32_t units = __shfl_sync(0xFFFFFFFFu, unitsOf, (int)t);
-    uint32_t sTile = 0, sPos = 0, sEnd = 0;   // a small batch's current unit: remaining positions
+    // a small batch's current unit: its first query, its query count, this lane's material type
+    // and the lanes not yet shaded
+    const uint32_t warpId = blockIdx.x * (kShadeThreads / 32) + (tid >> 5), warps = gridDim.x * (kShadeThreads / 32);
+    uint32_t sUnit = warpId, sBase = 0, sCount = 0, sType = 0, sLeft = 0;
+    bool sStarted = false;
     uint32_t t0q = 0;   // the queue the current unit came from
 #if PLT_LEAD_TILES
     // a warp whose own queue leads the slowest queue by more than PLT_LEAD_TILES tiles takes its
@@ -438,26 +433,27 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) 
     uint32_t ownTile = 0, sinceCheck = 0, helpLeft = 0, helpType = 0;
 #endif
     for (;;) {
-        uint32_t tile, lo, hi;
+        uint32_t tile, lo, hi, mask = 0xFFFFFFFFu;
         if (small) {
-            if (sPos >= sEnd) {
-                uint32_t u = 0;
-                if (lane == 0) u = atomicAdd(P.ctrl + C_SMALL, 1u);
-                u = __shfl_sync(0xFFFFFFFFu, u, 0);
-                if (u >= nTiles * kMaxUnits) break;
-                sTile = u / kMaxUnits;
-                sPos = (u - sTile * kMaxUnits) * 32u;
-                sEnd = min(sPos + 32u, min((uint32_t)kBatchTile, P.q.n - sTile * kBatchTile));
-                if (sPos >= sEnd) continue;
+            if (sLeft == 0u) {
+                if (sStarted) sUnit += warps;
+                sStarted = true;
+                if (sUnit >= (P.q.n + 31u) / 32u) break;
+                sBase = sUnit * 32u;
+                sCount = min(32u, P.q.n - sBase);
+                if (lane < sCount) {
+                    const uint32_t mid = ldPlane(P.q.material + sBase + lane);
+                    sType = (mid < P.nMats ? (uint32_t)__ldg(P.matType + mid) : 14u) & 15u;
+                }
+                sLeft = __ballot_sync(0xFFFFFFFFu, lane < sCount);
             }
-            // the type whose range of the tile's permutation holds sPos, and where that range ends
-            const uint16_t* off = P.tileTypeOff + sTile * (kTypeSlots + 1);
-            t = 0;
-            while (t + 1 < kTypeSlots && (uint32_t)__ldg(off + t + 1) <= sPos) ++t;
-            tile = sTile;
-            lo = sPos;
-            hi = min(sEnd, max(lo + 1u, (uint32_t)__ldg(off + t + 1)));
-            sPos = hi;
+            // the type of the lowest lane not yet shaded, and every remaining lane of that type
+            t = __shfl_sync(0xFFFFFFFFu, sType, __ffs((int)sLeft) - 1);
+            mask = __ballot_sync(0xFFFFFFFFu, ((sLeft >> lane) & 1u) && sType == t);
+            sLeft &= ~mask;
+            tile = 0;
+            lo = 0;
+            hi = sCount;
         } else {
             uint32_t qt = t, qunits = units;
 #if PLT_LEAD_TILES
@@ -503,8 +499,16 @@ __global__ void __launch_bounds__(plt::kShadeThreads, plt::shadeMinBlocks<H>()) 
             t0q = qt;
         }
         const uint32_t st = small ? t : t0q;
+        const uint32_t base = small ? sBase : tile * kBatchTile;
         const long long t0 = clock64();
-        shadeRange<H>(P, c, st, tile * kBatchTile, lo, hi, lane);
+        // one pass for the schedule's 32-query units and for a small batch's unit
+        for (uint32_t pos = lo; pos < hi; pos += 32) {
+            const uint32_t k = pos + lane;
+            const bool inUnit = k < hi && ((mask >> lane) & 1u);
+            uint32_t idx = 0;
+            if (inUnit) idx = small ? base + k : base + __ldg(P.perm + pltIdx(P.status, base + k, permSlots(P.q.n), kSitePerm));
+            shadeRange<H>(P, c, st, idx, inUnit && idx < P.q.n);
+        }
         __syncwarp();
         if (lane == 0 && !small) atomicAdd(&cycles[st], (unsigned long long)(clock64() - t0));
     }
@@ -538,8 +542,10 @@ inline float defaultTypeCost(uint32_t t) {
     }
 }
 
-// Batches of at most this many tiles (65,536 queries) skip the per-type schedule: its last-CTA
-// build and the queue look-ups cost more latency than a few-tile batch loses to mixed-type warps.
+// Batches of at most this many tiles (65,536 queries) are not classified: the classify launch, its
+// last-CTA schedule build and the queue look-ups cost more latency than a few-tile batch loses to
+// mixed-type warps (configuration 0, 65,536 single-material queries: 8.2 us per batch unclassified,
+// 14.4 us classified).
 constexpr uint32_t kSmallBatchTiles = 32;
 
 // classify: one CTA per tile; shade: persistent grid of SM count x resident CTAs per SM
@@ -585,9 +591,13 @@ cudaError_t launchBsdfBatchH(const BatchParams& p0, int numSMs, cudaStream_t str
     }
     const uint32_t classifyGrid = min(nTiles, (uint32_t)(numSMs * cb));
     if (p.timing[0]) cudaEventRecord((cudaEvent_t)p.timing[0], stream);
-    pltdev::bsdfClassifyKernel<<<classifyGrid, kBatchThreads, 0, stream>>>(p);
+    // a small batch is not classified: one ordinary launch of the shade kernel
+    if (!p.smallBatch) pltdev::bsdfClassifyKernel<<<classifyGrid, kBatchThreads, 0, stream>>>(p);
     cudaError_t e = cudaSuccess;
-    if (p.timing[1]) {
+    if (p.smallBatch) {
+        if (p.timing[1]) cudaEventRecord((cudaEvent_t)p.timing[1], stream);
+        pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);
+    } else if (p.timing[1]) {
         // per-kernel timing: an event between the kernels, so an ordinary launch
         cudaEventRecord((cudaEvent_t)p.timing[1], stream);
         pltdev::bsdfShadeKernel<H><<<grid, kShadeThreads, smem, stream>>>(p);

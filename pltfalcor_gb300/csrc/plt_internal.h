@@ -71,7 +71,7 @@ struct BatchParams {
     uint32_t* ctrl;            // BatchCtrl words (see plt_bsdf_kernel.cuh)
     uint8_t* smType;           // [kMaxSmIds] material type each SM starts on
     uint32_t unitQueries;      // target queries per work unit (a multiple of 32)
-    uint32_t smallBatch;       // at most kSmallBatchTiles tiles: no per-type schedule (see plt_bsdf_kernel.cuh)
+    uint32_t smallBatch;       // at most kSmallBatchTiles tiles: not classified (see plt_bsdf_kernel.cuh)
     uint32_t copyPolls;        // poll budget of the spectral-table copy wait (0 under PLT_OPTION_FAULT_COPY_WAIT)
     float typeCost[16];        // relative cost per query of each material type (the schedule's SM shares)
     // optional cudaEvent_t handles recorded on the launch stream before the classify kernel,
