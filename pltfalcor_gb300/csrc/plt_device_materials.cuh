@@ -794,7 +794,7 @@ PLT_NI float mlRecursion(float sqrtm00, uint32_t layers, MLLayer l0, MLLayer l1,
         const RT d = (RT)2 * (RT)L.th / (RT)L.ct * (RT)k * (RT)L.ior;
         RT sd, cd;
         if constexpr (sizeof(RT) == 8) sincos(d, &sd, &cd);
-        else sincosf(d, &sd, &cd);
+        else sincosReduced(d, &sd, &cd);
         const RT R = l == layers - 1 ? (RT)Rout : (RT)L.r;
         // G = G * p
         const RT x = gx * cd - gy * sd, y = gx * sd + gy * cd;

@@ -62,6 +62,17 @@ PLT_DI f3 cross(f3 a, f3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b
 PLT_DI f3 normalize(f3 a) { return a / sqrtf(dot(a, a)); }
 PLT_DI float sqr(float x) { return x * x; }
 // x^y for x > 0 as exp2(y log2 x) on the SFU (relative error ~1e-6 for |y log2 x| < 64), used where
+// Sine and cosine of a phase of up to a few thousand radians: Cody-Waite additive reduction by
+// 2 pi (split into the float nearest 2 pi and the remainder, 2 pi - 6.28318548f), then sincosf on
+// [-pi, pi].  Where sincosf is the SFU approximation its error grows with |x| without the
+// reduction (the multilayer recursion's phases reach ~100 rad).
+PLT_DI void sincosReduced(float x, float* s, float* c) {
+    const float k = rintf(x * 0.159154943091895336f);
+    float r = fmaf(-k, 6.28318548202514648f, x);
+    r = fmaf(-k, -1.74845553e-7f, r);
+    sincosf(r, s, c);
+}
+
 // the reference calls pow on positive bases; PLT_FAST_POW=0 keeps the correctly rounded powf.
 #ifndef PLT_FAST_POW
 #define PLT_FAST_POW 1
