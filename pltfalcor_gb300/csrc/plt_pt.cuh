@@ -1615,7 +1615,6 @@ PLT_DI bool deferReplay(const PtParams& P, uint32_t pid, int p, bool evalCurrent
 #endif
 template <int H, bool MNEE>
 __global__ void __launch_bounds__(128, PLT_SOLVE_MIN_BLOCKS) ptSolveKernel(const PtParams P) {
-    const uint32_t n = P.npix;
     const float4* nodes = reinterpret_cast<const float4*>(P.nodes);
     const Ctx c{P.profiles, P.nProfiles, P.flags};
     const bool hwssMis = (P.opt & plt::kPtHwssMis) != 0;
