@@ -559,7 +559,8 @@ plt_status plt_proposal_train(plt_context* ctx, uint32_t steps, uint32_t batch, 
 /* Per-kernel timing of plt_bsdf_batch (a profiling aid; no counterpart in the reference, whose
  * shaders are timed only as a whole render pass).  Each later plt_bsdf_batch
  * on this context records the given cudaEvent_t handles (any may be NULL) on its stream: before the
- * classify kernel, between classify and shade, and after the shade kernel.  NULLs switch it off. */
+ * classify kernel, between classify and shade, and after the shade kernel (a batch of at most 65,536
+ * queries is not classified: the first two events are recorded back to back).  NULLs switch it off. */
 plt_status plt_set_timing_events(plt_context* ctx, void* before_classify, void* before_shade, void* after_shade);
 
 /* Largest batch plt_bsdf_batch_noalloc accepts. */
