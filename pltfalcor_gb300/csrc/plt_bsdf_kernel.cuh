@@ -2,11 +2,12 @@
 // queries of any mix of PLT materials (the batched form of IMaterialInstance,
 // Source/Falcor/Rendering/Materials/IMaterialInstance.slang:122-184 in ssteinberg/PLTFalcor).
 //
-// Work layout on sm_103a, two launches:
-//  1. classify: one CTA per tile of 2048 queries counting-sorts the tile by (material type, lobe
-//     class) in shared memory, writes the tile's permutation (16-bit local indices) and the start of
-//     each material type's range in it, and adds the tile's per-type counts to the batch totals.
-//     The last CTA to finish builds the schedule from those totals: per material type, a queue of
+// Work layout on sm_103a, two launches (one for a batch of at most kSmallBatchTiles tiles, shaded
+// unsorted by the shade kernel alone):
+//  1. classify: a persistent grid whose CTAs counting-sort tiles of 2048 queries by (material type,
+//     lobe class) in shared memory, write each tile's permutation (16-bit local indices) and the
+//     start of each material type's range in it, and add their tiles' per-type counts to the batch
+//     totals.  The last CTA to finish builds the schedule from those totals: per material type, a queue of
 //     work units (each a slice of one tile's range of that type, tiles in order) and, per SM, the
 //     type it starts on, with SM shares proportional to each type's queries x relative cost.
 //  2. shade: a persistent, barrier-free grid.  Every warp of an SM takes units from the queue of
